@@ -1,0 +1,284 @@
+/*
+ * vdvc.h -- C ABI of the GB300 (sm_103a) voxelDVC global Gauss-Newton path.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream,
+ * enqueues its kernels on that stream and returns an int status
+ * (VDVC_OK == 0).  Nothing here takes ownership of a pointer.  Outputs are
+ * caller-allocated; scratch memory is passed in as (ws, ws_bytes) and its
+ * required size is given by the matching *_workspace_bytes() query.
+ *
+ * Layouts (identical to the reference's xp arrays):
+ *   voxel fields  : flat, x fastest, vidx = vx + vy*Nvx + vz*Nvx*Nvy,
+ *                   Nv? = N?*h + 1 ("vox" layout = F-order ravel of pix[x,y,z])
+ *   grad          : (Nvox, 3) interleaved, component fastest
+ *   masks         : (Nvox) uint8, 0/1
+ *   dof vectors   : (Ndof) with dof = 3*node + c, node = i + j*(Nx+1) + k*(Nx+1)*(Ny+1)
+ *   element index : e = i + j*Nx + k*Nx*Ny
+ *   images (pix)  : C-order (nx, ny, nz) arrays, z fastest, as numpy holds pix[x,y,z]
+ *
+ * `dtype` arguments select the floating type of every floating array of
+ * the call: VDVC_F32 or VDVC_F64.
+ *
+ * Citations name the reference function each entry point replaces
+ * (paths inside the voxelDVC project, src/voxeldvc/...).
+ */
+#ifndef VDVC_H
+#define VDVC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* vdvc_stream_t; /* == cudaStream_t */
+
+/* ---- status codes --------------------------------------------------- */
+enum {
+  VDVC_OK = 0,
+  VDVC_ERR_ARG = 1,          /* invalid argument (size, pointer, dtype)          */
+  VDVC_ERR_INDEX_RANGE = 2,  /* Nvox or Ndof beyond int32 (correlate_gpu.py:933) */
+  VDVC_ERR_CUDA = 3,         /* CUDA runtime / launch error                      */
+  VDVC_ERR_WORKSPACE = 4,    /* ws_bytes smaller than the query returned         */
+  VDVC_ERR_NONFINITE = 5,    /* NaN/Inf met where a finite value is required     */
+  VDVC_ERR_ZERO_DIVISION = 6,/* a normalisation std of zero (the reference raises
+                                ZeroDivisionError at correlate_gpu.py:1095)      */
+  VDVC_ERR_CUFFT = 7,        /* cuFFT plan/exec failure                          */
+  VDVC_ERR_UNSUPPORTED = 8   /* valid request this build does not implement      */
+};
+
+/* element types for dtype / pix_dtype arguments */
+enum {
+  VDVC_F32 = 0,
+  VDVC_F64 = 1,
+  VDVC_U8 = 2,
+  VDVC_U16 = 3,
+  VDVC_I16 = 4,
+  VDVC_I32 = 5
+};
+
+/* regularizer kinds (correlate_gpu.py:966-967, reg_type) */
+enum {
+  VDVC_REG_NONE = 0,
+  VDVC_REG_LAPLACIAN = 1,
+  VDVC_REG_EQUILIBRIUM_GAP = 2
+};
+
+/* ---- library info ---------------------------------------------------- */
+int vdvc_abi_version(void);
+const char* vdvc_status_string(int status);
+/* Detail of the last non-OK status raised on the calling host thread. */
+const char* vdvc_last_error(void);
+/* Number of kernels this library has enqueued since load (graph nodes
+   count once per replay). */
+long long vdvc_launch_count(void);
+
+/* ---- scratch size query -------------------------------------------- */
+/* Bytes of scratch that any single operator call below needs for this mesh
+   (element vectors + reduction partials).  Solver calls have their own
+   queries further down. */
+size_t vdvc_workspace_bytes(int dtype, int h, int Nx, int Ny, int Nz);
+
+/* ---- image layout ---------------------------------------------------- */
+/* pix (C-order nx*ny*nz of pix_dtype) -> vox (x fastest, dtype), with the
+   cast.  Replaces xp.asarray(pix, dtype) + xp.ravel(order='F')
+   (engine/correlate_gpu.py:59-60, :938-939). */
+int vdvc_pix_to_vox(const void* pix, int pix_dtype, int nx, int ny, int nz,
+                    void* vox, int dtype, vdvc_stream_t stream);
+
+/* Strided decimation in vox layout: out = in[::s, ::s, ::s]
+   (engine/correlate_gpu.py:1257-1258).  out has ceil(n/s) per axis. */
+int vdvc_decimate(const void* in, int dtype, int nx, int ny, int nz, int s,
+                  void* out, vdvc_stream_t stream);
+
+/* ---- reference-image preparation ------------------------------------ */
+/* grad = per-axis xp.gradient (central differences, one-sided first order at
+   the borders) of the vox field f (engine/correlate_gpu.py:49-72).  When
+   mask0 != NULL also: mask0 = f > glt (:951) and grad zeroed where the
+   6-neighbour erosion (mode 'nearest') of mask0 is false (:952-953,
+   erode_mask0_vox :75-94). */
+int vdvc_image_grad(const void* f_vox, int dtype, int Nvx, int Nvy, int Nvz,
+                    double glt, void* grad, uint8_t* mask0,
+                    vdvc_stream_t stream);
+
+/* 6-neighbour minimum filter, mode 'nearest' (erode_mask0_vox,
+   engine/correlate_gpu.py:75-94). */
+int vdvc_erode_mask(const uint8_t* mask, int Nvx, int Nvy, int Nvz,
+                    uint8_t* out, vdvc_stream_t stream);
+
+/* ---- statistics ------------------------------------------------------ */
+/* Multiplicity-weighted masked sums over the (element, stencil point)
+   array: out3[0] = count, out3[1] = sum x, out3[2] = sum x^2 (float64, on
+   the device).  masked_quadpoint_mean_std, engine/correlate_gpu.py:113-157. */
+int vdvc_masked_stats(const void* field, int dtype, const uint8_t* mask,
+                      int h, int Nx, int Ny, int Nz, double* out3,
+                      void* ws, size_t ws_bytes, vdvc_stream_t stream);
+
+/* ---- operators (engine/kernels_dvc.py) -------------------------------- */
+/* out = H v, matrix-free correlation Hessian (matvec_H, kernels_dvc.py:452-506). */
+int vdvc_matvec_H(const void* v, const void* grad, const uint8_t* mask,
+                  int dtype, int h, int Nx, int Ny, int Nz, void* out,
+                  void* ws, size_t ws_bytes, vdvc_stream_t stream);
+
+/* out = diag(H) (build_diagonal_H, kernels_dvc.py:509-543). */
+int vdvc_diag_H(const void* grad, const uint8_t* mask, int dtype, int h,
+                int Nx, int Ny, int Nz, void* out, void* ws, size_t ws_bytes,
+                vdvc_stream_t stream);
+
+/* out = sum_e P_e^T sum_q w m res N (x) grad (compute_b_gpu,
+   engine/correlate_gpu.py:341-378). */
+int vdvc_compute_b(const void* res, const uint8_t* mask, const void* grad,
+                   int dtype, int h, int Nx, int Ny, int Nz, void* out,
+                   void* ws, size_t ws_bytes, vdvc_stream_t stream);
+
+/* out = sum_e E_e P_e^T K_ref P_e v (matvec_K_ref, kernels_dvc.py:349-374).
+   K_ref: host 24x24 row-major float64.  E_elem: device (Ne) array of dtype,
+   or NULL to use the scalar E. */
+int vdvc_matvec_K_ref(const void* v, int dtype, const double* K_ref,
+                      const void* E_elem, double E, int Nx, int Ny, int Nz,
+                      void* out, vdvc_stream_t stream);
+
+/* out = diag of the operator above (build_diagonal_K_ref, kernels_dvc.py:377-392). */
+int vdvc_diag_K_ref(int dtype, const double* K_ref, const void* E_elem,
+                    double E, int Nx, int Ny, int Nz, void* out,
+                    vdvc_stream_t stream);
+
+/* out = K (P_i (K v)), K = sum_e E_e P_e^T K_el P_e
+   (matvec_equilibrium_gap, kernels_dvc.py:402-417).  interior: device
+   (Ndof) array of dtype (the P_i diagonal). */
+int vdvc_matvec_equilibrium_gap(const void* v, int dtype, const double* K_el,
+                                const void* interior, const void* E_elem,
+                                double E, int Nx, int Ny, int Nz, void* out,
+                                void* ws, size_t ws_bytes,
+                                vdvc_stream_t stream);
+
+/* Hutchinson estimate of diag(K P_i K) in float64 from n_probes Rademacher
+   probes given as int8 (+1/-1), probe-major (n_probes x Ndof), then the
+   clip at 1e-12*max|diag| (build_diagonal_equilibrium_gap,
+   kernels_dvc.py:420-437). */
+int vdvc_diag_equilibrium_gap(const int8_t* probes, int n_probes,
+                              const double* K_el, const double* interior,
+                              const double* E_elem, double E, int Nx, int Ny,
+                              int Nz, double* out, void* ws, size_t ws_bytes,
+                              vdvc_stream_t stream);
+
+/* g(x + u(x)) at every voxel and the active mask in_bounds & mask0 & g>glt
+   (sample_deformed_field, engine/correlate_gpu.py:201-281).  U: (Ndof) of
+   dtype; g_vox: (gnx*gny*gnz) vox layout of dtype; mask0 may be NULL (all
+   ones).  Voxels shared by elements take the highest element's u. */
+int vdvc_sample_deformed(const void* U, const void* g_vox, int dtype,
+                         int gnx, int gny, int gnz, double gx0, double gy0,
+                         double gz0, const uint8_t* mask0, double glt, int h,
+                         int Nx, int Ny, int Nz, void* g_vals,
+                         uint8_t* mask_out, vdvc_stream_t stream);
+
+/* u(x) at every voxel centre, (Nvox,3) or channels-first (3,Nvox)
+   (interp_field_vox, engine/correlate_gpu.py:160-198). */
+int vdvc_interp_field(const void* U, int dtype, int h, int Nx, int Ny,
+                      int Nz, int channels_first, void* out,
+                      vdvc_stream_t stream);
+
+/* ---- reductions and pre-alignment ------------------------------------- */
+/* *out_host = sum a*b (b != NULL) or sum a, accumulated in float64;
+   synchronises the stream (the xp.dot / .sum() calls of the lambda
+   calibration, engine/correlate_gpu.py:1007-1025).  ws: >= 16 KiB. */
+int vdvc_dot(const void* a, const void* b, int dtype, long long n,
+             double* out_host, void* ws, size_t ws_bytes,
+             vdvc_stream_t stream);
+
+/* Rigid voxel shift d (host, 3 doubles, pix axis order x,y,z) with
+   g(x) ~= f(x - d) by phase correlation of the common corner crop
+   (fft_rigid_shift, engine/correlate_gpu.py:381-414).  f_vox, g_vox: vox
+   layout of dtype.  Synchronises the stream. */
+int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz,
+                         const void* g_vox, int gnx, int gny, int gnz,
+                         int dtype, double* d_out3, vdvc_stream_t stream);
+
+/* ---- preconditioned CG around an external matvec ------------------------
+   The pieces of pcg(matvec, b, M_inv, xp, x0, max_iter, tol)
+   (engine/kernels_dvc.py:550-583) for a caller that applies A itself:
+     begin      r = b - Ax (Ax may be NULL for x0 = 0), z = M r, p = z,
+                rz = r.z, r0 = b.b + 1e-30
+     step       alpha = rz / (p.Ap + 1e-30); x += alpha p; r -= alpha Ap;
+                z = M r; *res_out = sqrt(r.r / r0) (synchronises the stream)
+     direction  p = z + beta p
+   Dot products are float64.  ws is vdvc_pcg_workspace_bytes() bytes and
+   carries the scalar state between the calls of one solve. */
+size_t vdvc_pcg_workspace_bytes(void);
+int vdvc_pcg_begin(const void* b, const void* Ax, const void* Minv, int dtype,
+                   long long n, void* r, void* z, void* p, int max_iter,
+                   double tol, void* ws, size_t ws_bytes, vdvc_stream_t stream);
+int vdvc_pcg_step(const void* Ap, const void* Minv, int dtype, long long n,
+                  void* x, void* r, void* z, void* p, void* ws,
+                  size_t ws_bytes, double* res_out, int* done_out,
+                  vdvc_stream_t stream);
+int vdvc_pcg_direction(const void* z, void* p, int dtype, long long n,
+                       void* ws, size_t ws_bytes, vdvc_stream_t stream);
+
+/* ---- Gauss-Newton solver of one pyramid level ----------------------------
+   Device-resident form of the correlate_gpu iteration
+   (engine/correlate_gpu.py:1065-1138).  One GN iteration is
+     vdvc_gn_sample -> vdvc_gn_rhs -> vdvc_gn_pcg -> vdvc_gn_update.
+   All inputs are device pointers that must outlive the solver; the
+   workspace (vdvc_gn_workspace_bytes) holds every per-iteration buffer. */
+typedef struct vdvc_gn_desc {
+  int dtype;                 /* VDVC_F32 (plain solve) or VDVC_F64          */
+  int h, Nx, Ny, Nz;
+  int gnx, gny, gnz;         /* deformed image shape                          */
+  double gx0, gy0, gz0;      /* g_origin                                      */
+  double glt;                /* gray-level threshold                          */
+  int reg_type;              /* VDVC_REG_*                                     */
+  double ll;                 /* regularization weight lambda                  */
+  double eps_reg;            /* Laplacian share of the equilibrium-gap R      */
+  const double* K_lap;       /* host 24x24 (required when reg_type != NONE)    */
+  const double* K_el;        /* host 24x24 (equilibrium gap)                  */
+  int dynamic_mask;          /* 1: H and M follow the b mask each iteration   */
+  int pcg_chunk;             /* PCG iterations per replayed graph (0: 8)      */
+  const void* f_vox;         /* reference values, vox layout, uncentred       */
+  const void* g_vox;         /* deformed image, vox layout                    */
+  const void* grad;          /* (Nvox,3) eroded gradient of f                 */
+  const uint8_t* mask0;      /* f > glt                                       */
+  const void* interior;      /* (Ndof) P_i diagonal (equilibrium gap)         */
+  const double* diag_eqgap;  /* (Ndof) float64 Hutchinson diag of K P_i K     */
+  double mean0, std0;        /* multiplicity-weighted stats of f over mask0   */
+  vdvc_stream_t stream;      /* stream used for the set-up in vdvc_gn_create   */
+} vdvc_gn_desc;
+
+typedef struct vdvc_gn_solver vdvc_gn_solver;
+
+/* buffers readable with vdvc_gn_read */
+enum { VDVC_GN_U = 0, VDVC_GN_DU = 1, VDVC_GN_RES = 2, VDVC_GN_LIVE_MASK = 3 };
+
+size_t vdvc_gn_workspace_bytes(int dtype, int h, int Nx, int Ny, int Nz);
+int vdvc_gn_create(const vdvc_gn_desc* desc, void* ws, size_t ws_bytes,
+                   vdvc_gn_solver** out);
+/* U <- U0 (device float64, Ndof) or zeros when U0 == NULL. */
+int vdvc_gn_set_U(vdvc_gn_solver* solver, const double* U0,
+                  vdvc_stream_t stream);
+/* dynamic_mask == 0: diag(H over mask0) + lambda diag(R) and M^-1, once. */
+int vdvc_gn_frozen_diag(vdvc_gn_solver* solver, vdvc_stream_t stream);
+/* g(x+u), live mask, stats of g over the b mask; freeze_now fixes the b
+   mask to this iteration's live mask for the rest of the solve. */
+int vdvc_gn_sample(vdvc_gn_solver* solver, int freeze_now,
+                   vdvc_stream_t stream);
+/* residual, b - lambda R U, diag and M^-1 (dynamic_mask). */
+int vdvc_gn_rhs(vdvc_gn_solver* solver, vdvc_stream_t stream);
+/* PCG from dU = 0; returns iterations, final relative residual and the
+   device status (VDVC_OK or VDVC_ERR_NONFINITE). Synchronises the stream. */
+int vdvc_gn_pcg(vdvc_gn_solver* solver, int max_iter, double tol, int* iters,
+                double* res, int* status, vdvc_stream_t stream);
+/* U += dU and the iteration scalars (synchronises the stream):
+   out8 = {|dU|^2, |U|^2, count, sum, sum^2 of res over the live mask,
+           active voxels, b-mask weight, status}. */
+int vdvc_gn_update(vdvc_gn_solver* solver, double* out8, vdvc_stream_t stream);
+/* Copy a solver buffer to dst (float64 when dst_f64, else float32; masks
+   as uint8). */
+int vdvc_gn_read(vdvc_gn_solver* solver, int which, void* dst, int dst_f64,
+                 vdvc_stream_t stream);
+void vdvc_gn_destroy(vdvc_gn_solver* solver);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VDVC_H */

@@ -1,0 +1,518 @@
+"""CPU oracle of the voxelDVC global Gauss-Newton path -- TEST INFRASTRUCTURE.
+
+A NumPy/SciPy restatement of the reference algorithm (project voxelDVC,
+src/voxeldvc/engine/{geometry_dvc,kernels_dvc,correlate_gpu}.py), written
+for checking the CUDA implementation: only tests, the smoke check and the
+benchmark's CPU-baseline leg may import it.  It is never the product path.
+
+Parity pinning: every function here is checked against golden vectors
+produced by running the reference's own NumPy code
+(tests/golden/make_golden.py -> tests/golden/*.npz, see
+tests/test_oracle_golden.py).
+
+Third-party arithmetic the reference relies on and this oracle also uses
+(same published algorithms): scipy.ndimage.map_coordinates (order 1,
+mode 'nearest'), scipy.ndimage.minimum_filter, numpy.gradient, numpy.fft.
+
+Conventions (kernels_dvc.py:9-21): node i + j(Nx+1) + k(Nx+1)(Ny+1),
+dof 3*node + c, element i + j Nx + k Nx Ny, voxel vx + vy Nvx + vz Nvx Nvy.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# ----------------------------------------------------------------------------
+# geometry (geometry_dvc.py)
+# ----------------------------------------------------------------------------
+
+# local corner order 000,100,110,010,001,101,111,011 (geometry_dvc.py:14-17)
+CORNER = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+
+
+def voxel_center_stencil(h):
+    """geometry_dvc.py:26-51: xi = 2k/h - 1 on a (h+1)^3 'ij' grid, trapezoid
+    weights (1/2 on the two end planes per axis)."""
+    xi = 2 * np.arange(h + 1) / h - 1
+    w1 = np.where((np.arange(h + 1) == 0) | (np.arange(h + 1) == h), 0.5, 1.0)
+    g = np.meshgrid(xi, xi, xi, indexing='ij')
+    wg = np.meshgrid(w1, w1, w1, indexing='ij')
+    return g[0].ravel(), g[1].ravel(), g[2].ravel(), (wg[0] * wg[1] * wg[2]).ravel()
+
+
+def hex8_shape(x, y, z):
+    """geometry_dvc.py:155-168: N_a = 1/8 (1 +- x)(1 +- y)(1 +- z)."""
+    sx = 2 * CORNER[:, 0] - 1
+    sy = 2 * CORNER[:, 1] - 1
+    sz = 2 * CORNER[:, 2] - 1
+    return 0.125 * (1 + x[:, None] * sx) * (1 + y[:, None] * sy) * (1 + z[:, None] * sz)
+
+
+def n_stencil(h):
+    """geometry_dvc.py:171-184."""
+    x, y, z, w = voxel_center_stencil(h)
+    return hex8_shape(x, y, z), w
+
+
+def _dN_unit(p):
+    """geometry_dvc.py:113-125: (3, 8) physical gradients on [0,1]^3."""
+    out = np.empty((3, 8))
+    for a in range(8):
+        f = [p[d] if CORNER[a, d] else 1 - p[d] for d in range(3)]
+        s = [1.0 if CORNER[a, d] else -1.0 for d in range(3)]
+        out[0, a] = s[0] * f[1] * f[2]
+        out[1, a] = f[0] * s[1] * f[2]
+        out[2, a] = f[0] * f[1] * s[2]
+    return out
+
+
+_GAUSS = (-1 / np.sqrt(3), 1 / np.sqrt(3))
+
+
+def k_ref_laplacian():
+    """geometry_dvc.py:88-110: 2x2x2 Gauss, detJ = 1/8, per-component blocks."""
+    L8 = np.zeros((8, 8))
+    for a in _GAUSS:
+        for b in _GAUSS:
+            for c in _GAUSS:
+                dN = _dN_unit(0.5 * (np.array([a, b, c]) + 1))
+                L8 += 0.125 * dN.T @ dN
+    K = np.zeros((24, 24))
+    for c in range(3):
+        K[c::3, c::3] = L8
+    return K
+
+
+def k_ref_elastic(nu):
+    """geometry_dvc.py:58-85, 128-148: int B^T D B, E = 1, engineering shear."""
+    c1 = (1 - nu) / ((1 + nu) * (1 - 2 * nu))
+    c2 = nu / ((1 + nu) * (1 - 2 * nu))
+    c3 = 1 / (2 * (1 + nu))
+    Dm = np.array([[c1, c2, c2, 0, 0, 0], [c2, c1, c2, 0, 0, 0], [c2, c2, c1, 0, 0, 0],
+                   [0, 0, 0, c3, 0, 0], [0, 0, 0, 0, c3, 0], [0, 0, 0, 0, 0, c3]])
+    K = np.zeros((24, 24))
+    for a in _GAUSS:
+        for b in _GAUSS:
+            for c in _GAUSS:
+                dN = _dN_unit(0.5 * (np.array([a, b, c]) + 1))
+                B = np.zeros((6, 24))
+                B[0, 0::3] = dN[0]
+                B[1, 1::3] = dN[1]
+                B[2, 2::3] = dN[2]
+                B[3, 0::3], B[3, 1::3] = dN[1], dN[0]
+                B[4, 1::3], B[4, 2::3] = dN[2], dN[1]
+                B[5, 0::3], B[5, 2::3] = dN[2], dN[0]
+                K += 0.125 * B.T @ Dm @ B
+    return K
+
+
+def node_index(Nx, Ny, Nz):
+    """geometry_dvc.py:191-198: (Nx+1, Ny+1, Nz+1) ids, x fastest."""
+    return np.arange((Nx + 1) * (Ny + 1) * (Nz + 1)).reshape(Nz + 1, Ny + 1, Nx + 1).transpose(2, 1, 0)
+
+
+def interior_dof_mask(Nx, Ny, Nz):
+    """geometry_dvc.py:201-217."""
+    ni = node_index(Nx, Ny, Nz)
+    inner = np.zeros(ni.shape, dtype=bool)
+    inner[1:Nx, 1:Ny, 1:Nz] = True
+    m = np.zeros(3 * ni.size, dtype=bool)
+    for c in range(3):
+        m[3 * ni.ravel() + c] = inner.ravel()
+    return m
+
+
+def element_nodes(Nx, Ny, Nz):
+    """geometry_dvc.py:220-239: (Ne, 8) node ids."""
+    ni = node_index(Nx, Ny, Nz)
+    cols = [ni[dx:dx + Nx, dy:dy + Ny, dz:dz + Nz] for dx, dy, dz in CORNER]
+    return np.stack(cols, axis=-1).transpose(2, 1, 0, 3).reshape(-1, 8)
+
+
+# ----------------------------------------------------------------------------
+# implicit connectivity (kernels_dvc.py:32-89)
+# ----------------------------------------------------------------------------
+
+def elem_dofs(e, Nx, Ny):
+    """kernels_dvc.py:32-61."""
+    e = np.asarray(e)
+    i, j, k = e % Nx, (e // Nx) % Ny, e // (Nx * Ny)
+    n0 = i + j * (Nx + 1) + k * (Nx + 1) * (Ny + 1)
+    off = CORNER[:, 0] + CORNER[:, 1] * (Nx + 1) + CORNER[:, 2] * (Nx + 1) * (Ny + 1)
+    nodes = n0[:, None] + off.astype(e.dtype)[None, :]
+    return (3 * nodes[:, :, None] + np.arange(3, dtype=e.dtype)).reshape(-1, 24)
+
+
+def voxel_offsets(h, Nx, Ny):
+    """kernels_dvc.py:64-78."""
+    Nvx, Nvy = Nx * h + 1, Ny * h + 1
+    q = np.arange(h + 1, dtype=np.int32)
+    qx, qy, qz = np.meshgrid(q, q, q, indexing='ij')
+    return (qx + qy * Nvx + qz * Nvx * Nvy).ravel()
+
+
+def elem_voxel_origins(e, h, Nx, Ny):
+    """kernels_dvc.py:81-89."""
+    e = np.asarray(e)
+    Nvx, Nvy = Nx * h + 1, Ny * h + 1
+    return h * (e % Nx + ((e // Nx) % Ny) * Nvx + (e // (Nx * Ny)) * Nvx * Nvy)
+
+
+def _chunks(Ne, size):
+    for s in range(0, Ne, size):
+        yield np.arange(s, min(s + size, Ne), dtype=np.int32)
+
+
+def _scatter(f, idx, vals):
+    # np.add.at semantics, via bincount (same sums, CPU friendly)
+    f += np.bincount(idx.ravel(), weights=vals.ravel(), minlength=f.shape[0]).astype(f.dtype)
+
+
+# ----------------------------------------------------------------------------
+# regularizers (kernels_dvc.py:349-437)
+# ----------------------------------------------------------------------------
+
+def matvec_k_ref(v, K, E, Nx, Ny, Nz, chunk=500_000):
+    """kernels_dvc.py:349-374: f = sum_e E_e P_e^T K P_e v."""
+    Ne = Nx * Ny * Nz
+    f = np.zeros(v.shape[0], dtype=v.dtype)
+    Kx = np.asarray(K, dtype=v.dtype)
+    Ee = np.broadcast_to(np.asarray(E, dtype=v.dtype), (Ne,))
+    for e in _chunks(Ne, chunk):
+        d = elem_dofs(e, Nx, Ny)
+        loc = v[d] @ Kx.T
+        loc *= Ee[e][:, None]
+        _scatter(f, d, loc)
+    return f
+
+
+def diag_k_ref(K, E, Nx, Ny, Nz, Ndof):
+    """kernels_dvc.py:377-392 (float64, from K's diagonal)."""
+    dk = np.diag(np.asarray(K))
+    Ne = Nx * Ny * Nz
+    Ee = np.broadcast_to(np.asarray(E), (Ne,))
+    out = np.zeros(Ndof, dtype=dk.dtype)
+    e = np.arange(Ne, dtype=np.int32)
+    _scatter(out, elem_dofs(e, Nx, Ny), Ee[:, None] * dk[None, :])
+    return out
+
+
+def matvec_eqgap(v, K_el, interior, E, Nx, Ny, Nz):
+    """kernels_dvc.py:402-417: K (P_i (K v))."""
+    w = interior * matvec_k_ref(v, K_el, E, Nx, Ny, Nz)
+    return matvec_k_ref(w, K_el, E, Nx, Ny, Nz)
+
+
+def diag_eqgap(K_el, interior, E, Nx, Ny, Nz, Ndof, n_probes=32, seed=0):
+    """kernels_dvc.py:420-437: Hutchinson with default_rng(seed) Rademacher
+    probes, then clip at 1e-12 max|diag|."""
+    rng = np.random.default_rng(seed)
+    acc = np.zeros(Ndof)
+    for _ in range(n_probes):
+        z = rng.choice([-1.0, 1.0], size=Ndof)
+        acc = acc + z * matvec_eqgap(z, K_el, interior, E, Nx, Ny, Nz)
+    d = acc / n_probes
+    return np.clip(d, 1e-12 * float(np.abs(d).max()), None)
+
+
+# ----------------------------------------------------------------------------
+# correlation Hessian (kernels_dvc.py:444-543)
+# ----------------------------------------------------------------------------
+
+def _hchunk(nq):
+    return max(1, 20_000_000 // (nq * 24))  # kernels_dvc.py:444-449
+
+
+def matvec_h(v, grad, mask, h, Nx, Ny, Nz, chunk=None):
+    """kernels_dvc.py:452-506: H v, separable einsum form."""
+    N, w = n_stencil(h)
+    N = N.astype(v.dtype)
+    w = w.astype(v.dtype)
+    offs = voxel_offsets(h, Nx, Ny)
+    Ne = Nx * Ny * Nz
+    f = np.zeros(v.shape[0], dtype=v.dtype)
+    for e in _chunks(Ne, chunk or _hchunk(offs.size)):
+        d = elem_dofs(e, Nx, Ny)
+        vl = v[d].reshape(-1, 8, 3)
+        vid = elem_voxel_origins(e, h, Nx, Ny)[:, None] + offs[None, :]
+        gq = grad[vid]
+        mq = mask[vid]
+        u = np.einsum('qa,cak->cqk', N, vl)
+        coef = w[None, :] * mq * np.einsum('cqk,cqk->cq', gq, u)
+        loc = np.einsum('qa,cqk->cak', N, coef[:, :, None] * gq).reshape(-1, 24)
+        _scatter(f, d, loc)
+    return f
+
+
+def diag_h(grad, mask, h, Nx, Ny, Nz, Ndof, chunk=None):
+    """kernels_dvc.py:509-543."""
+    N, w = n_stencil(h)
+    N2 = N.astype(grad.dtype) ** 2
+    w = w.astype(grad.dtype)
+    offs = voxel_offsets(h, Nx, Ny)
+    Ne = Nx * Ny * Nz
+    out = np.zeros(Ndof, dtype=grad.dtype)
+    for e in _chunks(Ne, chunk or _hchunk(offs.size)):
+        d = elem_dofs(e, Nx, Ny)
+        vid = elem_voxel_origins(e, h, Nx, Ny)[:, None] + offs[None, :]
+        gq = grad[vid]
+        t = (w[None, :] * mask[vid])[:, :, None] * gq ** 2
+        _scatter(out, d, np.einsum('qa,cqk->cak', N2, t).reshape(-1, 24))
+    return out
+
+
+def compute_b(res, mask, grad, h, Nx, Ny, Nz, Ndof, chunk=None):
+    """correlate_gpu.py:341-378."""
+    N, w = n_stencil(h)
+    N = N.astype(grad.dtype)
+    w = w.astype(grad.dtype)
+    offs = voxel_offsets(h, Nx, Ny)
+    Ne = Nx * Ny * Nz
+    out = np.zeros(Ndof, dtype=grad.dtype)
+    for e in _chunks(Ne, chunk or _hchunk(offs.size)):
+        d = elem_dofs(e, Nx, Ny)
+        vid = elem_voxel_origins(e, h, Nx, Ny)[:, None] + offs[None, :]
+        gq = grad[vid]
+        coef = w[None, :] * mask[vid] * res[vid]
+        _scatter(out, d, np.einsum('qa,cqk->cak', N, coef[:, :, None] * gq).reshape(-1, 24))
+    return out
+
+
+def pcg(matvec, b, M_inv, x0=None, max_iter=1000, tol=1e-8):
+    """kernels_dvc.py:550-583 (numpy promotion rules as in the reference)."""
+    x = np.zeros_like(b) if x0 is None else x0.copy()
+    r = b - matvec(x)
+    z = M_inv * r
+    p = z.copy()
+    rz = np.dot(r, z)
+    r0 = np.dot(b, b) + 1e-30
+    for _ in range(max_iter):
+        Ap = matvec(p)
+        alpha = rz / (np.dot(p, Ap) + 1e-30)
+        x = x + alpha * p
+        r = r - alpha * Ap
+        if float(np.sqrt(np.dot(r, r) / r0)) < tol:
+            break
+        z = M_inv * r
+        rz_new = np.dot(r, z)
+        p = z + rz_new / (rz + 1e-30) * p
+        rz = rz_new
+    return x
+
+
+# ----------------------------------------------------------------------------
+# voxel fields (correlate_gpu.py:49-338)
+# ----------------------------------------------------------------------------
+
+def image_grad_and_values(pix, dtype=np.float32):
+    """correlate_gpu.py:49-72: F-order values and per-axis np.gradient."""
+    p = np.asarray(pix, dtype=dtype)
+    g = np.empty((p.size, 3), dtype=dtype)
+    for c in range(3):
+        g[:, c] = np.gradient(p, axis=c).ravel(order='F')
+    return p.ravel(order='F'), g
+
+
+def erode(mask, Nvx, Nvy, Nvz):
+    """correlate_gpu.py:75-94: 6-neighbour minimum filter, mode 'nearest'."""
+    from scipy.ndimage import minimum_filter
+    fp = np.zeros((3, 3, 3), dtype=bool)
+    fp[1, 1, :] = fp[1, :, 1] = fp[:, 1, 1] = True
+    out = minimum_filter(mask.reshape(Nvx, Nvy, Nvz, order='F'), footprint=fp, mode='nearest')
+    return out.ravel(order='F')
+
+
+def masked_mean_std(field, mask, h, Nx, Ny, Nz):
+    """correlate_gpu.py:113-157: multiplicity-weighted masked mean / std
+    with float64 sums."""
+    offs = voxel_offsets(h, Nx, Ny)
+    Ne = Nx * Ny * Nz
+    cnt = s1 = s2 = 0.0
+    for e in _chunks(Ne, _hchunk(offs.size)):
+        vid = elem_voxel_origins(e, h, Nx, Ny)[:, None] + offs[None, :]
+        m = mask[vid].astype(np.float64)
+        v = field[vid].astype(np.float64) * m
+        cnt += m.sum()
+        s1 += v.sum()
+        s2 += (v * v).sum()
+    if cnt < 1:
+        return 0.0, 0.0
+    mean = s1 / cnt
+    var = s2 / cnt - mean * mean
+    return mean, (var if var > 0.0 else 0.0) ** 0.5
+
+
+def interp_field(U, h, Nx, Ny, Nz):
+    """correlate_gpu.py:160-198: u at every voxel, later elements win."""
+    N, _ = n_stencil(h)
+    N = N.astype(U.dtype)
+    offs = voxel_offsets(h, Nx, Ny)
+    Nvox = (Nx * h + 1) * (Ny * h + 1) * (Nz * h + 1)
+    out = np.zeros((Nvox, 3), dtype=U.dtype)
+    e = np.arange(Nx * Ny * Nz, dtype=np.int32)
+    ul = U[elem_dofs(e, Nx, Ny)].reshape(-1, 8, 3)
+    vid = elem_voxel_origins(e, h, Nx, Ny)[:, None] + offs[None, :]
+    out[vid.reshape(-1)] = np.einsum('qa,kac->kqc', N, ul).reshape(-1, 3)
+    return out
+
+
+def sample_deformed(U, g_pix, h, Nx, Ny, Nz, g_origin=(0, 0, 0), mask0=None, glt=0.0):
+    """correlate_gpu.py:201-281: g at (u + x) - g_origin, clipped, order-1
+    map_coordinates; mask in_bounds & mask0 & g > glt."""
+    from scipy.ndimage import map_coordinates
+    Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, Nz * h + 1
+    Nvox = Nvx * Nvy * Nvz
+    if mask0 is None:
+        mask0 = np.ones(Nvox, dtype=bool)
+    dt = U.dtype
+    u = interp_field(U, h, Nx, Ny, Nz)
+    v = np.arange(Nvox)
+    c = [u[:, 0] + (v % Nvx).astype(dt) - g_origin[0],
+         u[:, 1] + ((v // Nvx) % Nvy).astype(dt) - g_origin[1],
+         u[:, 2] + (v // (Nvx * Nvy)).astype(dt) - g_origin[2]]
+    n = g_pix.shape
+    inb = np.ones(Nvox, dtype=bool)
+    for a in range(3):
+        inb &= (c[a] >= 0) & (c[a] <= n[a] - 1)
+        c[a] = np.clip(c[a], 0, n[a] - 1)
+    gv = map_coordinates(g_pix, np.stack(c), order=1, mode='nearest')  # g_pix dtype
+    return gv.astype(dt), inb & mask0 & (gv > glt)
+
+
+# ----------------------------------------------------------------------------
+# FFT pre-alignment (correlate_gpu.py:381-414)
+# ----------------------------------------------------------------------------
+
+def fft_rigid_shift(f_pix, g_pix):
+    f = np.asarray(f_pix)
+    g = np.asarray(g_pix)
+    shp = tuple(min(a, b) for a, b in zip(f.shape, g.shape))
+    sl = tuple(slice(0, s) for s in shp)
+    X = np.fft.fftn(f[sl]) * np.conj(np.fft.fftn(g[sl]))
+    r = np.fft.ifftn(X / (np.abs(X) + 1e-12)).real
+    peak = np.unravel_index(np.argmax(r), r.shape)
+    d = []
+    for p, s in zip(peak, shp):
+        p = int(p)
+        d.append(-float(p - s if p > s // 2 else p))
+    return np.array(d)
+
+
+# ----------------------------------------------------------------------------
+# Gauss-Newton driver (correlate_gpu.py:828-1140) and pyramid (:1143-1305)
+# ----------------------------------------------------------------------------
+
+def correlate(f_pix, g_pix, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_lap=None, reg_exponent=2,
+              c_reg=1.0, reg_type='laplacian', K_el=None, eps_reg=1e-3, dynamic_mask=False, freeze_mask_after=None,
+              U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000, dtype=np.float32, log=None):
+    """Returns (U, res, dU); `log` (a list) receives one dict per GN iteration."""
+    Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, Nz * h + 1
+    Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    Nvox = Nvx * Nvy * Nvz
+    g_pix = np.asarray(g_pix, dtype=dtype)
+    f_vox, grad = image_grad_and_values(f_pix, dtype)
+    mask0 = f_vox > glt
+    grad[~erode(mask0, Nvx, Nvy, Nvz)] = 0
+    mean0, std0 = masked_mean_std(f_vox, mask0, h, Nx, Ny, Nz)
+    f_vox -= mean0
+    interior = interior_dof_mask(Nx, Ny, Nz).astype(dtype) if reg_type == 'equilibrium_gap' else None
+
+    def reg(v):
+        if reg_type == 'laplacian':
+            return matvec_k_ref(v, K_lap, h, Nx, Ny, Nz)
+        return matvec_eqgap(v, K_el, interior, h, Nx, Ny, Nz) + eps_reg * matvec_k_ref(v, K_lap, h, Nx, Ny, Nz)
+
+    def reg_diag():
+        if reg_type == 'laplacian':
+            return diag_k_ref(K_lap, h, Nx, Ny, Nz, Ndof)
+        return diag_eqgap(K_el, interior, h, Nx, Ny, Nz, Ndof) + eps_reg * diag_k_ref(K_lap, h, Nx, Ny, Nz, Ndof)
+
+    ll = 0.0
+    if l0 is not None:
+        T = 10 * h
+        if reg_type == 'equilibrium_gap':
+            H0 = float(diag_h(grad, mask0, h, Nx, Ny, Nz, Ndof).sum())
+            L0 = float(reg_diag().sum())
+        else:
+            jj = (np.arange((Nx + 1) * (Ny + 1) * (Nz + 1)) // (Nx + 1)) % (Ny + 1)
+            V = np.zeros(Ndof, dtype=dtype)
+            V[0::3] = np.cos(jj.astype(dtype) * h / T * 2 * np.pi)
+            H0 = float(np.dot(V, matvec_h(V, grad, mask0, h, Nx, Ny, Nz)))
+            L0 = float(np.dot(V, reg(V)))
+        ll = c_reg * (l0 / T) ** reg_exponent * H0 / L0
+
+    U = np.zeros(Ndof, dtype=dtype) if U0 is None else np.asarray(U0, dtype=dtype).copy()
+    res = np.zeros(Nvox, dtype=dtype)
+    dU = np.zeros(Ndof, dtype=dtype)
+    if not dynamic_mask:
+        dg = diag_h(grad, mask0, h, Nx, Ny, Nz, Ndof)
+        if l0 is not None:
+            dg = dg + ll * reg_diag()
+        M_inv = 1.0 / (dg + 1e-5 * float(dg.min()))
+        H_mask = mask0
+    frozen = None
+    for ik in range(maxiter):
+        gv, live = sample_deformed(U, g_pix, h, Nx, Ny, Nz, g_origin, mask0, glt)
+        if freeze_mask_after is not None and frozen is None and ik >= freeze_mask_after:
+            frozen = live.copy()
+        bm = frozen if frozen is not None else live
+        gmean, std1 = masked_mean_std(gv, bm, h, Nx, Ny, Nz)
+        gv = gv - gmean
+        gv = gv * -(std0 / std1)
+        res = gv + f_vox
+        res[~bm] = 0.0
+        b = compute_b(res, bm, grad, h, Nx, Ny, Nz, Ndof)
+        if l0 is not None:
+            b = b - ll * reg(U)
+        if dynamic_mask:
+            dg = diag_h(grad, bm, h, Nx, Ny, Nz, Ndof)
+            if l0 is not None:
+                dg = dg + ll * reg_diag()
+            M_inv = 1.0 / (dg + 1e-5 * float(dg.min()))
+            H_mask = bm
+
+        def A(v, _m=H_mask):
+            out = matvec_h(v, grad, _m, h, Nx, Ny, Nz)
+            return out + ll * reg(v) if l0 is not None else out
+
+        dU = pcg(A, b, M_inv, max_iter=pcg_max_iter, tol=pcg_tol)
+        U = U + dU
+        err = float(np.linalg.norm(dU) / np.linalg.norm(U))
+        if log is not None:
+            _, stdr = masked_mean_std(res, live, h, Nx, Ny, Nz)
+            log.append({"err": err, "stdr": stdr, "n_active": int(live.sum()), "ll": ll})
+        if err < eps:
+            break
+    return U, res, dU
+
+
+def multiscale(f_pix, g_pix, Nx, Ny, Nz, h, scales=(2, 1, 0), g_origin=(0, 0, 0), l0=None, fft_prealign=True,
+               ext_affine=None, **kw):
+    """correlate_gpu.py:1143-1305 (without the Powell affine pre-alignment)."""
+    dtype = kw.get('dtype', np.float32)
+    U = None
+    prev = None
+    res = dU = None
+    for i in sorted(set(scales), reverse=True):
+        s = 2 ** i
+        if h % s != 0:
+            raise ValueError("h=%d not divisible by 2**%d=%d" % (h, i, s))
+        if any(o % s for o in g_origin):
+            raise ValueError("g_origin=%r not divisible by 2**%d=%d" % (g_origin, i, s))
+        hi = h // s
+        fi = np.asarray(f_pix)[::s, ::s, ::s]
+        gi = np.asarray(g_pix)[::s, ::s, ::s]
+        if U is not None:
+            U = U * (prev / s)
+        elif ext_affine is not None:
+            A, t, c = (np.asarray(q, dtype=np.float64) for q in ext_affine)
+            nn = np.arange((Nx + 1) * (Ny + 1) * (Nz + 1))
+            X = np.stack([nn % (Nx + 1), (nn // (Nx + 1)) % (Ny + 1), nn // ((Nx + 1) * (Ny + 1))], 1) * float(hi)
+            u = (X - c / s) @ A.T + c / s + t / s - X
+            U = u.reshape(-1).astype(dtype)
+        elif fft_prealign:
+            d = fft_rigid_shift(fi, gi)
+            U = np.tile(d, (Nx + 1) * (Ny + 1) * (Nz + 1)).astype(dtype)
+        U, res, dU = correlate(fi, gi, Nx, Ny, Nz, hi, g_origin=tuple(o // s for o in g_origin),
+                               l0=None if l0 is None else l0 / s, U0=U, **kw)
+        prev = s
+    return U, res, dU

@@ -1,0 +1,205 @@
+"""Generate the golden vectors of tests/golden/*.npz by running the
+reference's own engine code (voxelDVC, src/voxeldvc/engine/*) on NumPy.
+
+Run in a checkout where the reference source is available:
+
+    PYTHONPATH=/root/reference/src python tests/golden/make_golden.py
+
+Each .npz stores the seeded inputs together with the reference outputs, so
+the tests (and the GPU machine, which has no copy of the reference) replay the
+exact same cases.  The reference cannot be imported at test time.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+REF_SRC = os.environ.get("VOXELDVC_REF_SRC", "/root/reference/src")
+if REF_SRC not in sys.path:
+    sys.path.insert(0, REF_SRC)
+
+from voxeldvc.engine import geometry_dvc as G  # noqa: E402
+from voxeldvc.engine import kernels_dvc as KD  # noqa: E402
+from voxeldvc.engine import correlate_gpu as CG  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def _texture(shape, rng, sigma=1.5, zero_frac=0.0):
+    from scipy.ndimage import gaussian_filter
+    t = gaussian_filter(rng.standard_normal(shape), sigma)
+    t = (t - t.min()) / (t.max() - t.min()) + 0.05
+    if zero_frac > 0:
+        t[rng.random(shape) < zero_frac] = 0.0
+    return t
+
+
+def geometry():
+    d = {}
+    for h in (1, 2, 3, 4, 5, 8):
+        N, w = G.build_N_stencil(h)
+        d[f"N_h{h}"], d[f"w_h{h}"] = N, w
+        for i, a in enumerate(G.VoxelCenterStencil(h)):
+            d[f"vcs{i}_h{h}"] = a
+    d["K_lap"] = G.build_K_ref_laplacian()
+    for nu in (0.0, 0.3, 0.45):
+        d[f"K_el_{nu}"] = G.build_K_ref(nu)
+    d["shape_grads"] = G._shape_grads(0.2, 0.7, 0.4)
+    d["B_matrix"] = G._B_matrix(-0.3, 0.5, 0.9)[0]
+    for (Nx, Ny, Nz) in ((3, 2, 2), (1, 1, 1), (2, 4, 3)):
+        tag = f"{Nx}_{Ny}_{Nz}"
+        ni = G.build_node_index(Nx, Ny, Nz)
+        d[f"node_index_{tag}"] = ni
+        d[f"interior_{tag}"] = G.build_interior_dof_mask(Nx, Ny, Nz)
+        d[f"elem_nodes_{tag}"] = G.element_node_ids(ni, Nx, Ny, Nz)
+        e = np.arange(Nx * Ny * Nz, dtype=np.int32)
+        d[f"elem_dofs_{tag}"] = KD.get_elem_dofs(e, Nx, Ny, np)
+        for h in (1, 3, 4):
+            d[f"vox_offsets_{tag}_h{h}"] = KD.get_voxel_offsets(h, Nx, Ny, np)
+            d[f"vox_origins_{tag}_h{h}"] = KD.get_elem_voxel_origins(e, h, Nx, Ny, np)
+    np.savez_compressed(os.path.join(OUT, "geometry.npz"), **d)
+
+
+def operators(name, Nx, Ny, Nz, h, seed):
+    rng = np.random.default_rng(seed)
+    Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, Nz * h + 1
+    Nvox = Nvx * Nvy * Nvz
+    Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    N, w = G.build_N_stencil(h)
+    K_lap = G.build_K_ref_laplacian()
+    K_el = G.build_K_ref(0.3)
+    inp = {
+        "dims": np.array([Nx, Ny, Nz, h]),
+        "grad": rng.standard_normal((Nvox, 3)).astype(np.float32),
+        "mask": rng.random(Nvox) < 0.85,
+        "v": rng.standard_normal(Ndof).astype(np.float32),
+        "res": rng.standard_normal(Nvox).astype(np.float32),
+        "U": (1.5 * rng.standard_normal(Ndof)).astype(np.float32),
+        "f_pix": _texture((Nvx, Nvy, Nvz), rng, zero_frac=0.05).astype(np.float32),
+        "g_pix": _texture((Nvx + 3, max(2, Nvy - 1), Nvz + 2), rng, zero_frac=0.05).astype(np.float32),
+        "g_origin": np.array([1, 0, 2]),
+        "interior": G.build_interior_dof_mask(Nx, Ny, Nz).astype(np.float32),
+    }
+    inp["b_pcg"] = rng.standard_normal(Ndof).astype(np.float32)
+    out = {}
+    out["matvec_H"] = KD.matvec_H(inp["v"], inp["grad"], inp["mask"], N, w, h, Nx, Ny, Nz, np)
+    out["matvec_H_f64"] = KD.matvec_H(inp["v"].astype(np.float64), inp["grad"].astype(np.float64), inp["mask"], N,
+                                      w, h, Nx, Ny, Nz, np)
+    out["diag_H"] = KD.build_diagonal_H(inp["grad"], inp["mask"], N, w, h, Nx, Ny, Nz, Ndof, np)
+    out["compute_b"] = CG.compute_b_gpu(inp["res"], inp["mask"], inp["grad"], N, w, h, Nx, Ny, Nz, Ndof, np)
+    out["matvec_K_lap"] = KD.matvec_K_ref(inp["v"], K_lap, h, Nx, Ny, Nz, np)
+    out["diag_K_lap"] = KD.build_diagonal_K_ref(K_lap, h, Nx, Ny, Nz, Ndof, np)
+    out["matvec_eqgap"] = KD.matvec_equilibrium_gap(inp["v"].astype(np.float64), K_el, inp["interior"], h, Nx, Ny,
+                                                    Nz, np)
+    out["diag_eqgap"] = KD.build_diagonal_equilibrium_gap(K_el, inp["interior"], h, Nx, Ny, Nz, Ndof, np)
+    out["stats"] = np.array(CG.masked_quadpoint_mean_std(inp["res"], inp["mask"], h, Nx, Ny, Nz, np))
+    out["interp"] = CG.interp_field_vox(inp["U"], N, h, Nx, Ny, Nz, np)
+    gv, gm = CG.sample_deformed_field(inp["U"], inp["g_pix"], N, h, Nx, Ny, Nz, np,
+                                      g_origin=tuple(int(o) for o in inp["g_origin"]), mask0_vox=inp["mask"])
+    out["sample_g"], out["sample_mask"] = gv, gm
+    f_vox, grad_f = CG.image_grad_and_values(inp["f_pix"], np, dtype=np.float32)
+    out["f_vox"], out["grad_f"] = f_vox, grad_f
+    mask0 = f_vox > 0.0
+    out["eroded"] = CG.erode_mask0_vox(mask0, Nvx, Nvy, Nvz, np)
+    # PCG on (H + ll R) with the Jacobi preconditioner of the solve
+    ll = 0.37
+    dg = KD.build_diagonal_H(inp["grad"], inp["mask"], N, w, h, Nx, Ny, Nz, Ndof, np) + \
+        ll * KD.build_diagonal_K_ref(K_lap, h, Nx, Ny, Nz, Ndof, np)
+    Minv = 1.0 / (dg + 1e-5 * float(dg.min()))
+
+    def A(x):
+        return KD.matvec_H(x, inp["grad"], inp["mask"], N, w, h, Nx, Ny, Nz, np) + \
+            ll * KD.matvec_K_ref(x, K_lap, h, Nx, Ny, Nz, np)
+
+    out["pcg_x"] = KD.pcg(A, inp["b_pcg"], Minv, np, max_iter=300, tol=1e-7)
+    out["pcg_ll"] = np.array(ll)
+    np.savez_compressed(os.path.join(OUT, f"ops_{name}.npz"), **inp, **{"out_" + k: v for k, v in out.items()})
+
+
+def _sinusoid_problem():
+    # a smooth texture with a rigid 1-voxel shift, 2x2x2 elements of h=8
+    from scipy.ndimage import shift
+    n = 17
+    x = np.arange(n)
+    X, Y, Z = np.meshgrid(x, x, x, indexing='ij')
+    f = (np.sin(2 * np.pi * X / n) + np.sin(2 * np.pi * Y / n) + np.sin(2 * np.pi * Z / n)
+         + 0.5 * np.cos(2 * np.pi * (X + Y) / n))
+    g = shift(f, (1.0, 0, 0), order=3, mode='nearest')
+    return f, g
+
+
+def _warped_problem(Nx, Ny, Nz, h, seed, shift=(0.8, -0.6, 0.4), pad=0):
+    from scipy.ndimage import map_coordinates
+    rng = np.random.default_rng(seed)
+    shp = (Nx * h + 1, Ny * h + 1, Nz * h + 1)
+    big = tuple(s + 8 for s in shp)
+    t = _texture(big, rng, sigma=1.2)
+    f = t[4:4 + shp[0], 4:4 + shp[1], 4:4 + shp[2]].copy()
+    X = np.indices(shp).astype(np.float64)
+    u = [shift[0] + 0.01 * (X[0] - shp[0] / 2), shift[1] - 0.004 * (X[1] - shp[1] / 2),
+         shift[2] + 0.006 * (X[2] - shp[2] / 2)]
+    coords = np.stack([X[a] - u[a] + 4 for a in range(3)])
+    g = map_coordinates(t, coords.reshape(3, -1), order=1, mode='nearest').reshape(shp)
+    if pad:
+        f[:pad] = 0.0
+        g[-pad:] = 0.0
+    return f.astype(np.float32), g.astype(np.float32)
+
+
+def solves():
+    K_lap = G.build_K_ref_laplacian()
+    K_el = G.build_K_ref(0.3)
+    f, g = _sinusoid_problem()
+    kw = dict(K_ref_laplacian=K_lap, l0=4.5 * 8, maxiter=20, eps=1e-3, disp=False)
+    U, res, dU = CG.correlate_gpu(f, g, 2, 2, 2, 8, xp=np, **kw)
+    Um, resm, dUm = CG.multiscale_correlate_gpu(f, g, 2, 2, 2, 8, xp=np, scales=(2, 1, 0),
+                                                K_ref_laplacian=K_lap, l0=4.5 * 8, maxiter=30, eps=1e-3,
+                                                disp=False)
+    np.savez_compressed(os.path.join(OUT, "solve_sinusoid.npz"), f=f, g=g, U=U, res=res, dU=dU, U_ms=Um,
+                        res_ms=resm, dU_ms=dUm)
+
+    f2, g2 = _warped_problem(4, 4, 4, 4, seed=5, pad=2)
+    kw2 = dict(K_ref_laplacian=K_lap, l0=2 * 4, maxiter=12, eps=1e-4, disp=False, dynamic_mask=True,
+               freeze_mask_after=2, glt=0.0)
+    U2, res2, dU2 = CG.correlate_gpu(f2, g2, 4, 4, 4, 4, xp=np, **kw2)
+    np.savez_compressed(os.path.join(OUT, "solve_dynamic.npz"), f=f2, g=g2, U=U2, res=res2, dU=dU2)
+
+    f3, g3 = _warped_problem(3, 3, 3, 4, seed=6)
+    kw3 = dict(K_ref_laplacian=K_lap, K_ref_elastic=K_el, reg_type='equilibrium_gap', reg_exponent=4,
+               l0=4.5 * 4, maxiter=10, eps=1e-4, disp=False, dynamic_mask=True, freeze_mask_after=4)
+    U3, res3, dU3 = CG.correlate_gpu(f3, g3, 3, 3, 3, 4, xp=np, **kw3)
+    np.savez_compressed(os.path.join(OUT, "solve_eqgap.npz"), f=f3, g=g3, U=U3, res=res3, dU=dU3)
+
+    f4, g4 = _warped_problem(4, 3, 2, 8, seed=7, shift=(2.6, -1.2, 0.9))
+    U4, res4, dU4 = CG.multiscale_correlate_gpu(f4, g4, 4, 3, 2, 8, xp=np, scales=(2, 1, 0), K_ref_laplacian=K_lap,
+                                                l0=4.5 * 8, maxiter=20, eps=1e-3, disp=False, dynamic_mask=True,
+                                                freeze_mask_after=4, fft_prealign=True)
+    np.savez_compressed(os.path.join(OUT, "solve_multiscale.npz"), f=f4, g=g4, U=U4, res=res4, dU=dU4)
+
+
+def fft_cases():
+    rng = np.random.default_rng(42)
+    f = rng.uniform(0, 1, size=(32, 32, 32))
+    g = np.roll(f, (3, -2, 1), axis=(0, 1, 2))
+    d1 = CG.fft_rigid_shift(f, g, np)
+    f2 = rng.uniform(0, 1, size=(20, 24, 18))
+    g2 = np.roll(rng.uniform(0, 1, size=(22, 20, 18)), (-4, 5, 2), axis=(0, 1, 2))
+    g2[:20, :20, :18] = np.roll(f2[:20, :20, :18], (-4, 5, 2), axis=(0, 1, 2))
+    d2 = CG.fft_rigid_shift(f2, g2, np)
+    np.savez_compressed(os.path.join(OUT, "fft.npz"), f1=f, g1=g, d1=d1, f2=f2, g2=g2, d2=d2)
+
+
+if __name__ == "__main__":
+    geometry()
+    operators("A", 3, 2, 2, 4, seed=1)
+    operators("B", 2, 3, 1, 3, seed=2)
+    operators("C", 1, 1, 1, 2, seed=3)
+    operators("D", 4, 3, 2, 8, seed=4)
+    operators("E", 5, 1, 2, 1, seed=8)
+    solves()
+    fft_cases()
+    for fn in sorted(os.listdir(OUT)):
+        if fn.endswith(".npz"):
+            print(fn, os.path.getsize(os.path.join(OUT, fn)))

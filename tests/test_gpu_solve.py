@@ -1,0 +1,129 @@
+"""End-to-end GN solves on the GPU against the reference's golden solves
+(displacement tolerance: 1e-3 voxel RMS at FP32, per the parity bar) and
+the reference's own multiscale tests, replayed on the drop-in API."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+RMS_TOL = 1e-3  # voxel RMS of nodal displacements, FP32 solve vs reference
+
+
+def rms(a, b):
+    return float(np.sqrt(np.mean((np.asarray(a, np.float64) - np.asarray(b, np.float64)) ** 2)))
+
+
+@pytest.fixture(scope="module")
+def api(cuda):
+    from voxeldvc_gb300.engine import correlate_gpu as CG, geometry_dvc as G
+    return CG, G
+
+
+def test_correlate_sinusoid(api):
+    CG, G = api
+    c = load_golden("solve_sinusoid.npz")
+    kw = dict(K_ref_laplacian=G.build_K_ref_laplacian(), l0=4.5 * 8, maxiter=20, eps=1e-3, disp=False)
+    U, res, dU = CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, **kw)
+    assert rms(U, c["U"]) < RMS_TOL
+    assert np.abs(res - c["res"]).max() < 1e-2
+    assert U.shape == c["U"].shape and res.shape == c["res"].shape and dU.shape == c["dU"].shape
+
+
+def test_multiscale_single_scale_matches_direct(api):
+    # reference tests/test_dvc_gpu_multiscale.py:43-57 on this API
+    CG, G = api
+    c = load_golden("solve_sinusoid.npz")
+    kw = dict(K_ref_laplacian=G.build_K_ref_laplacian(), l0=4.5 * 8, maxiter=20, eps=1e-3, disp=False)
+    Ud, rd, _ = CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, **kw)
+    Um, rm, _ = CG.multiscale_correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, scales=(0,), fft_prealign=False, **kw)
+    assert np.allclose(Ud, Um, atol=1e-12)
+    assert np.allclose(rd, rm, atol=1e-12)
+
+
+def test_multiscale_pyramid(api):
+    # reference tests/test_dvc_gpu_multiscale.py:60-72, plus the golden pyramid
+    CG, G = api
+    c = load_golden("solve_sinusoid.npz")
+    kw = dict(K_ref_laplacian=G.build_K_ref_laplacian(), l0=4.5 * 8, maxiter=30, eps=1e-3, disp=False)
+    Ud, _, _ = CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, **kw)
+    Um, _, _ = CG.multiscale_correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, scales=(2, 1, 0), **kw)
+    assert np.all(np.isfinite(Um))
+    assert np.allclose(Ud, Um, atol=1e-2)
+    assert rms(Um, c["U_ms"]) < RMS_TOL
+
+
+def test_dynamic_mask_freeze(api):
+    CG, G = api
+    c = load_golden("solve_dynamic.npz")
+    U, res, _ = CG.correlate_gpu(c["f"], c["g"], 4, 4, 4, 4, xp=np, K_ref_laplacian=G.build_K_ref_laplacian(),
+                                 l0=8.0, maxiter=12, eps=1e-4, disp=False, dynamic_mask=True, freeze_mask_after=2,
+                                 glt=0.0)
+    assert rms(U, c["U"]) < RMS_TOL
+
+
+def test_equilibrium_gap(api):
+    CG, G = api
+    c = load_golden("solve_eqgap.npz")
+    U, res, _ = CG.correlate_gpu(c["f"], c["g"], 3, 3, 3, 4, xp=np, K_ref_laplacian=G.build_K_ref_laplacian(),
+                                 K_ref_elastic=G.build_K_ref(0.3), reg_type='equilibrium_gap', reg_exponent=4,
+                                 l0=18.0, maxiter=10, eps=1e-4, disp=False, dynamic_mask=True, freeze_mask_after=4)
+    assert rms(U, c["U"]) < RMS_TOL
+
+
+def test_multiscale_fft_dynamic(api):
+    CG, G = api
+    c = load_golden("solve_multiscale.npz")
+    U, res, _ = CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, scales=(2, 1, 0),
+                                            K_ref_laplacian=G.build_K_ref_laplacian(), l0=36.0, maxiter=20,
+                                            eps=1e-3, disp=False, dynamic_mask=True, freeze_mask_after=4,
+                                            fft_prealign=True)
+    assert rms(U, c["U"]) < RMS_TOL
+
+
+def test_float64_solve_tighter(api):
+    CG, G = api
+    c = load_golden("solve_sinusoid.npz")
+    kw = dict(K_ref_laplacian=G.build_K_ref_laplacian(), l0=4.5 * 8, maxiter=20, eps=1e-3, disp=False,
+              dtype=np.float64)
+    U, _, _ = CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, **kw)
+    assert rms(U, c["U"]) < 1e-4
+
+
+def test_device_arrays_in_and_out(api, cuda):
+    torch = cuda
+    CG, G = api
+    c = load_golden("solve_sinusoid.npz")
+    kw = dict(K_ref_laplacian=G.build_K_ref_laplacian(), l0=4.5 * 8, maxiter=20, eps=1e-3, disp=False)
+    U, res, dU = CG.correlate_gpu(torch.from_numpy(c["f"]).cuda(), torch.from_numpy(c["g"]).cuda(), 2, 2, 2, 8,
+                                  xp=torch, **kw)
+    assert U.is_cuda and res.is_cuda
+    assert rms(U.cpu().numpy(), c["U"]) < RMS_TOL
+
+
+def test_error_paths(api):
+    CG, G = api
+    c = load_golden("solve_sinusoid.npz")
+    K_lap = G.build_K_ref_laplacian()
+    with pytest.raises(ValueError):
+        CG.multiscale_correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, scales=(4, 0), K_ref_laplacian=K_lap,
+                                    l0=36.0, disp=False)
+    with pytest.raises(ValueError):
+        CG.multiscale_correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, scales=(1, 0), g_origin=(1, 0, 0),
+                                    K_ref_laplacian=K_lap, l0=36.0, disp=False)
+    with pytest.raises(ValueError):
+        CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, reg_type='tv', disp=False)
+    with pytest.raises(ValueError):
+        CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, l0=36.0, disp=False)
+    with pytest.raises(ValueError):
+        CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, reg_type='equilibrium_gap', l0=36.0,
+                         K_ref_laplacian=K_lap, disp=False)
+
+
+def test_zero_std_raises(api):
+    CG, G = api
+    f = np.random.default_rng(0).random((9, 9, 9)).astype(np.float32) + 0.1
+    g = np.zeros((9, 9, 9), dtype=np.float32)  # no voxel survives g > glt
+    with pytest.raises(ZeroDivisionError):
+        CG.correlate_gpu(f, g, 2, 2, 2, 4, xp=np, maxiter=2, disp=False)

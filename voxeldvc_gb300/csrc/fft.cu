@@ -1,0 +1,228 @@
+// Rigid voxel shift by FFT phase correlation (fft_rigid_shift,
+// engine/correlate_gpu.py:381-414), plus a float64 dot/sum reduction.
+//
+// The volumes are vox layout (x fastest), i.e. C-order arrays of shape
+// (nz, ny, nx); the transforms are cuFFT D2Z/Z2D of that shape (library
+// calls), the cross-power normalisation and the arg-max are kernels here.
+// numpy's argmax returns the first maximum in C order of pix[x,y,z]
+// (x slowest); the arg-max kernel breaks ties the same way.
+#include <cufft.h>
+
+#include "ops.cuh"
+
+namespace vdvc {
+
+template <typename T>
+__global__ void k_crop_to_f64(const T* __restrict__ in, int nx, int ny, int sx, int sy, int sz,
+                              double* __restrict__ out) {
+  const long long n = (long long)sx * sy * sz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(t % sx);
+    const long long r = t / sx;
+    const int y = (int)(r % sy), z = (int)(r / sy);
+    out[t] = (double)in[(long long)x + (long long)y * nx + (long long)z * nx * ny];
+  }
+}
+
+// R = F conj(G) / (|F conj(G)| + 1e-12), written over F.
+__global__ void k_cross_power(cufftDoubleComplex* __restrict__ F, const cufftDoubleComplex* __restrict__ G,
+                              long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const cufftDoubleComplex a = F[i], b = G[i];
+    const double re = a.x * b.x + a.y * b.y;  // a * conj(b)
+    const double im = a.y * b.x - a.x * b.y;
+    const double den = hypot(re, im) + 1e-12;
+    F[i].x = re / den;
+    F[i].y = im / den;
+  }
+}
+
+struct ArgMax {
+  double v;
+  long long cidx;  // C-order index of pix[x,y,z]
+};
+
+__device__ __forceinline__ ArgMax better(ArgMax a, ArgMax b) {
+  if (b.v > a.v || (b.v == a.v && b.cidx < a.cidx)) return b;
+  return a;
+}
+
+__global__ void __launch_bounds__(256) k_argmax(const double* __restrict__ r, int sx, int sy, int sz,
+                                                ArgMax* __restrict__ partial, unsigned int* ticket,
+                                                ArgMax* __restrict__ result) {
+  __shared__ ArgMax s[256];
+  __shared__ bool s_last;
+  const long long n = (long long)sx * sy * sz;
+  ArgMax best{-1.0e300, (long long)1 << 62};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(t % sx);
+    const long long q = t / sx;
+    const int y = (int)(q % sy), z = (int)(q / sy);
+    const ArgMax c{r[t], ((long long)x * sy + y) * sz + z};
+    best = better(best, c);
+  }
+  s[threadIdx.x] = best;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] = better(s[threadIdx.x], s[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = s[0];
+    __threadfence();
+    s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    ArgMax b, b2;
+    b.v = ((volatile double*)&partial[0].v)[0];
+    b.cidx = ((volatile long long*)&partial[0].cidx)[0];
+    for (unsigned int i = 1; i < gridDim.x; ++i) {
+      b2.v = ((volatile double*)&partial[i].v)[0];
+      b2.cidx = ((volatile long long*)&partial[i].cidx)[0];
+      b = better(b, b2);
+    }
+    *result = b;
+    *ticket = 0u;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dot(const T* __restrict__ a, const T* __restrict__ b, long long n,
+                                             GridReduce red, double* __restrict__ out) {
+  __shared__ double s_red[8];
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += b ? (double)a[i] * (double)b[i] : (double)a[i];
+  double mine[1] = {block_sum(acc, s_red)}, o[1];
+  if (grid_reduce_sum<1>(red, mine, o, s_red) && threadIdx.x == 0) *out = o[0];
+}
+
+}  // namespace vdvc
+
+using namespace vdvc;
+
+#define VDVC_CUFFT(expr)                                                                 \
+  do {                                                                                   \
+    cufftResult r_ = (expr);                                                             \
+    if (r_ != CUFFT_SUCCESS) {                                                           \
+      st = set_error(VDVC_ERR_CUFFT, "%s failed with cufftResult %d", #expr, (int)r_);  \
+      goto cleanup;                                                                      \
+    }                                                                                    \
+  } while (0)
+
+extern "C" {
+
+int vdvc_dot(const void* a, const void* b, int dtype, long long n, double* out_host, void* ws, size_t ws_bytes,
+             vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(a && out_host && n >= 1, "bad arguments");
+  Carve cv(ws, ws_bytes);
+  double* partials = cv.take<double>(kReduceBlocks);
+  unsigned int* ticket = cv.take<unsigned int>(1);
+  double* res = cv.take<double>(1);
+  if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "dot needs %zu bytes", cv.off);
+  cudaStream_t s = (cudaStream_t)stream;
+  VDVC_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
+  GridReduce red{partials, ticket};
+  const int nb = grid_blocks(n, 256, kReduceBlocks);
+  if (dtype == VDVC_F32)
+    k_dot<float><<<nb, 256, 0, s>>>((const float*)a, (const float*)b, n, red, res);
+  else if (dtype == VDVC_F64)
+    k_dot<double><<<nb, 256, 0, s>>>((const double*)a, (const double*)b, n, red, res);
+  else
+    return set_error(VDVC_ERR_ARG, "dtype %d", dtype);
+  VDVC_LAUNCHED();
+  VDVC_CUDA(cudaMemcpyAsync(out_host, res, sizeof(double), cudaMemcpyDeviceToHost, s));
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  return VDVC_OK;
+}
+
+int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz, const void* g_vox, int gnx, int gny, int gnz,
+                         int dtype, double* d_out3, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(f_vox && g_vox && d_out3, "null pointer");
+  VDVC_CHECK_ARG(fnx >= 1 && fny >= 1 && fnz >= 1 && gnx >= 1 && gny >= 1 && gnz >= 1, "bad shapes");
+  const int sx = fnx < gnx ? fnx : gnx, sy = fny < gny ? fny : gny, sz = fnz < gnz ? fnz : gnz;
+  const long long n = (long long)sx * sy * sz;
+  const long long nc = (long long)sz * sy * (sx / 2 + 1);
+  cudaStream_t s = (cudaStream_t)stream;
+  int st = VDVC_OK;
+  double *fr = nullptr, *gr = nullptr;
+  cufftDoubleComplex *Fc = nullptr, *Gc = nullptr;
+  ArgMax *partial = nullptr, *result = nullptr;
+  unsigned int* ticket = nullptr;
+  cufftHandle pf = 0, pi = 0;
+  bool have_pf = false, have_pi = false;
+  ArgMax host;
+  const int nb = grid_blocks(n, 256, kReduceBlocks);
+  if (cudaMallocAsync((void**)&fr, n * sizeof(double), s) != cudaSuccess ||
+      cudaMallocAsync((void**)&gr, n * sizeof(double), s) != cudaSuccess ||
+      cudaMallocAsync((void**)&Fc, nc * sizeof(cufftDoubleComplex), s) != cudaSuccess ||
+      cudaMallocAsync((void**)&Gc, nc * sizeof(cufftDoubleComplex), s) != cudaSuccess ||
+      cudaMallocAsync((void**)&partial, kReduceBlocks * sizeof(ArgMax), s) != cudaSuccess ||
+      cudaMallocAsync((void**)&result, sizeof(ArgMax), s) != cudaSuccess ||
+      cudaMallocAsync((void**)&ticket, sizeof(unsigned int), s) != cudaSuccess) {
+    st = set_error(VDVC_ERR_CUDA, "fft_rigid_shift: device allocation failed");
+    goto cleanup;
+  }
+  if (cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s) != cudaSuccess) {
+    st = set_error(VDVC_ERR_CUDA, "memset");
+    goto cleanup;
+  }
+  if (dtype == VDVC_F32) {
+    k_crop_to_f64<float><<<nb, 256, 0, s>>>((const float*)f_vox, fnx, fny, sx, sy, sz, fr);
+    k_crop_to_f64<float><<<nb, 256, 0, s>>>((const float*)g_vox, gnx, gny, sx, sy, sz, gr);
+  } else if (dtype == VDVC_F64) {
+    k_crop_to_f64<double><<<nb, 256, 0, s>>>((const double*)f_vox, fnx, fny, sx, sy, sz, fr);
+    k_crop_to_f64<double><<<nb, 256, 0, s>>>((const double*)g_vox, gnx, gny, sx, sy, sz, gr);
+  } else {
+    st = set_error(VDVC_ERR_ARG, "dtype %d", dtype);
+    goto cleanup;
+  }
+  count_launch(2);
+  VDVC_CUFFT(cufftPlan3d(&pf, sz, sy, sx, CUFFT_D2Z));
+  have_pf = true;
+  VDVC_CUFFT(cufftPlan3d(&pi, sz, sy, sx, CUFFT_Z2D));
+  have_pi = true;
+  VDVC_CUFFT(cufftSetStream(pf, s));
+  VDVC_CUFFT(cufftSetStream(pi, s));
+  VDVC_CUFFT(cufftExecD2Z(pf, fr, Fc));
+  VDVC_CUFFT(cufftExecD2Z(pf, gr, Gc));
+  k_cross_power<<<grid_blocks(nc, 256, 152 * 16), 256, 0, s>>>(Fc, Gc, nc);
+  count_launch();
+  VDVC_CUFFT(cufftExecZ2D(pi, Fc, fr));
+  k_argmax<<<nb, 256, 0, s>>>(fr, sx, sy, sz, partial, ticket, result);
+  count_launch();
+  if (cudaMemcpyAsync(&host, result, sizeof(ArgMax), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    st = set_error(VDVC_ERR_CUDA, "fft_rigid_shift: %s", cudaGetErrorString(cudaGetLastError()));
+    goto cleanup;
+  }
+  {
+    // C-order index of pix[x,y,z] -> (x,y,z); wrap to (-n/2, n/2]; d = -peak
+    long long c = host.cidx;
+    const int pz = (int)(c % sz);
+    c /= sz;
+    const int py = (int)(c % sy);
+    const int px = (int)(c / sy);
+    const int p[3] = {px, py, pz}, ns[3] = {sx, sy, sz};
+    for (int a = 0; a < 3; ++a) {
+      int q = p[a];
+      if (q > ns[a] / 2) q -= ns[a];
+      d_out3[a] = -(double)q;
+    }
+  }
+cleanup:
+  if (have_pf) cufftDestroy(pf);
+  if (have_pi) cufftDestroy(pi);
+  if (fr) cudaFreeAsync(fr, s);
+  if (gr) cudaFreeAsync(gr, s);
+  if (Fc) cudaFreeAsync(Fc, s);
+  if (Gc) cudaFreeAsync(Gc, s);
+  if (partial) cudaFreeAsync(partial, s);
+  if (result) cudaFreeAsync(result, s);
+  if (ticket) cudaFreeAsync(ticket, s);
+  return st;
+}
+
+}  // extern "C"

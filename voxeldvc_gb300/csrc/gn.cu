@@ -1,0 +1,684 @@
+// Gauss-Newton DVC solver at one pyramid level (engine/correlate_gpu.py:
+// 828-1140) as a device-resident object.  The host drives one GN iteration
+// with four calls -- sample, rhs, pcg, update -- and reads back a handful of
+// scalars once per iteration; everything between those calls stays on the
+// GPU (scalars included).
+//
+// Per iteration, for T = float (the plain solve) or double:
+//   sample : g(x+u), live mask, [freeze], stats of g over the b mask
+//   rhs    : R U (regularizer stencils), res = f - (std0/std1)(g - mean) on the b
+//            mask, element vectors of b and diag H, display stats of res;
+//            gather b = sum - ll R U, diag = sum + ll diag_R, min diag; M^-1
+//   pcg    : Jacobi PCG on (H + ll R) dU = b, replayed as a CUDA graph of
+//            `chunk` iterations until the device state says done
+//   update : U += dU (float64 master copy), |dU|^2, |U|^2
+#include <cstdlib>
+#include <new>
+
+#include "ops.cuh"
+#include "pcg.cuh"
+
+namespace vdvc {
+
+struct GnScalars {
+  double gstats[4];  // count, s1, s2 of g over the b mask; n_active
+  double dstats[3];  // count, s1, s2 of res over the live mask
+  double dmin;       // min diag
+  double norms[2];   // |dU|^2, |U|^2
+  int status;
+  int pad;
+};
+
+template <typename T>
+struct GnSolver {
+  Mesh m;
+  vdvc_gn_desc d;
+  Kmat Klap, Kel;
+  // device buffers (carved from the caller's workspace)
+  double* U64;
+  T *U32, *x, *r, *z, *p, *Ap, *Minv, *b, *w, *ru, *t1, *gvals, *res, *evA, *evD;
+  double *diag, *diag_reg;
+  uint8_t *live, *frozen;
+  double* partials;
+  unsigned int* ticket;
+  GnScalars* sc;
+  PcgState* pcg;
+  Kpair<T>* kp;
+  bool frozen_set;
+  // PCG graph
+  cudaStream_t cap_stream;
+  cudaGraph_t graph;
+  cudaGraphExec_t gexec;
+  int chunk, kernels_per_iter;
+  // pinned readback slots
+  PcgState* h_pcg;
+  GnScalars* h_sc;
+  cudaEvent_t ev[2];
+};
+
+template <typename T>
+static size_t carve_solver(const Mesh& m, GnSolver<T>* S, void* ws, size_t bytes) {
+  Carve cv(ws, bytes);
+  const size_t nd = (size_t)m.Ndof, nv = (size_t)m.Nvox;
+  S->U64 = cv.take<double>(nd);
+  S->U32 = cv.take<T>(nd);
+  S->x = cv.take<T>(nd);
+  S->r = cv.take<T>(nd);
+  S->z = cv.take<T>(nd);
+  S->p = cv.take<T>(nd);
+  S->Ap = cv.take<T>(nd);
+  S->Minv = cv.take<T>(nd);
+  S->b = cv.take<T>(nd);
+  S->w = cv.take<T>(nd);
+  S->ru = cv.take<T>(nd);
+  S->t1 = cv.take<T>(nd);
+  S->diag = cv.take<double>(nd);
+  S->diag_reg = cv.take<double>(nd);
+  S->gvals = cv.take<T>(nv);
+  S->res = cv.take<T>(nv);
+  S->live = cv.take<uint8_t>(nv);
+  S->frozen = cv.take<uint8_t>(nv);
+  S->evA = cv.take<T>((size_t)24 * m.Ne);
+  S->evD = cv.take<T>((size_t)24 * m.Ne);
+  const long long nb = strip_grid_blocks(m);
+  S->partials = cv.take<double>((size_t)(nb > kReduceBlocks ? nb : kReduceBlocks) * 4);
+  S->ticket = cv.take<unsigned int>(4);
+  S->sc = cv.take<GnScalars>(1);
+  S->pcg = cv.take<PcgState>(1);
+  S->kp = cv.take<Kpair<T>>(1);
+  return cv.off;  // bytes used from ws
+}
+
+// ---- small kernels -----------------------------------------------------------
+
+template <typename T>
+__global__ void k_set_U(const double* __restrict__ U0, long long n, double* __restrict__ U64, T* __restrict__ U32) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double u = U0 ? U0[i] : 0.0;
+    U64[i] = u;
+    U32[i] = (T)u;
+  }
+}
+
+// b = sum of element vectors - ll R U ; diag = sum + ll diag_R (float64),
+// min diag -> sc->dmin.
+template <typename T>
+__global__ void __launch_bounds__(256) k_gn_gather_rhs(const Mesh m, const T* __restrict__ evA,
+                                                       const T* __restrict__ evD, const T* __restrict__ ru, double ll,
+                                                       const double* __restrict__ diag_reg, T* __restrict__ b,
+                                                       double* __restrict__ diag, GnScalars* sc, GridReduce red,
+                                                       bool with_diag) {
+  __shared__ double s_red[8];
+  double dmin = 1.0e300;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < m.Nnodes;
+       n += (long long)gridDim.x * blockDim.x) {
+    const int ni = (int)(n % m.Nnx);
+    const long long rr = n / m.Nnx;
+    const int nj = (int)(rr % m.Nny), nk = (int)(rr / m.Nny);
+    T sb[3] = {T(0), T(0), T(0)}, sd[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int ei = ni - corner_dx(a), ej = nj - corner_dy(a), ek = nk - corner_dz(a);
+      if (ei < 0 || ej < 0 || ek < 0 || ei >= m.Nx || ej >= m.Ny || ek >= m.Nz) continue;
+      const long long e = (long long)ei + (long long)ej * m.Nx + (long long)ek * m.Nx * m.Ny;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sb[c] += evA[(long long)(3 * a + c) * m.Ne + e];
+        if (with_diag) sd[c] += evD[(long long)(3 * a + c) * m.Ne + e];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long long dof = 3 * n + c;
+      b[dof] = ru ? (T)((double)sb[c] - ll * (double)ru[dof]) : sb[c];
+      if (with_diag) {
+        const double dg = (double)sd[c] + (diag_reg ? ll * diag_reg[dof] : 0.0);
+        diag[dof] = dg;
+        dmin = fmin(dmin, dg);
+      }
+    }
+  }
+  if (!with_diag) return;
+  double bm = block_min(dmin, s_red);
+  // grid min through the deterministic reduction slots (values, not sums)
+  __shared__ bool s_last;
+  const unsigned int nb = gridDim.x;
+  if (threadIdx.x == 0) {
+    red.partials[blockIdx.x] = bm;
+    __threadfence();
+    s_last = (atomicAdd(red.ticket, 1u) == nb - 1);
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    double v = 1.0e300;
+    for (unsigned int q = threadIdx.x; q < nb; q += blockDim.x) v = fmin(v, __ldcg(red.partials + q));
+    v = block_min(v, s_red);
+    if (threadIdx.x == 0) {
+      sc->dmin = v;
+      *red.ticket = 0u;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_gn_minv(const double* __restrict__ diag, long long n, const GnScalars* sc, T* __restrict__ Minv) {
+  const double eps = 1e-5 * sc->dmin;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    Minv[i] = (T)(1.0 / (diag[i] + eps));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_gn_update(const T* __restrict__ dU, long long n, double* __restrict__ U64,
+                                                   T* __restrict__ U32, GnScalars* sc, GridReduce red) {
+  __shared__ double s_red[8];
+  double dd = 0.0, uu = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double du = (double)dU[i];
+    const double u = U64[i] + du;
+    U64[i] = u;
+    U32[i] = (T)u;
+    dd += du * du;
+    uu += u * u;
+  }
+  double mine[2] = {block_sum(dd, s_red), block_sum(uu, s_red)}, out[2];
+  if (grid_reduce_sum<2>(red, mine, out, s_red) && threadIdx.x == 0) {
+    sc->norms[0] = out[0];
+    sc->norms[1] = out[1];
+  }
+}
+
+template <typename T>
+__global__ void k_copy_out(const T* __restrict__ src, long long n, void* __restrict__ dst, int dst_f64) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (dst_f64)
+      ((double*)dst)[i] = (double)src[i];
+    else
+      ((float*)dst)[i] = (float)src[i];
+  }
+}
+
+__global__ void k_add_scaled_f64(double* a, const double* b, double s, long long n) {  // a may alias b
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] += s * b[i];
+}
+
+inline int nblk(long long n) { return grid_blocks(n, 256, 152 * 16); }
+
+// ---- the regularizer applied to a nodal vector (stencil chain) --------------
+
+// out = R v with R = h K_lap (Laplacian) or h K_el P h K_el + eps h K_lap.
+// With p_old != null the input is p_new = v + beta p_old (PCG).
+template <typename T>
+static int apply_reg(GnSolver<T>* S, const T* v, T* out, cudaStream_t s) {
+  const vdvc_gn_desc& d = S->d;
+  StencilArgs<T> a{};
+  a.m = S->m;
+  a.E = (double)d.h;
+  a.scale = 1.0;
+  if (d.reg_type == VDVC_REG_LAPLACIAN) {
+    a.v = v;
+    a.out = out;
+    return launch_kref_apply<T>(a, S->Klap, s);
+  }
+  int st;
+  a.v = v;
+  a.interior = (const T*)d.interior;
+  a.out = S->t1;
+  if ((st = launch_kref_apply<T>(a, S->Kel, s))) return st;
+  StencilArgs<T> b2 = a;  // eps h K_lap v
+  b2.interior = nullptr;
+  b2.v = v;
+  b2.scale = d.eps_reg;
+  b2.out = out;
+  if ((st = launch_kref_apply<T>(b2, S->Klap, s))) return st;
+  StencilArgs<T> c2 = a;  // + h K_el t1
+  c2.interior = nullptr;
+  c2.v = S->t1;
+  c2.add_to = out;
+  c2.out = out;
+  return launch_kref_apply<T>(c2, S->Kel, s);
+}
+
+// ---- one PCG iteration (captured into the graph) ----------------------------
+
+template <typename T>
+static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
+  const vdvc_gn_desc& d = S->d;
+  GridReduce red{S->partials, S->ticket};
+  int st;
+  if (d.reg_type == VDVC_REG_EQUILIBRIUM_GAP && d.ll != 0.0) {
+    StencilArgs<T> a{};
+    a.m = S->m;
+    a.v = S->z;
+    a.p_old = S->p;
+    a.st = S->pcg;
+    a.E = (double)d.h;
+    a.scale = 1.0;
+    a.interior = (const T*)d.interior;
+    a.out = S->w;
+    if ((st = launch_kref_apply<T>(a, S->Kel, s))) return st;
+  }
+  StripArgs<T> sa{};
+  sa.m = S->m;
+  sa.v = S->z;
+  sa.p_old = S->p;
+  sa.st = S->pcg;
+  sa.grad = (const T*)d.grad;
+  // H mask: the b mask buffer (dynamic_mask) or mask0 -- fixed pointers, so
+  // the captured graph stays valid for the solver's lifetime
+  sa.mask = d.dynamic_mask ? S->frozen : d.mask0;
+  sa.evA = S->evA;
+  sa.nreg = 0;
+  if (d.ll != 0.0 && d.reg_type == VDVC_REG_LAPLACIAN) {
+    sa.nreg = 1;
+    sa.c1 = (T)(d.ll * d.h);
+  } else if (d.ll != 0.0 && d.reg_type == VDVC_REG_EQUILIBRIUM_GAP) {
+    sa.nreg = 2;
+    sa.c1 = (T)(d.ll * d.eps_reg * d.h);
+    sa.c2 = (T)(d.ll * d.h);
+    sa.w = S->w;
+  }
+  if ((st = launch_strip<T, kModeHv | kModePcg>(sa, S->kp, s))) return st;
+  if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s))) return st;
+  return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
+}
+
+template <typename T>
+static int build_graph(GnSolver<T>* S) {
+  if (S->gexec) {
+    cudaGraphExecDestroy(S->gexec);
+    S->gexec = nullptr;
+  }
+  if (S->graph) {
+    cudaGraphDestroy(S->graph);
+    S->graph = nullptr;
+  }
+  cudaStream_t cs = S->cap_stream;
+  VDVC_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  const long long before = vdvc_launch_count();
+  int st = VDVC_OK;
+  for (int it = 0; it < S->chunk && st == VDVC_OK; ++it) st = pcg_iteration<T>(S, cs);
+  const long long captured = vdvc_launch_count() - before;
+  count_launch(-captured);  // captured launches run at replay time
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(cs, &g);
+  if (st) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) return set_error(VDVC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  S->graph = g;
+  S->kernels_per_iter = (int)(captured / S->chunk);
+  VDVC_CUDA(cudaGraphInstantiate(&S->gexec, g, 0));
+  return VDVC_OK;
+}
+
+template <typename T>
+static size_t solver_bytes(const Mesh& m) {
+  GnSolver<T> tmp{};
+  return carve_solver<T>(m, &tmp, nullptr, 0) + 256;
+}
+
+template <typename T>
+static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) {
+  Mesh m;
+  int st = make_mesh(d->h, d->Nx, d->Ny, d->Nz, &m);
+  if (st) return st;
+  VDVC_CHECK_ARG(d->f_vox && d->g_vox && d->grad && d->mask0, "null input pointer");
+  VDVC_CHECK_ARG(d->gnx >= 1 && d->gny >= 1 && d->gnz >= 1, "bad g shape");
+  VDVC_CHECK_ARG(d->reg_type >= VDVC_REG_NONE && d->reg_type <= VDVC_REG_EQUILIBRIUM_GAP, "bad reg_type");
+  if (d->reg_type != VDVC_REG_NONE) VDVC_CHECK_ARG(d->K_lap != nullptr, "K_lap required");
+  if (d->reg_type == VDVC_REG_EQUILIBRIUM_GAP)
+    VDVC_CHECK_ARG(d->K_el && d->interior && d->diag_eqgap, "equilibrium gap needs K_el, interior, diag_eqgap");
+  GnSolver<T>* S = new (std::nothrow) GnSolver<T>();
+  if (!S) return set_error(VDVC_ERR_ARG, "host allocation failed");
+  S->m = m;
+  S->d = *d;
+  size_t need = solver_bytes<T>(m);
+  if (!ws || ws_bytes < need) {
+    delete S;
+    return set_error(VDVC_ERR_WORKSPACE, "solver needs %zu bytes of workspace (got %zu)", need, ws_bytes);
+  }
+  carve_solver<T>(m, S, ws, ws_bytes);
+  if (d->K_lap) load_K(d->K_lap, &S->Klap);
+  if (d->K_el) load_K(d->K_el, &S->Kel);
+  S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 8;
+  cudaStream_t s = (cudaStream_t)d->stream;
+  int e = VDVC_OK;
+  auto fail = [&](int code) {
+    if (S->cap_stream) cudaStreamDestroy(S->cap_stream);
+    if (S->h_pcg) cudaFreeHost(S->h_pcg);
+    delete S;
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&S->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMallocHost((void**)&S->h_pcg, 2 * sizeof(PcgState) + sizeof(GnScalars)) != cudaSuccess ||
+      cudaEventCreateWithFlags(&S->ev[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&S->ev[1], cudaEventDisableTiming) != cudaSuccess)
+    return fail(set_error(VDVC_ERR_CUDA, "solver stream/event/pinned setup failed"));
+  S->h_sc = (GnScalars*)(S->h_pcg + 2);
+  // device-side constants: the fused K pair, zeroed reduction tickets, scalars
+  Kpair<T> kh;
+  for (int q = 0; q < 576; ++q) {
+    kh.K1[q] = (T)S->Klap.k[q];
+    kh.K2[q] = (T)S->Kel.k[q];
+  }
+  if (cudaMemcpyAsync(S->kp, &kh, sizeof(kh), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemsetAsync(S->ticket, 0, 4 * sizeof(unsigned int), s) != cudaSuccess ||
+      cudaMemsetAsync(S->sc, 0, sizeof(GnScalars), s) != cudaSuccess)
+    return fail(set_error(VDVC_ERR_CUDA, "solver upload failed"));
+  // regularizer diagonal in float64: h diag(K_lap) [+ eq. gap Hutchinson]
+  if (d->reg_type != VDVC_REG_NONE) {
+    if ((e = launch_kref_diag<double>(m, S->Klap, nullptr, (double)d->h, S->diag_reg, s))) return fail(e);
+    if (d->reg_type == VDVC_REG_EQUILIBRIUM_GAP) {
+      // diag_reg = diag_eqgap + eps * h diag(K_lap)
+      const long long n = m.Ndof;
+      k_add_scaled_f64<<<nblk(n), 256, 0, s>>>(S->diag_reg, S->diag_reg, d->eps_reg - 1.0, n);
+      k_add_scaled_f64<<<nblk(n), 256, 0, s>>>(S->diag_reg, d->diag_eqgap, 1.0, n);
+      count_launch(2);
+    }
+  }
+  k_set_U<T><<<nblk(m.Ndof), 256, 0, s>>>(nullptr, m.Ndof, S->U64, S->U32);
+  count_launch();
+  // sync before the graph (captured on a private stream) sees the buffers
+  if (cudaStreamSynchronize(s) != cudaSuccess) return fail(set_error(VDVC_ERR_CUDA, "solver setup sync failed"));
+  *out = S;
+  return VDVC_OK;
+}
+
+template <typename T>
+static int set_U(GnSolver<T>* S, const double* U0, cudaStream_t s) {
+  k_set_U<T><<<nblk(S->m.Ndof), 256, 0, s>>>(U0, S->m.Ndof, S->U64, S->U32);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+// Frozen-H preconditioner (dynamic_mask == 0): diag H over mask0, built once.
+template <typename T>
+static int frozen_diag(GnSolver<T>* S, cudaStream_t s) {
+  StripArgs<T> a{};
+  a.m = S->m;
+  a.grad = (const T*)S->d.grad;
+  a.mask = S->d.mask0;
+  a.evD = S->evD;
+  int st = launch_strip<T, kModeDiag>(a, nullptr, s);
+  if (st) return st;
+  GridReduce red{S->partials, S->ticket};
+  k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, kReduceBlocks), 256, 0, s>>>(
+      S->m, S->evD, S->evD, nullptr, S->d.ll, S->d.reg_type != VDVC_REG_NONE ? S->diag_reg : nullptr, S->t1,
+      S->diag, S->sc, red, true);
+  VDVC_LAUNCHED();
+  k_gn_minv<T><<<nblk(S->m.Ndof), 256, 0, s>>>(S->diag, S->m.Ndof, S->sc, S->Minv);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+template <typename T>
+static int sample(GnSolver<T>* S, int freeze_now, cudaStream_t s) {
+  const vdvc_gn_desc& d = S->d;
+  SampleArgs<T> a{};
+  a.m = S->m;
+  a.U = S->U32;
+  a.g = (const T*)d.g_vox;
+  a.gnx = d.gnx; a.gny = d.gny; a.gnz = d.gnz;
+  a.gx0 = (T)d.gx0; a.gy0 = (T)d.gy0; a.gz0 = (T)d.gz0;
+  a.mask0 = d.mask0;
+  a.glt = (T)d.glt;
+  a.gvals = S->gvals;
+  a.mask_out = S->live;
+  // S->frozen is the b mask buffer: it follows the live mask until the freeze
+  // iteration (engine/correlate_gpu.py:1079-1081) and is kept after it.
+  a.bmask_frozen = S->frozen_set ? S->frozen : nullptr;
+  a.freeze_out = S->frozen_set ? nullptr : S->frozen;
+  a.red = GridReduce{S->partials, S->ticket};
+  a.stats = S->sc->gstats;
+  int st = launch_sample<T, true, false>(a, s);
+  if (st) return st;
+  if (freeze_now && !S->frozen_set) S->frozen_set = true;
+  return VDVC_OK;
+}
+
+template <typename T>
+static int rhs(GnSolver<T>* S, cudaStream_t s) {
+  const vdvc_gn_desc& d = S->d;
+  int st;
+  const bool reg = d.reg_type != VDVC_REG_NONE && d.ll != 0.0;
+  if (reg && (st = apply_reg<T>(S, S->U32, S->ru, s))) return st;
+  StripArgs<T> a{};
+  a.m = S->m;
+  a.grad = (const T*)d.grad;
+  a.mask = S->frozen;  // b mask
+  a.f = (const T*)d.f_vox;
+  a.gvals = S->gvals;
+  a.live = S->live;
+  a.gstats = S->sc->gstats;
+  a.mean0 = d.mean0;
+  a.std0 = d.std0;
+  a.res_out = S->res;
+  a.red = GridReduce{S->partials, S->ticket};
+  a.dstats = S->sc->dstats;
+  a.status = &S->sc->status;
+  a.evA = S->evA;
+  a.evD = S->evD;
+  if (d.dynamic_mask)
+    st = launch_strip<T, kModeB | kModeRes | kModeDiag>(a, nullptr, s);
+  else
+    st = launch_strip<T, kModeB | kModeRes>(a, nullptr, s);
+  if (st) return st;
+  GridReduce red{S->partials, S->ticket};
+  k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, kReduceBlocks), 256, 0, s>>>(
+      S->m, S->evA, S->evD, reg ? S->ru : nullptr, d.ll, d.reg_type != VDVC_REG_NONE ? S->diag_reg : nullptr, S->b,
+      S->diag, S->sc, red, d.dynamic_mask != 0);
+  VDVC_LAUNCHED();
+  if (d.dynamic_mask) {
+    k_gn_minv<T><<<nblk(S->m.Ndof), 256, 0, s>>>(S->diag, S->m.Ndof, S->sc, S->Minv);
+    VDVC_LAUNCHED();
+  }
+  return VDVC_OK;
+}
+
+template <typename T>
+static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res, int* status, cudaStream_t s) {
+  // a residual normalisation failure of the rhs pass stops the iteration here,
+  // where the reference raises (engine/correlate_gpu.py:1095)
+  VDVC_CUDA(cudaMemcpyAsync(&S->h_sc->status, &S->sc->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  if (S->h_sc->status != VDVC_OK) {
+    const int code = S->h_sc->status;
+    VDVC_CUDA(cudaMemsetAsync(&S->sc->status, 0, sizeof(int), s));
+    return set_error(code, "float division by zero (std of g over the b mask is 0)");
+  }
+  GridReduce red{S->partials, S->ticket};
+  int st = launch_pcg_init<T>(S->b, nullptr, S->Minv, S->m.Ndof, S->r, S->z, S->p, false, S->x, S->pcg, red,
+                              max_iter, tol, s);
+  if (st) return st;
+  if (!S->gexec && (st = build_graph<T>(S))) return st;
+  // Two chunks in flight: launch chunk k+1 before waiting on chunk k's state.
+  int launched = 0, checked = 0;
+  const int max_chunks = max_iter <= 0 ? 0 : (max_iter + S->chunk - 1) / S->chunk;
+  bool done = max_iter <= 0;
+  while (!done) {
+    while (launched < max_chunks && launched - checked < 2) {
+      VDVC_CUDA(cudaGraphLaunch(S->gexec, s));
+      count_launch((long long)S->chunk * S->kernels_per_iter);
+      VDVC_CUDA(cudaMemcpyAsync(S->h_pcg + (launched & 1), S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
+      VDVC_CUDA(cudaEventRecord(S->ev[launched & 1], s));
+      ++launched;
+    }
+    if (checked == launched) break;
+    VDVC_CUDA(cudaEventSynchronize(S->ev[checked & 1]));
+    const PcgState& h = S->h_pcg[checked & 1];
+    ++checked;
+    if (h.done) done = true;
+    if (checked == max_chunks) done = true;
+  }
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  PcgState fin;
+  VDVC_CUDA(cudaMemcpy(&fin, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost));
+  if (iters) *iters = fin.iter;
+  if (res) *res = fin.res;
+  if (status) *status = fin.status;
+  return VDVC_OK;
+}
+
+template <typename T>
+static int update(GnSolver<T>* S, double* out8, cudaStream_t s) {
+  GridReduce red{S->partials, S->ticket};
+  k_gn_update<T><<<grid_blocks(S->m.Ndof, 256, kReduceBlocks), 256, 0, s>>>(S->x, S->m.Ndof, S->U64, S->U32, S->sc,
+                                                                            red);
+  VDVC_LAUNCHED();
+  VDVC_CUDA(cudaMemcpyAsync(S->h_sc, S->sc, sizeof(GnScalars), cudaMemcpyDeviceToHost, s));
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  const GnScalars& h = *S->h_sc;
+  if (out8) {
+    out8[0] = h.norms[0];
+    out8[1] = h.norms[1];
+    out8[2] = h.dstats[0];
+    out8[3] = h.dstats[1];
+    out8[4] = h.dstats[2];
+    out8[5] = h.gstats[3];
+    out8[6] = h.gstats[0];
+    out8[7] = (double)h.status;
+  }
+  if (h.status != VDVC_OK) {
+    const int code = h.status;
+    cudaMemsetAsync(&S->sc->status, 0, sizeof(int), s);
+    return set_error(code, code == VDVC_ERR_ZERO_DIVISION ? "float division by zero (std of g over the mask is 0)"
+                                                          : "solver status %d", code);
+  }
+  return VDVC_OK;
+}
+
+template <typename T>
+static int read(GnSolver<T>* S, int which, void* dst, int dst_f64, cudaStream_t s) {
+  const long long nd = S->m.Ndof, nv = S->m.Nvox;
+  switch (which) {
+    case VDVC_GN_U:
+      if (dst_f64) {
+        VDVC_CUDA(cudaMemcpyAsync(dst, S->U64, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      } else {
+        k_copy_out<double><<<nblk(nd), 256, 0, s>>>(S->U64, nd, dst, 0);
+        VDVC_LAUNCHED();
+      }
+      return VDVC_OK;
+    case VDVC_GN_DU:
+      k_copy_out<T><<<nblk(nd), 256, 0, s>>>(S->x, nd, dst, dst_f64);
+      VDVC_LAUNCHED();
+      return VDVC_OK;
+    case VDVC_GN_RES:
+      k_copy_out<T><<<nblk(nv), 256, 0, s>>>(S->res, nv, dst, dst_f64);
+      VDVC_LAUNCHED();
+      return VDVC_OK;
+    case VDVC_GN_LIVE_MASK:
+      VDVC_CUDA(cudaMemcpyAsync(dst, S->live, nv, cudaMemcpyDeviceToDevice, s));
+      return VDVC_OK;
+  }
+  return set_error(VDVC_ERR_ARG, "unknown buffer %d", which);
+}
+
+template <typename T>
+static void destroy(GnSolver<T>* S) {
+  if (!S) return;
+  if (S->gexec) cudaGraphExecDestroy(S->gexec);
+  if (S->graph) cudaGraphDestroy(S->graph);
+  if (S->cap_stream) cudaStreamDestroy(S->cap_stream);
+  if (S->ev[0]) cudaEventDestroy(S->ev[0]);
+  if (S->ev[1]) cudaEventDestroy(S->ev[1]);
+  if (S->h_pcg) cudaFreeHost(S->h_pcg);
+  delete S;
+}
+
+}  // namespace vdvc
+
+using namespace vdvc;
+
+struct vdvc_gn_solver {
+  int dtype;
+  void* impl;
+};
+
+extern "C" {
+
+size_t vdvc_gn_workspace_bytes(int dtype, int h, int Nx, int Ny, int Nz) {
+  Mesh m;
+  if (make_mesh(h, Nx, Ny, Nz, &m)) return 0;
+  if (dtype == VDVC_F32) return solver_bytes<float>(m);
+  if (dtype == VDVC_F64) return solver_bytes<double>(m);
+  return 0;
+}
+
+int vdvc_gn_create(const vdvc_gn_desc* desc, void* ws, size_t ws_bytes, vdvc_gn_solver** out) {
+  VDVC_CHECK_ARG(desc && out, "null pointer");
+  vdvc_gn_solver* h = new (std::nothrow) vdvc_gn_solver();
+  if (!h) return set_error(VDVC_ERR_ARG, "host allocation failed");
+  h->dtype = desc->dtype;
+  int st;
+  if (desc->dtype == VDVC_F32)
+    st = create<float>(desc, ws, ws_bytes, &h->impl);
+  else if (desc->dtype == VDVC_F64)
+    st = create<double>(desc, ws, ws_bytes, &h->impl);
+  else
+    st = set_error(VDVC_ERR_ARG, "dtype %d", desc->dtype);
+  if (st) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return VDVC_OK;
+}
+
+#define VDVC_GN_DISPATCH(call_f, call_d)                                      \
+  do {                                                                        \
+    VDVC_CHECK_ARG(solver != nullptr, "null solver");                         \
+    if (solver->dtype == VDVC_F32) {                                          \
+      GnSolver<float>* S = (GnSolver<float>*)solver->impl;                    \
+      return call_f;                                                          \
+    } else {                                                                  \
+      GnSolver<double>* S = (GnSolver<double>*)solver->impl;                  \
+      return call_d;                                                          \
+    }                                                                         \
+  } while (0)
+
+int vdvc_gn_set_U(vdvc_gn_solver* solver, const double* U0, vdvc_stream_t stream) {
+  VDVC_GN_DISPATCH(set_U<float>(S, U0, (cudaStream_t)stream), set_U<double>(S, U0, (cudaStream_t)stream));
+}
+
+int vdvc_gn_frozen_diag(vdvc_gn_solver* solver, vdvc_stream_t stream) {
+  VDVC_GN_DISPATCH(frozen_diag<float>(S, (cudaStream_t)stream), frozen_diag<double>(S, (cudaStream_t)stream));
+}
+
+int vdvc_gn_sample(vdvc_gn_solver* solver, int freeze_now, vdvc_stream_t stream) {
+  VDVC_GN_DISPATCH(sample<float>(S, freeze_now, (cudaStream_t)stream),
+                   sample<double>(S, freeze_now, (cudaStream_t)stream));
+}
+
+int vdvc_gn_rhs(vdvc_gn_solver* solver, vdvc_stream_t stream) {
+  VDVC_GN_DISPATCH(rhs<float>(S, (cudaStream_t)stream), rhs<double>(S, (cudaStream_t)stream));
+}
+
+int vdvc_gn_pcg(vdvc_gn_solver* solver, int max_iter, double tol, int* iters, double* res, int* status,
+                vdvc_stream_t stream) {
+  VDVC_GN_DISPATCH(pcg<float>(S, max_iter, tol, iters, res, status, (cudaStream_t)stream),
+                   pcg<double>(S, max_iter, tol, iters, res, status, (cudaStream_t)stream));
+}
+
+int vdvc_gn_update(vdvc_gn_solver* solver, double* out8, vdvc_stream_t stream) {
+  VDVC_GN_DISPATCH(update<float>(S, out8, (cudaStream_t)stream), update<double>(S, out8, (cudaStream_t)stream));
+}
+
+int vdvc_gn_read(vdvc_gn_solver* solver, int which, void* dst, int dst_f64, vdvc_stream_t stream) {
+  VDVC_GN_DISPATCH(read<float>(S, which, dst, dst_f64, (cudaStream_t)stream),
+                   read<double>(S, which, dst, dst_f64, (cudaStream_t)stream));
+}
+
+void vdvc_gn_destroy(vdvc_gn_solver* solver) {
+  if (!solver) return;
+  if (solver->dtype == VDVC_F32)
+    destroy<float>((GnSolver<float>*)solver->impl);
+  else
+    destroy<double>((GnSolver<double>*)solver->impl);
+  delete solver;
+}
+
+}  // extern "C"

@@ -1,0 +1,193 @@
+// Image layout and reference-image preparation kernels:
+//   pix -> vox transpose with cast, strided decimation, the xp.gradient
+//   stencil with the mask0 / 6-neighbour erosion fused in, and the erosion
+//   on its own.
+#include "common.cuh"
+
+namespace vdvc {
+namespace {
+
+// C-order (nx,ny,nz) -> x-fastest, one y plane per blockIdx.z, 32x32
+// (z,x) tiles staged through shared memory so both sides are coalesced.
+template <typename Tin, typename Tout>
+__global__ void __launch_bounds__(256) k_pix_to_vox(const Tin* __restrict__ in, Tout* __restrict__ out,
+                                                    int nx, int ny, int nz) {
+  __shared__ Tout tile[32][33];
+  const int z0 = blockIdx.x * 32, x0 = blockIdx.y * 32, y = blockIdx.z;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int x = x0 + r, z = z0 + threadIdx.x;
+    if (x < nx && z < nz) tile[r][threadIdx.x] = (Tout)in[((size_t)x * ny + y) * nz + z];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int z = z0 + r, x = x0 + threadIdx.x;
+    if (x < nx && z < nz) out[(size_t)x + (size_t)y * nx + (size_t)z * nx * ny] = tile[threadIdx.x][r];
+  }
+}
+
+template <typename E>
+__global__ void k_decimate(const E* __restrict__ in, E* __restrict__ out, int nx, int ny, int ox, int oy,
+                           int oz, int s) {
+  const long long n = (long long)ox * oy * oz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(t % ox);
+    const long long r = t / ox;
+    const int y = (int)(r % oy), z = (int)(r / oy);
+    out[t] = in[(size_t)x * s + (size_t)y * s * nx + (size_t)z * s * nx * ny];
+  }
+}
+
+// One component of xp.gradient with edge_order=1 (numpy's default): central
+// difference / 2 inside, first-order one-sided difference at both ends.
+template <typename T>
+__device__ __forceinline__ T gradient_1d(T fm, T f0, T fp, int i, int n) {
+  if (i == 0) return fp - f0;
+  if (i == n - 1) return f0 - fm;
+  return (fp - fm) * T(0.5);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_image_grad(const T* __restrict__ f, int nx, int ny, int nz, T glt,
+                                                    T* __restrict__ grad, uint8_t* __restrict__ mask0,
+                                                    bool with_mask) {
+  const long long nxy = (long long)nx * ny, n = nxy * nz;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(v % nx);
+    const long long r = v / nx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    const long long xm = v - (x > 0), xp = v + (x < nx - 1);
+    const long long ym = v - (y > 0) * nx, yp = v + (y < ny - 1) * (long long)nx;
+    const long long zm = v - (z > 0) * nxy, zp = v + (z < nz - 1) * nxy;
+    const T c = f[v];
+    const T fxm = f[xm], fxp = f[xp], fym = f[ym], fyp = f[yp], fzm = f[zm], fzp = f[zp];
+    T gx = gradient_1d(fxm, c, fxp, x, nx);
+    T gy = gradient_1d(fym, c, fyp, y, ny);
+    T gz = gradient_1d(fzm, c, fzp, z, nz);
+    if (with_mask) {
+      const bool m = c > glt;
+      // minimum_filter with the 6-neighbour footprint, mode 'nearest': a
+      // clamped neighbour is the voxel itself.
+      const bool keep = m && (fxm > glt) && (fxp > glt) && (fym > glt) && (fyp > glt) && (fzm > glt) &&
+                        (fzp > glt);
+      mask0[v] = m ? 1 : 0;
+      if (!keep) gx = gy = gz = T(0);
+    }
+    grad[3 * v + 0] = gx;
+    grad[3 * v + 1] = gy;
+    grad[3 * v + 2] = gz;
+  }
+}
+
+__global__ void k_erode(const uint8_t* __restrict__ m, int nx, int ny, int nz, uint8_t* __restrict__ out) {
+  const long long nxy = (long long)nx * ny, n = nxy * nz;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(v % nx);
+    const long long r = v / nx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    bool keep = m[v] && m[v - (x > 0)] && m[v + (x < nx - 1)] && m[v - (y > 0) * nx] &&
+                m[v + (y < ny - 1) * (long long)nx] && m[v - (z > 0) * nxy] && m[v + (z < nz - 1) * nxy];
+    out[v] = keep ? 1 : 0;
+  }
+}
+
+inline int grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b > 152LL * 64) b = 152LL * 64;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+template <typename Tin, typename Tout>
+int launch_p2v(const void* pix, int nx, int ny, int nz, void* vox, cudaStream_t s) {
+  dim3 grid((nz + 31) / 32, (nx + 31) / 32, ny), block(32, 8);
+  k_pix_to_vox<Tin, Tout><<<grid, block, 0, s>>>((const Tin*)pix, (Tout*)vox, nx, ny, nz);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+template <typename Tout>
+int p2v_dispatch(const void* pix, int pix_dtype, int nx, int ny, int nz, void* vox, cudaStream_t s) {
+  switch (pix_dtype) {
+    case VDVC_F32: return launch_p2v<float, Tout>(pix, nx, ny, nz, vox, s);
+    case VDVC_F64: return launch_p2v<double, Tout>(pix, nx, ny, nz, vox, s);
+    case VDVC_U8: return launch_p2v<uint8_t, Tout>(pix, nx, ny, nz, vox, s);
+    case VDVC_U16: return launch_p2v<uint16_t, Tout>(pix, nx, ny, nz, vox, s);
+    case VDVC_I16: return launch_p2v<int16_t, Tout>(pix, nx, ny, nz, vox, s);
+    case VDVC_I32: return launch_p2v<int32_t, Tout>(pix, nx, ny, nz, vox, s);
+  }
+  return set_error(VDVC_ERR_ARG, "pix_dtype %d not supported", pix_dtype);
+}
+
+}  // namespace
+}  // namespace vdvc
+
+using namespace vdvc;
+
+extern "C" {
+
+int vdvc_pix_to_vox(const void* pix, int pix_dtype, int nx, int ny, int nz, void* vox, int dtype,
+                    vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(pix && vox, "null pointer");
+  VDVC_CHECK_ARG(nx >= 1 && ny >= 1 && nz >= 1 && ny <= 65535, "bad image shape (%d,%d,%d)", nx, ny, nz);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == VDVC_F32) return p2v_dispatch<float>(pix, pix_dtype, nx, ny, nz, vox, s);
+  if (dtype == VDVC_F64) return p2v_dispatch<double>(pix, pix_dtype, nx, ny, nz, vox, s);
+  return set_error(VDVC_ERR_ARG, "dtype %d must be VDVC_F32 or VDVC_F64", dtype);
+}
+
+int vdvc_decimate(const void* in, int dtype, int nx, int ny, int nz, int s, void* out, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(in && out, "null pointer");
+  VDVC_CHECK_ARG(nx >= 1 && ny >= 1 && nz >= 1 && s >= 1, "bad shape/stride");
+  const int ox = (nx + s - 1) / s, oy = (ny + s - 1) / s, oz = (nz + s - 1) / s;
+  const long long n = (long long)ox * oy * oz;
+  const int threads = 256, blocks = grid_for(n, threads);
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t es = dtype_size(dtype);
+  if (es == 4)
+    k_decimate<uint32_t><<<blocks, threads, 0, st>>>((const uint32_t*)in, (uint32_t*)out, nx, ny, ox, oy, oz, s);
+  else if (es == 8)
+    k_decimate<uint64_t><<<blocks, threads, 0, st>>>((const uint64_t*)in, (uint64_t*)out, nx, ny, ox, oy, oz, s);
+  else if (es == 2)
+    k_decimate<uint16_t><<<blocks, threads, 0, st>>>((const uint16_t*)in, (uint16_t*)out, nx, ny, ox, oy, oz, s);
+  else if (es == 1)
+    k_decimate<uint8_t><<<blocks, threads, 0, st>>>((const uint8_t*)in, (uint8_t*)out, nx, ny, ox, oy, oz, s);
+  else
+    return set_error(VDVC_ERR_ARG, "dtype %d not supported", dtype);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_image_grad(const void* f_vox, int dtype, int Nvx, int Nvy, int Nvz, double glt, void* grad,
+                    uint8_t* mask0, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(f_vox && grad, "null pointer");
+  // numpy's gradient needs at least 2 samples per axis (edge_order + 1).
+  VDVC_CHECK_ARG(Nvx >= 2 && Nvy >= 2 && Nvz >= 2, "gradient needs >= 2 voxels per axis");
+  const long long n = (long long)Nvx * Nvy * Nvz;
+  const int threads = 256, blocks = grid_for(n, threads);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == VDVC_F32)
+    k_image_grad<float><<<blocks, threads, 0, s>>>((const float*)f_vox, Nvx, Nvy, Nvz, (float)glt, (float*)grad,
+                                                   mask0, mask0 != nullptr);
+  else if (dtype == VDVC_F64)
+    k_image_grad<double><<<blocks, threads, 0, s>>>((const double*)f_vox, Nvx, Nvy, Nvz, glt, (double*)grad,
+                                                    mask0, mask0 != nullptr);
+  else
+    return set_error(VDVC_ERR_ARG, "dtype %d must be VDVC_F32 or VDVC_F64", dtype);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_erode_mask(const uint8_t* mask, int Nvx, int Nvy, int Nvz, uint8_t* out, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(mask && out && mask != out, "null or aliased pointer");
+  VDVC_CHECK_ARG(Nvx >= 1 && Nvy >= 1 && Nvz >= 1, "bad shape");
+  const long long n = (long long)Nvx * Nvy * Nvz;
+  const int threads = 256, blocks = grid_for(n, threads);
+  k_erode<<<blocks, threads, 0, (cudaStream_t)stream>>>(mask, Nvx, Nvy, Nvz, out);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+}  // extern "C"

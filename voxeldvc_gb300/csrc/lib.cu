@@ -1,0 +1,74 @@
+// Library-level entry points: ABI version, status strings, per-thread error
+// detail, launch counter and mesh validation.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <climits>
+
+#include "common.cuh"
+
+namespace vdvc {
+
+static thread_local char g_last_error[512] = "";
+static std::atomic<long long> g_launches{0};
+
+int set_error(int status, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int make_mesh(int h, int Nx, int Ny, int Nz, Mesh* m) {
+  VDVC_CHECK_ARG(h >= 1 && h <= 1024, "h=%d must be in [1, 1024]", h);
+  VDVC_CHECK_ARG(Nx >= 1 && Ny >= 1 && Nz >= 1, "element counts must be >= 1 (got %d,%d,%d)", Nx, Ny, Nz);
+  m->Nx = Nx; m->Ny = Ny; m->Nz = Nz; m->h = h;
+  const long long nvx = (long long)Nx * h + 1, nvy = (long long)Ny * h + 1, nvz = (long long)Nz * h + 1;
+  const long long nvox = nvx * nvy * nvz;
+  const long long nnodes = (long long)(Nx + 1) * (Ny + 1) * (Nz + 1);
+  // Same int32 guard as the reference (engine/correlate_gpu.py:933-936).
+  if (nvox > INT_MAX || 3 * nnodes > INT_MAX)
+    return set_error(VDVC_ERR_INDEX_RANGE,
+                     "Nvox=%lld / Ndof=%lld exceed int32 range; matrix-free index arrays assume int32 indices",
+                     nvox, 3 * nnodes);
+  m->Nvx = (int)nvx; m->Nvy = (int)nvy; m->Nvz = (int)nvz;
+  m->Nnx = Nx + 1; m->Nny = Ny + 1; m->Nnz = Nz + 1;
+  m->Nvox = nvox;
+  m->Nnodes = nnodes;
+  m->Ndof = 3 * nnodes;
+  m->Ne = (long long)Nx * Ny * Nz;
+  m->NvxNvy = nvx * nvy;
+  m->NnxNny = (long long)(Nx + 1) * (Ny + 1);
+  m->inv_h = 1.0f / (float)h;
+  return VDVC_OK;
+}
+
+}  // namespace vdvc
+
+extern "C" {
+
+int vdvc_abi_version(void) { return 1; }
+
+const char* vdvc_status_string(int status) {
+  switch (status) {
+    case VDVC_OK: return "ok";
+    case VDVC_ERR_ARG: return "invalid argument";
+    case VDVC_ERR_INDEX_RANGE: return "index range exceeds int32";
+    case VDVC_ERR_CUDA: return "CUDA error";
+    case VDVC_ERR_WORKSPACE: return "workspace too small";
+    case VDVC_ERR_NONFINITE: return "non-finite value";
+    case VDVC_ERR_ZERO_DIVISION: return "division by zero";
+    case VDVC_ERR_CUFFT: return "cuFFT error";
+    case VDVC_ERR_UNSUPPORTED: return "unsupported";
+  }
+  return "unknown status";
+}
+
+const char* vdvc_last_error(void) { return vdvc::g_last_error; }
+
+long long vdvc_launch_count(void) { return vdvc::g_launches.load(); }
+
+}  // extern "C"

@@ -1,0 +1,84 @@
+// Declarations shared between the kernel translation units.
+#pragma once
+
+#include "common.cuh"
+#include "strip.cuh"
+
+namespace vdvc {
+
+struct PcgState;
+
+// Node-centric K application (reg.cu).
+template <typename T>
+struct StencilArgs {
+  Mesh m;
+  const T* v;          // nodal input
+  const T* p_old;      // when non-null: input is v + beta * p_old (PCG p_new)
+  const PcgState* st;  // beta source / done flag (with p_old)
+  const T* E_elem;     // per-element scale, or null for scalar E
+  double E;
+  const T* interior;   // per-dof multiplier applied to the result, or null
+  double scale;        // global multiplier
+  T* out;
+  const T* add_to;     // when non-null: out = add_to + result
+};
+
+template <typename T>
+int launch_kref_apply(const StencilArgs<T>& a, const Kmat& K, cudaStream_t s);
+template <typename T>
+int launch_kref_diag(const Mesh& m, const Kmat& K, const T* E_elem, double E, T* out, cudaStream_t s);
+int load_K(const double* K_host, Kmat* K);
+
+// Element-strip passes and node gather (strip.cu).
+template <typename T, int MODE>
+int launch_strip(const StripArgs<T>& args, const Kpair<T>* kp, cudaStream_t s);
+template <typename T>
+int launch_gather(const Mesh& m, const T* ev, T* out, cudaStream_t s);
+long long strip_grid_blocks(const Mesh& m);
+
+// PCG pieces (pcg.cu).
+template <typename T>
+int launch_pcg_init(const T* b, const T* Ax, const T* Minv, long long n, T* r, T* z, T* p, bool p_is_z, T* x0,
+                    PcgState* st, GridReduce red, int max_iter, double tol, cudaStream_t s);
+template <typename T>
+int launch_pcg_gather(const Mesh& m, const T* ev, const T* z, T* p, T* Ap, PcgState* st, GridReduce red,
+                      cudaStream_t s);
+template <typename T>
+int launch_pcg_update(const T* p, const T* Ap, const T* Minv, long long n, T* x, T* r, T* z, PcgState* st,
+                      GridReduce red, cudaStream_t s);
+
+// Sampling and statistics (sample.cu).
+template <typename T>
+struct SampleArgs {
+  Mesh m;
+  int EX;
+  const T* U;             // nodal displacement (Ndof)
+  const T* g;             // deformed image, vox layout (gnx*gny*gnz)
+  int gnx, gny, gnz;
+  T gx0, gy0, gz0;        // origin of g in f's voxel frame
+  const uint8_t* mask0;   // may be null (all ones)
+  T glt;
+  T* gvals;               // out (Nvox)
+  uint8_t* mask_out;      // out (Nvox)
+  // GN extras (stats != null): stats of g over the b mask and the active count
+  const uint8_t* bmask_frozen;  // null: b mask = live mask
+  uint8_t* freeze_out;          // non-null: also write the live mask here (freezing now)
+  GridReduce red;
+  double* stats;                // out: count, s1, s2 over the b mask, n_active
+  // interp mode (uvox != null): write u(x) instead of sampling
+  T* uvox;
+  int channels_first;
+};
+template <typename T, bool STATS, bool INTERP>
+int launch_sample(const SampleArgs<T>& args, cudaStream_t s);
+template <typename T>
+int launch_masked_stats(const T* field, const uint8_t* mask, const Mesh& m, GridReduce red, double* out3,
+                        cudaStream_t s);
+
+inline int grid_blocks(long long n, int threads, long long cap) {
+  long long b = (n + threads - 1) / threads;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace vdvc

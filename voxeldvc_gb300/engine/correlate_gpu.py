@@ -1,0 +1,537 @@
+"""Matrix-free Gauss-Newton DVC correlation on the GPU.
+
+Drop-in counterpart of the reference module engine/correlate_gpu.py: the
+same public functions with the same arguments and printed output.  The GN
+iteration itself runs in a device-resident solver object of libvdvc.so
+(one sample/rhs/pcg/update round per iteration, one host read-back of a
+few scalars per iteration); images travel to the GPU once and the pyramid
+levels are decimated there.
+
+`xp` chooses the type of the returned arrays (numpy -> numpy, anything else
+-> torch CUDA tensors).  Images may be numpy arrays or torch tensors in the
+reference's pix[x,y,z] C-order layout.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .. import _device as D
+from .. import _lib
+from .geometry_dvc import build_N_stencil, build_interior_dof_mask
+from . import kernels_dvc as K
+
+
+# ---------------------------------------------------------------------------
+# image layout helpers
+# ---------------------------------------------------------------------------
+
+def _pix_code_and_tensor(pix):
+    """(device tensor holding pix's bytes, libvdvc element code, shape)."""
+    T = D.torch()
+    if D.is_tensor(pix):
+        t = pix if pix.is_cuda else pix.to(D.device())
+        t = t.contiguous()
+        npd = D.np_dtype_of(t)
+        if npd == np.bool_:
+            t = t.to(T.uint8)
+            npd = np.dtype(np.uint8)
+        if npd == np.int64:
+            t = t.to(T.int32)
+            npd = np.dtype(np.int32)
+        return t, D.code_of(npd), tuple(t.shape)
+    a = np.asarray(pix)
+    if a.dtype == np.bool_:
+        a = a.astype(np.uint8)
+    if a.dtype not in (np.float32, np.float64, np.uint8, np.uint16, np.int16, np.int32):
+        a = a.astype(np.float64)
+    a = np.ascontiguousarray(a)
+    shape = a.shape
+    raw = T.from_numpy(a.reshape(-1).view(np.uint8)).to(D.device())
+    return raw, D.code_of(a.dtype), shape
+
+
+def pix_to_vox(pix, dtype=np.float32):
+    """Device copy of pix[x,y,z] in vox layout (x fastest), cast to dtype.
+    Returns (tensor (Nvox,), shape)."""
+    t, code, shape = _pix_code_and_tensor(pix)
+    if len(shape) != 3:
+        raise ValueError(f"expected a 3-D volume, got shape {shape}")
+    nx, ny, nz = shape
+    out = D.empty(nx * ny * nz, dtype)
+    _lib.check(_lib.lib().vdvc_pix_to_vox(t.data_ptr(), code, nx, ny, nz, out.data_ptr(), D.code_of(dtype),
+                                          D.stream()), "pix_to_vox")
+    return out, (nx, ny, nz)
+
+
+def _vox_to_pix_host(vox, shape):
+    return D.out(vox, np).reshape(shape[2], shape[1], shape[0]).transpose(2, 1, 0)
+
+
+def _decimate(vox, shape, s, dtype):
+    nx, ny, nz = shape
+    if s == 1:
+        return vox, shape
+    o = ((nx + s - 1) // s, (ny + s - 1) // s, (nz + s - 1) // s)
+    out = D.empty(o[0] * o[1] * o[2], dtype)
+    _lib.check(_lib.lib().vdvc_decimate(vox.data_ptr(), D.code_of(dtype), nx, ny, nz, s, out.data_ptr(),
+                                        D.stream()), "decimate")
+    return out, o
+
+
+def _dot(a, b=None):
+    """float64 sum(a*b) or sum(a) on the device (one host sync)."""
+    dt = D.np_dtype_of(a)
+    ws = D.scratch.get(1 << 16)
+    out = C.c_double(0.0)
+    _lib.check(_lib.lib().vdvc_dot(a.data_ptr(), D.ptr(b), D.code_of(dt), a.numel(), C.byref(out), ws.data_ptr(),
+                                   ws.numel(), D.stream()), "dot")
+    return out.value
+
+
+# ---------------------------------------------------------------------------
+# reference-image preparation (correlate_gpu.py:49-157)
+# ---------------------------------------------------------------------------
+
+def _grad_vox(f_vox, shape, dtype, glt=None):
+    nx, ny, nz = shape
+    grad = D.empty(3 * nx * ny * nz, dtype)
+    mask0 = D.empty(nx * ny * nz, np.uint8) if glt is not None else None
+    _lib.check(_lib.lib().vdvc_image_grad(f_vox.data_ptr(), D.code_of(dtype), nx, ny, nz,
+                                          float(glt if glt is not None else 0.0), grad.data_ptr(), D.ptr(mask0),
+                                          D.stream()), "image_grad")
+    return grad, mask0
+
+
+def image_grad_and_values(pix, xp, dtype=np.float32):
+    """(f_vox (Nvox,), grad_f_vox (Nvox, 3)): values and xp.gradient of the
+    image, x-fastest voxel order."""
+    dtype = np.dtype(dtype)
+    f_vox, shape = pix_to_vox(pix, dtype)
+    grad, _ = _grad_vox(f_vox, shape, dtype)
+    return D.out(f_vox, xp), D.out(grad.reshape(-1, 3), xp)
+
+
+def erode_mask0_vox(mask0_vox, Nvx, Nvy, Nvz, xp):
+    """6-neighbour erosion (minimum filter, mode 'nearest') of a voxel mask."""
+    m = D.mask_u8(mask0_vox).reshape(-1)
+    if m.numel() != Nvx * Nvy * Nvz:
+        raise ValueError("mask size does not match (Nvx, Nvy, Nvz)")
+    out = D.empty(m.numel(), np.uint8)
+    _lib.check(_lib.lib().vdvc_erode_mask(m.data_ptr(), Nvx, Nvy, Nvz, out.data_ptr(), D.stream()), "erode")
+    return D.out(out.to(D.torch().bool), xp)
+
+
+def _stats_sums(field, mask, h, Nx, Ny, Nz):
+    dt = D.np_dtype_of(field)
+    sums = D.empty(3, np.float64)
+    ws = D.scratch.get(1 << 16)
+    _lib.check(_lib.lib().vdvc_masked_stats(field.data_ptr(), D.code_of(dt), mask.data_ptr(), h, Nx, Ny, Nz,
+                                            sums.data_ptr(), ws.data_ptr(), ws.numel(), D.stream()), "masked_stats")
+    return sums.cpu().numpy()
+
+
+def _mean_std(c, s1, s2):
+    # engine/correlate_gpu.py:152-157
+    if c < 1:
+        return 0.0, 0.0
+    mean = float(s1) / c
+    var = float(s2) / c - mean * mean
+    return mean, (var if var > 0.0 else 0.0) ** 0.5
+
+
+def masked_quadpoint_mean_std(field_vox, mask_vox, h, Nx, Ny, Nz, xp, chunk_size=None):
+    """Mean and population std of field_vox over the (element, stencil
+    point) array restricted to mask_vox (float64 sums)."""
+    dt = K._float_dtype(field_vox)
+    f = D.to_device(field_vox, dt).reshape(-1)
+    m = D.mask_u8(mask_vox).reshape(-1)
+    c, s1, s2 = _stats_sums(f, m, h, Nx, Ny, Nz)
+    return _mean_std(c, s1, s2)
+
+
+def gather_quadpoint_values(field_vox, h, Nx, Ny, Nz, xp):
+    """(Ne*(h+1)^3,) per-(element, stencil point) copy of a voxel field.
+    A host-side index gather kept for API compatibility (the solve itself
+    never materialises it)."""
+    vals = np.asarray(D.out(D.to_device(field_vox), np)).reshape(-1)
+    Ne = Nx * Ny * Nz
+    offs = np.asarray(K.get_voxel_offsets(h, Nx, Ny, np))
+    org = np.asarray(K.get_elem_voxel_origins(np.arange(Ne, dtype=np.int32), h, Nx, Ny, np))
+    out = vals[(org[:, None] + offs[None, :]).reshape(-1)]
+    return out if D.wants_host(xp) else D.to_device(out)
+
+
+def interp_field_vox(U, N_stencil, h, Nx, Ny, Nz, xp, chunk_size=200_000, channels_first=False):
+    """u(x) = sum_a N_a U_a at every voxel centre: (Nvox, 3) or (3, Nvox)."""
+    dt = K._float_dtype(U)
+    Ud = D.to_device(U, dt).reshape(-1)
+    Nvox, Ndof = K._mesh_sizes(h, Nx, Ny, Nz)
+    if Ud.numel() != Ndof:
+        raise ValueError(f"U has {Ud.numel()} entries, expected {Ndof}")
+    out = D.empty(3 * Nvox, dt)
+    _lib.check(_lib.lib().vdvc_interp_field(Ud.data_ptr(), D.code_of(dt), h, Nx, Ny, Nz, int(bool(channels_first)),
+                                            out.data_ptr(), D.stream()), "interp_field_vox")
+    out = out.reshape(3, Nvox) if channels_first else out.reshape(Nvox, 3)
+    return D.out(out, xp)
+
+
+def _sample(U, g_vox, gshape, h, Nx, Ny, Nz, g_origin, mask0, glt, dt):
+    Nvox, Ndof = K._mesh_sizes(h, Nx, Ny, Nz)
+    g_vals = D.empty(Nvox, dt)
+    mask = D.empty(Nvox, np.uint8)
+    gx0, gy0, gz0 = g_origin
+    _lib.check(_lib.lib().vdvc_sample_deformed(U.data_ptr(), g_vox.data_ptr(), D.code_of(dt), gshape[0], gshape[1],
+                                               gshape[2], float(gx0), float(gy0), float(gz0), D.ptr(mask0),
+                                               float(glt), h, Nx, Ny, Nz, g_vals.data_ptr(), mask.data_ptr(),
+                                               D.stream()), "sample_deformed_field")
+    return g_vals, mask
+
+
+def sample_deformed_field(U, g_pix_x, N_stencil, h, Nx, Ny, Nz, xp, g_origin=(0, 0, 0), mask0_vox=None,
+                          chunk_size=None, glt=0.0):
+    """(g_vals, mask_vox): g sampled at x + u(x) (order-1, clipped) and the
+    active mask in_bounds & mask0 & g > glt."""
+    dt = K._float_dtype(U)
+    Ud = D.to_device(U, dt).reshape(-1)
+    g_vox, gshape = pix_to_vox(g_pix_x, dt)
+    m0 = None if mask0_vox is None else D.mask_u8(mask0_vox).reshape(-1)
+    g_vals, mask = _sample(Ud, g_vox, gshape, h, Nx, Ny, Nz, g_origin, m0, glt, dt)
+    return D.out(g_vals, xp), D.out(mask.to(D.torch().bool), xp)
+
+
+def compute_active_mask(U, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0), mask0_vox=None, glt=0.0):
+    """Per-voxel active mask (mask0 & in_bounds(x+u) & g(x+u) > glt)."""
+    _, mask = sample_deformed_field(U, g_pix, None, h, Nx, Ny, Nz, D.torch(), g_origin=g_origin,
+                                    mask0_vox=mask0_vox, glt=glt)
+    return D.out(mask, xp)
+
+
+def compute_b_gpu(res_vox, mask_vox, grad_f_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, Ndof, xp, chunk_size=None):
+    """b = sum_e P_e^T sum_q w_q m_q res_q N_q (x) grad f_q."""
+    K._check_stencil(N_stencil, w_stencil, h)
+    Nvox, nd = K._mesh_sizes(h, Nx, Ny, Nz)
+    dt = K._float_dtype(grad_f_vox)
+    cdt = K._float_dtype(grad_f_vox, res_vox)
+    g, m = K._grad_mask(grad_f_vox, mask_vox, cdt, Nvox)
+    r = D.to_device(res_vox, cdt).reshape(-1)
+    out = D.empty(Ndof, cdt)
+    ws, n = K._ws(cdt, h, Nx, Ny, Nz)
+    _lib.check(_lib.lib().vdvc_compute_b(r.data_ptr(), m.data_ptr(), g.data_ptr(), D.code_of(cdt), h, Nx, Ny, Nz,
+                                         out.data_ptr(), ws.data_ptr(), n, D.stream()), "compute_b_gpu")
+    if cdt != dt:
+        out = out.to(D.torch_dtype(dt))  # the reference accumulates into a grad-dtype array
+    return D.out(out, xp)
+
+
+# ---------------------------------------------------------------------------
+# FFT pre-alignment (correlate_gpu.py:381-414)
+# ---------------------------------------------------------------------------
+
+def _fft_shift_vox(f_vox, fshape, g_vox, gshape, dt):
+    d = (C.c_double * 3)()
+    _lib.check(_lib.lib().vdvc_fft_rigid_shift(f_vox.data_ptr(), *fshape, g_vox.data_ptr(), *gshape, D.code_of(dt),
+                                               C.cast(d, _lib.pd), D.stream()), "fft_rigid_shift")
+    return np.array([d[0], d[1], d[2]], dtype=np.float64)
+
+
+def fft_rigid_shift(f_pix, g_pix, xp):
+    """Integer voxel shift d with g(x) ~= f(x - d) by phase correlation."""
+    f_vox, fs = pix_to_vox(f_pix, np.float64)
+    g_vox, gs = pix_to_vox(g_pix, np.float64)
+    return _fft_shift_vox(f_vox, fs, g_vox, gs, np.float64)
+
+
+# ---------------------------------------------------------------------------
+# Gauss-Newton solve at one level (correlate_gpu.py:828-1140)
+# ---------------------------------------------------------------------------
+
+class _Level:
+    """Device inputs of one pyramid level, kept alive for the solver."""
+
+    def __init__(self, f_vox, fshape, g_vox, gshape):
+        self.f_vox, self.fshape, self.g_vox, self.gshape = f_vox, fshape, g_vox, gshape
+
+
+def _plane_wave(Nx, Ny, Nz, h, dtype):
+    # V = cos(j h / T 2 pi) on the x components, T = 10 h, evaluated in the
+    # solve dtype (correlate_gpu.py:1016-1020)
+    T = 10 * h
+    nn = (Nx + 1) * (Ny + 1) * (Nz + 1)
+    jj = (np.arange(nn) // (Nx + 1)) % (Ny + 1)
+    Vs = np.cos(jj.astype(dtype) * h / T * 2 * np.pi)
+    V = np.zeros(3 * nn, dtype=dtype)
+    V[0::3] = Vs
+    return V
+
+
+def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
+                 c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False,
+                 freeze_mask_after=None, U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
+                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None):
+    dtype = np.dtype(dtype)
+    Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, Nz * h + 1
+    Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    Nvox = Nvx * Nvy * Nvz
+    if Nvox > np.iinfo(np.int32).max or Ndof > np.iinfo(np.int32).max:
+        raise ValueError(
+            "Nvox=%d / Ndof=%d exceed int32 range; matrix-free index "
+            "arrays assume int32 indices" % (Nvox, Ndof))
+    if tuple(lv.fshape) != (Nvx, Nvy, Nvz):
+        raise ValueError(f"f_pix has shape {tuple(lv.fshape)}, expected (Nx*h+1, Ny*h+1, Nz*h+1) = "
+                         f"{(Nvx, Nvy, Nvz)}")
+    L = _lib.lib()
+    grad, mask0 = _grad_vox(lv.f_vox, lv.fshape, dtype, glt)
+    c0, s10, s20 = _stats_sums(lv.f_vox, mask0, h, Nx, Ny, Nz)
+    mean0, std0 = _mean_std(c0, s10, s20)
+
+    N_stencil, w_stencil = build_N_stencil(h)
+    if reg_type not in ('laplacian', 'equilibrium_gap'):
+        raise ValueError("reg_type must be 'laplacian' or 'equilibrium_gap'")
+
+    interior = None
+    diag_eq = None
+    if reg_type == 'equilibrium_gap':
+        interior = D.to_device(build_interior_dof_mask(Nx, Ny, Nz), dtype)
+
+    ll = 0.0
+    reg_code = _lib.REG_NONE
+    if l0 is not None:
+        if K_ref_laplacian is None:
+            raise ValueError("K_ref_laplacian is required when l0 is given")
+        if reg_type == 'equilibrium_gap' and K_ref_elastic is None:
+            raise ValueError("K_ref_elastic is required when l0 is given and "
+                             "reg_type='equilibrium_gap'")
+        T_ = 10 * h
+        if reg_type == 'equilibrium_gap':
+            reg_code = _lib.REG_EQUILIBRIUM_GAP
+            diag_eq = K.build_diagonal_equilibrium_gap(K_ref_elastic, interior.to(D.torch().float64), h, Nx, Ny, Nz,
+                                                       Ndof, D.torch())
+            dH = K.build_diagonal_H(grad.reshape(-1, 3), mask0, N_stencil, w_stencil, h, Nx, Ny, Nz, Ndof,
+                                    D.torch())
+            dlap = K.build_diagonal_K_ref(K_ref_laplacian, h, Nx, Ny, Nz, Ndof, D.torch())
+            H0 = _dot(dH)
+            L0 = _dot(diag_eq) + eps_reg * _dot(dlap)
+        else:
+            reg_code = _lib.REG_LAPLACIAN
+            V = D.to_device(_plane_wave(Nx, Ny, Nz, h, dtype))
+            Hv = K.matvec_H(V, grad.reshape(-1, 3), mask0, N_stencil, w_stencil, h, Nx, Ny, Nz, D.torch())
+            Lv = K.matvec_K_ref(V, K_ref_laplacian, h, Nx, Ny, Nz, D.torch())
+            H0 = _dot(V, Hv)
+            L0 = _dot(V, Lv)
+        ll = c_reg * (l0 / T_) ** reg_exponent * H0 / L0
+        if disp:
+            print('Regularization: %s with lambda = %2.3e' % (reg_type, ll))
+    else:
+        if disp:
+            print('Regularization: None')
+
+    out_dt = np.dtype(np.float64) if (l0 is not None or dtype == np.float64) else dtype
+    # U0 is read in the solve dtype (correlate_gpu.py:1037), kept as float64
+    U64 = D.zeros(Ndof, np.float64) if U0 is None else \
+        D.to_device(U0, dtype).reshape(-1).to(D.torch().float64)
+    if U64.numel() != Ndof:
+        raise ValueError(f"U0 has {U64.numel()} entries, expected {Ndof}")
+    if maxiter < 1:
+        return U64.to(D.torch_dtype(out_dt)), D.zeros(Nvox, out_dt), D.zeros(Ndof, out_dt), {}
+
+    Klap = np.ascontiguousarray(K_ref_laplacian if K_ref_laplacian is not None else np.zeros((24, 24)),
+                                dtype=np.float64)
+    Kel = np.ascontiguousarray(K_ref_elastic if K_ref_elastic is not None else np.zeros((24, 24)), dtype=np.float64)
+    desc = _lib.GnDesc()
+    desc.dtype = D.code_of(dtype)
+    desc.h, desc.Nx, desc.Ny, desc.Nz = h, Nx, Ny, Nz
+    desc.gnx, desc.gny, desc.gnz = lv.gshape
+    desc.gx0, desc.gy0, desc.gz0 = (float(o) for o in g_origin)
+    desc.glt = float(glt)
+    desc.reg_type = reg_code
+    desc.ll = float(ll)
+    desc.eps_reg = float(eps_reg)
+    desc.K_lap = Klap.ctypes.data_as(_lib.pd)
+    desc.K_el = Kel.ctypes.data_as(_lib.pd)
+    desc.dynamic_mask = int(bool(dynamic_mask))
+    desc.pcg_chunk = int(pcg_chunk)
+    desc.f_vox = lv.f_vox.data_ptr()
+    desc.g_vox = lv.g_vox.data_ptr()
+    desc.grad = grad.data_ptr()
+    desc.mask0 = mask0.data_ptr()
+    desc.interior = D.ptr(interior)
+    desc.diag_eqgap = D.ptr(diag_eq)
+    desc.mean0, desc.std0 = mean0, std0
+    desc.stream = D.stream()
+    nbytes = L.vdvc_gn_workspace_bytes(desc.dtype, h, Nx, Ny, Nz)
+    ws = D.torch().empty(nbytes, dtype=D.torch().uint8, device=D.device())
+    solver = C.c_void_p()
+    _lib.check(L.vdvc_gn_create(C.byref(desc), ws.data_ptr(), nbytes, C.byref(solver)), "correlate_gpu")
+    info = {"gn_iters": 0, "pcg_iters": [], "ll": ll}
+    try:
+        st = D.stream()
+        _lib.check(L.vdvc_gn_set_U(solver, U64.data_ptr(), st), "set_U")
+        if not dynamic_mask:
+            _lib.check(L.vdvc_gn_frozen_diag(solver, st), "frozen_diag")
+        frozen = False
+        out8 = (C.c_double * 8)()
+        iters, pres, pstat = C.c_int(0), C.c_double(0.0), C.c_int(0)
+        for ik in range(maxiter):
+            freeze_now = freeze_mask_after is not None and not frozen and ik >= freeze_mask_after
+            _lib.check(L.vdvc_gn_sample(solver, int(freeze_now), st), "sample")
+            frozen = frozen or freeze_now
+            _lib.check(L.vdvc_gn_rhs(solver, st), "rhs")
+            _lib.check(L.vdvc_gn_pcg(solver, int(pcg_max_iter), float(pcg_tol), C.byref(iters), C.byref(pres),
+                                     C.byref(pstat), st), "pcg")
+            _lib.check(L.vdvc_gn_update(solver, C.cast(out8, _lib.pd), st), "update")
+            info["gn_iters"] = ik + 1
+            info["pcg_iters"].append(iters.value)
+            dd, uu = out8[0], out8[1]
+            with np.errstate(divide='ignore', invalid='ignore'):
+                err = float(np.sqrt(np.float64(dd)) / np.sqrt(np.float64(uu)))
+            if disp:
+                _, stdr = _mean_std(out8[2], out8[3], out8[4])
+                n_active = int(out8[5])
+                print("Iter # %2d | std(res)=%2.2f gl | dU/U=%1.2e | active pts=%d/%d (%.1f%%)"
+                      % (ik + 1, stdr, err, n_active, Nvox, 100 * n_active / Nvox))
+            if err < eps:
+                break
+        Uo = D.empty(Ndof, out_dt)
+        res = D.empty(Nvox, out_dt)
+        dU = D.empty(Ndof, out_dt)
+        f64 = int(out_dt == np.float64)
+        _lib.check(L.vdvc_gn_read(solver, _lib.GN_U, Uo.data_ptr(), f64, st), "read")
+        _lib.check(L.vdvc_gn_read(solver, _lib.GN_RES, res.data_ptr(), f64, st), "read")
+        _lib.check(L.vdvc_gn_read(solver, _lib.GN_DU, dU.data_ptr(), f64, st), "read")
+    finally:
+        L.vdvc_gn_destroy(solver)
+        D.torch().cuda.current_stream().synchronize()
+        del ws
+    if stats is not None:
+        stats.append(info)
+    return Uo, res, dU, info
+
+
+def correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0),
+                  glt=0.0,
+                  l0=None, K_ref_laplacian=None, reg_exponent=2, c_reg=1.0,
+                  reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3,
+                  dynamic_mask=False, freeze_mask_after=None, U0=None,
+                  maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
+                  disp=True, dtype=np.float32, **solver_opts):
+    """Matrix-free GN-PCG DVC solve of f_pix/g_pix on an (Nx,Ny,Nz) mesh of
+    edge h; returns (U, res, dU) as in the reference."""
+    dtype = np.dtype(dtype)
+    f_vox, fs = pix_to_vox(f_pix, dtype)
+    g_vox, gs = pix_to_vox(g_pix, dtype)
+    U, res, dU, _ = _solve_level(_Level(f_vox, fs, g_vox, gs), Nx, Ny, Nz, h, g_origin=g_origin, glt=glt, l0=l0,
+                                 K_ref_laplacian=K_ref_laplacian, reg_exponent=reg_exponent, c_reg=c_reg,
+                                 reg_type=reg_type, K_ref_elastic=K_ref_elastic, eps_reg=eps_reg,
+                                 dynamic_mask=dynamic_mask, freeze_mask_after=freeze_mask_after, U0=U0,
+                                 maxiter=maxiter, eps=eps, pcg_tol=pcg_tol, pcg_max_iter=pcg_max_iter, disp=disp,
+                                 dtype=dtype, **solver_opts)
+    return D.out(U, xp), D.out(res, xp), D.out(dU, xp)
+
+
+def _affine_U0(A_aff, t_aff, c_aff, s, h_i, Nx, Ny, Nz):
+    # u_i(X_i) = A (X_i - c_i) + c_i + t_i - X_i at the nodes, c_i = c/s,
+    # t_i = t/s (correlate_gpu.py:1264-1281); float64 on the host
+    c_i = c_aff / s
+    t_i = t_aff / s
+    n_nodes = (Nx + 1) * (Ny + 1) * (Nz + 1)
+    node = np.arange(n_nodes)
+    X = np.stack([node % (Nx + 1), (node // (Nx + 1)) % (Ny + 1), node // ((Nx + 1) * (Ny + 1))],
+                 axis=1).astype(np.float64) * h_i
+    u = (X - c_i) @ A_aff.T + c_i + t_i - X
+    return u.reshape(-1)
+
+
+def multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, scales=(2, 1, 0),
+                             g_origin=(0, 0, 0), l0=None, fft_prealign=True,
+                             prealign_affine=False, ext_affine=None,
+                             **kwargs):
+    """Coarse-to-fine pyramid of correlate_gpu solves (strided decimation by
+    2**iscale, fixed element grid, h_i = h / 2**iscale, U carried between
+    levels); returns the finest level's (U, res, dU)."""
+    scales = sorted(set(scales), reverse=True)
+    dtype = np.dtype(kwargs.get('dtype', np.float32))
+    disp = kwargs.get('disp', True)
+    # The reference checks each level as it reaches it (correlate_gpu.py:
+    # 1248-1254).  Levels run coarsest first and divisibility by 2**i implies
+    # it for every smaller i, so the first failing level is always the first
+    # level: checking all of them here raises the same error at the same
+    # point, before any image reaches the device.
+    for iscale in scales:
+        s = 2 ** iscale
+        if h % s != 0:
+            raise ValueError("h=%d not divisible by 2**%d=%d" % (h, iscale, s))
+        if any(o % s != 0 for o in g_origin):
+            raise ValueError("g_origin=%r not divisible by 2**%d=%d for all "
+                             "requested scales" % (g_origin, iscale, s))
+
+    A_aff = t_aff = c_aff = None
+    if ext_affine is not None:
+        A_aff, t_aff, c_aff = ext_affine
+        A_aff = np.asarray(A_aff, dtype=np.float64)
+        t_aff = np.asarray(t_aff, dtype=np.float64)
+        c_aff = np.asarray(c_aff, dtype=np.float64)
+        if disp:
+            print("External affine: t = (%.1f, %.1f, %.1f) voxels, "
+                  "c = (%.1f, %.1f, %.1f)" % (*t_aff, *c_aff))
+    elif prealign_affine:
+        A_aff, t_aff, c_aff, aff_info = affine_prealign(f_pix, g_pix, xp)
+        if disp:
+            rx, ry, rz = (180 / np.pi) * np.array([
+                np.arctan2(A_aff[2, 1], A_aff[2, 2]),
+                np.arctan2(-A_aff[2, 0], np.hypot(A_aff[2, 1], A_aff[2, 2])),
+                np.arctan2(A_aff[1, 0], A_aff[0, 0])])
+            sx, sy, sz = np.linalg.norm(A_aff, axis=0)
+            print("Affine pre-alignment (full res): rotation (deg) = (%.3f, %.3f, %.3f), "
+                  "scale = (%.4f, %.4f, %.4f), t = (%.1f, %.1f, %.1f) voxels "
+                  "(1-ZNCC %.4f -> %.4f)"
+                  % (rx, ry, rz, sx, sy, sz, t_aff[0], t_aff[1], t_aff[2],
+                     aff_info['cost_translation_only'], aff_info['cost_final']))
+
+    # full-resolution images on the device once, vox layout, solve dtype
+    f_full, fs = pix_to_vox(f_pix, dtype)
+    g_full, gs = pix_to_vox(g_pix, dtype)
+
+    U = None
+    prev_s = None
+    res = dU = None
+    for iscale in scales:
+        s = 2 ** iscale
+        h_i = h // s
+        f_i, fs_i = _decimate(f_full, fs, s, dtype)
+        g_i, gs_i = _decimate(g_full, gs, s, dtype)
+        g_origin_i = tuple(o // s for o in g_origin)
+        l0_i = None if l0 is None else l0 / s
+
+        if U is not None:
+            # the reference rescales the promoted U, and the next level
+            # re-reads it in the solve dtype (correlate_gpu.py:1263, :1037)
+            U = (U * (prev_s / s)).to(D.torch_dtype(dtype))
+        elif A_aff is not None:
+            U = D.to_device(_affine_U0(A_aff, t_aff, c_aff, s, h_i, Nx, Ny, Nz).astype(dtype))
+        elif fft_prealign:
+            d = _fft_shift_vox(f_i, fs_i, g_i, gs_i, dtype)
+            n_nodes = (Nx + 1) * (Ny + 1) * (Nz + 1)
+            Uh = np.zeros(3 * n_nodes, dtype=dtype)
+            Uh[0::3], Uh[1::3], Uh[2::3] = d[0], d[1], d[2]
+            U = D.to_device(Uh)
+            if disp:
+                print("FFT pre-alignment: rigid shift d = (%.1f, %.1f, %.1f) voxels"
+                      % (d[0] * s, d[1] * s, d[2] * s))
+
+        if disp:
+            print("=== MULTISCALE: scale 2^%d (image decimated by %d, h_i=%d/%d=%d) ==="
+                  % (iscale, s, h, s, h_i))
+        U, res, dU, _ = _solve_level(_Level(f_i, fs_i, g_i, gs_i), Nx, Ny, Nz, h_i, g_origin=g_origin_i, l0=l0_i,
+                                     U0=U, **kwargs)
+        prev_s = s
+    return D.out(U, xp), D.out(res, xp), D.out(dU, xp)
+
+
+def affine_prealign(*args, **kwargs):
+    raise NotImplementedError("affine_prealign is not built yet")
+
+
+def affine_refine_gn(*args, **kwargs):
+    raise NotImplementedError("affine_refine_gn is not built yet")

@@ -1,0 +1,304 @@
+"""Matrix-free operators and PCG of the DVC Hessian and regularizers.
+
+Drop-in counterpart of the reference module engine/kernels_dvc.py: same
+function names and positional layout.  Every operator runs on the GPU
+through libvdvc.so; `xp` selects the type of the returned arrays (numpy ->
+host numpy arrays, anything else -> torch CUDA tensors), inputs may be
+numpy arrays or torch tensors.  `chunk_size` is accepted and ignored: the
+kernels work on whole meshes.
+
+Dtype behaviour follows the reference: an operator computes in the
+promoted type of its floating inputs and returns the dtype the reference
+returns (v.dtype for matvecs, grad dtype for diag H).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .. import _device as D
+from .. import _lib
+from .geometry_dvc import build_N_stencil
+
+# ---------------------------------------------------------------------------
+# Implicit connectivity (kernels_dvc.py:32-89) -- index tables for callers;
+# the kernels compute the same indices in registers.
+# ---------------------------------------------------------------------------
+
+_CORNER_NODE_OFFSETS = ((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1))
+
+
+def _host_index(x):
+    return x.detach().cpu().numpy() if D.is_tensor(x) else np.asarray(x)
+
+
+def _index_out(a, xp, like=None):
+    if D.wants_host(xp) and not D.is_tensor(like):
+        return a
+    return D.to_device(a)
+
+
+def get_elem_dofs(elem_ids, Nx, Ny, xp):
+    """(chunk, 24) dof ids, node-major with the Hex8 corner order."""
+    e = _host_index(elem_ids)
+    i, j, k = e % Nx, (e // Nx) % Ny, e // (Nx * Ny)
+    base = i + j * (Nx + 1) + k * (Nx + 1) * (Ny + 1)
+    offs = np.array([dx + dy * (Nx + 1) + dz * (Nx + 1) * (Ny + 1) for dx, dy, dz in _CORNER_NODE_OFFSETS],
+                    dtype=e.dtype)
+    nodes = base[:, None] + offs[None, :]
+    dofs = (3 * nodes[:, :, None] + np.arange(3, dtype=e.dtype)[None, None, :]).reshape(-1, 24)
+    return _index_out(dofs, xp, elem_ids)
+
+
+def get_voxel_offsets(h, Nx, Ny, xp):
+    """((h+1)^3,) flat voxel offsets of the stencil points (meshgrid 'ij')."""
+    Nvx, Nvy = Nx * h + 1, Ny * h + 1
+    q = np.arange(h + 1, dtype=np.int32)
+    offs = (q[:, None, None] + q[None, :, None] * Nvx + q[None, None, :] * (Nvx * Nvy)).reshape(-1)
+    return _index_out(offs.astype(np.int32), xp)
+
+
+def get_elem_voxel_origins(elem_ids, h, Nx, Ny, xp):
+    """Flat voxel index of each element's q = (0,0,0) voxel."""
+    e = _host_index(elem_ids)
+    Nvx, Nvy = Nx * h + 1, Ny * h + 1
+    i, j, k = e % Nx, (e // Nx) % Ny, e // (Nx * Ny)
+    return _index_out(h * (i + j * Nvx + k * Nvx * Nvy), xp, elem_ids)
+
+
+def auto_chunk_size(nq, max_tensor_elems=20_000_000):
+    """Element-chunk size of the reference's chunked loops (kept for API
+    compatibility; the kernels here do not chunk)."""
+    return max(1, max_tensor_elems // (nq * 24))
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+
+def _float_dtype(*arrays):
+    dt = np.result_type(*[D.np_dtype_of(a) for a in arrays])
+    if dt not in (np.float32, np.float64):
+        dt = np.dtype(np.float64) if dt.kind == 'f' and dt.itemsize > 4 else np.dtype(np.float32)
+    return np.dtype(dt)
+
+
+def _check_stencil(N_stencil, w_stencil, h):
+    """The kernels evaluate the standard voxel-centre Hex8 stencil in
+    registers; refuse any other table instead of silently ignoring it."""
+    N = _host_index(N_stencil)
+    w = _host_index(w_stencil)
+    nq = (h + 1) ** 3
+    if N.shape != (nq, 8) or w.shape != (nq,):
+        raise ValueError(f"N_stencil/w_stencil must have shapes ({nq}, 8)/({nq},) for h={h}")
+    Nr, wr = build_N_stencil(h)
+    tol = 1e-6 if N.dtype == np.float32 else 1e-12
+    if not (np.allclose(N, Nr, rtol=0, atol=tol) and np.allclose(w, wr, rtol=0, atol=tol)):
+        raise ValueError("only the voxel-centre Hex8 stencil of build_N_stencil(h) is supported")
+
+
+def _mesh_sizes(h, Nx, Ny, Nz):
+    Nvox = (Nx * h + 1) * (Ny * h + 1) * (Nz * h + 1)
+    Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    return Nvox, Ndof
+
+
+def _ws(dtype, h, Nx, Ny, Nz):
+    n = _lib.lib().vdvc_workspace_bytes(D.code_of(dtype), h, Nx, Ny, Nz)
+    if n == 0:
+        _lib.check(_lib.ERR_ARG, "workspace size query")
+    return D.scratch.get(n), n
+
+
+def _kmat(K):
+    K = np.ascontiguousarray(_host_index(K), dtype=np.float64)
+    if K.shape != (24, 24):
+        raise ValueError("K_ref must be 24x24")
+    return K, K.ctypes.data_as(_lib.pd)
+
+
+def _E_args(E_elem, Ne, dtype):
+    """(device array or None, scalar) for a per-element modulus argument."""
+    if D.is_tensor(E_elem) or (np.ndim(E_elem) > 0 and np.size(E_elem) > 1):
+        a = D.to_device(E_elem, dtype).reshape(-1)
+        if a.numel() != Ne:
+            raise ValueError(f"E_elem has {a.numel()} entries, expected {Ne}")
+        return a, 0.0
+    return None, float(np.asarray(_host_index(E_elem)).reshape(-1)[0])
+
+
+# ---------------------------------------------------------------------------
+# Regularizer operators (kernels_dvc.py:349-437)
+# ---------------------------------------------------------------------------
+
+def matvec_K_ref(v, K_ref, E_elem, Nx, Ny, Nz, xp, chunk_size=500_000):
+    """f = sum_e E_e P_e^T K_ref P_e v (node-centric stencil, no scatter)."""
+    out_dt = D.np_dtype_of(v)
+    dt = _float_dtype(v)
+    vd = D.to_device(v, dt).reshape(-1)
+    Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    if vd.numel() != Ndof:
+        raise ValueError(f"v has {vd.numel()} entries, expected Ndof={Ndof}")
+    Kh, Kp = _kmat(K_ref)
+    Ed, Es = _E_args(E_elem, Nx * Ny * Nz, dt)
+    out = D.empty(Ndof, dt)
+    L = _lib.lib()
+    _lib.check(L.vdvc_matvec_K_ref(vd.data_ptr(), D.code_of(dt), Kp, D.ptr(Ed), Es, Nx, Ny, Nz, out.data_ptr(),
+                                   D.stream()), "matvec_K_ref")
+    if out_dt != dt and out_dt.kind == 'f':
+        out = out.to(D.torch_dtype(out_dt))
+    return D.out(out, xp)
+
+
+def build_diagonal_K_ref(K_ref, E_elem, Nx, Ny, Nz, Ndof, xp):
+    """Diagonal of the K_ref operator (float64, like the reference's
+    np.diag of the float64 K_ref)."""
+    Kh, Kp = _kmat(K_ref)
+    dt = np.dtype(np.float64)
+    Ed, Es = _E_args(E_elem, Nx * Ny * Nz, dt)
+    out = D.empty(Ndof, dt)
+    _lib.check(_lib.lib().vdvc_diag_K_ref(D.code_of(dt), Kp, D.ptr(Ed), Es, Nx, Ny, Nz, out.data_ptr(),
+                                          D.stream()), "build_diagonal_K_ref")
+    return D.out(out, xp)
+
+
+def matvec_equilibrium_gap(v, K_ref_elastic, interior_mask, E_elem, Nx, Ny, Nz, xp, chunk_size=500_000):
+    """f = K (P_i (K v)), K = sum_e E_e P_e^T K_el P_e."""
+    out_dt = D.np_dtype_of(v)
+    dt = _float_dtype(v, interior_mask) if D.np_dtype_of(interior_mask).kind == 'f' else _float_dtype(v)
+    vd = D.to_device(v, dt).reshape(-1)
+    Pi = D.to_device(interior_mask, dt).reshape(-1)
+    Kh, Kp = _kmat(K_ref_elastic)
+    Ed, Es = _E_args(E_elem, Nx * Ny * Nz, dt)
+    Ndof = vd.numel()
+    out = D.empty(Ndof, dt)
+    ws, n = _ws(dt, 1, Nx, Ny, Nz)
+    _lib.check(_lib.lib().vdvc_matvec_equilibrium_gap(vd.data_ptr(), D.code_of(dt), Kp, Pi.data_ptr(), D.ptr(Ed),
+                                                      Es, Nx, Ny, Nz, out.data_ptr(), ws.data_ptr(), n,
+                                                      D.stream()), "matvec_equilibrium_gap")
+    res_dt = np.result_type(out_dt, dt)
+    if res_dt != dt:
+        out = out.to(D.torch_dtype(res_dt))
+    return D.out(out, xp)
+
+
+def rademacher_probes(Ndof, n_probes=32, seed=0):
+    """The reference's probe sequence: n_probes draws of
+    np.random.default_rng(seed).choice([-1., 1.], size=Ndof), as int8."""
+    rng = np.random.default_rng(seed)
+    z = np.empty((n_probes, Ndof), dtype=np.int8)
+    for p in range(n_probes):
+        z[p] = rng.choice([-1.0, 1.0], size=Ndof).astype(np.int8)
+    return z
+
+
+def build_diagonal_equilibrium_gap(K_ref_elastic, interior_mask, E_elem, Nx, Ny, Nz, Ndof, xp, n_probes=32,
+                                   seed=0):
+    """Hutchinson estimate of diag(K P_i K) with the reference's Rademacher
+    probes (generated on the host with numpy's default_rng(seed), as in
+    kernels_dvc.py:430-433), clipped at 1e-12 max|diag|; float64."""
+    probes = D.to_device(rademacher_probes(Ndof, n_probes, seed))
+    Pi = D.to_device(interior_mask, np.float64).reshape(-1)
+    Kh, Kp = _kmat(K_ref_elastic)
+    Ed, Es = _E_args(E_elem, Nx * Ny * Nz, np.float64)
+    out = D.empty(Ndof, np.float64)
+    ws, n = _ws(np.float64, 1, Nx, Ny, Nz)
+    _lib.check(_lib.lib().vdvc_diag_equilibrium_gap(probes.data_ptr(), n_probes, Kp, Pi.data_ptr(), D.ptr(Ed), Es,
+                                                    Nx, Ny, Nz, out.data_ptr(), ws.data_ptr(), n, D.stream()),
+               "build_diagonal_equilibrium_gap")
+    return D.out(out, xp)
+
+
+# ---------------------------------------------------------------------------
+# Correlation Hessian (kernels_dvc.py:452-543)
+# ---------------------------------------------------------------------------
+
+def _grad_mask(grad_f_vox, mask0_vox, dt, Nvox):
+    g = D.to_device(grad_f_vox, dt).reshape(-1)
+    if g.numel() != 3 * Nvox:
+        raise ValueError(f"grad_f_vox must have shape ({Nvox}, 3)")
+    m = D.mask_u8(mask0_vox).reshape(-1)
+    if m.numel() != Nvox:
+        raise ValueError(f"mask must have {Nvox} entries")
+    return g, m
+
+
+def matvec_H(v, grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, xp, chunk_size=None):
+    """f = H v = sum_e sum_q w_q m_q (v_eq . v_loc) v_eq, matrix-free."""
+    _check_stencil(N_stencil, w_stencil, h)
+    Nvox, Ndof = _mesh_sizes(h, Nx, Ny, Nz)
+    out_dt = D.np_dtype_of(v)
+    dt = _float_dtype(v, grad_f_vox)
+    vd = D.to_device(v, dt).reshape(-1)
+    if vd.numel() != Ndof:
+        raise ValueError(f"v has {vd.numel()} entries, expected Ndof={Ndof}")
+    g, m = _grad_mask(grad_f_vox, mask0_vox, dt, Nvox)
+    out = D.empty(Ndof, dt)
+    ws, n = _ws(dt, h, Nx, Ny, Nz)
+    _lib.check(_lib.lib().vdvc_matvec_H(vd.data_ptr(), g.data_ptr(), m.data_ptr(), D.code_of(dt), h, Nx, Ny, Nz,
+                                        out.data_ptr(), ws.data_ptr(), n, D.stream()), "matvec_H")
+    if out_dt != dt and out_dt.kind == 'f':
+        out = out.to(D.torch_dtype(out_dt))
+    return D.out(out, xp)
+
+
+def build_diagonal_H(grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, Ndof, xp, chunk_size=None):
+    """diag(H)[i] = sum over (e,q) touching dof i of w_q m_q v_eq[i]^2."""
+    _check_stencil(N_stencil, w_stencil, h)
+    Nvox, nd = _mesh_sizes(h, Nx, Ny, Nz)
+    if nd != Ndof:
+        raise ValueError(f"Ndof={Ndof} does not match the mesh ({nd})")
+    dt = _float_dtype(grad_f_vox)
+    g, m = _grad_mask(grad_f_vox, mask0_vox, dt, Nvox)
+    out = D.empty(Ndof, dt)
+    ws, n = _ws(dt, h, Nx, Ny, Nz)
+    _lib.check(_lib.lib().vdvc_diag_H(g.data_ptr(), m.data_ptr(), D.code_of(dt), h, Nx, Ny, Nz, out.data_ptr(),
+                                      ws.data_ptr(), n, D.stream()), "build_diagonal_H")
+    return D.out(out, xp)
+
+
+# ---------------------------------------------------------------------------
+# Preconditioned conjugate gradient (kernels_dvc.py:550-583)
+# ---------------------------------------------------------------------------
+
+def pcg(matvec, b, M_inv, xp, x0=None, max_iter=1000, tol=1e-8, verbose=False):
+    """Jacobi PCG for an arbitrary callable matvec (v -> A v) on device
+    vectors.  The vector updates and the float64 dot products are libvdvc
+    kernels; `matvec` is called with CUDA tensors and may return a CUDA
+    tensor or anything convertible to one.  Solver objects of this package
+    bypass this loop with their fused, graph-replayed PCG."""
+    dt = _float_dtype(b, M_inv)
+    bd = D.to_device(b, dt).reshape(-1)
+    Md = D.to_device(M_inv, dt).reshape(-1)
+    n = bd.numel()
+    x = D.zeros(n, dt) if x0 is None else D.to_device(x0, dt).reshape(-1).clone()
+    r, z, p = D.empty(n, dt), D.empty(n, dt), D.empty(n, dt)
+    L = _lib.lib()
+    ws = D.torch().empty(L.vdvc_pcg_workspace_bytes(), dtype=D.torch().uint8, device=D.device())
+    wsn = ws.numel()
+    code = D.code_of(dt)
+
+    def _apply(v):
+        out = matvec(v)
+        return D.to_device(out, dt).reshape(-1)
+
+    Ax = _apply(x)
+    _lib.check(L.vdvc_pcg_begin(bd.data_ptr(), Ax.data_ptr(), Md.data_ptr(), code, n, r.data_ptr(), z.data_ptr(),
+                                p.data_ptr(), int(max_iter), float(tol), ws.data_ptr(), wsn, D.stream()), "pcg")
+    res = C.c_double(0.0)
+    done = C.c_int(0)
+    for it in range(max_iter):
+        Ap = _apply(p)
+        _lib.check(L.vdvc_pcg_step(Ap.data_ptr(), Md.data_ptr(), code, n, x.data_ptr(), r.data_ptr(),
+                                   z.data_ptr(), p.data_ptr(), ws.data_ptr(), wsn, C.byref(res), C.byref(done),
+                                   D.stream()), "pcg")
+        rv = res.value
+        if verbose and (it % 10 == 0 or it < 5):
+            print(f"  PCG iter {it:4d}  rel.residual = {rv:.3e}")
+        if rv < tol:
+            if verbose:
+                print(f"  Converged at iter {it}, residual = {rv:.3e}")
+            break
+        _lib.check(L.vdvc_pcg_direction(z.data_ptr(), p.data_ptr(), code, n, ws.data_ptr(), wsn, D.stream()), "pcg")
+    return D.out(x, xp)
