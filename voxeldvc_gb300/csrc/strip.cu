@@ -102,6 +102,8 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
     const long long x = (long long)i * h + qxc;
     const T fx1 = s_phi[qxc], fx0 = T(1) - fx1;
     const int mx = (qxc == 0 && i > 0) ? 2 : 1;
+    // outer-face quadrature weight along x (1/2 on the first and last plane)
+    const T wx = (x == 0 || x == (long long)m.Nvx - 1) ? T(0.5) : T(1);
     T ux[12];
     if constexpr (HV) {
 #pragma unroll
@@ -120,6 +122,8 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
     for (int qz = 0; qz < nz_e; ++qz) {
       const T fz1 = s_phi[qz], fz0 = T(1) - fz1;
       const int mxz = mx * ((qz == 0 && k > 0) ? 2 : 1);
+      const int vz = k * h + qz;
+      const T wz = (vz == 0 || vz == m.Nvz - 1) ? T(0.5) : T(1);
       T u0[3], du[3];
       if constexpr (HV) {
 #pragma unroll
@@ -137,12 +141,14 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
       for (int qy = 0; qy < ny_e; ++qy) {
         const T fy1 = s_phi[qy];
         const long long vv = vbase + (long long)qy * m.Nvx;
+        const int vy = j * h + qy;
+        const T wy = (vy == 0 || vy == m.Nvy - 1) ? T(0.5) : T(1);
         const T g0 = a.grad[3 * vv + 0], g1 = a.grad[3 * vv + 1], g2 = a.grad[3 * vv + 2];
         const bool mm = a.mask[vv] != 0;
         if constexpr (HV) {
           const T uu0 = u0[0] + fy1 * du[0], uu1 = u0[1] + fy1 * du[1], uu2 = u0[2] + fy1 * du[2];
           T d = g0 * uu0 + g1 * uu1 + g2 * uu2;
-          d = mm ? d : T(0);
+          d = mm ? d * wy : T(0);
           const T t0 = d * g0, t1 = d * g1, t2 = d * g2;
           S[0] += t0; S[1] += t1; S[2] += t2;
           S1[0] += fy1 * t0; S1[1] += fy1 * t1; S1[2] += fy1 * t2;
@@ -164,13 +170,14 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
           } else {
             r = mm ? a.res_in[vv] : T(0);
           }
+          r *= wy;
           const T t0 = r * g0, t1 = r * g1, t2 = r * g2;
           S[0] += t0; S[1] += t1; S[2] += t2;
           S1[0] += fy1 * t0; S1[1] += fy1 * t1; S1[2] += fy1 * t2;
         }
         if constexpr (DG) {
           const T fy0 = T(1) - fy1;
-          const T w0 = fy0 * fy0, w1 = fy1 * fy1;
+          const T w0 = wy * fy0 * fy0, w1 = wy * fy1 * fy1;
           const T d0 = mm ? g0 * g0 : T(0), d1 = mm ? g1 * g1 : T(0), d2 = mm ? g2 * g2 : T(0);
           D0[0] += w0 * d0; D0[1] += w0 * d1; D0[2] += w0 * d2;
           D1[0] += w1 * d0; D1[1] += w1 * d1; D1[2] += w1 * d2;
@@ -182,17 +189,18 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
         dsum[2] += (double)ds2;
       }
       if constexpr (HV || BB) {
+        const T gz0 = wz * fz0, gz1 = wz * fz1;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const T s0 = S[c] - S1[c];
-          accA[0 * 6 + 0 * 3 + c] += fz0 * s0;
-          accA[0 * 6 + 1 * 3 + c] += fz1 * s0;
-          accA[1 * 6 + 0 * 3 + c] += fz0 * S1[c];
-          accA[1 * 6 + 1 * 3 + c] += fz1 * S1[c];
+          accA[0 * 6 + 0 * 3 + c] += gz0 * s0;
+          accA[0 * 6 + 1 * 3 + c] += gz1 * s0;
+          accA[1 * 6 + 0 * 3 + c] += gz0 * S1[c];
+          accA[1 * 6 + 1 * 3 + c] += gz1 * S1[c];
         }
       }
       if constexpr (DG) {
-        const T z0 = fz0 * fz0, z1 = fz1 * fz1;
+        const T z0 = wz * fz0 * fz0, z1 = wz * fz1 * fz1;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           accD[0 * 6 + 0 * 3 + c] += z0 * D0[c];
@@ -203,14 +211,15 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
       }
     }
     if constexpr (HV || BB) {
+      const T gx0 = wx * fx0, gx1 = wx * fx1;
 #pragma unroll
       for (int r = 0; r < 12; ++r) {
-        s_accA[t * 25 + r] += fx0 * accA[r];
-        s_accA[t * 25 + 12 + r] += fx1 * accA[r];
+        s_accA[t * 25 + r] += gx0 * accA[r];
+        s_accA[t * 25 + 12 + r] += gx1 * accA[r];
       }
     }
     if constexpr (DG) {
-      const T x0 = fx0 * fx0, x1 = fx1 * fx1;
+      const T x0 = wx * fx0 * fx0, x1 = wx * fx1 * fx1;
 #pragma unroll
       for (int r = 0; r < 12; ++r) {
         s_accD[t * 25 + r] += x0 * accD[r];

@@ -4,11 +4,14 @@
 // Decomposition ("owner computes").  Every voxel is visited exactly once, by
 // the element with the highest index containing it, i.e. element
 // (min(vx/h, Nx-1), ...).  The reference visits each voxel once per element
-// containing it with trapezoid weights 1/2 per shared axis; those weights sum
-// to 1 over the elements sharing the voxel and the Hex8 shape functions are
-// continuous across element faces, so visiting once with weight 1 gives the
-// same assembled operator (engine/kernels_dvc.py:452-506,
-// engine/geometry_dvc.py:26-51).
+// containing it, with trapezoid weights 1/2 per axis on element end planes
+// (engine/kernels_dvc.py:452-506, engine/geometry_dvc.py:26-51).  On an
+// interior element plane the two halves of the two elements sharing the
+// voxel add up to 1, and the Hex8 shape functions are continuous across the
+// plane, so one visit with weight 1 assembles the same operator.  On the
+// outer faces of the mesh only one element holds the voxel and its weight
+// stays 1/2 per axis: the kernels apply w = prod over axes of (1/2 on the
+// first/last voxel plane, 1 elsewhere).
 //
 // A CTA owns a strip of EX consecutive elements along x in element row
 // (j,k).  Thread t owns voxel column x = i*h + qx (i = strip element t/h,
