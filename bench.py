@@ -1,0 +1,410 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 voxelDVC Gauss-Newton path.
+
+Workload (default `necking_512`): the 513^3 float32 pair of a fiber-composite
+texture (5000 cylinders) under tensile necking, h = 8 (64^3 elements,
+823,875 dof), equilibrium-gap regularizer, 3-level pyramid with FFT seed,
+dynamic mask frozen after 4 iterations (the `voxeldvc run` settings).  One
+step = one complete plain-FP32 multiscale GN-PCG solve to the reference's
+stopping rules.  Data are synthetic and generated on the GPU (seeded);
+the inputs (540 MB each) are larger than L2, so no flush is needed.
+
+  value   device-resident solve time (s/solve), CUDA events on the stream
+  e2e     the same solve through the public API with host numpy inputs:
+          host->device image upload and device->host read of (U, res, dU)
+          inside the timed region
+  roofline  the matrix-free Hessian matvec at the finest level, timed with
+          CUDA events right after the timed solves on the same data
+  cpu_baseline  the CPU oracle (NumPy restatement of the reference) per
+          operation on a bounded sample, extrapolated to the solve with the
+          operation counts of the GPU solve
+
+`--impl reference` times only the CPU oracle leg (the reference has no CPU
+solver of its own besides its NumPy execution) and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "512³ h=8 DVC time to 0.02vx RMS, plain vs mixed/learned; matvec GB/s"
+
+# Operation counts of the FP32 GB300 solve of necking_512 (per level, coarse
+# to fine): GN iterations and total PCG iterations.  The CPU leg multiplies
+# its measured per-operation times by these; the GPU leg reports its own
+# counts next to them in every run.
+SOLVE_COUNTS = {"necking_512": {"gn": [30, 4, 2], "pcg": [752, 84, 41]},
+                "necking_512_eqgap": {"gn": [30, 30, 30], "pcg": [60000, 60000, 60000]},
+                "necking_256": {"gn": [8, 6, 3], "pcg": [200, 108, 57]},
+                "plain_small": {"gn": [10, 5, 3], "pcg": [200, 100, 60]}}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="necking_512")
+    p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-layers", type=int, default=1)
+    p.add_argument("--only", default=None, choices=[None, "matvec"],
+                   help="matvec: time only the finest-level Hessian matvec (the profiling command)")
+    return p.parse_args()
+
+
+def matvec_only(args):
+    """Generate the workload's reference image, then run `--warmup` + `--steps`
+    finest-level Hessian matvecs (vdvc_matvec_H) and print their mean time."""
+    import torch
+    from voxeldvc_gb300 import _lib, synth
+    from voxeldvc_gb300.engine import correlate_gpu as CG
+    wl = synth.WORKLOADS[args.workload]()
+    Nx, Ny, Nz = wl.mesh
+    f = synth.texture(wl.shape, wl.n_cyl)
+    grad, mask0 = CG._grad_vox(f, wl.shape, np.float32, 0.0)
+    del f
+    ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    v = torch.randn(ndof, device="cuda", dtype=torch.float32)
+    out = torch.empty_like(v)
+    L = _lib.lib()
+    nws = L.vdvc_workspace_bytes(_lib.F32, wl.h, Nx, Ny, Nz)
+    ws = torch.empty(nws, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+
+    def mv():
+        _lib.check(L.vdvc_matvec_H(v.data_ptr(), grad.data_ptr(), mask0.data_ptr(), _lib.F32, wl.h, Nx, Ny, Nz,
+                                   out.data_ptr(), ws.data_ptr(), nws, s.cuda_stream))
+
+    for _ in range(args.warmup):
+        mv()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(args.steps):
+        mv()
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, args.steps)
+    nvox = wl.shape[0] * wl.shape[1] * wl.shape[2]
+    print(json.dumps({"workload": wl.name, "matvec_ms": round(ms, 4),
+                      "algorithmic_GBs": round((nvox * 13 + ndof * 8) / ms / 1e6, 1)}))
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle leg: per-operation times on a bounded sample, extrapolated
+# ---------------------------------------------------------------------------
+
+def _timed(fn, *a, **k):
+    t0 = time.perf_counter()
+    fn(*a, **k)
+    return time.perf_counter() - t0
+
+
+def cpu_model(wl, counts, layers=1):
+    """Seconds of the reference path on this host's cores for one solve,
+    from the oracle's per-operation times on `layers` element layers of each
+    pyramid level (extrapolated linearly in elements) and the operation
+    counts of the solve."""
+    from oracle import dvc_oracle as O
+    rng = np.random.default_rng(0)
+    Nx, Ny, Nz = wl.mesh
+    Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    K_lap, K_el = O.k_ref_laplacian(), O.k_ref_elastic(wl.solve.get("nu", 0.3))
+    eqgap = wl.solve["reg_type"] == "equilibrium_gap"
+    t_start = time.perf_counter()
+    # regularizer operators act on the full dof vector at every level
+    v64 = rng.standard_normal(Ndof)
+    interior = O.interior_dof_mask(Nx, Ny, Nz).astype(np.float32)
+    t_k = _timed(O.matvec_k_ref, v64, K_lap, float(wl.h), Nx, Ny, Nz)
+    t_reg = (3 if eqgap else 1) * t_k          # K P K + eps K_lap  (or K_lap)
+    t_reg_diag = (2 * 32 * t_k + t_k) if eqgap else t_k  # Hutchinson (32 probes x K P K) + diag K_lap
+    t_vec = _timed(lambda: [v64 * 1.0001 + v64 for _ in range(10)] and float(np.dot(v64, v64)))
+    levels = []
+    total = 0.0
+    scales = sorted(wl.solve["scales"], reverse=True)
+    for li, s in enumerate(scales):
+        h = wl.h // 2 ** s
+        nz = layers
+        Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, nz * h + 1
+        nvox = Nvx * Nvy * Nvz
+        grad = rng.standard_normal((nvox, 3)).astype(np.float32)
+        mask = rng.random(nvox) < 0.95
+        res = rng.standard_normal(nvox)
+        nd = 3 * (Nx + 1) * (Ny + 1) * (nz + 1)
+        vs = rng.standard_normal(nd)
+        gimg = rng.random((Nvx, Nvy, Nvz)).astype(np.float32)
+        scale = Nz / nz
+        t_mv = _timed(O.matvec_h, vs, grad, mask, h, Nx, Ny, nz) * scale
+        t_dg = _timed(O.diag_h, grad, mask, h, Nx, Ny, nz, nd) * scale
+        t_b = _timed(O.compute_b, res, mask, grad, h, Nx, Ny, nz, nd) * scale
+        t_st = _timed(O.masked_mean_std, res, mask, h, Nx, Ny, nz) * scale
+        t_sm = _timed(O.sample_deformed, 0.3 * vs, gimg, h, Nx, Ny, nz, (0, 0, 0), mask) * scale
+        t_pcg = t_mv + t_reg + t_vec
+        t_gn = t_sm + 2 * t_st + t_b + t_reg + t_dg + t_reg_diag + t_st
+        n_gn, n_pcg = counts["gn"][li], counts["pcg"][li]
+        t_level = n_gn * t_gn + (n_pcg + n_gn) * t_pcg
+        total += t_level
+        levels.append({"h": h, "matvec_s": round(t_mv, 3), "gn_fixed_s": round(t_gn, 3), "level_s": round(t_level, 1)})
+    wall = time.perf_counter() - t_start
+    return total, {"levels": levels, "reg_matvec_s": round(t_k, 3), "sample_wall_s": round(wall, 1),
+                   "sample": f"oracle per-op timing on {layers} element layer(s) of each level "
+                             f"(x{Nz // layers} to the full mesh) + one full-mesh regularizer matvec; "
+                             f"extrapolated with the solve's GN/PCG counts {counts}",
+                   "threads": 1}
+
+
+def reference_arm(args):
+    from voxeldvc_gb300 import synth
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = synth.WORKLOADS[args.workload]()
+    counts = SOLVE_COUNTS[args.workload]
+    vals = []
+    info = None
+    # the CPU leg has no warm-up effects worth discarding beyond numpy's first
+    # call; each step re-measures every operation on fresh samples
+    for _ in range(max(1, args.steps)):
+        v, info = cpu_model(wl, counts, args.cpu_sample_layers)
+        vals.append(v)
+    value = float(np.median(vals))
+    line = {"metric": METRIC, "value": round(value, 2), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1e3, 1), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (PCG promoted to f64 as in the reference)",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": wl.name, "mesh": list(wl.mesh), "h": wl.h, "extrapolated": True},
+            "cpu_baseline": {"value": round(value, 2), "unit": "s", "cores": 1, "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": round(value, 2), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "detail": info}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def solve_kwargs(wl):
+    from voxeldvc_gb300.engine import geometry_dvc as G
+    s = wl.solve
+    kw = dict(scales=s["scales"], l0=s["l0"], K_ref_laplacian=G.build_K_ref_laplacian(), reg_type=s["reg_type"],
+              dynamic_mask=True, freeze_mask_after=4, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
+              glt=0.0, fft_prealign=True, disp=False)
+    if s["reg_type"] == "equilibrium_gap":
+        kw["K_ref_elastic"] = G.build_K_ref(s.get("nu", 0.3))
+        kw["reg_exponent"] = s.get("reg_exponent", 4)
+    return kw
+
+
+def gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+    from voxeldvc_gb300 import _lib, synth
+    from voxeldvc_gb300.engine import correlate_gpu as CG
+    from voxeldvc_gb300.engine import kernels_dvc as K
+    from voxeldvc_gb300.engine import geometry_dvc as G
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    wl = synth.WORKLOADS[args.workload]()
+    Nx, Ny, Nz = wl.mesh
+    f_pix, g_pix = wl.make()
+    torch.cuda.synchronize()
+    kw = solve_kwargs(wl)
+
+    def step(stats=None):
+        return CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, xp=torch, stats=stats, **kw)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = _lib.launch_count()
+    level_stats = []
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for i in range(args.steps):
+            U, res, dU = step(level_stats if i == 0 else None)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = (_lib.launch_count() - n0) // max(1, args.steps)
+    ms = e0.elapsed_time(e1) / args.steps
+    barrier()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    clocks = clk.summary()
+
+    # accuracy vs the analytic field (sanity; the solve's own error)
+    Uh = U.double().cpu().numpy()
+    rms_true = float(np.sqrt(np.mean((Uh - wl.true_U()) ** 2)))
+
+    # roofline: the finest-level Hessian matvec on the same data
+    grad, mask0 = CG._grad_vox(CG.pix_to_vox(f_pix, np.float32)[0], wl.shape, np.float32, 0.0)
+    v = torch.randn(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), device="cuda", dtype=torch.float32)
+    nvox = wl.shape[0] * wl.shape[1] * wl.shape[2]
+    ndof = v.numel()
+    out = torch.empty_like(v)
+    nws = _lib.lib().vdvc_workspace_bytes(_lib.F32, wl.h, Nx, Ny, Nz)
+    ws = torch.empty(nws, dtype=torch.uint8, device="cuda")
+    L = _lib.lib()
+
+    def mv():
+        _lib.check(L.vdvc_matvec_H(v.data_ptr(), grad.data_ptr(), mask0.data_ptr(), _lib.F32, wl.h, Nx, Ny, Nz,
+                                   out.data_ptr(), ws.data_ptr(), nws, stream.cuda_stream))
+
+    for _ in range(5):
+        mv()
+    reps = 50
+    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    m0.record(stream)
+    for _ in range(reps):
+        mv()
+    m1.record(stream)
+    torch.cuda.synchronize()
+    mv_ms = m0.elapsed_time(m1) / reps
+    alg_bytes = nvox * 13 + ndof * 8
+    peaks = {}
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        peaks = json.load(open(pp))
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (mv_ms * 1e-3) / 1e9
+    del grad, mask0, ws
+
+    # e2e through the public API with host arrays
+    e2e = None
+    if args.e2e_steps > 0 and rank == 0:
+        f_host = f_pix.cpu().pin_memory().numpy()
+        g_host = g_pix.cpu().pin_memory().numpy()
+        t_e2e = []
+        for _ in range(args.e2e_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Ue, re, de = CG.multiscale_correlate_gpu(f_host, g_host, Nx, Ny, Nz, wl.h, xp=np, **kw)
+            t_e2e.append(time.perf_counter() - t0)
+        e2e = {"value": round(float(np.median(t_e2e)), 4), "unit": "s",
+               "h2d_bytes_per_step": int(f_host.nbytes + g_host.nbytes),
+               "d2h_bytes_per_step": int(Ue.nbytes + re.nbytes + de.nbytes)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        counts = {"gn": [s["gn_iters"] for s in level_stats], "pcg": [int(sum(s["pcg_iters"])) for s in level_stats]}
+        cv, cinfo = cpu_model(wl, counts, args.cpu_sample_layers)
+        cpu = {"value": round(cv, 2), "unit": "s", "cores": 1, "kind": "port", "sample": cinfo["sample"],
+               "detail": cinfo["levels"]}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(ms / 1e3, 4), "unit": "s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": wl.name, "mesh": list(wl.mesh), "h": wl.h, "ndof": ndof,
+                           "reg": wl.solve["reg_type"], "scales": list(wl.solve["scales"]),
+                           "parallelism": f"replicas x{world}", "l2": "inputs (540 MB each) larger than L2"},
+                "gpu_launches": int(launches),
+                "solve": {"gn_iters": [s["gn_iters"] for s in level_stats],
+                          "pcg_iters": [s["pcg_iters"] for s in level_stats],
+                          "level_gn_wall_s": [round(s["gn_wall_s"], 4) for s in level_stats],
+                          "rms_vs_true_field_vx": round(rms_true, 5)},
+                "roofline": {"bound": "hbm", "kernel": "matvec_H f32 (strip + gather)", "achieved": round(achieved, 1),
+                             "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                             "algorithmic_bytes": int(alg_bytes), "ms": round(mv_ms, 4)},
+                "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    elif args.only == "matvec":
+        matvec_only(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

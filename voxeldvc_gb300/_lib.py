@@ -74,6 +74,10 @@ SIGNATURES = {
     "vdvc_gn_update": (ci, [vp, pd, vp]),
     "vdvc_gn_read": (ci, [vp, ci, vp, ci, vp]),
     "vdvc_gn_destroy": (None, [vp]),
+    # include/vdvc_synth.h
+    "vdvc_synth_workspace_bytes": (cz, [ci, ci, ci]),
+    "vdvc_synth_texture": (ci, [vp, ci, ci, ci, C.c_ulonglong, cd, cd, vp, ci, cd, vp, cz, vp]),
+    "vdvc_synth_warp": (ci, [vp, ci, ci, ci, ci, pd, ci, cd, C.c_ulonglong, vp, vp]),
 }
 
 GN_U, GN_DU, GN_RES, GN_LIVE_MASK = 0, 1, 2, 3

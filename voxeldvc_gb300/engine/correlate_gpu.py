@@ -14,6 +14,7 @@ reference's pix[x,y,z] C-order layout.
 from __future__ import annotations
 
 import ctypes as C
+import time
 
 import numpy as np
 
@@ -364,7 +365,8 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     ws = D.torch().empty(nbytes, dtype=D.torch().uint8, device=D.device())
     solver = C.c_void_p()
     _lib.check(L.vdvc_gn_create(C.byref(desc), ws.data_ptr(), nbytes, C.byref(solver)), "correlate_gpu")
-    info = {"gn_iters": 0, "pcg_iters": [], "ll": ll}
+    info = {"gn_iters": 0, "pcg_iters": [], "ll": ll, "h": h}
+    t_start = time.perf_counter()
     try:
         st = D.stream()
         _lib.check(L.vdvc_gn_set_U(solver, U64.data_ptr(), st), "set_U")
@@ -404,6 +406,7 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
         L.vdvc_gn_destroy(solver)
         D.torch().cuda.current_stream().synchronize()
         del ws
+    info["gn_wall_s"] = time.perf_counter() - t_start
     if stats is not None:
         stats.append(info)
     return Uo, res, dU, info

@@ -1,0 +1,155 @@
+"""Seeded synthetic DVC workloads, generated on the GPU (include/vdvc_synth.h).
+
+Textures: Gaussian-filtered white noise (sigma 2 vx) plus bright randomly
+oriented cylinders (radius 3 vx, length 40 vx) mimicking a fiber
+composite, normalised to [0,1].  Deformed images: g(x) = f(x - u(x)) +
+N(0, sigma_n^2) for analytic fields u.  Volumes are snapped to n*h + 1
+voxels so the Hex8 mesh covers them exactly.
+
+Seeds: texture noise 0, cylinder placement 2, deformed-image noise 1.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _device as D
+from . import _lib
+
+FIELD_AFFINE, FIELD_NECKING, FIELD_AFFINE_SIN = 0, 1, 2
+
+def _L():
+    return _lib.lib()
+
+
+def cylinders(n, shape, radius=3.0, length=40.0, seed=2):
+    """(n, 8) float32: centre uniform in the volume, direction uniform on
+    the sphere, radius, half length."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 3)) * (np.array(shape) - 1)
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    out = np.concatenate([c, d, np.full((n, 1), radius), np.full((n, 1), length / 2)], axis=1)
+    return out.astype(np.float32)
+
+
+def texture(shape, n_cyl, seed=0, sigma=2.0, noise_amp=0.15, cyl_value=1.0, cyl_seed=2):
+    """Texture volume in vox layout (float32 CUDA tensor, x fastest)."""
+    L = _L()
+    nx, ny, nz = shape
+    out = D.empty(nx * ny * nz, np.float32)
+    cyl = D.to_device(cylinders(n_cyl, shape, seed=cyl_seed)) if n_cyl else None
+    nb = L.vdvc_synth_workspace_bytes(nx, ny, nz)
+    ws = D.torch().empty(nb, dtype=D.torch().uint8, device=D.device())
+    _lib.check(L.vdvc_synth_texture(out.data_ptr(), nx, ny, nz, seed, sigma, noise_amp, D.ptr(cyl), n_cyl,
+                                    cyl_value, ws.data_ptr(), nb, D.stream()), "synth_texture")
+    return out
+
+
+def warp(f_vox, shape, field_kind, params, noise_sigma=0.01, seed=1):
+    L = _L()
+    nx, ny, nz = shape
+    g = D.empty(nx * ny * nz, np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    _lib.check(L.vdvc_synth_warp(f_vox.data_ptr(), nx, ny, nz, field_kind, p.ctypes.data_as(_lib.pd), p.size,
+                                 noise_sigma, seed, g.data_ptr(), D.stream()), "synth_warp")
+    return g
+
+
+def vox_to_pix(vox, shape):
+    """vox layout -> pix[x,y,z] C-order device tensor (a layout copy)."""
+    nx, ny, nz = shape
+    return vox.view(nz, ny, nx).permute(2, 1, 0).contiguous()
+
+
+def field_at(kind, params, X):
+    """Analytic u at points X (n, 3), float64 host -- the true field."""
+    p = np.asarray(params, dtype=np.float64)
+    x, y, z = X[:, 0], X[:, 1], X[:, 2]
+    if kind == FIELD_NECKING:
+        ez, a, zc, s, xc, yc, R = p[:7]
+        gz = a * np.exp(-(z - zc) ** 2 / (2 * s * s)) / R
+        return np.stack([-gz * (x - xc), -gz * (y - yc), ez * z], 1)
+    G = p[3:12].reshape(3, 3)
+    u = p[:3][None, :] + (X - p[12:15][None, :]) @ G.T
+    if kind == FIELD_AFFINE_SIN:
+        amp, wl = p[15], p[16]
+        for k in range(3):
+            u[:, k] += amp * np.sin(2 * np.pi * X[:, (k + 1) % 3] / wl)
+    return u
+
+
+@dataclass
+class Workload:
+    name: str
+    shape: tuple
+    h: int
+    n_cyl: int
+    field: int
+    params: list
+    noise: float = 0.01
+    solve: dict = field(default_factory=dict)
+
+    @property
+    def mesh(self):
+        return tuple((s - 1) // self.h for s in self.shape)
+
+    def make(self):
+        """(f_pix, g_pix) float32 CUDA tensors in pix[x,y,z] layout."""
+        f = texture(self.shape, self.n_cyl)
+        g = warp(f, self.shape, self.field, self.params, self.noise)
+        return vox_to_pix(f, self.shape), vox_to_pix(g, self.shape)
+
+    def true_U(self):
+        """True nodal displacement (Ndof,) float64: g(x) = f(x - u(x))."""
+        Nx, Ny, Nz = self.mesh
+        nn = np.arange((Nx + 1) * (Ny + 1) * (Nz + 1))
+        X = np.stack([nn % (Nx + 1), (nn // (Nx + 1)) % (Ny + 1), nn // ((Nx + 1) * (Ny + 1))], 1) * float(self.h)
+        return field_at(self.field, self.params, X).reshape(-1)
+
+
+def plain_small():
+    """129^3, 200 cylinders, 1 % z strain with 0.4 Poisson contraction plus a
+    (0.5, -0.3, 0.2) vx translation; h = 16, Laplacian with l0 = 2h,
+    3-level pyramid."""
+    c = 64.0
+    G = np.diag([-0.004, -0.004, 0.01]).reshape(-1)
+    params = [0.5, -0.3, 0.2, *G, c, c, c]
+    return Workload("plain_small_129^3_h16", (129, 129, 129), 16, 200, FIELD_AFFINE, params,
+                    solve=dict(reg_type='laplacian', l0=2 * 16, scales=(2, 1, 0)))
+
+
+def _necking(n, reg):
+    params = [0.02, 3.0, (n - 1) / 2, 64.0 * n / 513, (n - 1) / 2, (n - 1) / 2, (n - 1) / 2]
+    solve = dict(reg_type=reg, l0=4.5 * 8, scales=(2, 1, 0))
+    if reg == 'equilibrium_gap':
+        solve.update(reg_exponent=4, nu=0.3)
+    tag = "" if reg == 'laplacian' else "_eqgap"
+    return Workload(f"necking_{n}^3_h8{tag}", (n, n, n), 8, int(round(5000 * (n / 513) ** 3)), FIELD_NECKING, params,
+                    solve=solve)
+
+
+def necking_512():
+    """513^3, 5000 cylinders, tensile necking: u_z = 0.02 z plus a
+    Gaussian-profile radial contraction of up to 3 vx at mid-height (profile
+    width s = 64 vx); h = 8 (64^3 elements, 823,875 dof), 3-level pyramid,
+    Laplacian regularizer with l0 = 4.5 h (the `voxeldvc run` settings)."""
+    return _necking(513, 'laplacian')
+
+
+def necking_512_eqgap():
+    """necking_512 with the equilibrium-gap regularizer (nu = 0.3,
+    reg_exponent 4).  The reference algorithm does not converge on this
+    pyramid (its coarse levels diverge); kept for the parity checks."""
+    return _necking(513, 'equilibrium_gap')
+
+
+def necking_256():
+    """necking_512 scaled to 257^3 (h = 8, 32^3 elements): the profiling case."""
+    return _necking(257, 'laplacian')
+
+
+WORKLOADS = {"plain_small": plain_small, "necking_512": necking_512, "necking_512_eqgap": necking_512_eqgap,
+             "necking_256": necking_256}
