@@ -34,6 +34,15 @@ template <typename T, int MODE>
 int launch_strip(const StripArgs<T>& args, const Kpair<T>* kp, cudaStream_t s);
 template <typename T>
 int launch_gather(const Mesh& m, const T* ev, T* out, cudaStream_t s);
+// TMA-staged float32 Hessian pass (strip_tma.cu); needs 16-byte aligned
+// grad and mask buffers.
+template <bool PCG>
+int launch_strip_tma(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s);
+// Compile-time-h float32 Hessian pass (strip_fast.cu); VDVC_ERR_UNSUPPORTED
+// when h has no specialisation.
+template <bool PCG>
+int launch_strip_fast(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s);
+bool tma_enabled();
 long long strip_grid_blocks(const Mesh& m);
 
 // PCG pieces (pcg.cu).

@@ -1,6 +1,9 @@
 // Element-strip quadrature kernels (see strip.cuh for the decomposition) and
 // the node gather that assembles element vectors into dof vectors.
-#include "strip.cuh"
+#include <cstdlib>
+#include <type_traits>
+
+#include "ops.cuh"
 #include "pcg.cuh"
 
 namespace vdvc {
@@ -311,8 +314,34 @@ size_t strip_smem_bytes(int h, int mode, size_t tsize) {
   return n * tsize;
 }
 
+// Kernel selection for the float32 Hessian pass: VDVC_HV_KERNEL=fast (the
+// default: compile-time-h specialisation, strip_fast.cu), tma (bulk-copy
+// staging, strip_tma.cu) or generic (runtime h, this file).
+static int hv_kernel_choice() {
+  static int choice = -1;
+  if (choice < 0) {
+    const char* e = getenv("VDVC_HV_KERNEL");
+    choice = 0;
+    if (e && e[0] == 't') choice = 1;
+    if (e && e[0] == 'g') choice = 2;
+  }
+  return choice;
+}
+
+bool tma_enabled() { return hv_kernel_choice() == 1; }
+
 template <typename T, int MODE>
 int launch_strip(const StripArgs<T>& args, const Kpair<T>* kp, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value && (MODE == kModeHv || MODE == (kModeHv | kModePcg))) {
+    constexpr bool pcg = (MODE & kModePcg) != 0;
+    const int choice = hv_kernel_choice();
+    const bool aligned = (((uintptr_t)args.grad | (uintptr_t)args.mask) & 15) == 0;
+    if (choice == 1 && aligned) return launch_strip_tma<pcg>(args, kp, s);
+    if (choice == 0) {
+      const int st = launch_strip_fast<pcg>(args, kp, s);
+      if (st != VDVC_ERR_UNSUPPORTED) return st;
+    }
+  }
   StripShape sh = strip_shape(args.m.h);
   if (args.m.h > 128) return set_error(VDVC_ERR_UNSUPPORTED, "element edge h=%d > 128 not supported", args.m.h);
   if (args.m.Ny > 65535 || args.m.Nz > 65535) return set_error(VDVC_ERR_ARG, "Ny/Nz > 65535");
