@@ -234,7 +234,8 @@ typedef struct vdvc_gn_desc {
   const double* K_lap;       /* host 24x24 (required when reg_type != NONE)    */
   const double* K_el;        /* host 24x24 (equilibrium gap)                  */
   int dynamic_mask;          /* 1: H and M follow the b mask each iteration   */
-  int pcg_chunk;             /* PCG iterations per replayed graph (0: 8)      */
+  int pcg_chunk;             /* PCG iterations per body of the graph's
+                                device-driven WHILE loop (0: 4)              */
   const void* f_vox;         /* reference values, vox layout, uncentred       */
   const void* g_vox;         /* deformed image, vox layout                    */
   const void* grad;          /* (Nvox,3) eroded gradient of f                 */

@@ -270,6 +270,7 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
   sa.mask = d.dynamic_mask ? S->frozen : d.mask0;
   sa.evA = S->evA;
   sa.nreg = 0;
+  sa.k1_blockdiag = 1;  // K1 is the vector Laplacian in both regularizers
   if (d.ll != 0.0 && d.reg_type == VDVC_REG_LAPLACIAN) {
     sa.nreg = 1;
     sa.c1 = (T)(d.ll * d.h);
@@ -284,6 +285,14 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
   return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
 }
 
+// Keeps the WHILE node of the PCG graph running until the state says done.
+__global__ void k_pcg_continue(cudaGraphConditionalHandle h, const PcgState* st) {
+  if (threadIdx.x == 0) cudaGraphSetConditional(h, st->done ? 0u : 1u);
+}
+
+// The whole PCG loop as one CUDA graph: a WHILE conditional node whose body
+// is `chunk` captured iterations followed by k_pcg_continue, so the device
+// itself decides when to stop and the host launches once per solve.
 template <typename T>
 static int build_graph(GnSolver<T>* S) {
   if (S->gexec) {
@@ -294,21 +303,34 @@ static int build_graph(GnSolver<T>* S) {
     cudaGraphDestroy(S->graph);
     S->graph = nullptr;
   }
+  cudaGraph_t g = nullptr;
+  VDVC_CUDA(cudaGraphCreate(&g, 0));
+  S->graph = g;
+  cudaGraphConditionalHandle hnd;
+  VDVC_CUDA(cudaGraphConditionalHandleCreate(&hnd, g, 1u, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = hnd;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  VDVC_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
   cudaStream_t cs = S->cap_stream;
-  VDVC_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  VDVC_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   const long long before = vdvc_launch_count();
   int st = VDVC_OK;
   for (int it = 0; it < S->chunk && st == VDVC_OK; ++it) st = pcg_iteration<T>(S, cs);
   const long long captured = vdvc_launch_count() - before;
-  count_launch(-captured);  // captured launches run at replay time
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamEndCapture(cs, &g);
-  if (st) {
-    if (g) cudaGraphDestroy(g);
-    return st;
+  count_launch(-captured);  // captured launches run (and are counted) at replay time
+  if (st == VDVC_OK) {
+    k_pcg_continue<<<1, 32, 0, cs>>>(hnd, S->pcg);
+    if (cudaGetLastError() != cudaSuccess) st = set_error(VDVC_ERR_CUDA, "continue kernel capture failed");
   }
+  cudaGraph_t body_out = nullptr;
+  cudaError_t e = cudaStreamEndCapture(cs, &body_out);
+  if (st) return st;
   if (e != cudaSuccess) return set_error(VDVC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-  S->graph = g;
   S->kernels_per_iter = (int)(captured / S->chunk);
   VDVC_CUDA(cudaGraphInstantiate(&S->gexec, g, 0));
   return VDVC_OK;
@@ -343,7 +365,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   carve_solver<T>(m, S, ws, ws_bytes);
   if (d->K_lap) load_K(d->K_lap, &S->Klap);
   if (d->K_el) load_K(d->K_el, &S->Kel);
-  S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 8;
+  S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 4;
   cudaStream_t s = (cudaStream_t)d->stream;
   int e = VDVC_OK;
   auto fail = [&](int code) {
@@ -494,28 +516,15 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
                               max_iter, tol, s);
   if (st) return st;
   if (!S->gexec && (st = build_graph<T>(S))) return st;
-  // Two chunks in flight: launch chunk k+1 before waiting on chunk k's state.
-  int launched = 0, checked = 0;
-  const int max_chunks = max_iter <= 0 ? 0 : (max_iter + S->chunk - 1) / S->chunk;
-  bool done = max_iter <= 0;
-  while (!done) {
-    while (launched < max_chunks && launched - checked < 2) {
-      VDVC_CUDA(cudaGraphLaunch(S->gexec, s));
-      count_launch((long long)S->chunk * S->kernels_per_iter);
-      VDVC_CUDA(cudaMemcpyAsync(S->h_pcg + (launched & 1), S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
-      VDVC_CUDA(cudaEventRecord(S->ev[launched & 1], s));
-      ++launched;
-    }
-    if (checked == launched) break;
-    VDVC_CUDA(cudaEventSynchronize(S->ev[checked & 1]));
-    const PcgState& h = S->h_pcg[checked & 1];
-    ++checked;
-    if (h.done) done = true;
-    if (checked == max_chunks) done = true;
-  }
+  if (max_iter > 0) VDVC_CUDA(cudaGraphLaunch(S->gexec, s));
+  VDVC_CUDA(cudaMemcpyAsync(S->h_pcg, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
   VDVC_CUDA(cudaStreamSynchronize(s));
-  PcgState fin;
-  VDVC_CUDA(cudaMemcpy(&fin, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost));
+  const PcgState& fin = S->h_pcg[0];
+  if (max_iter > 0) {
+    // body executions = ceil(iter / chunk); each runs chunk iterations' kernels + the continue kernel
+    const long long bodies = (fin.iter + S->chunk - 1) / S->chunk;
+    count_launch(bodies * ((long long)S->chunk * S->kernels_per_iter + 1));
+  }
   if (iters) *iters = fin.iter;
   if (res) *res = fin.res;
   if (status) *status = fin.status;

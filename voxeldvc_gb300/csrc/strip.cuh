@@ -88,6 +88,7 @@ struct StripArgs {
   const T* w;  // nodal vector for K2 (may be null)
   T c1, c2;
   int nreg;    // 0, 1 (K1) or 2 (K1 and K2)
+  int k1_blockdiag;  // K1 couples equal components only (the vector Laplacian)
 };
 
 }  // namespace vdvc

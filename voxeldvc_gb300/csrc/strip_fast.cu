@@ -17,9 +17,12 @@ __global__ void __launch_bounds__(128, 8) k_strip_hv_fast(const StripArgs<float>
   constexpr int EX = (H >= 128) ? 1 : 128 / H;
   const int nthr = blockDim.x;
   float* s_acc = (float*)smem_raw;            // nthr*25
-  float* s_v = s_acc + (size_t)nthr * 25;     // EX*24
-  float* s_w = s_v + EX * 24;                 // EX*24
-  float* s_K = s_w + EX * 24;                 // 2*576
+  // nodal vectors of the strip's elements, 25 floats per element (odd pitch:
+  // consecutive elements fall in different shared-memory banks)
+  constexpr int NP = 25;
+  float* s_v = s_acc + (size_t)nthr * 25;     // EX*NP
+  float* s_w = s_v + EX * NP;                 // EX*NP
+  float* s_K = s_w + EX * NP;                 // 2*576
   const Mesh& m = a.m;
 
   if constexpr (PCG) {
@@ -47,8 +50,8 @@ __global__ void __launch_bounds__(128, 8) k_strip_hv_fast(const StripArgs<float>
                              (long long)(k + corner_dz(cn)) * m.NnxNny;
       float val = a.v[3 * node + c];
       if constexpr (PCG) val = val + beta * a.p_old[3 * node + c];
-      s_v[idx] = val;
-      if (a.nreg == 2) s_w[idx] = a.w[3 * node + c];
+      s_v[e * NP + r] = val;
+      if (a.nreg == 2) s_w[e * NP + r] = a.w[3 * node + c];
     }
     if (a.nreg >= 1)
       for (int q = t; q < 576 * a.nreg; q += nthr) s_K[q] = (q < 576) ? kp->K1[q] : kp->K2[q - 576];
@@ -69,8 +72,8 @@ __global__ void __launch_bounds__(128, 8) k_strip_hv_fast(const StripArgs<float>
       for (int az = 0; az < 2; ++az)
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-          ux[ay * 6 + az * 3 + c] = fx0 * s_v[el * 24 + 3 * corner_of(0, ay, az) + c] +
-                                    fx1 * s_v[el * 24 + 3 * corner_of(1, ay, az) + c];
+          ux[ay * 6 + az * 3 + c] = fx0 * s_v[el * NP + 3 * corner_of(0, ay, az) + c] +
+                                    fx1 * s_v[el * NP + 3 * corner_of(1, ay, az) + c];
     float acc[12];
 #pragma unroll
     for (int r = 0; r < 12; ++r) acc[r] = 0.f;
@@ -157,13 +160,19 @@ __global__ void __launch_bounds__(128, 8) k_strip_hv_fast(const StripArgs<float>
     for (int q = 0; q < H; ++q) s += s_acc[(e * H + q) * 25 + r];
     if (a.nreg >= 1) {
       float k1 = 0.f;
+      if (a.k1_blockdiag) {
+        // K1 couples equal displacement components only (vector Laplacian)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) k1 += s_K[row * 24 + 3 * b + c] * s_v[e * NP + 3 * b + c];
+      } else {
 #pragma unroll 8
-      for (int b = 0; b < 24; ++b) k1 += s_K[row * 24 + b] * s_v[e * 24 + b];
+        for (int b = 0; b < 24; ++b) k1 += s_K[row * 24 + b] * s_v[e * NP + b];
+      }
       s += a.c1 * k1;
       if (a.nreg == 2) {
         float k2 = 0.f;
 #pragma unroll 8
-        for (int b = 0; b < 24; ++b) k2 += s_K[576 + row * 24 + b] * s_w[e * 24 + b];
+        for (int b = 0; b < 24; ++b) k2 += s_K[576 + row * 24 + b] * s_w[e * NP + b];
         s += a.c2 * k2;
       }
     }
@@ -175,7 +184,7 @@ template <int H, bool PCG>
 static int launch_h(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s) {
   constexpr int EX = (H >= 128) ? 1 : 128 / H;
   const int threads = (EX * H + 31) / 32 * 32;
-  const size_t smem = ((size_t)threads * 25 + EX * 48 + 1152) * sizeof(float);
+  const size_t smem = ((size_t)threads * 25 + EX * 50 + 1152) * sizeof(float);
   static bool attr_set = false;
   if (!attr_set && smem > 48 * 1024) {
     VDVC_CUDA(cudaFuncSetAttribute(k_strip_hv_fast<H, PCG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
