@@ -121,6 +121,21 @@ int vdvc_matvec_H(const void* v, const void* grad, const uint8_t* mask,
                   int dtype, int h, int Nx, int Ny, int Nz, void* out,
                   void* ws, size_t ws_bytes, vdvc_stream_t stream);
 
+/* out = H v in float32 for callers that cannot allocate device memory (a
+   plugin whose host owns all device memory through its own pool, a
+   latency-critical loop where cudaMalloc is not allowed).  No counterpart
+   in the reference.  Same result as vdvc_matvec_H; the element-vector
+   scratch is a fixed 32 MiB file-scope device array (meshes of at most
+   vdvc_matvec_H_noalloc_max_elements() elements, larger ones are rejected
+   with VDVC_ERR_ARG), held by every GPU that loads the library until exit.
+   The first call on a device looks the array's address up
+   (cudaGetSymbolAddress) and should come before any stream capture.  All
+   calls share the array: calls whose kernels overlap on the GPU race. */
+int vdvc_matvec_H_noalloc(const float* v, const float* grad,
+                          const uint8_t* mask, int h, int Nx, int Ny, int Nz,
+                          float* out, vdvc_stream_t stream);
+size_t vdvc_matvec_H_noalloc_max_elements(void);
+
 /* out = diag(H) (build_diagonal_H, kernels_dvc.py:509-543). */
 int vdvc_diag_H(const void* grad, const uint8_t* mask, int dtype, int h,
                 int Nx, int Ny, int Nz, void* out, void* ws, size_t ws_bytes,

@@ -50,6 +50,8 @@ SIGNATURES = {
     "vdvc_erode_mask": (ci, [vp, ci, ci, ci, vp, vp]),
     "vdvc_masked_stats": (ci, [vp, ci, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_matvec_H": (ci, [vp, vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
+    "vdvc_matvec_H_noalloc": (ci, [vp, vp, vp, ci, ci, ci, ci, vp, vp]),
+    "vdvc_matvec_H_noalloc_max_elements": (cz, []),
     "vdvc_diag_H": (ci, [vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_compute_b": (ci, [vp, vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_matvec_K_ref": (ci, [vp, ci, pd, vp, cd, ci, ci, ci, vp, vp]),
