@@ -43,6 +43,10 @@ METRIC = "512³ h=8 DVC time to 0.02vx RMS, plain vs mixed/learned; matvec GB/s"
 # to fine): GN iterations and total PCG iterations.  The CPU leg multiplies
 # its measured per-operation times by these; the GPU leg reports its own
 # counts next to them in every run.
+# DRAM bytes per voxel of one float32 matvec (k_strip_hv_fast<8> + k_gather),
+# ncu dram__bytes_read + write on the 257^3 case.
+TRAFFIC_B_PER_VOXEL = 14.04
+
 SOLVE_COUNTS = {"necking_512": {"gn": [30, 4, 2], "pcg": [752, 84, 41]},
                 "necking_512_eqgap": {"gn": [30, 30, 30], "pcg": [60000, 60000, 60000]},
                 "necking_256": {"gn": [8, 6, 3], "pcg": [200, 108, 57]},
@@ -387,8 +391,14 @@ def gpu_arm(args):
                           "pcg_iters": [s["pcg_iters"] for s in level_stats],
                           "level_gn_wall_s": [round(s["gn_wall_s"], 4) for s in level_stats],
                           "rms_vs_true_field_vx": round(rms_true, 5)},
-                "roofline": {"bound": "hbm", "kernel": "matvec_H f32 (strip + gather)", "achieved": round(achieved, 1),
-                             "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "roofline": {"bound": "hbm", "kernel": "matvec_H f32 (k_strip_hv_fast + k_gather)",
+                             "achieved": round(achieved, 1), "peak": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs"
+                             if "hbm_gbs" in peaks else "fallback 6800", "unit": "GB/s",
+                             "frac": round(achieved / peak, 4),
+                             # DRAM bytes per launch from ncu on the 257^3 case (14.04 B per
+                             # voxel, profiles/strip_hv_fast_f32_necking257.md), scaled to
+                             # this launch's voxel count
+                             "traffic": int(TRAFFIC_B_PER_VOXEL * nvox),
                              "algorithmic_bytes": int(alg_bytes), "ms": round(mv_ms, 4)},
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
         print(json.dumps(line))
