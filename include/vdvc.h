@@ -210,6 +210,52 @@ int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz,
                          const void* g_vox, int gnx, int gny, int gnz,
                          int dtype, double* d_out3, vdvc_stream_t stream);
 
+/* ---- affine pre-alignment (engine/correlate_gpu.py:417-825) ------------ */
+/* Scratch bytes of the affine entry points below. */
+size_t vdvc_affine_workspace_bytes(void);
+
+/* ZNCC sums of affine_prealign's cost (warp_and_cost, :523-536): over the
+   voxels x of f whose warped position A (x - c) + c + t lies inside g,
+   out6_host = {n, sum f, sum g, sum f^2, sum g^2, sum f g} (float64, g
+   sampled at order 1).  A9 row-major; synchronises the stream. */
+int vdvc_affine_zncc_sums(const float* f_vox, int nx, int ny, int nz,
+                          const float* g_vox, int gnx, int gny, int gnz,
+                          const double* A9, const double* t3, const double* c3,
+                          double* out6_host, void* ws, size_t ws_bytes,
+                          vdvc_stream_t stream);
+
+/* scipy.ndimage.gaussian_filter(in, sigma, mode) with truncate 4 (_smooth_plain,
+   :578-582): mode 0 'nearest', 1 'constant' (cval beyond the edges).  When
+   mul != NULL the input is multiplied by it first.  tmp: one volume. */
+int vdvc_gaussian_filter(const float* in, float* out, int nx, int ny, int nz,
+                         double sigma, int mode, double cval, const float* mul,
+                         float* tmp, vdvc_stream_t stream);
+
+/* Normalised-convolution smoothing G(img valid)/G(valid), valid = img != cval,
+   keeping img where G(valid) <= 1e-6 (_smooth_masked, :585-597).
+   tmp1..tmp3: one volume each. */
+int vdvc_smooth_masked(const float* img, int nx, int ny, int nz, double sigma,
+                       double cval, float* out, float* tmp1, float* tmp2,
+                       float* tmp3, vdvc_stream_t stream);
+
+/* One Gauss-Newton system of affine_refine_gn (:757-791): H (12x12, host,
+   row-major) and b (12) of the 12-parameter warp s(x) = x - M (x - c) - t_r
+   over voxels with s in bounds and g_raw != cval, from the smoothed f_s, its
+   (Nvox,3) gradient and the smoothed g_s.  Synchronises the stream. */
+int vdvc_affine_normal_equations(const float* f_s, const float* grad_fs,
+                                 const float* g_s, const float* g_raw, int nx,
+                                 int ny, int nz, const double* M9,
+                                 const double* tr3, const double* c3,
+                                 double cval, double* H144_host,
+                                 double* b12_host, void* ws, size_t ws_bytes,
+                                 vdvc_stream_t stream);
+
+/* Masked residual sums of _rms (:724-741): out2_host = {sum e^2, n}. */
+int vdvc_affine_rms_sums(const float* f, const float* g, int nx, int ny,
+                         int nz, const double* M9, const double* tr3,
+                         const double* c3, double cval, double* out2_host,
+                         void* ws, size_t ws_bytes, vdvc_stream_t stream);
+
 /* ---- preconditioned CG around an external matvec ------------------------
    The pieces of pcg(matvec, b, M_inv, xp, x0, max_iter, tol)
    (engine/kernels_dvc.py:550-583) for a caller that applies A itself:

@@ -516,3 +516,101 @@ def multiscale(f_pix, g_pix, Nx, Ny, Nz, h, scales=(2, 1, 0), g_origin=(0, 0, 0)
                                l0=None if l0 is None else l0 / s, U0=U, **kw)
         prev = s
     return U, res, dU
+
+
+# ----------------------------------------------------------------------------
+# affine pre-alignment (correlate_gpu.py:417-825)
+# ----------------------------------------------------------------------------
+
+def affine_matrix(p):
+    """correlate_gpu.py:436-448: R = Rz Ry Rx, A = R diag(s)."""
+    rx, ry, rz, sx, sy, sz = p[:6]
+    cx, sxr, cy, syr, cz, szr = np.cos(rx), np.sin(rx), np.cos(ry), np.sin(ry), np.cos(rz), np.sin(rz)
+    Rx = np.array([[1, 0, 0], [0, cx, -sxr], [0, sxr, cx]])
+    Ry = np.array([[cy, 0, syr], [0, 1, 0], [-syr, 0, cy]])
+    Rz = np.array([[cz, -szr, 0], [szr, cz, 0], [0, 0, 1]])
+    return Rz @ Ry @ Rx @ np.diag([sx, sy, sz])
+
+
+def zncc_cost(f_flat, g_samp, valid):
+    """correlate_gpu.py:417-433: 1 - ZNCC over `valid`, 2.0 when degenerate."""
+    if int(valid.sum()) < 1000:
+        return 2.0
+    fv = f_flat[valid] - f_flat[valid].mean()
+    gv = g_samp[valid] - g_samp[valid].mean()
+    den = np.sqrt((fv * fv).sum() * (gv * gv).sum())
+    if float(den) < 1e-8:
+        return 2.0
+    return 1.0 - float((fv * gv).sum() / den)
+
+
+def affine_cost(f_d, g_d, p):
+    """warp_and_cost of affine_prealign (correlate_gpu.py:523-536)."""
+    from scipy.ndimage import map_coordinates
+    c = np.array([(n - 1) / 2.0 for n in f_d.shape])
+    X = np.stack([a.ravel() for a in np.meshgrid(*[np.arange(n) for n in f_d.shape], indexing='ij')]).astype(float)
+    Xp = affine_matrix(p) @ (X - c[:, None]) + c[:, None] + np.asarray(p[6:9])[:, None]
+    n = g_d.shape
+    inb = np.all([(Xp[a] >= 0) & (Xp[a] <= n[a] - 1) for a in range(3)], axis=0)
+    gs = map_coordinates(g_d, Xp, order=1, mode='nearest')
+    return zncc_cost(f_d.ravel(), gs, inb)
+
+
+def affine_normal_equations(f_s, grads, g_s, g, M, tr, c, cval=0.0):
+    """The 12x12 float64 system of one affine_refine_gn iteration
+    (correlate_gpu.py:757-791), whole volume at once."""
+    from scipy.ndimage import map_coordinates
+    Mf, trf, cf = M.astype(np.float32), tr.astype(np.float32), np.asarray(c, np.float32)
+    shp = f_s.shape
+    Xc = [(np.arange(shp[a], dtype=np.float32) - cf[a]).reshape([-1 if b == a else 1 for b in range(3)])
+          for a in range(3)]
+    Xc = [np.broadcast_to(x, shp) for x in Xc]
+    base = [np.broadcast_to(np.arange(shp[a], dtype=np.float32).reshape([-1 if b == a else 1 for b in range(3)]), shp)
+            for a in range(3)]
+    coords = np.stack([base[i] - (Mf[i, 0] * Xc[0] + Mf[i, 1] * Xc[1] + Mf[i, 2] * Xc[2]) - trf[i] for i in range(3)])
+    warped = map_coordinates(f_s, coords, order=1, mode='constant', cval=cval)
+    inb = np.all([(coords[a] >= 0) & (coords[a] <= shp[a] - 1) for a in range(3)], axis=0)
+    mask = (inb & (g != cval)).astype(np.float32)
+    e = (g_s - warped) * mask
+    gs = [map_coordinates(grads[i], coords, order=1, mode='nearest') for i in range(3)]
+    J = [-gs[i] * Xc[j] * mask for i in range(3) for j in range(3)] + [-gs[i] * mask for i in range(3)]
+    Jf = np.stack([j.ravel() for j in J]).astype(np.float64)
+    return Jf @ Jf.T, Jf @ e.ravel().astype(np.float64)
+
+
+def affine_refine(f, g, A0, t0, c, sigmas=(4.0, 2.0, 1.0, 0.0), max_iter=50, tol=1e-6, patience=3, cval=0.0):
+    """correlate_gpu.py:600-825 (whole-volume assembly instead of slabs)."""
+    from scipy.ndimage import gaussian_filter
+    f = np.asarray(f, np.float32)
+    g = np.asarray(g, np.float32)
+    Ai = np.linalg.inv(np.asarray(A0, float))
+    M, tr = np.eye(3) - Ai, Ai @ np.asarray(t0, float)
+    valid = (g != cval).astype(np.float32)
+    for sigma in sigmas:
+        if sigma > 0:
+            fs = gaussian_filter(f, sigma, mode='nearest')
+            num = gaussian_filter(g * valid, sigma, mode='constant', cval=0.0)
+            den = gaussian_filter(valid, sigma, mode='constant', cval=0.0)
+            gs = g.copy()
+            ok = den > 1e-6
+            gs[ok] = num[ok] / den[ok]
+        else:
+            fs, gs = f, g
+        grads = [np.ascontiguousarray(q) for q in np.gradient(fs)]
+        best, stall = np.inf, 0
+        for _ in range(max_iter):
+            H, b = affine_normal_equations(fs, grads, gs, g, M, tr, c, cval)
+            H += np.eye(12) * (1e-9 * np.trace(H) / 12.0 + 1e-30)
+            dp = np.linalg.solve(H, b)
+            M, tr = M + dp[:9].reshape(3, 3), tr + dp[9:]
+            step = float(np.linalg.norm(dp))
+            if step < tol:
+                break
+            if step < best - 1e-12:
+                best, stall = step, 0
+            else:
+                stall += 1
+                if stall >= patience:
+                    break
+    A = np.linalg.inv(np.eye(3) - M)
+    return A, A @ tr

@@ -191,7 +191,40 @@ def fft_cases():
     np.savez_compressed(os.path.join(OUT, "fft.npz"), f1=f, g1=g, d1=d1, f2=f2, g2=g2, d2=d2)
 
 
+def affine_cases():
+    """A smooth texture and its image under a known affine, x' = A (x - c) + c
+    + t with f(x) ~ g(x'); the reference's prealign / refine results on it and
+    its ZNCC cost at a few parameter vectors."""
+    from scipy.ndimage import map_coordinates
+    rng = np.random.default_rng(9)
+    n = 41
+    f = (_texture((n, n, n), rng, sigma=1.6) * 100.0).astype(np.float32)
+    A = CG._build_affine_matrix(np.array([0.03, -0.02, 0.04, 1.02, 0.98, 1.01]))
+    t = np.array([1.5, -2.0, 0.7])
+    c = np.full(3, (n - 1) / 2.0)
+    Y = np.indices((n, n, n)).reshape(3, -1).astype(np.float64)
+    X = np.linalg.solve(A, Y - c[:, None] - t[:, None]) + c[:, None]
+    g = map_coordinates(f, X, order=1, mode='constant', cval=0.0).reshape(n, n, n).astype(np.float32)
+    costs = []
+    ps = [np.array([0, 0, 0, 1, 1, 1, 0, 0, 0.0]), np.array([0.03, -0.02, 0.04, 1.02, 0.98, 1.01, 0.75, -1.0, 0.35]),
+          np.array([0.1, 0.05, -0.05, 0.95, 1.05, 1.0, -0.5, 0.5, 1.0])]
+    f_d, g_d = f[::2, ::2, ::2], g[::2, ::2, ::2]
+    cd = np.array([(s - 1) / 2.0 for s in f_d.shape])
+    Xf = np.stack([a.ravel() for a in np.meshgrid(*[np.arange(s) for s in f_d.shape], indexing='ij')]).astype(float)
+    for p in ps:
+        Xp = CG._build_affine_matrix(p) @ (Xf - cd[:, None]) + cd[:, None] + p[6:9, None]
+        inb = np.all([(Xp[a] >= 0) & (Xp[a] <= g_d.shape[a] - 1) for a in range(3)], axis=0)
+        costs.append(CG._zncc_masked(f_d.ravel(), CG._map_coordinates(g_d, Xp, np, order=1), inb, np))
+    Ap, tp, cp, info = CG.affine_prealign(f, g, np, decimate=2, maxiter=60)
+    Ar, tr, rinfo = CG.affine_refine_gn(f, g, np, Ap, tp, cp, sigmas=(2.0, 0.0), max_iter=20)
+    np.savez_compressed(os.path.join(OUT, "affine.npz"), f=f, g=g, A_true=A, t_true=t, ps=np.stack(ps),
+                        costs=np.array(costs), A_pre=Ap, t_pre=tp, c_pre=cp, cost_final=info['cost_final'],
+                        A_ref=Ar, t_ref=tr, rms_initial=rinfo['rms_initial'], rms_final=rinfo['rms_final'],
+                        iters=np.array(rinfo['iters']))
+
+
 if __name__ == "__main__":
+    affine_cases()
     geometry()
     operators("A", 3, 2, 2, 4, seed=1)
     operators("B", 2, 3, 1, 3, seed=2)

@@ -82,6 +82,16 @@ def test_pcg_matches_reference(case):
     assert rel(x, c["out_pcg_x"]) < 1e-6
 
 
+def test_affine_matches_reference():
+    c = load_golden("affine.npz")
+    f_d, g_d = c["f"][::2, ::2, ::2], c["g"][::2, ::2, ::2]
+    for p, cost in zip(c["ps"], c["costs"]):
+        assert abs(O.affine_cost(f_d, g_d, p) - cost) < 1e-6
+    A, t = O.affine_refine(c["f"], c["g"], c["A_pre"], c["t_pre"], c["c_pre"], sigmas=(2.0, 0.0), max_iter=20)
+    assert np.abs(A - c["A_ref"]).max() < 1e-6
+    assert np.abs(t - c["t_ref"]).max() < 1e-5
+
+
 def test_fft_shift_matches_reference():
     c = load_golden("fft.npz")
     assert np.array_equal(O.fft_rigid_shift(c["f1"], c["g1"]), c["d1"])

@@ -76,6 +76,12 @@ SIGNATURES = {
     "vdvc_gn_update": (ci, [vp, pd, vp]),
     "vdvc_gn_read": (ci, [vp, ci, vp, ci, vp]),
     "vdvc_gn_destroy": (None, [vp]),
+    "vdvc_affine_workspace_bytes": (cz, []),
+    "vdvc_affine_zncc_sums": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, pd, pd, pd, pd, vp, cz, vp]),
+    "vdvc_gaussian_filter": (ci, [vp, vp, ci, ci, ci, cd, ci, cd, vp, vp, vp]),
+    "vdvc_smooth_masked": (ci, [vp, ci, ci, ci, cd, cd, vp, vp, vp, vp, vp]),
+    "vdvc_affine_normal_equations": (ci, [vp, vp, vp, vp, ci, ci, ci, pd, pd, pd, cd, pd, pd, vp, cz, vp]),
+    "vdvc_affine_rms_sums": (ci, [vp, vp, ci, ci, ci, pd, pd, pd, cd, pd, vp, cz, vp]),
     # include/vdvc_synth.h
     "vdvc_synth_workspace_bytes": (cz, [ci, ci, ci]),
     "vdvc_synth_texture": (ci, [vp, ci, ci, ci, C.c_ulonglong, cd, cd, vp, ci, cd, vp, cz, vp]),

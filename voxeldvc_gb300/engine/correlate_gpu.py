@@ -532,9 +532,174 @@ def multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, scales=(2, 1, 0),
     return D.out(U, xp), D.out(res, xp), D.out(dU, xp)
 
 
-def affine_prealign(*args, **kwargs):
-    raise NotImplementedError("affine_prealign is not built yet")
+# ---------------------------------------------------------------------------
+# affine pre-alignment (correlate_gpu.py:417-825)
+# ---------------------------------------------------------------------------
+
+def _ptr3(a):
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    return a, a.ctypes.data_as(_lib.pd)
 
 
-def affine_refine_gn(*args, **kwargs):
-    raise NotImplementedError("affine_refine_gn is not built yet")
+def _zncc_cost(sums):
+    """1 - ZNCC from (n, sum f, sum g, sum f^2, sum g^2, sum fg), with the
+    reference's guards: fewer than 1000 voxels or a degenerate variance
+    give 2.0 (correlate_gpu.py:417-433)."""
+    n, sf, sg, sff, sgg, sfg = sums
+    if int(n) < 1000:
+        return 2.0
+    vf = sff - sf * sf / n
+    vg = sgg - sg * sg / n
+    denom = np.sqrt(max(vf, 0.0) * max(vg, 0.0))
+    if denom < 1e-8:
+        return 2.0
+    return 1.0 - float((sfg - sf * sg / n) / denom)
+
+
+def _build_affine_matrix(p):
+    """A = Rz(rz) Ry(ry) Rx(rx) diag(sx, sy, sz) from p = (rx, ry, rz, sx, sy,
+    sz, ...) (correlate_gpu.py:436-448)."""
+    rx, ry, rz, sx, sy, sz = (float(v) for v in p[:6])
+
+    def rot(axis, a):
+        c, s = np.cos(a), np.sin(a)
+        R = np.eye(3)
+        i, j = [(1, 2), (0, 2), (0, 1)][axis]
+        R[i, i], R[j, j] = c, c
+        R[i, j], R[j, i] = -s, s
+        if axis == 1:  # rotation about y: R[0,2] = +sin, R[2,0] = -sin
+            R[i, j], R[j, i] = s, -s
+        return R
+
+    return rot(2, rz) @ rot(1, ry) @ rot(0, rx) @ np.diag([sx, sy, sz])
+
+
+def affine_prealign(f_pix, g_pix, xp, decimate=4, t0=None, angle_bound=0.3, scale_bound=0.15, maxiter=200,
+                    disp=False):
+    """9-DOF (rotation, per-axis scale, translation) alignment maximising the
+    ZNCC of f(x) and g(A (x - c) + c + t) on copies decimated by `decimate`;
+    the cost is evaluated on the GPU, the Powell search runs on the host
+    (scipy).  Returns (A, t, c, info) in full-resolution voxel units."""
+    from scipy.optimize import minimize
+    f_full, fs = pix_to_vox(f_pix, np.float32)
+    g_full, gs = pix_to_vox(g_pix, np.float32)
+    f_d, fsd = _decimate(f_full, fs, decimate, np.float32)
+    g_d, gsd = _decimate(g_full, gs, decimate, np.float32)
+    del f_full, g_full
+    c = np.array([(n - 1) / 2.0 for n in fsd], dtype=np.float64)
+    if t0 is None:
+        t0_dec = _fft_shift_vox(f_d, fsd, g_d, gsd, np.float32)
+    else:
+        t0_dec = np.asarray(t0, dtype=np.float64) / decimate
+    L = _lib.lib()
+    ws = D.torch().empty(L.vdvc_affine_workspace_bytes(), dtype=D.torch().uint8, device=D.device())
+    cb, cp = _ptr3(c)
+    out6 = (C.c_double * 6)()
+
+    def warp_and_cost(p):
+        A, Ap = _ptr3(_build_affine_matrix(p))
+        t, tp = _ptr3(p[6:9])
+        _lib.check(L.vdvc_affine_zncc_sums(f_d.data_ptr(), *fsd, g_d.data_ptr(), *gsd, Ap, tp, cp,
+                                           C.cast(out6, _lib.pd), ws.data_ptr(), ws.numel(), D.stream()),
+                   "affine_prealign")
+        return _zncc_cost(list(out6))
+
+    p_identity = np.array([0., 0., 0., 1., 1., 1., 0., 0., 0.])
+    p_translation_only = p_identity.copy()
+    p_translation_only[6:9] = t0_dec
+    cost_identity = warp_and_cost(p_identity)
+    cost_translation_only = warp_and_cost(p_translation_only)
+    bounds = ([(-angle_bound, angle_bound)] * 3 + [(1 - scale_bound, 1 + scale_bound)] * 3 + [(None, None)] * 3)
+    result = minimize(warp_and_cost, p_translation_only, method='Powell', bounds=bounds,
+                      options={'maxiter': maxiter, 'disp': disp})
+    p_opt = result.x
+    A = _build_affine_matrix(p_opt)
+    info = {'cost_identity': cost_identity, 'cost_translation_only': cost_translation_only,
+            'cost_final': float(result.fun), 'nfev': result.nfev, 'p': p_opt}
+    return A, p_opt[6:9] * decimate, c * decimate, info
+
+
+def affine_refine_gn(f_pix, g_pix, xp, A0, t0, c, sigmas=(4.0, 2.0, 1.0, 0.0), max_iter=50, tol=1e-6, patience=3,
+                     cval=0.0, chunk_voxels=8_000_000, disp=False):
+    """Forward-additive Gauss-Newton refinement of a full 3x3 affine +
+    translation in the generative convention def(x) ~ ref(x - M (x - c) - t_r)
+    over a Gaussian scale space; each iteration's 12x12 float64 normal
+    equations are assembled on the GPU in one pass.  Returns (A, t, info) in
+    the affine_prealign convention.  `chunk_voxels` is accepted and ignored."""
+    T = D.torch()
+    f, shape = pix_to_vox(f_pix, np.float32)
+    g, gshape = pix_to_vox(g_pix, np.float32)
+    if tuple(gshape) != tuple(shape):
+        raise ValueError("affine_refine_gn needs f_pix and g_pix of the same shape")
+    nx, ny, nz = shape
+    n = nx * ny * nz
+    I3 = np.eye(3)
+    A0 = np.asarray(A0, dtype=np.float64)
+    t0 = np.asarray(t0, dtype=np.float64)
+    A0inv = np.linalg.inv(A0)
+    M = I3 - A0inv
+    tr = A0inv @ t0
+    c = np.asarray(c, dtype=np.float64)
+    L = _lib.lib()
+    ws = T.empty(L.vdvc_affine_workspace_bytes(), dtype=T.uint8, device=D.device())
+    cb, cp = _ptr3(c)
+    tmp = [D.empty(n, np.float32) for _ in range(3)]
+    f_s_buf, g_s_buf = D.empty(n, np.float32), D.empty(n, np.float32)
+    st = D.stream()
+
+    def _rms(M_, tr_):
+        Mb, Mp = _ptr3(M_)
+        tb, tp = _ptr3(tr_)
+        out2 = (C.c_double * 2)()
+        _lib.check(L.vdvc_affine_rms_sums(f.data_ptr(), g.data_ptr(), nx, ny, nz, Mp, tp, cp, float(cval),
+                                          C.cast(out2, _lib.pd), ws.data_ptr(), ws.numel(), st), "affine_refine_gn")
+        return float(np.sqrt(out2[0] / max(out2[1], 1.0)))
+
+    rms_initial = _rms(M, tr)
+    iters = []
+    H = np.empty(144)
+    b = np.empty(12)
+    for sigma in sigmas:
+        if sigma > 0:
+            _lib.check(L.vdvc_gaussian_filter(f.data_ptr(), f_s_buf.data_ptr(), nx, ny, nz, float(sigma), 0, 0.0,
+                                              None, tmp[0].data_ptr(), st), "gaussian_filter")
+            _lib.check(L.vdvc_smooth_masked(g.data_ptr(), nx, ny, nz, float(sigma), float(cval), g_s_buf.data_ptr(),
+                                            tmp[0].data_ptr(), tmp[1].data_ptr(), tmp[2].data_ptr(), st),
+                       "smooth_masked")
+            f_s, g_s = f_s_buf, g_s_buf
+        else:
+            f_s, g_s = f, g
+        grad, _ = _grad_vox(f_s, shape, np.float32)
+        n_it = 0
+        best_step = np.inf
+        stall = 0
+        for it in range(max_iter):
+            Mb, Mp = _ptr3(M)
+            tb, tp = _ptr3(tr)
+            _lib.check(L.vdvc_affine_normal_equations(f_s.data_ptr(), grad.data_ptr(), g_s.data_ptr(), g.data_ptr(),
+                                                      nx, ny, nz, Mp, tp, cp, float(cval), H.ctypes.data_as(_lib.pd),
+                                                      b.ctypes.data_as(_lib.pd), ws.data_ptr(), ws.numel(), st),
+                       "affine_refine_gn")
+            Hm = H.reshape(12, 12).copy()
+            Hm += np.eye(12) * (1e-9 * float(np.trace(Hm)) / 12.0 + 1e-30)
+            dp = np.linalg.solve(Hm, b)
+            M = M + dp[:9].reshape(3, 3)
+            tr = tr + dp[9:]
+            step = float(np.linalg.norm(dp))
+            n_it = it + 1
+            if disp:
+                print(f"    sigma={sigma:g} iter {it:2d}: ||dp||={step:.3e}", flush=True)
+            if step < tol:
+                break
+            if step < best_step - 1e-12:
+                best_step = step
+                stall = 0
+            else:
+                stall += 1
+                if stall >= patience:
+                    break
+        iters.append(n_it)
+        del grad
+    rms = _rms(M, tr)
+    A = np.linalg.inv(I3 - M)
+    return A, A @ tr, {'rms_initial': rms_initial, 'rms_final': rms, 'iters': iters}
