@@ -34,6 +34,8 @@ struct GnSolver {
   Mesh m;
   vdvc_gn_desc d;
   Kmat Klap, Kel;
+  bool lap_blockdiag;  // K_lap = L8 on each displacement component
+  float L8[64];
   // device buffers (carved from the caller's workspace)
   double* U64;
   T *U32, *x, *r, *z, *p, *Ap, *Minv, *b, *w, *ru, *t1, *gvals, *res, *evA, *evD;
@@ -270,7 +272,10 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
   sa.mask = d.dynamic_mask ? S->frozen : d.mask0;
   sa.evA = S->evA;
   sa.nreg = 0;
-  sa.k1_blockdiag = 1;  // K1 is the vector Laplacian in both regularizers
+  // K1 is the vector Laplacian in both regularizers; pass its 8x8 block when
+  // it has the block structure of build_K_ref_laplacian
+  sa.k1_blockdiag = S->lap_blockdiag ? 1 : 0;
+  for (int q = 0; q < 64; ++q) sa.L8[q] = S->L8[q];
   if (d.ll != 0.0 && d.reg_type == VDVC_REG_LAPLACIAN) {
     sa.nreg = 1;
     sa.c1 = (T)(d.ll * d.h);
@@ -365,6 +370,19 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   carve_solver<T>(m, S, ws, ws_bytes);
   if (d->K_lap) load_K(d->K_lap, &S->Klap);
   if (d->K_el) load_K(d->K_el, &S->Kel);
+  // K_lap[3a+c][3b+c'] == (c == c') * L8[a][b] ?
+  S->lap_blockdiag = d->K_lap != nullptr;
+  for (int r = 0; r < 24 && S->lap_blockdiag; ++r)
+    for (int q = 0; q < 24; ++q) {
+      const double v = S->Klap.k[r * 24 + q];
+      const double ref = (r % 3 == q % 3) ? S->Klap.k[(r / 3) * 3 * 24 + (q / 3) * 3] : 0.0;
+      if (v != ref) {
+        S->lap_blockdiag = false;
+        break;
+      }
+    }
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 8; ++b) S->L8[a * 8 + b] = (float)S->Klap.k[(3 * a) * 24 + 3 * b];
   S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 4;
   cudaStream_t s = (cudaStream_t)d->stream;
   int e = VDVC_OK;

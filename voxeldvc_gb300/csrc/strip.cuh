@@ -88,7 +88,8 @@ struct StripArgs {
   const T* w;  // nodal vector for K2 (may be null)
   T c1, c2;
   int nreg;    // 0, 1 (K1) or 2 (K1 and K2)
-  int k1_blockdiag;  // K1 couples equal components only (the vector Laplacian)
+  int k1_blockdiag;  // K1 = the same 8x8 block L8 on each component (vector Laplacian)
+  float L8[64];      // that block, row-major over local corners (k1_blockdiag)
 };
 
 }  // namespace vdvc

@@ -17,12 +17,14 @@ __global__ void __launch_bounds__(128, 8) k_strip_hv_fast(const StripArgs<float>
   constexpr int EX = (H >= 128) ? 1 : 128 / H;
   const int nthr = blockDim.x;
   float* s_acc = (float*)smem_raw;            // nthr*25
-  // nodal vectors of the strip's elements, 25 floats per element (odd pitch:
-  // consecutive elements fall in different shared-memory banks)
-  constexpr int NP = 25;
-  float* s_v = s_acc + (size_t)nthr * 25;     // EX*NP
-  float* s_w = s_v + EX * NP;                 // EX*NP
-  float* s_K = s_w + EX * NP;                 // 2*576
+  // Unique nodes of the strip: 4 node lines (dy,dz) of EX+1 nodes x 3
+  // components, so adjacent elements share their common face instead of each
+  // loading all 8 corners.  Corner (dx,dy,dz) of strip element e is
+  // s_v[((dy*2+dz)*NL + e + dx)*3 + c].
+  constexpr int NL = EX + 1;
+  float* s_v = s_acc + (size_t)nthr * 25;     // 12*NL
+  float* s_w = s_v + 12 * NL;                 // 12*NL
+  float* s_K = s_w + 12 * NL;                 // 2*576
   const Mesh& m = a.m;
 
   if constexpr (PCG) {
@@ -44,17 +46,22 @@ __global__ void __launch_bounds__(128, 8) k_strip_hv_fast(const StripArgs<float>
   {
     float beta = 0.f;
     if constexpr (PCG) beta = (float)a.st->beta;
-    for (int idx = t; idx < nel * 24; idx += nthr) {
-      const int e = idx / 24, r = idx - e * 24, c = r % 3, cn = r / 3;
-      const long long node = (long long)(i0 + e + corner_dx(cn)) + (long long)(j + corner_dy(cn)) * m.Nnx +
-                             (long long)(k + corner_dz(cn)) * m.NnxNny;
+    const int line = (nel + 1) * 3;
+    for (int idx = t; idx < 4 * line; idx += nthr) {
+      const int dyz = idx / line, rem = idx - dyz * line, ii = rem / 3, c = rem - ii * 3;
+      const long long node = (long long)(i0 + ii) + (long long)(j + (dyz >> 1)) * m.Nnx +
+                             (long long)(k + (dyz & 1)) * m.NnxNny;
       float val = a.v[3 * node + c];
       if constexpr (PCG) val = val + beta * a.p_old[3 * node + c];
-      s_v[e * NP + r] = val;
-      if (a.nreg == 2) s_w[e * NP + r] = a.w[3 * node + c];
+      s_v[(dyz * NL + ii) * 3 + c] = val;
+      if (a.nreg == 2) s_w[(dyz * NL + ii) * 3 + c] = a.w[3 * node + c];
     }
-    if (a.nreg >= 1)
-      for (int q = t; q < 576 * a.nreg; q += nthr) s_K[q] = (q < 576) ? kp->K1[q] : kp->K2[q - 576];
+    // dense K rows are staged only when needed: K1 unless it is the
+    // block-diagonal Laplacian (then its 8x8 block rides in the parameters)
+    if (a.nreg >= 1) {
+      const int k_lo = a.k1_blockdiag ? 576 : 0, k_hi = 576 * a.nreg;
+      for (int q = k_lo + t; q < k_hi; q += nthr) s_K[q] = (q < 576) ? kp->K1[q] : kp->K2[q - 576];
+    }
     for (int r = 0; r < 25; ++r) s_acc[t * 25 + r] = 0.f;
   }
   __syncthreads();
@@ -72,8 +79,8 @@ __global__ void __launch_bounds__(128, 8) k_strip_hv_fast(const StripArgs<float>
       for (int az = 0; az < 2; ++az)
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-          ux[ay * 6 + az * 3 + c] = fx0 * s_v[el * NP + 3 * corner_of(0, ay, az) + c] +
-                                    fx1 * s_v[el * NP + 3 * corner_of(1, ay, az) + c];
+          ux[ay * 6 + az * 3 + c] = fx0 * s_v[((ay * 2 + az) * NL + el) * 3 + c] +
+                                    fx1 * s_v[((ay * 2 + az) * NL + el + 1) * 3 + c];
     float acc[12];
 #pragma unroll
     for (int r = 0; r < 12; ++r) acc[r] = 0.f;
@@ -159,20 +166,31 @@ __global__ void __launch_bounds__(128, 8) k_strip_hv_fast(const StripArgs<float>
 #pragma unroll
     for (int q = 0; q < H; ++q) s += s_acc[(e * H + q) * 25 + r];
     if (a.nreg >= 1) {
+      const int acorner = corner_of(ax, ay, az);
       float k1 = 0.f;
       if (a.k1_blockdiag) {
-        // K1 couples equal displacement components only (vector Laplacian)
+        // K1 couples equal displacement components only (vector Laplacian):
+        // its 8x8 block, read from the kernel parameters (warp-uniform)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) k1 += s_K[row * 24 + 3 * b + c] * s_v[e * NP + 3 * b + c];
+        for (int b = 0; b < 8; ++b)
+          k1 += a.L8[acorner * 8 + b] *
+                s_v[(((corner_dy(b) << 1) | corner_dz(b)) * NL + e + corner_dx(b)) * 3 + c];
       } else {
 #pragma unroll 8
-        for (int b = 0; b < 24; ++b) k1 += s_K[row * 24 + b] * s_v[e * NP + b];
+        for (int b = 0; b < 24; ++b) {
+          const int bn = b / 3;
+          k1 += s_K[row * 24 + b] * s_v[(((corner_dy(bn) << 1) | corner_dz(bn)) * NL + e + corner_dx(bn)) * 3 + b % 3];
+        }
       }
       s += a.c1 * k1;
       if (a.nreg == 2) {
         float k2 = 0.f;
 #pragma unroll 8
-        for (int b = 0; b < 24; ++b) k2 += s_K[576 + row * 24 + b] * s_w[e * NP + b];
+        for (int b = 0; b < 24; ++b) {
+          const int bn = b / 3;
+          k2 += s_K[576 + row * 24 + b] *
+                s_w[(((corner_dy(bn) << 1) | corner_dz(bn)) * NL + e + corner_dx(bn)) * 3 + b % 3];
+        }
         s += a.c2 * k2;
       }
     }
@@ -184,7 +202,7 @@ template <int H, bool PCG>
 static int launch_h(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s) {
   constexpr int EX = (H >= 128) ? 1 : 128 / H;
   const int threads = (EX * H + 31) / 32 * 32;
-  const size_t smem = ((size_t)threads * 25 + EX * 50 + 1152) * sizeof(float);
+  const size_t smem = ((size_t)threads * 25 + 24 * (EX + 1) + 1152) * sizeof(float);
   static bool attr_set = false;
   if (!attr_set && smem > 48 * 1024) {
     VDVC_CUDA(cudaFuncSetAttribute(k_strip_hv_fast<H, PCG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
