@@ -136,6 +136,19 @@ int vdvc_matvec_H_noalloc(const float* v, const float* grad,
                           float* out, vdvc_stream_t stream);
 size_t vdvc_matvec_H_noalloc_max_elements(void);
 
+/* Precision form of matvec_H (kernels_dvc.py:452-506): the gradient is
+   rounded to BF16, the 162 distinct entries of every 24x24 element Hessian
+   are formed with FP32 accumulation, and out = H v is applied from them in
+   FP32.  float32 v/grad/out; h in {1,2,3,4,6,8,12,16}.  The Gauss-Newton
+   solver forms the element Hessians once per iteration and reuses them for
+   every PCG step; this entry forms them on each call.  Workspace:
+   vdvc_eh_workspace_bytes(h, Nx, Ny, Nz). */
+int vdvc_matvec_H_mixed(const float* v, const float* grad,
+                        const uint8_t* mask, int h, int Nx, int Ny, int Nz,
+                        float* out, void* ws, size_t ws_bytes,
+                        vdvc_stream_t stream);
+size_t vdvc_eh_workspace_bytes(int h, int Nx, int Ny, int Nz);
+
 /* out = diag(H) (build_diagonal_H, kernels_dvc.py:509-543). */
 int vdvc_diag_H(const void* grad, const uint8_t* mask, int dtype, int h,
                 int Nx, int Ny, int Nz, void* out, void* ws, size_t ws_bytes,
@@ -305,7 +318,16 @@ typedef struct vdvc_gn_desc {
   const double* diag_eqgap;  /* (Ndof) float64 Hutchinson diag of K P_i K     */
   double mean0, std0;        /* multiplicity-weighted stats of f over mask0   */
   vdvc_stream_t stream;      /* stream used for the set-up in vdvc_gn_create   */
+  int precision;             /* VDVC_PREC_PLAIN, or VDVC_PREC_MIXED: BF16
+                                gradient, element Hessians formed once per GN
+                                iteration (once per solve after the b mask
+                                freezes), FP32 element-Hessian matvecs in the
+                                PCG; dtype VDVC_F32, Laplacian K_lap          */
+  void* eh_ws;               /* VDVC_PREC_MIXED: device workspace of          */
+  size_t eh_ws_bytes;        /*   vdvc_eh_workspace_bytes(h, Nx, Ny, Nz) bytes */
 } vdvc_gn_desc;
+
+enum { VDVC_PREC_PLAIN = 0, VDVC_PREC_MIXED = 1 };
 
 typedef struct vdvc_gn_solver vdvc_gn_solver;
 

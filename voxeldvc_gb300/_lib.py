@@ -52,6 +52,8 @@ SIGNATURES = {
     "vdvc_matvec_H": (ci, [vp, vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_matvec_H_noalloc": (ci, [vp, vp, vp, ci, ci, ci, ci, vp, vp]),
     "vdvc_matvec_H_noalloc_max_elements": (cz, []),
+    "vdvc_matvec_H_mixed": (ci, [vp, vp, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
+    "vdvc_eh_workspace_bytes": (cz, [ci, ci, ci, ci]),
     "vdvc_diag_H": (ci, [vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_compute_b": (ci, [vp, vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_matvec_K_ref": (ci, [vp, ci, pd, vp, cd, ci, ci, ci, vp, vp]),
@@ -106,6 +108,7 @@ class GnDesc(C.Structure):
         ("interior", vp), ("diag_eqgap", vp),
         ("mean0", cd), ("std0", cd),
         ("stream", vp),
+        ("precision", ci), ("eh_ws", vp), ("eh_ws_bytes", cz),
     ]
 
 _lock = threading.Lock()

@@ -12,8 +12,15 @@
 //   pcg    : Jacobi PCG on (H + ll R) dU = b, replayed as a CUDA graph of
 //            `chunk` iterations until the device state says done
 //   update : U += dU (float64 master copy), |dU|^2, |U|^2
+//
+// Precision form (float solver, VDVC_PREC_MIXED): the gradient is rounded to
+// BF16 once at create; rhs forms the element Hessians T[162][Ne] and the
+// diagonal from them instead of the diag strip pass; the PCG applies H from T.
+// Once the b mask is frozen (or with a fixed mask0), H, diag and M^-1 no
+// longer change and are formed only once.
 #include <cstdlib>
 #include <new>
+#include <type_traits>
 
 #include "ops.cuh"
 #include "pcg.cuh"
@@ -47,6 +54,11 @@ struct GnSolver {
   PcgState* pcg;
   Kpair<T>* kp;
   bool frozen_set;
+  // precision form
+  bool mixed;
+  bool eh_fixed;     // T, diag and M^-1 are final (b mask frozen, or mask0)
+  float* T_eh;       // [162][Ne] element Hessians
+  void* grad_bf16;   // (Nvox,3) BF16
   // PCG graph
   cudaStream_t cap_stream;
   cudaGraph_t graph;
@@ -261,6 +273,31 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
     a.out = S->w;
     if ((st = launch_kref_apply<T>(a, S->Kel, s))) return st;
   }
+  if constexpr (std::is_same<T, float>::value) {
+    if (S->mixed) {
+      EhMatvecArgs ma{};
+      ma.m = S->m;
+      ma.T = S->T_eh;
+      ma.v = S->z;
+      ma.p_old = S->p;
+      ma.st = S->pcg;
+      ma.ev = S->evA;
+      for (int q = 0; q < 64; ++q) ma.L8[q] = S->L8[q];
+      if (d.ll != 0.0 && d.reg_type == VDVC_REG_LAPLACIAN) {
+        ma.nreg = 1;
+        ma.c1 = (float)(d.ll * d.h);
+      } else if (d.ll != 0.0 && d.reg_type == VDVC_REG_EQUILIBRIUM_GAP) {
+        ma.nreg = 2;
+        ma.c1 = (float)(d.ll * d.eps_reg * d.h);
+        ma.c2 = (float)(d.ll * d.h);
+        ma.w = S->w;
+        ma.K2 = S->kp->K2;  // device address of the float K_el copy
+      }
+      if ((st = launch_eh_matvec<true>(ma, s))) return st;
+      if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s))) return st;
+      return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
+    }
+  }
   StripArgs<T> sa{};
   sa.m = S->m;
   sa.v = S->z;
@@ -368,6 +405,25 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
     return set_error(VDVC_ERR_WORKSPACE, "solver needs %zu bytes of workspace (got %zu)", need, ws_bytes);
   }
   carve_solver<T>(m, S, ws, ws_bytes);
+  S->mixed = d->precision == VDVC_PREC_MIXED;
+  if (d->precision != VDVC_PREC_PLAIN && !S->mixed) {
+    delete S;
+    return set_error(VDVC_ERR_ARG, "precision %d", d->precision);
+  }
+  if (S->mixed) {
+    Carve cv(d->eh_ws, d->eh_ws_bytes);
+    S->T_eh = cv.take<float>((size_t)162 * m.Ne);
+    S->grad_bf16 = cv.take<uint16_t>((size_t)3 * m.Nvox);
+    const bool ok = std::is_same<T, float>::value;
+    const bool h_ok = d->h == 1 || d->h == 2 || d->h == 3 || d->h == 4 || d->h == 6 || d->h == 8 || d->h == 12 ||
+                      d->h == 16;
+    if (!ok || !h_ok || !d->eh_ws || !cv.fits()) {
+      delete S;
+      if (!ok) return set_error(VDVC_ERR_ARG, "the precision form is a float32 solve");
+      if (!h_ok) return set_error(VDVC_ERR_UNSUPPORTED, "precision form for h=%d (h in {1,2,3,4,6,8,12,16})", d->h);
+      return set_error(VDVC_ERR_WORKSPACE, "precision form needs eh_ws of vdvc_eh_workspace_bytes bytes");
+    }
+  }
   if (d->K_lap) load_K(d->K_lap, &S->Klap);
   if (d->K_el) load_K(d->K_el, &S->Kel);
   // K_lap[3a+c][3b+c'] == (c == c') * L8[a][b] ?
@@ -383,6 +439,10 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
     }
   for (int a = 0; a < 8; ++a)
     for (int b = 0; b < 8; ++b) S->L8[a * 8 + b] = (float)S->Klap.k[(3 * a) * 24 + 3 * b];
+  if (S->mixed && d->reg_type != VDVC_REG_NONE && !S->lap_blockdiag) {
+    delete S;
+    return set_error(VDVC_ERR_UNSUPPORTED, "precision form needs K_lap = one 8x8 block per component");
+  }
   S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 4;
   cudaStream_t s = (cudaStream_t)d->stream;
   int e = VDVC_OK;
@@ -421,6 +481,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   }
   k_set_U<T><<<nblk(m.Ndof), 256, 0, s>>>(nullptr, m.Ndof, S->U64, S->U32);
   count_launch();
+  if (S->mixed && (e = launch_grad_bf16((const float*)d->grad, 3 * m.Nvox, S->grad_bf16, s))) return fail(e);
   // sync before the graph (captured on a private stream) sees the buffers
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail(set_error(VDVC_ERR_CUDA, "solver setup sync failed"));
   *out = S;
@@ -437,13 +498,19 @@ static int set_U(GnSolver<T>* S, const double* U0, cudaStream_t s) {
 // Frozen-H preconditioner (dynamic_mask == 0): diag H over mask0, built once.
 template <typename T>
 static int frozen_diag(GnSolver<T>* S, cudaStream_t s) {
-  StripArgs<T> a{};
-  a.m = S->m;
-  a.grad = (const T*)S->d.grad;
-  a.mask = S->d.mask0;
-  a.evD = S->evD;
-  int st = launch_strip<T, kModeDiag>(a, nullptr, s);
-  if (st) return st;
+  int st;
+  if (S->mixed) {
+    EhFormArgs fa{S->m, S->grad_bf16, S->d.mask0, S->T_eh, (float*)S->evD};
+    if ((st = launch_eh_form(fa, s))) return st;
+    S->eh_fixed = true;
+  } else {
+    StripArgs<T> a{};
+    a.m = S->m;
+    a.grad = (const T*)S->d.grad;
+    a.mask = S->d.mask0;
+    a.evD = S->evD;
+    if ((st = launch_strip<T, kModeDiag>(a, nullptr, s))) return st;
+  }
   GridReduce red{S->partials, S->ticket};
   k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, kReduceBlocks), 256, 0, s>>>(
       S->m, S->evD, S->evD, nullptr, S->d.ll, S->d.reg_type != VDVC_REG_NONE ? S->diag_reg : nullptr, S->t1,
@@ -501,17 +568,25 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
   a.status = &S->sc->status;
   a.evA = S->evA;
   a.evD = S->evD;
-  if (d.dynamic_mask)
+  // diag H from the strip pass (plain), from the element Hessians (mixed), or
+  // not at all once it is final
+  const bool with_diag = d.dynamic_mask && !S->eh_fixed;
+  if (with_diag && !S->mixed)
     st = launch_strip<T, kModeB | kModeRes | kModeDiag>(a, nullptr, s);
   else
     st = launch_strip<T, kModeB | kModeRes>(a, nullptr, s);
   if (st) return st;
+  if (with_diag && S->mixed) {
+    EhFormArgs fa{S->m, S->grad_bf16, S->frozen, S->T_eh, (float*)S->evD};
+    if ((st = launch_eh_form(fa, s))) return st;
+    if (S->frozen_set) S->eh_fixed = true;
+  }
   GridReduce red{S->partials, S->ticket};
   k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, kReduceBlocks), 256, 0, s>>>(
       S->m, S->evA, S->evD, reg ? S->ru : nullptr, d.ll, d.reg_type != VDVC_REG_NONE ? S->diag_reg : nullptr, S->b,
-      S->diag, S->sc, red, d.dynamic_mask != 0);
+      S->diag, S->sc, red, with_diag);
   VDVC_LAUNCHED();
-  if (d.dynamic_mask) {
+  if (with_diag) {
     k_gn_minv<T><<<nblk(S->m.Ndof), 256, 0, s>>>(S->diag, S->m.Ndof, S->sc, S->Minv);
     VDVC_LAUNCHED();
   }

@@ -1,0 +1,300 @@
+// Precision form of the Hessian: BF16 image gradient, element Hessians
+// formed once per Gauss-Newton iteration with FP32 accumulation, FP32
+// element-Hessian matvecs in the PCG.
+//
+// Element Hessian structure.  With owner-computes quadrature (strip.cuh),
+//   K_e[(a,k),(b,l)] = sum_q w_q m_q N_a(q) N_b(q) g_k(q) g_l(q),
+// N_a = phi_ax phi_ay phi_az.  Per axis, phi_ax phi_bx takes one of three
+// values psi_s (s = ax + bx: phi0^2, phi0 phi1, phi1^2), and g_k g_l is
+// symmetric, so K_e has 27 x 6 = 162 distinct entries
+//   T[sx][sy][sz][kl] = sum_q w m psi_sx(qx) psi_sy(qy) psi_sz(qz) G_kl(q),
+// G = (g0g0, g0g1, g0g2, g1g1, g1g2, g2g2).  T is formed separably (per
+// voxel 18 FMAs along y, 54 per z plane, the x sum as a shared-memory
+// reduction over the element's voxel columns) and stored SoA [162][Ne].
+// A BF16 x BF16 product is exact in FP32, so G carries no rounding beyond
+// the BF16 gradient itself.
+#include <cuda_bf16.h>
+
+#include "ops.cuh"
+#include "pcg.cuh"
+
+namespace vdvc {
+
+__global__ void k_grad_to_bf16(const float* __restrict__ g, long long n, __nv_bfloat16* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = __float2bfloat16_rn(g[i]);
+}
+
+
+constexpr int kRP = 55;  // shared-memory pitch of a column's 54 partial sums (odd: no bank conflicts)
+
+template <int H>
+__global__ void __launch_bounds__(128) k_eh_form(const EhFormArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int EX = (H >= 128) ? 1 : 128 / H;
+  float* s_R = (float*)smem_raw;  // (nthr + 1) * kRP: one row per column, +1 for the mesh's last column
+  const Mesh& m = a.m;
+  const int nthr = blockDim.x;
+  const int t = threadIdx.x;
+  const int el = t / H, qx = t - el * H;
+  const int i0 = blockIdx.x * EX, i = i0 + el;
+  const int j = blockIdx.y, k = blockIdx.z;
+  const int nel = min(EX, m.Nx - i0);
+  const bool active = el < nel;
+  const bool y_last = (j == m.Ny - 1), z_last = (k == m.Nz - 1);
+  const int ncol = active ? ((i == m.Nx - 1 && qx == H - 1) ? 2 : 1) : 0;
+  const float wy_first = (j == 0) ? 0.5f : 1.f;
+  const long long row_stride = m.Nvx;
+
+  for (int r = 0; r < kRP; ++r) s_R[t * kRP + r] = 0.f;
+  if (t == 0)
+    for (int r = 0; r < kRP; ++r) s_R[nthr * kRP + r] = 0.f;
+  __syncthreads();
+
+  for (int col = 0; col < ncol; ++col) {
+    const int qxc = qx + col;
+    const long long x = (long long)i * H + qxc;
+    float R[54];  // [sy][sz][kl]
+#pragma unroll
+    for (int q = 0; q < 54; ++q) R[q] = 0.f;
+#pragma unroll 1
+    for (int qz = 0; qz <= H; ++qz) {
+      if (qz == H && !z_last) break;
+      const float fz1 = (float)qz / (float)H, fz0 = 1.f - fz1;
+      const long long vz = (long long)k * H + qz;
+      const float wz = (vz == 0 || vz == m.Nvz - 1) ? 0.5f : 1.f;
+      const float pz[3] = {wz * fz0 * fz0, wz * fz0 * fz1, wz * fz1 * fz1};
+      const long long v0 = x + (long long)j * H * row_stride + vz * m.NvxNvy;
+      float S[18];  // [sy][kl]
+#pragma unroll
+      for (int q = 0; q < 18; ++q) S[q] = 0.f;
+#pragma unroll
+      for (int qy = 0; qy <= H; ++qy) {
+        if (qy == H && !y_last) break;
+        const long long v = v0 + (long long)qy * row_stride;
+        const __nv_bfloat16* gb = (const __nv_bfloat16*)a.grad + 3 * v;
+        const float g0 = __bfloat162float(gb[0]);
+        const float g1 = __bfloat162float(gb[1]);
+        const float g2 = __bfloat162float(gb[2]);
+        float W = a.mask[v] ? 1.f : 0.f;
+        if (qy == 0) W *= wy_first;
+        if (qy == H) W *= 0.5f;
+        const float fy1 = (float)qy / (float)H, fy0 = 1.f - fy1;
+        const float py[3] = {W * fy0 * fy0, W * fy0 * fy1, W * fy1 * fy1};
+        const float G[6] = {g0 * g0, g0 * g1, g0 * g2, g1 * g1, g1 * g2, g2 * g2};
+#pragma unroll
+        for (int sy = 0; sy < 3; ++sy)
+#pragma unroll
+          for (int kl = 0; kl < 6; ++kl) S[sy * 6 + kl] += py[sy] * G[kl];
+      }
+#pragma unroll
+      for (int sy = 0; sy < 3; ++sy)
+#pragma unroll
+        for (int sz = 0; sz < 3; ++sz)
+#pragma unroll
+          for (int kl = 0; kl < 6; ++kl) R[(sy * 3 + sz) * 6 + kl] += pz[sz] * S[sy * 6 + kl];
+    }
+    const float wx = (x == 0 || x == (long long)m.Nvx - 1) ? 0.5f : 1.f;
+    float* row = s_R + (size_t)(col == 0 ? t : nthr) * kRP;
+#pragma unroll
+    for (int q = 0; q < 54; ++q) row[q] = wx * R[q];
+  }
+  __syncthreads();
+
+  // x reduction: T[sx][sy][sz][kl] = sum over the element's columns of psi_sx(qx) R
+  const bool last_strip = (i0 + nel == m.Nx);
+  const long long e_base = (long long)i0 + (long long)j * m.Nx + (long long)k * m.Nx * m.Ny;
+  for (int idx = t; idx < nel * 162; idx += nthr) {
+    const int o = idx / nel, e = idx - o * nel;  // element fastest: coalesced stores
+    const int sx = o / 54, rest = o - sx * 54;    // rest = (sy*3+sz)*6 + kl
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < H; ++q) {
+      const float f1 = (float)q / (float)H, f0 = 1.f - f1;
+      const float px = sx == 0 ? f0 * f0 : (sx == 1 ? f0 * f1 : f1 * f1);
+      s += px * s_R[(e * H + q) * kRP + rest];
+    }
+    if (last_strip && e == nel - 1 && sx == 2) s += s_R[nthr * kRP + rest];  // column x = Nx*h: psi = (0,0,1)
+    a.T[(long long)o * m.Ne + e_base + e] = s;
+    // diagonal of K_e: a = (sx/2, sy/2, sz/2) with sx,sy,sz in {0,2}, kl in {00,11,22}
+    const int sy = rest / 18, sz = (rest / 6) % 3, kl = rest % 6;
+    if ((sx & 1) == 0 && (sy & 1) == 0 && (sz & 1) == 0 && (kl == 0 || kl == 3 || kl == 5)) {
+      const int corner = corner_of(sx >> 1, sy >> 1, sz >> 1);
+      const int kk = kl == 0 ? 0 : (kl == 3 ? 1 : 2);
+      a.evD[(long long)(3 * corner + kk) * m.Ne + e_base + e] = s;
+    }
+  }
+}
+
+// kl index of the unordered component pair (k,l)
+__host__ __device__ constexpr int kl_index(int k, int l) {
+  return k > l ? kl_index(l, k) : (k == 0 ? l : (k == 1 ? 2 + l : 5));
+}
+
+
+// One thread per element: out_e = K_e v_e (+ regularizer), 576 FMAs from the
+// 162 distinct entries.
+template <bool PCG>
+__global__ void __launch_bounds__(256, 3) k_eh_matvec(const EhMatvecArgs a) {
+  if constexpr (PCG) {
+    if (a.st->done) return;
+  }
+  const Mesh& m = a.m;
+  float beta = 0.f;
+  if constexpr (PCG) beta = (float)a.st->beta;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m.Ne;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int ei = (int)(e % m.Nx);
+    const long long rr = e / m.Nx;
+    const int ej = (int)(rr % m.Ny), ek = (int)(rr / m.Ny);
+    float vl[24], out[24];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const long long node = (long long)(ei + corner_dx(b)) + (long long)(ej + corner_dy(b)) * m.Nnx +
+                             (long long)(ek + corner_dz(b)) * m.NnxNny;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float val = a.v[3 * node + c];
+        if constexpr (PCG) val += beta * a.p_old[3 * node + c];
+        vl[3 * b + c] = val;
+        out[3 * b + c] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int sx = 0; sx < 3; ++sx)
+#pragma unroll
+      for (int sy = 0; sy < 3; ++sy)
+#pragma unroll
+        for (int sz = 0; sz < 3; ++sz) {
+          const int type = (sx * 3 + sy) * 3 + sz;
+          float tv[6];
+#pragma unroll
+          for (int kl = 0; kl < 6; ++kl) tv[kl] = __ldg(a.T + (long long)(type * 6 + kl) * m.Ne + e);
+#pragma unroll
+          for (int aa = 0; aa < 8; ++aa)
+#pragma unroll
+            for (int bb = 0; bb < 8; ++bb) {
+              if (corner_dx(aa) + corner_dx(bb) != sx || corner_dy(aa) + corner_dy(bb) != sy ||
+                  corner_dz(aa) + corner_dz(bb) != sz)
+                continue;
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+                for (int ll = 0; ll < 3; ++ll) out[3 * aa + kk] += tv[kl_index(kk, ll)] * vl[3 * bb + ll];
+            }
+        }
+    if (a.nreg >= 1) {
+#pragma unroll
+      for (int aa = 0; aa < 8; ++aa)
+#pragma unroll
+        for (int bb = 0; bb < 8; ++bb) {
+          const float lw = a.c1 * a.L8[aa * 8 + bb];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) out[3 * aa + c] += lw * vl[3 * bb + c];
+        }
+      if (a.nreg == 2) {
+        // the element's w values reuse the registers of v (no longer needed)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+          const long long node = (long long)(ei + corner_dx(b)) + (long long)(ej + corner_dy(b)) * m.Nnx +
+                                 (long long)(ek + corner_dz(b)) * m.NnxNny;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) vl[3 * b + c] = a.w[3 * node + c];
+        }
+#pragma unroll 4
+        for (int r = 0; r < 24; ++r) {
+          float s = 0.f;
+#pragma unroll
+          for (int q = 0; q < 24; ++q) s += __ldg(a.K2 + r * 24 + q) * vl[q];
+          out[r] += a.c2 * s;
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 24; ++r) a.ev[(long long)r * m.Ne + e] = out[r];
+  }
+}
+
+template <int H>
+static int launch_form(const EhFormArgs& args, cudaStream_t s) {
+  constexpr int EX = (H >= 128) ? 1 : 128 / H;
+  const int threads = (EX * H + 31) / 32 * 32;
+  const size_t smem = (size_t)(threads + 1) * kRP * sizeof(float);
+  dim3 grid((args.m.Nx + EX - 1) / EX, args.m.Ny, args.m.Nz);
+  k_eh_form<H><<<grid, threads, smem, s>>>(args);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int launch_eh_form(const EhFormArgs& a, cudaStream_t s) {
+  switch (a.m.h) {
+    case 1: return launch_form<1>(a, s);
+    case 2: return launch_form<2>(a, s);
+    case 3: return launch_form<3>(a, s);
+    case 4: return launch_form<4>(a, s);
+    case 6: return launch_form<6>(a, s);
+    case 8: return launch_form<8>(a, s);
+    case 12: return launch_form<12>(a, s);
+    case 16: return launch_form<16>(a, s);
+  }
+  return set_error(VDVC_ERR_UNSUPPORTED, "element Hessians for h=%d are not built (h in {1,2,3,4,6,8,12,16})", a.m.h);
+}
+
+template <bool PCG>
+int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s) {
+  k_eh_matvec<PCG><<<grid_blocks(a.m.Ne, 256, 152 * 16), 256, 0, s>>>(a);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+template int launch_eh_matvec<false>(const EhMatvecArgs&, cudaStream_t);
+template int launch_eh_matvec<true>(const EhMatvecArgs&, cudaStream_t);
+
+int launch_grad_bf16(const float* g, long long n, void* out, cudaStream_t s) {
+  k_grad_to_bf16<<<grid_blocks(n, 256, 152 * 32), 256, 0, s>>>(g, n, (__nv_bfloat16*)out);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+}  // namespace vdvc
+
+using namespace vdvc;
+
+extern "C" {
+
+size_t vdvc_eh_workspace_bytes(int h, int Nx, int Ny, int Nz) {
+  Mesh m;
+  if (make_mesh(h, Nx, Ny, Nz, &m)) return 0;
+  Carve cv(nullptr, 0);
+  cv.take<float>((size_t)162 * m.Ne);
+  cv.take<float>((size_t)24 * m.Ne);
+  cv.take<float>((size_t)24 * m.Ne);
+  cv.take<uint16_t>((size_t)3 * m.Nvox);
+  return cv.off + 256;
+}
+
+int vdvc_matvec_H_mixed(const float* v, const float* grad, const uint8_t* mask, int h, int Nx, int Ny, int Nz,
+                        float* out, void* ws, size_t ws_bytes, vdvc_stream_t stream) {
+  Mesh m;
+  int st = make_mesh(h, Nx, Ny, Nz, &m);
+  if (st) return st;
+  VDVC_CHECK_ARG(v && grad && mask && out, "null pointer");
+  Carve cv(ws, ws_bytes);
+  float* T = cv.take<float>((size_t)162 * m.Ne);
+  float* evD = cv.take<float>((size_t)24 * m.Ne);
+  float* ev = cv.take<float>((size_t)24 * m.Ne);
+  uint16_t* gb = cv.take<uint16_t>((size_t)3 * m.Nvox);
+  if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "mixed matvec needs %zu bytes of workspace", cv.off);
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((st = launch_grad_bf16(grad, 3 * m.Nvox, gb, s))) return st;
+  EhFormArgs fa{m, (const __nv_bfloat16*)gb, mask, T, evD};
+  if ((st = launch_eh_form(fa, s))) return st;
+  EhMatvecArgs ma{};
+  ma.m = m;
+  ma.T = T;
+  ma.v = v;
+  ma.ev = ev;
+  if ((st = launch_eh_matvec<false>(ma, s))) return st;
+  return launch_gather<float>(m, ev, out, s);
+}
+
+}  // extern "C"

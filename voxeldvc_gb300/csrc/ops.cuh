@@ -42,6 +42,10 @@ int launch_strip_tma(const StripArgs<float>& args, const Kpair<float>* kp, cudaS
 // when h has no specialisation.
 template <bool PCG>
 int launch_strip_fast(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s);
+// Thread-per-element float32 Hessian pass for h <= 4 (elem_fast.cu);
+// VDVC_ERR_UNSUPPORTED when h has no specialisation.
+template <bool PCG>
+int launch_elem_fast(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s);
 bool tma_enabled();
 long long strip_grid_blocks(const Mesh& m);
 
@@ -83,6 +87,35 @@ int launch_sample(const SampleArgs<T>& args, cudaStream_t s);
 template <typename T>
 int launch_masked_stats(const T* field, const uint8_t* mask, const Mesh& m, GridReduce red, double* out3,
                         cudaStream_t s);
+
+// Precision form (mixed.cu): BF16 gradient, element Hessians T[162][Ne].
+struct EhFormArgs {
+  Mesh m;
+  const void* grad;       // __nv_bfloat16  // (Nvox,3)
+  const uint8_t* mask;        // H mask
+  float* T;                   // [162][Ne]
+  float* evD;                 // [24][Ne] diagonal contributions
+};
+
+struct EhMatvecArgs {
+  Mesh m;
+  const float* T;      // [162][Ne]
+  const float* v;      // nodal input (PCG: z)
+  const float* p_old;  // PCG: p_new = z + beta p_old
+  const PcgState* st;
+  float* ev;           // [24][Ne]
+  // regularizer: c1 * (L8 on each component) v_e + c2 * K2 w_e
+  int nreg;
+  float c1, c2;
+  float L8[64];
+  const float* w;
+  const float* K2;     // 576 (device)
+};
+
+int launch_eh_form(const EhFormArgs& a, cudaStream_t s);
+template <bool PCG>
+int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s);
+int launch_grad_bf16(const float* g, long long n, void* out, cudaStream_t s);
 
 inline int grid_blocks(long long n, int threads, long long cap) {
   long long b = (n + threads - 1) / threads;

@@ -8,9 +8,17 @@
 //   update     x += alpha p ; r -= alpha Ap ; z = M r ; res = sqrt(r.r / r0)
 //              done if res < tol or it+1 == max_iter ; beta = r.z_new/(rz + 1e-30)
 // p_new is formed on the fly from z and p_old by the kernels that need it,
-// so there is no separate p-update pass.  Every kernel returns at once when
+// so there is no separate p-update pass.
+//
+// Dot products: each thread sums its few products in the vector type (FP32
+// for float vectors: the products' own rounding), converts once, and the
+// block and grid sums run in float64 in a fixed order.  FP64 arithmetic per
+// vector entry would run on GB300's much narrower FP64 pipe.  Every kernel returns at once when
 // state.done is set, which makes a captured chunk of iterations safe to
 // replay past convergence.
+#include <cstdint>
+#include <type_traits>
+
 #include "ops.cuh"
 #include "pcg.cuh"
 
@@ -61,7 +69,7 @@ __global__ void __launch_bounds__(256) k_pcg_gather(const Mesh m, const T* __res
   __shared__ double s_red[8];
   if (st->done) return;
   const T beta = (T)st->beta;
-  double pap = 0.0;
+  T pap = T(0);
   for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < m.Nnodes;
        n += (long long)gridDim.x * blockDim.x) {
     const int ni = (int)(n % m.Nnx);
@@ -82,10 +90,10 @@ __global__ void __launch_bounds__(256) k_pcg_gather(const Mesh m, const T* __res
       const T pn = z[d] + beta * p[d];
       p[d] = pn;
       Ap[d] = s[c];
-      pap += (double)pn * (double)s[c];
+      pap += pn * s[c];
     }
   }
-  double mine[1] = {block_sum(pap, s_red)}, out[1];
+  double mine[1] = {block_sum((double)pap, s_red)}, out[1];
   if (grid_reduce_sum<1>(red, mine, out, s_red) && threadIdx.x == 0) st->alpha = st->rz / (out[0] + 1e-30);
 }
 
@@ -106,21 +114,42 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_update(const T* __restrict__ p, const T* __restrict__ Ap,
                                                     const T* __restrict__ Minv, long long n, T* __restrict__ x,
                                                     T* __restrict__ r, T* __restrict__ z, PcgState* st,
-                                                    GridReduce red) {
+                                                    GridReduce red, bool vec4) {
   __shared__ double s_red[8];
   if (st->done) return;
   const T alpha = (T)st->alpha;
-  double rr = 0.0, rz = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+  T rr = T(0), rz = T(0);
+  const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i0 = 0;
+  if constexpr (std::is_same<T, float>::value) {
+    if (vec4) {  // every pointer 16-byte aligned: float4 body, scalar tail
+      const long long n4 = n >> 2;
+      for (long long q = gtid; q < n4; q += stride) {
+        const float4 pv = ((const float4*)p)[q], av = ((const float4*)Ap)[q], mv = ((const float4*)Minv)[q];
+        float4 xv = ((float4*)x)[q], rv = ((float4*)r)[q], zv;
+        xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+        rv.x -= alpha * av.x; rv.y -= alpha * av.y; rv.z -= alpha * av.z; rv.w -= alpha * av.w;
+        zv.x = mv.x * rv.x; zv.y = mv.y * rv.y; zv.z = mv.z * rv.z; zv.w = mv.w * rv.w;
+        ((float4*)x)[q] = xv;
+        ((float4*)r)[q] = rv;
+        ((float4*)z)[q] = zv;
+        rr += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+        rz += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z + rv.w * zv.w;
+      }
+      i0 = n4 << 2;
+    }
+  }
+  for (long long i = i0 + gtid; i < n; i += stride) {
     x[i] = x[i] + alpha * p[i];
     const T ri = r[i] - alpha * Ap[i];
     const T zi = Minv[i] * ri;
     r[i] = ri;
     z[i] = zi;
-    rr += (double)ri * (double)ri;
-    rz += (double)ri * (double)zi;
+    rr += ri * ri;
+    rz += ri * zi;
   }
-  double mine[2] = {block_sum(rr, s_red), block_sum(rz, s_red)}, out[2];
+  double mine[2] = {block_sum((double)rr, s_red), block_sum((double)rz, s_red)}, out[2];
   if (grid_reduce_sum<2>(red, mine, out, s_red) && threadIdx.x == 0) {
     const double res = sqrt(out[0] / st->r0);
     st->rr = out[0];
@@ -148,6 +177,7 @@ __global__ void __launch_bounds__(256) k_pcg_pupdate(const T* __restrict__ z, T*
 }
 
 inline int vec_blocks(long long n) { return grid_blocks(n, 256, kReduceBlocks); }
+inline bool aligned16(const void* q) { return ((uintptr_t)q & 15u) == 0; }
 
 template <typename T>
 int launch_pcg_init(const T* b, const T* Ax, const T* Minv, long long n, T* r, T* z, T* p, bool p_is_z, T* x0,
@@ -168,7 +198,8 @@ int launch_pcg_gather(const Mesh& m, const T* ev, const T* z, T* p, T* Ap, PcgSt
 template <typename T>
 int launch_pcg_update(const T* p, const T* Ap, const T* Minv, long long n, T* x, T* r, T* z, PcgState* st,
                       GridReduce red, cudaStream_t s) {
-  k_pcg_update<T><<<vec_blocks(n), 256, 0, s>>>(p, Ap, Minv, n, x, r, z, st, red);
+  const bool vec4 = aligned16(p) && aligned16(Ap) && aligned16(Minv) && aligned16(x) && aligned16(r) && aligned16(z);
+  k_pcg_update<T><<<vec_blocks(vec4 ? (n + 3) / 4 : n), 256, 0, s>>>(p, Ap, Minv, n, x, r, z, st, red, vec4);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }

@@ -315,7 +315,8 @@ size_t strip_smem_bytes(int h, int mode, size_t tsize) {
 }
 
 // Kernel selection for the float32 Hessian pass: VDVC_HV_KERNEL=fast (the
-// default: compile-time-h specialisation, strip_fast.cu), tma (bulk-copy
+// default: thread per element for h <= kElemMaxH (elem_fast.cu), else the
+// compile-time-h strip specialisation, strip_fast.cu), elem, strip, tma (bulk-copy
 // staging, strip_tma.cu) or generic (runtime h, this file).
 static int hv_kernel_choice() {
   static int choice = -1;
@@ -324,9 +325,14 @@ static int hv_kernel_choice() {
     choice = 0;
     if (e && e[0] == 't') choice = 1;
     if (e && e[0] == 'g') choice = 2;
+    if (e && e[0] == 'e') choice = 3;  // thread per element wherever specialised
+    if (e && e[0] == 's') choice = 4;  // strip kernels at every h
   }
   return choice;
 }
+
+// Default split: thread per element up to this h, strips above it.
+constexpr int kElemMaxH = 4;
 
 bool tma_enabled() { return hv_kernel_choice() == 1; }
 
@@ -337,7 +343,11 @@ int launch_strip(const StripArgs<T>& args, const Kpair<T>* kp, cudaStream_t s) {
     const int choice = hv_kernel_choice();
     const bool aligned = (((uintptr_t)args.grad | (uintptr_t)args.mask) & 15) == 0;
     if (choice == 1 && aligned) return launch_strip_tma<pcg>(args, kp, s);
-    if (choice == 0) {
+    if (choice == 3 || (choice == 0 && args.m.h <= kElemMaxH)) {
+      const int st = launch_elem_fast<pcg>(args, kp, s);
+      if (st != VDVC_ERR_UNSUPPORTED) return st;
+    }
+    if (choice == 0 || choice == 3 || choice == 4) {
       const int st = launch_strip_fast<pcg>(args, kp, s);
       if (st != VDVC_ERR_UNSUPPORTED) return st;
     }

@@ -270,8 +270,18 @@ def _plane_wave(Nx, Ny, Nz, h, dtype):
 def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
                  c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False,
                  freeze_mask_after=None, U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
-                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None):
+                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=6):
     dtype = np.dtype(dtype)
+    if precision not in ('plain', 'mixed'):
+        raise ValueError("precision must be 'plain' or 'mixed'")
+    if precision == 'mixed' and dtype != np.float32:
+        raise ValueError("precision='mixed' is a float32 solve (BF16 gradient, FP32 element Hessians)")
+    # The element-Hessian form pays where an element's 162 stored entries
+    # weigh less than its voxels' gradient and mask (13 B x h^3): h >= 6.
+    # Below that the matrix-free FP32 pass moves less data and is kept.
+    if precision == 'mixed' and h < mixed_min_h:
+        precision = 'plain'
+
     Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, Nz * h + 1
     Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
     Nvox = Nvx * Nvy * Nvz
@@ -363,9 +373,15 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     desc.stream = D.stream()
     nbytes = L.vdvc_gn_workspace_bytes(desc.dtype, h, Nx, Ny, Nz)
     ws = D.torch().empty(nbytes, dtype=D.torch().uint8, device=D.device())
+    eh_ws = None
+    if precision == 'mixed':
+        desc.precision = 1
+        eh_bytes = L.vdvc_eh_workspace_bytes(h, Nx, Ny, Nz)
+        eh_ws = D.torch().empty(eh_bytes, dtype=D.torch().uint8, device=D.device())
+        desc.eh_ws, desc.eh_ws_bytes = eh_ws.data_ptr(), eh_bytes
     solver = C.c_void_p()
     _lib.check(L.vdvc_gn_create(C.byref(desc), ws.data_ptr(), nbytes, C.byref(solver)), "correlate_gpu")
-    info = {"gn_iters": 0, "pcg_iters": [], "ll": ll, "h": h}
+    info = {"gn_iters": 0, "pcg_iters": [], "ll": ll, "h": h, "precision": precision}
     t_start = time.perf_counter()
     try:
         st = D.stream()
@@ -405,7 +421,7 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     finally:
         L.vdvc_gn_destroy(solver)
         D.torch().cuda.current_stream().synchronize()
-        del ws
+        del ws, eh_ws
     info["gn_wall_s"] = time.perf_counter() - t_start
     if stats is not None:
         stats.append(info)

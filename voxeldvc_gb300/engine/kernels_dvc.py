@@ -243,6 +243,26 @@ def matvec_H(v, grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, xp, 
     return D.out(out, xp)
 
 
+def matvec_H_mixed(v, grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, xp, chunk_size=None):
+    """H v in the precision form: BF16 gradient, element Hessians formed with
+    FP32 accumulation, FP32 application.  Always computes in float32."""
+    _check_stencil(N_stencil, w_stencil, h)
+    Nvox, Ndof = _mesh_sizes(h, Nx, Ny, Nz)
+    dt = np.dtype(np.float32)
+    vd = D.to_device(v, dt).reshape(-1)
+    if vd.numel() != Ndof:
+        raise ValueError(f"v has {vd.numel()} entries, expected Ndof={Ndof}")
+    g, m = _grad_mask(grad_f_vox, mask0_vox, dt, Nvox)
+    out = D.empty(Ndof, dt)
+    n = _lib.lib().vdvc_eh_workspace_bytes(h, Nx, Ny, Nz)
+    if n == 0:
+        _lib.check(_lib.ERR_ARG, "element-Hessian workspace size query")
+    ws = D.scratch.get(n)
+    _lib.check(_lib.lib().vdvc_matvec_H_mixed(vd.data_ptr(), g.data_ptr(), m.data_ptr(), h, Nx, Ny, Nz,
+                                              out.data_ptr(), ws.data_ptr(), n, D.stream()), "matvec_H_mixed")
+    return D.out(out, xp)
+
+
 def build_diagonal_H(grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, Ndof, xp, chunk_size=None):
     """diag(H)[i] = sum over (e,q) touching dof i of w_q m_q v_eq[i]^2."""
     _check_stencil(N_stencil, w_stencil, h)
