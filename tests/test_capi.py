@@ -73,9 +73,24 @@ def test_status_mapping(lib):
     lib.check(lib.OK)
 
 
-def test_gn_desc_layout_matches_header(lib):
+def test_gn_desc_layout_matches_header(lib, tmp_path):
+    """Every field offset of the ctypes mirror equals the C compiler's."""
     import ctypes as C
-    # pointer-sized fields are 8-byte aligned; the struct ends with the stream
+    import shutil
+    import subprocess
     d = lib.GnDesc
-    assert d.stream.offset + C.sizeof(C.c_void_p) == C.sizeof(d)
-    assert d.K_lap.offset % 8 == 0 and d.f_vox.offset % 8 == 0
+    names = [f[0] for f in d._fields_]
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not found")
+    src = tmp_path / "layout.c"
+    body = "".join(f'  printf("{n} %zu\\n", offsetof(vdvc_gn_desc, {n}));\n' for n in names)
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "vdvc.h"\nint main(void) {\n' + body +
+                   '  printf("sizeof %zu\\n", sizeof(vdvc_gn_desc));\n  return 0;\n}\n')
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                       text=True).stdout.splitlines())
+    for n in names:
+        assert getattr(d, n).offset == int(out[n]), n
+    assert C.sizeof(d) == int(out["sizeof"])
