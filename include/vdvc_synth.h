@@ -22,8 +22,11 @@ enum {
   VDVC_FIELD_AFFINE = 0,   /* u = t + G (x - c); params: t[3], G[9] row-major, c[3]            */
   VDVC_FIELD_NECKING = 1,  /* u_z = ez*z; radial contraction a*exp(-(z-zc)^2/(2 s^2)) r/R;
                               params: ez, a, zc, s, xc, yc, R                                  */
-  VDVC_FIELD_AFFINE_SIN = 2 /* affine as above plus amp*sin(2 pi x_k / wl) on each component;
+  VDVC_FIELD_AFFINE_SIN = 2, /* affine as above plus amp*sin(2 pi x_k / wl) on each component;
                               params: t[3], G[9], c[3], amp, wl                               */
+  VDVC_FIELD_BUMPS = 3      /* affine as above plus n_b <= 6 Gaussian bumps
+                              A_b exp(-|x - c_b|^2 / (2 w_b^2)); params: t[3], G[9], c[3],
+                              n_b, then per bump c_b[3], w_b, A_b[3] (at most 64 params)     */
 };
 
 /* Bytes of scratch vdvc_synth_texture needs (one float volume + reductions). */
@@ -38,6 +41,12 @@ int vdvc_synth_texture(float* out, int nx, int ny, int nz,
                        double noise_amp, const float* cylinders, int n_cyl,
                        double cyl_value, void* ws, size_t ws_bytes,
                        vdvc_stream_t stream);
+
+/* u(x) at the grid points x = (i, j, k) * stride, FP32 (gx*gy*gz, 3),
+   x fastest: training targets of the learned initial guess. */
+int vdvc_synth_field_grid(int field, const double* params, int n_params,
+                          int gx, int gy, int gz, double stride, float* out,
+                          vdvc_stream_t stream);
 
 /* g(x) = f(x - u(x)) (trilinear, clamped) + N(0, noise_sigma^2). */
 int vdvc_synth_warp(const float* f, int nx, int ny, int nz, int field,

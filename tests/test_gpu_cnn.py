@@ -1,0 +1,235 @@
+"""CUDA kernels of the learned initial guess against the CPU oracle
+(oracle/cnn_oracle.py), kernel by kernel and as a whole network (forward
+output and every parameter gradient, BF16 rounding emulated in the oracle)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import cnn_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def env(cuda):
+    import torch
+    from voxeldvc_gb300 import _lib
+    from voxeldvc_gb300.learned import seednet as S
+    return torch, _lib, S
+
+
+def bf(torch, a):
+    """numpy (already BF16-representable) -> CUDA bfloat16 tensor, flat."""
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32).reshape(-1)).to("cuda").to(torch.bfloat16)
+
+
+def host(t):
+    return t.float().cpu().numpy().astype(np.float64)
+
+
+def stream(torch):
+    return torch.cuda.current_stream().cuda_stream
+
+
+CONV_CASES = [  # (cin, n_out, stride, source grid (x, y, z))
+    (2, 16, 1, (9, 7, 5)),
+    (16, 32, 2, (9, 8, 7)),
+    (32, 32, 1, (6, 5, 7)),
+    (64, 16, 1, (5, 5, 5)),
+    (16, 3, 1, (7, 6, 5)),
+    (32, 80, 2, (5, 7, 9)),
+]
+
+
+@pytest.mark.parametrize("cin,n_out,stride,src", CONV_CASES)
+def test_conv_forward_input_grad_wgrad(env, cin, n_out, stride, src):
+    torch, L, S = env
+    lib = L.lib()
+    rng = np.random.default_rng(cin * 7 + n_out)
+    sx, sy, sz = src
+    out = tuple((s - 1) // stride + 1 for s in src)
+    x = O.bf16_round(rng.standard_normal((sz, sy, sx, cin)))
+    W = rng.standard_normal((n_out, 27, cin)) * 0.2
+    bvec = rng.standard_normal(n_out).astype(np.float32)
+    Wr = O.bf16_round(W)
+    ref = O.conv(x, Wr, bvec.astype(np.float64), stride, relu=True)
+    # pack
+    npad8, npad16, kpad8 = (n_out + 7) // 8 * 8, (n_out + 15) // 16 * 16, (cin + 7) // 8 * 8
+    wt = torch.from_numpy(W.astype(np.float32).reshape(-1)).cuda()
+    wf = torch.zeros(npad8 * (64 if cin == 2 else 27 * cin), dtype=torch.bfloat16, device="cuda")
+    wb = torch.zeros(kpad8 * 27 * npad16, dtype=torch.bfloat16, device="cuda")
+    L.check(lib.vdvc_cnn_pack_weights(wt.data_ptr(), n_out, cin, wf.data_ptr(), wb.data_ptr(), stream(torch)))
+    xd = bf(torch, x)
+    bd = torch.from_numpy(bvec).cuda()
+    npos = out[0] * out[1] * out[2]
+    y = torch.zeros(npos * n_out, dtype=torch.bfloat16, device="cuda")
+    g = S.fwd_geom(out, src, stride)
+    L.check(lib.vdvc_cnn_conv(xd.data_ptr(), cin, 0, cin, wf.data_ptr(), bd.data_ptr(), n_out, 1, y.data_ptr(), 0,
+                              n_out, 0, 0, C.byref(g), stream(torch)))
+    yh = host(y).reshape(ref.shape)
+    assert np.allclose(yh, ref, rtol=8e-3, atol=8e-3 * np.abs(ref).max())
+
+    # FP32 output, no activation
+    yf = torch.zeros(npos * n_out, dtype=torch.float32, device="cuda")
+    L.check(lib.vdvc_cnn_conv(xd.data_ptr(), cin, 0, cin, wf.data_ptr(), None, n_out, 0, yf.data_ptr(), 1, n_out, 0,
+                              0, C.byref(g), stream(torch)))
+    ref_lin = O.conv(x, Wr, None, stride, relu=False)
+    assert rel(yf.cpu().numpy().reshape(ref.shape), ref_lin) < 1e-5
+
+    # input gradient through the transposed weights and the adjoint geometry
+    if cin != 2 and n_out <= 64:
+        dy = O.bf16_round(rng.standard_normal(ref.shape))
+        dyp = np.zeros(ref.shape[:3] + (npad16,))
+        dyp[..., :n_out] = dy
+        dx = torch.zeros(sx * sy * sz * cin, dtype=torch.bfloat16, device="cuda")
+        gb = S.bwd_geom(src, out, stride)
+        dypd = bf(torch, dyp)
+        L.check(lib.vdvc_cnn_conv(dypd.data_ptr(), npad16, 0, npad16, wb.data_ptr(), None, cin, 0,
+                                  dx.data_ptr(), 0, cin, 0, 0, C.byref(gb), stream(torch)))
+        ref_dx = O.conv_input_grad(dy, Wr, stride, (sz, sy, sx))
+        assert np.allclose(host(dx).reshape(ref_dx.shape), ref_dx, rtol=8e-3, atol=8e-3 * np.abs(ref_dx).max())
+
+    # weight and bias gradients
+    if n_out <= 32 and cin <= 64:
+        dy = O.bf16_round(rng.standard_normal(ref.shape))
+        dw = torch.zeros(n_out * 27 * cin, dtype=torch.float32, device="cuda")
+        db = torch.zeros(n_out, dtype=torch.float32, device="cuda")
+        nb = lib.vdvc_cnn_wgrad_workspace_bytes(n_out, cin)
+        ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        dyd = bf(torch, dy)
+        L.check(lib.vdvc_cnn_conv_wgrad(dyd.data_ptr(), n_out, 0, n_out, xd.data_ptr(), cin, 0, cin, C.byref(g),
+                                        dw.data_ptr(), 0, ws.data_ptr(), nb, stream(torch)))
+        L.check(lib.vdvc_cnn_bias_grad(dyd.data_ptr(), n_out, 0, n_out, npos, db.data_ptr(), 0, ws.data_ptr(), nb,
+                                       stream(torch)))
+        ref_dw, ref_db = O.conv_wgrad(dy, x, stride)
+        assert rel(dw.cpu().numpy().reshape(ref_dw.shape), ref_dw) < 1e-5
+        assert rel(db.cpu().numpy(), ref_db) < 1e-5
+        # accumulate mode adds
+        L.check(lib.vdvc_cnn_conv_wgrad(dyd.data_ptr(), n_out, 0, n_out, xd.data_ptr(), cin, 0, cin, C.byref(g),
+                                        dw.data_ptr(), 1, ws.data_ptr(), nb, stream(torch)))
+        assert rel(dw.cpu().numpy().reshape(ref_dw.shape), 2 * ref_dw) < 1e-5
+
+
+@pytest.mark.parametrize("m,n", [((3, 4, 5), (5, 7, 9)), ((3, 3, 3), (6, 6, 6))])
+def test_upsample(env, m, n):
+    torch, L, S = env
+    lib = L.lib()
+    rng = np.random.default_rng(1)
+    c = O.bf16_round(rng.standard_normal((m[2], m[1], m[0], 4)))
+    f = torch.zeros(n[0] * n[1] * n[2] * 8, dtype=torch.bfloat16, device="cuda")
+    cd = bf(torch, c)
+    L.check(lib.vdvc_cnn_upsample2(cd.data_ptr(), 4, 0, *m, f.data_ptr(), 8, 4, *n, 4, stream(torch)))
+    ref = O.upsample2(c, (n[2], n[1], n[0]))
+    fh = host(f).reshape(n[2], n[1], n[0], 8)
+    assert np.allclose(fh[..., 4:], ref, rtol=8e-3, atol=1e-2)
+    assert np.all(fh[..., :4] == 0)
+    df = O.bf16_round(rng.standard_normal((n[2], n[1], n[0], 4)))
+    dc = torch.zeros(m[0] * m[1] * m[2] * 4, dtype=torch.bfloat16, device="cuda")
+    dfd = bf(torch, df)
+    L.check(lib.vdvc_cnn_upsample2_bwd(dfd.data_ptr(), 4, 0, *n, dc.data_ptr(), 4, 0, *m, 4, stream(torch)))
+    ref_dc = O.upsample2_adjoint(df, (m[2], m[1], m[0]))
+    assert np.allclose(host(dc).reshape(ref_dc.shape), ref_dc, rtol=8e-3, atol=2e-2)
+
+
+def test_pool_input_mse_adam_seed(env):
+    torch, L, S = env
+    lib = L.lib()
+    rng = np.random.default_rng(2)
+    nx, ny, nz = 17, 13, 9
+    f = rng.random((nz, ny, nx)).astype(np.float32)
+    g = rng.random((nz, ny, nx)).astype(np.float32)
+    ms = np.array([0.4, 0.3, 0.6, 0.2])
+    gx, gy, gz = (nx - 1) // 4 + 1, (ny - 1) // 4 + 1, (nz - 1) // 4 + 1
+    out = torch.zeros(gx * gy * gz * 2, dtype=torch.bfloat16, device="cuda")
+    # device copies are held in names: a temporary's memory may be reused
+    # before the kernel runs
+    fd, gd_img = torch.from_numpy(f.reshape(-1)).cuda(), torch.from_numpy(g.reshape(-1)).cuda()
+    L.check(lib.vdvc_cnn_pool_input(fd.data_ptr(), gd_img.data_ptr(), nx, ny, nz, ms.ctypes.data_as(L.pd),
+                                    out.data_ptr(), stream(torch)))
+    ref = O.pool_input(f, g, ms)
+    assert np.allclose(host(out).reshape(ref.shape), ref, rtol=8e-3, atol=1e-2)
+
+    # mse and its gradient
+    npos = 50
+    pred = rng.standard_normal((npos, 8)).astype(np.float32)
+    tgt = rng.standard_normal((npos, 3)).astype(np.float32)
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    dp = torch.zeros(npos * 16, dtype=torch.bfloat16, device="cuda")
+    ws = torch.empty(1 << 16, dtype=torch.uint8, device="cuda")
+    pd_, td = torch.from_numpy(pred.reshape(-1)).cuda(), torch.from_numpy(tgt.reshape(-1)).cuda()
+    L.check(lib.vdvc_cnn_mse(pd_.data_ptr(), 8, td.data_ptr(), npos, loss.data_ptr(), dp.data_ptr(), 16, 2.0,
+                             ws.data_ptr(), ws.numel(), stream(torch)))
+    l_ref, d_ref = O.mse(pred[:, :3].astype(np.float64), tgt.astype(np.float64))
+    assert abs(loss.item() - l_ref) < 1e-12 * max(1, l_ref)
+    dph = host(dp).reshape(npos, 16)
+    assert np.allclose(dph[:, :3], 2.0 * d_ref, rtol=8e-3) and np.all(dph[:, 3:] == 0)
+
+    # Adam
+    n = 1000
+    w0 = rng.standard_normal(n).astype(np.float32)
+    gr = rng.standard_normal(n).astype(np.float32)
+    w, m, v = (torch.from_numpy(a.copy()).cuda() for a in (w0, np.zeros(n, np.float32), np.zeros(n, np.float32)))
+    gd = torch.from_numpy(gr).cuda()
+    for step in (1, 2):
+        L.check(lib.vdvc_cnn_adam(w.data_ptr(), gd.data_ptr(), m.data_ptr(), v.data_ptr(), n, 1e-2, 0.9, 0.999, 1e-8,
+                                  step, stream(torch)))
+    mr, vr, wr = np.zeros(n), np.zeros(n), w0.astype(np.float64)
+    for step in (1, 2):
+        mr = 0.9 * mr + 0.1 * gr
+        vr = 0.999 * vr + 0.001 * gr.astype(np.float64) ** 2
+        wr = wr - 1e-2 * (mr / (1 - 0.9 ** step)) / (np.sqrt(vr / (1 - 0.999 ** step)) + 1e-8)
+    assert np.allclose(w.cpu().numpy(), wr, rtol=1e-5, atol=1e-6)
+
+    # nodal seed: trilinear resampling of the stride-8 output at node * h
+    px, py, pz = 5, 4, 3
+    pr = rng.standard_normal((pz, py, px, 8)).astype(np.float32)
+    h, Nx, Ny, Nz = 4, 8, 6, 4
+    U = torch.zeros(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), dtype=torch.float64, device="cuda")
+    prd = torch.from_numpy(pr.reshape(-1)).cuda()
+    L.check(lib.vdvc_cnn_seed_nodes(prd.data_ptr(), 8, px, py, pz, h, Nx, Ny, Nz, U.data_ptr(), stream(torch)))
+    from scipy.ndimage import map_coordinates
+    k, j, i = np.meshgrid(np.arange(Nz + 1), np.arange(Ny + 1), np.arange(Nx + 1), indexing="ij")
+    coords = np.stack([k * h / 8.0, j * h / 8.0, i * h / 8.0]).reshape(3, -1)
+    ref = np.stack([map_coordinates(pr[..., c].astype(np.float64), coords, order=1, mode="nearest")
+                    for c in range(3)], axis=1).reshape(-1)
+    assert np.allclose(U.cpu().numpy(), ref, atol=1e-5)
+
+
+def test_network_forward_and_gradients(env):
+    """The whole network on the GPU vs the oracle with BF16 emulation."""
+    torch, L, S = env
+    from voxeldvc_gb300.learned.arch import LAYERS, grids
+    rng = np.random.default_rng(11)
+    params = O.init_params(LAYERS, seed=3)
+    params = {k: (W, rng.standard_normal(b.shape) * 0.05) for k, (W, b) in params.items()}
+    net = S.SeedNet(params)
+    G = (17, 13, 9)
+    G, n, m = grids(G)
+    x = O.bf16_round(rng.standard_normal((G[2], G[1], G[0], 2)))
+    target = rng.standard_normal((n[2], n[1], n[0], 3)).astype(np.float32)
+    b = net.buffers(G)
+    b["x"].copy_(bf(torch, x))
+    pred = net.forward(G)
+    tg = torch.from_numpy(target.reshape(-1)).cuda()
+    loss = net.loss(G, tg)
+    net.backward(G)
+    torch.cuda.synchronize()
+    pnp = {k: (v[0].astype(np.float32).astype(np.float64), v[1].astype(np.float32).astype(np.float64))
+           for k, v in params.items()}
+    ref_pred, cache = O.forward(pnp, x, LAYERS, bf16=True)
+    gp = pred.cpu().numpy().reshape(n[2], n[1], n[0], 8)[..., :3]
+    assert rel(gp, ref_pred) < 1e-2
+    l_ref, d_ref = O.mse(gp.astype(np.float64), target.astype(np.float64))
+    assert abs(loss.item() - l_ref) < 1e-6 * l_ref
+    grads = O.backward(cache, d_ref, LAYERS, bf16=True)
+    gg = net.grads_numpy()
+    for name in grads:
+        assert rel(gg[name][0], grads[name][0]) < 3e-2, name
+        assert rel(gg[name][1], grads[name][1]) < 3e-2, name

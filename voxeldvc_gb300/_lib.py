@@ -88,7 +88,26 @@ SIGNATURES = {
     "vdvc_synth_workspace_bytes": (cz, [ci, ci, ci]),
     "vdvc_synth_texture": (ci, [vp, ci, ci, ci, C.c_ulonglong, cd, cd, vp, ci, cd, vp, cz, vp]),
     "vdvc_synth_warp": (ci, [vp, ci, ci, ci, ci, pd, ci, cd, C.c_ulonglong, vp, vp]),
+    "vdvc_synth_field_grid": (ci, [ci, pd, ci, ci, ci, ci, cd, vp, vp]),
+    # include/vdvc_cnn.h
+    "vdvc_cnn_conv": (ci, [vp, ci, ci, ci, vp, vp, ci, ci, vp, ci, ci, ci, ci, vp, vp]),
+    "vdvc_cnn_conv_wgrad": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, vp, vp, ci, vp, cz, vp]),
+    "vdvc_cnn_wgrad_workspace_bytes": (cz, [ci, ci]),
+    "vdvc_cnn_bias_grad": (ci, [vp, ci, ci, ci, C.c_longlong, vp, ci, vp, cz, vp]),
+    "vdvc_cnn_relu_bwd": (ci, [vp, vp, C.c_longlong, vp]),
+    "vdvc_cnn_upsample2": (ci, [vp, ci, ci, ci, ci, ci, vp, ci, ci, ci, ci, ci, ci, vp]),
+    "vdvc_cnn_upsample2_bwd": (ci, [vp, ci, ci, ci, ci, ci, vp, ci, ci, ci, ci, ci, ci, vp]),
+    "vdvc_cnn_pool_input": (ci, [vp, vp, ci, ci, ci, pd, vp, vp]),
+    "vdvc_cnn_mse": (ci, [vp, ci, vp, C.c_longlong, vp, vp, ci, cd, vp, cz, vp]),
+    "vdvc_cnn_adam": (ci, [vp, vp, vp, vp, C.c_longlong, cd, cd, cd, cd, ci, vp]),
+    "vdvc_cnn_pack_weights": (ci, [vp, ci, ci, vp, vp, vp]),
+    "vdvc_cnn_seed_nodes": (ci, [vp, ci, ci, ci, ci, ci, ci, ci, ci, vp, vp]),
 }
+
+
+class ConvGeom(C.Structure):
+    """ctypes mirror of vdvc_conv_geom (include/vdvc_cnn.h)."""
+    _fields_ = [(n, ci) for n in ("nx", "ny", "nz", "sx", "sy", "sz", "a", "b", "c", "d")]
 
 GN_U, GN_DU, GN_RES, GN_LIVE_MASK = 0, 1, 2, 3
 

@@ -126,9 +126,11 @@ __global__ void k_normalize(float* __restrict__ a, long long n, const float* __r
     a[i] = (a[i] - mn) * inv;
 }
 
+constexpr int kMaxFieldParams = 64;
+
 struct FieldParams {
   int kind;
-  double p[24];
+  double p[kMaxFieldParams];
 };
 
 __device__ __forceinline__ void field_u(const FieldParams& fp, double x, double y, double z, double u[3]) {
@@ -148,6 +150,32 @@ __device__ __forceinline__ void field_u(const FieldParams& fp, double x, double 
     const double amp = p[15], wl = p[16];
     const double xs[3] = {x, y, z};
     for (int k = 0; k < 3; ++k) u[k] += amp * sin(2.0 * 3.14159265358979323846 * xs[(k + 1) % 3] / wl);
+  }
+  if (fp.kind == VDVC_FIELD_BUMPS) {
+    const int nb = (int)p[15];
+    for (int b = 0; b < nb; ++b) {
+      const double* q = p + 16 + 7 * b;  // centre[3], width, amplitude[3]
+      const double dx = x - q[0], dy = y - q[1], dz = z - q[2];
+      const double e = exp(-(dx * dx + dy * dy + dz * dz) / (2.0 * q[3] * q[3]));
+      u[0] += q[4] * e;
+      u[1] += q[5] * e;
+      u[2] += q[6] * e;
+    }
+  }
+}
+
+// u at the grid points (i, j, k) * stride, FP32 [point][3]
+__global__ void k_field_grid(FieldParams fp, int gx, int gy, int gz, double stride, float* __restrict__ out) {
+  const long long n = (long long)gx * gy * gz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % gx);
+    const long long r = i / gx;
+    const int y = (int)(r % gy), z = (int)(r / gy);
+    double u[3];
+    field_u(fp, x * stride, y * stride, z * stride, u);
+    out[3 * i] = (float)u[0];
+    out[3 * i + 1] = (float)u[1];
+    out[3 * i + 2] = (float)u[2];
   }
 }
 
@@ -240,14 +268,35 @@ int vdvc_synth_texture(float* out, int nx, int ny, int nz, unsigned long long se
   return VDVC_OK;
 }
 
+static int field_params(int field, const double* params, int n_params, FieldParams* fp) {
+  VDVC_CHECK_ARG(field >= VDVC_FIELD_AFFINE && field <= VDVC_FIELD_BUMPS, "unknown field %d", field);
+  VDVC_CHECK_ARG(params && n_params >= 0 && n_params <= kMaxFieldParams, "bad params");
+  if (field == VDVC_FIELD_BUMPS)
+    VDVC_CHECK_ARG(n_params >= 16 && params[15] >= 0 && params[15] <= 6 && n_params >= 16 + 7 * (int)params[15],
+                   "bumps field needs 16 + 7 * n_bumps params (n_bumps <= 6)");
+  *fp = FieldParams{};
+  fp->kind = field;
+  for (int i = 0; i < n_params; ++i) fp->p[i] = params[i];
+  return VDVC_OK;
+}
+
+int vdvc_synth_field_grid(int field, const double* params, int n_params, int gx, int gy, int gz, double stride,
+                          float* out, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(out && gx >= 1 && gy >= 1 && gz >= 1 && stride > 0.0, "bad arguments");
+  FieldParams fp;
+  int st = field_params(field, params, n_params, &fp);
+  if (st) return st;
+  k_field_grid<<<gblocks((long long)gx * gy * gz), 256, 0, (cudaStream_t)stream>>>(fp, gx, gy, gz, stride, out);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
 int vdvc_synth_warp(const float* f, int nx, int ny, int nz, int field, const double* params, int n_params,
                     double noise_sigma, unsigned long long seed, float* g, vdvc_stream_t stream) {
   VDVC_CHECK_ARG(f && g && f != g && nx >= 1 && ny >= 1 && nz >= 1, "bad arguments");
-  VDVC_CHECK_ARG(field >= VDVC_FIELD_AFFINE && field <= VDVC_FIELD_AFFINE_SIN, "unknown field %d", field);
-  VDVC_CHECK_ARG(params && n_params >= 0 && n_params <= 24, "bad params");
-  FieldParams fp{};
-  fp.kind = field;
-  for (int i = 0; i < n_params; ++i) fp.p[i] = params[i];
+  FieldParams fp;
+  int st = field_params(field, params, n_params, &fp);
+  if (st) return st;
   const long long n = (long long)nx * ny * nz;
   k_warp<<<gblocks(n), 256, 0, (cudaStream_t)stream>>>(f, nx, ny, nz, fp, (float)noise_sigma, seed, g);
   VDVC_LAUNCHED();

@@ -18,7 +18,7 @@ import numpy as np
 from . import _device as D
 from . import _lib
 
-FIELD_AFFINE, FIELD_NECKING, FIELD_AFFINE_SIN = 0, 1, 2
+FIELD_AFFINE, FIELD_NECKING, FIELD_AFFINE_SIN, FIELD_BUMPS = 0, 1, 2, 3
 
 def _L():
     return _lib.lib()
@@ -78,7 +78,23 @@ def field_at(kind, params, X):
         amp, wl = p[15], p[16]
         for k in range(3):
             u[:, k] += amp * np.sin(2 * np.pi * X[:, (k + 1) % 3] / wl)
+    if kind == FIELD_BUMPS:
+        for b in range(int(p[15])):
+            q = p[16 + 7 * b: 23 + 7 * b]
+            e = np.exp(-np.sum((X - q[None, :3]) ** 2, axis=1) / (2 * q[3] ** 2))
+            u += e[:, None] * q[None, 4:7]
     return u
+
+
+def field_grid(kind, params, grid, stride):
+    """u at the grid points (i, j, k) * stride on the GPU: float32 CUDA
+    tensor (gx*gy*gz, 3), x fastest."""
+    gx, gy, gz = grid
+    out = D.empty(gx * gy * gz * 3, np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    _lib.check(_L().vdvc_synth_field_grid(kind, p.ctypes.data_as(_lib.pd), p.size, gx, gy, gz, float(stride),
+                                          out.data_ptr(), D.stream()), "synth_field_grid")
+    return out.view(-1, 3)
 
 
 @dataclass
