@@ -6,6 +6,8 @@
 // calls), the cross-power normalisation and the arg-max are kernels here.
 // numpy's argmax returns the first maximum in C order of pix[x,y,z]
 // (x slowest); the arg-max kernel breaks ties the same way.
+#include <cstdint>
+#include <type_traits>
 #include <cufft.h>
 
 #include "ops.cuh"
@@ -88,12 +90,34 @@ __global__ void __launch_bounds__(256) k_argmax(const double* __restrict__ r, in
   }
 }
 
+// float: four products (or values) summed in FP32 per float4, then one FP64
+// add -- FP64 arithmetic per element would run on GB300's narrow FP64 pipe.
 template <typename T>
 __global__ void __launch_bounds__(256) k_dot(const T* __restrict__ a, const T* __restrict__ b, long long n,
-                                             GridReduce red, double* __restrict__ out) {
+                                             GridReduce red, double* __restrict__ out, bool vec4) {
   __shared__ double s_red[8];
   double acc = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+  const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i0 = 0;
+  if constexpr (std::is_same<T, float>::value) {
+    if (vec4) {
+      const long long n4 = n >> 2;
+      for (long long q = gtid; q < n4; q += stride) {
+        const float4 x = __ldg((const float4*)a + q);
+        float s4;
+        if (b) {
+          const float4 y = __ldg((const float4*)b + q);
+          s4 = x.x * y.x + x.y * y.y + x.z * y.z + x.w * y.w;
+        } else {
+          s4 = (x.x + x.y) + (x.z + x.w);
+        }
+        acc += (double)s4;
+      }
+      i0 = n4 << 2;
+    }
+  }
+  for (long long i = i0 + gtid; i < n; i += stride)
     acc += b ? (double)a[i] * (double)b[i] : (double)a[i];
   double mine[1] = {block_sum(acc, s_red)}, o[1];
   if (grid_reduce_sum<1>(red, mine, o, s_red) && threadIdx.x == 0) *out = o[0];
@@ -125,11 +149,12 @@ int vdvc_dot(const void* a, const void* b, int dtype, long long n, double* out_h
   cudaStream_t s = (cudaStream_t)stream;
   VDVC_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
   GridReduce red{partials, ticket};
-  const int nb = grid_blocks(n, 256, kReduceBlocks);
+  const bool vec4 = (((uintptr_t)a | (uintptr_t)b) & 15u) == 0;
+  const int nb = grid_blocks(dtype == VDVC_F32 && vec4 ? (n + 3) / 4 : n, 256, kReduceBlocks);
   if (dtype == VDVC_F32)
-    k_dot<float><<<nb, 256, 0, s>>>((const float*)a, (const float*)b, n, red, res);
+    k_dot<float><<<nb, 256, 0, s>>>((const float*)a, (const float*)b, n, red, res, vec4);
   else if (dtype == VDVC_F64)
-    k_dot<double><<<nb, 256, 0, s>>>((const double*)a, (const double*)b, n, red, res);
+    k_dot<double><<<nb, 256, 0, s>>>((const double*)a, (const double*)b, n, red, res, false);
   else
     return set_error(VDVC_ERR_ARG, "dtype %d", dtype);
   VDVC_LAUNCHED();

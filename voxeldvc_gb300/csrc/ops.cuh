@@ -46,6 +46,10 @@ int launch_strip_fast(const StripArgs<float>& args, const Kpair<float>* kp, cuda
 // VDVC_ERR_UNSUPPORTED when h has no specialisation.
 template <bool PCG>
 int launch_elem_fast(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s);
+// Compile-time-h float32 residual / b [/ diag H] pass (rhs_fast.cu);
+// VDVC_ERR_UNSUPPORTED when h has no specialisation.
+template <bool DG>
+int launch_rhs_fast(const StripArgs<float>& args, cudaStream_t s);
 bool tma_enabled();
 long long strip_grid_blocks(const Mesh& m);
 

@@ -82,9 +82,10 @@ __device__ __forceinline__ T trilinear(const T* __restrict__ g, int nx, int ny, 
   const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
   const T tx = cx - fx, ty = cy - fy, tz = cz - fz;
   const int ix1 = min(ix + 1, nx - 1), iy1 = min(iy + 1, ny - 1), iz1 = min(iz + 1, nz - 1);
-  const long long sy = nx, sz = (long long)nx * ny;
-  const long long b00 = (long long)iy * sy + (long long)iz * sz, b10 = (long long)iy1 * sy + (long long)iz * sz;
-  const long long b01 = (long long)iy * sy + (long long)iz1 * sz, b11 = (long long)iy1 * sy + (long long)iz1 * sz;
+  // 32-bit offsets: the launcher rejects volumes of 2^32 voxels or more
+  const unsigned sy = (unsigned)nx, sz = (unsigned)nx * (unsigned)ny;
+  const unsigned b00 = (unsigned)iy * sy + (unsigned)iz * sz, b10 = (unsigned)iy1 * sy + (unsigned)iz * sz;
+  const unsigned b01 = (unsigned)iy * sy + (unsigned)iz1 * sz, b11 = (unsigned)iy1 * sy + (unsigned)iz1 * sz;
   const T v000 = g[b00 + ix], v100 = g[b00 + ix1];
   const T v010 = g[b10 + ix], v110 = g[b10 + ix1];
   const T v001 = g[b01 + ix], v101 = g[b01 + ix1];
@@ -96,7 +97,7 @@ __device__ __forceinline__ T trilinear(const T* __restrict__ g, int nx, int ny, 
 }
 
 template <typename T, bool STATS, bool INTERP>
-__global__ void __launch_bounds__(128) k_sample(const SampleArgs<T> a) {
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 5 : 6) : 3) k_sample(const SampleArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_red[4];
   const Mesh& m = a.m;
@@ -152,11 +153,11 @@ __global__ void __launch_bounds__(128) k_sample(const SampleArgs<T> a) {
       const int vz = k * h + qz;
       const T vzf = (T)vz;
       float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f;
-#pragma unroll 2
+#pragma unroll 1
       for (int qy = 0; qy < ny_e; ++qy) {
         const T fy1 = s_phi[qy];
         const int vy = j * h + qy;
-        const long long vv = (long long)x + (long long)vy * m.Nvx + (long long)vz * m.NvxNvy;
+        const unsigned vv = (unsigned)x + (unsigned)vy * (unsigned)m.Nvx + (unsigned)vz * (unsigned)m.NvxNvy;
         const T ua = u0[0] + fy1 * du[0], ub = u0[1] + fy1 * du[1], uc = u0[2] + fy1 * du[2];
         if constexpr (INTERP) {
           if (a.channels_first) {
@@ -164,9 +165,9 @@ __global__ void __launch_bounds__(128) k_sample(const SampleArgs<T> a) {
             a.uvox[m.Nvox + vv] = ub;
             a.uvox[2 * m.Nvox + vv] = uc;
           } else {
-            a.uvox[3 * vv + 0] = ua;
-            a.uvox[3 * vv + 1] = ub;
-            a.uvox[3 * vv + 2] = uc;
+            a.uvox[3 * (size_t)vv + 0] = ua;
+            a.uvox[3 * (size_t)vv + 1] = ub;
+            a.uvox[3 * (size_t)vv + 2] = uc;
           }
         } else {
           // (u + x) - g_origin, then bounds, clip and order-1 sampling
@@ -214,6 +215,8 @@ __global__ void __launch_bounds__(128) k_sample(const SampleArgs<T> a) {
 template <typename T, bool STATS, bool INTERP>
 int launch_sample(const SampleArgs<T>& args, cudaStream_t s) {
   if (args.m.h > 128) return set_error(VDVC_ERR_UNSUPPORTED, "element edge h=%d > 128 not supported", args.m.h);
+  if ((unsigned long long)args.gnx * args.gny * args.gnz >= (1ull << 32))
+    return set_error(VDVC_ERR_UNSUPPORTED, "deformed image of 2^32 voxels or more");
   StripShape sh = strip_shape(args.m.h);
   dim3 grid((args.m.Nx + sh.EX - 1) / sh.EX, args.m.Ny, args.m.Nz);
   const size_t smem = ((size_t)sh.EX * 24 + args.m.h + 2) * sizeof(T);

@@ -352,6 +352,13 @@ int launch_strip(const StripArgs<T>& args, const Kpair<T>* kp, cudaStream_t s) {
       if (st != VDVC_ERR_UNSUPPORTED) return st;
     }
   }
+  if constexpr (std::is_same<T, float>::value &&
+                (MODE == (kModeB | kModeRes) || MODE == (kModeB | kModeRes | kModeDiag))) {
+    if (hv_kernel_choice() != 2) {
+      const int st = launch_rhs_fast<(MODE & kModeDiag) != 0>(args, s);
+      if (st != VDVC_ERR_UNSUPPORTED) return st;
+    }
+  }
   StripShape sh = strip_shape(args.m.h);
   if (args.m.h > 128) return set_error(VDVC_ERR_UNSUPPORTED, "element edge h=%d > 128 not supported", args.m.h);
   if (args.m.Ny > 65535 || args.m.Nz > 65535) return set_error(VDVC_ERR_ARG, "Ny/Nz > 65535");

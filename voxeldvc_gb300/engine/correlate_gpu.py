@@ -411,6 +411,12 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
                       % (ik + 1, stdr, err, n_active, Nvox, 100 * n_active / Nvox))
             if err < eps:
                 break
+        info["converged"] = bool(err < eps)
+        # 1 - ZNCC of the registered pair over the live mask, from the last
+        # residual: res/std0 = f^ - g^ for the standardised f^, g^ (the
+        # residual is built from the centred f, correlate_gpu.py:962, :1094)
+        c_l, s2_l = out8[2], out8[4]
+        info["norm_res"] = float(s2_l / c_l / (2.0 * std0 * std0)) if c_l > 0 else float("inf")
         Uo = D.empty(Ndof, out_dt)
         res = D.empty(Nvox, out_dt)
         dU = D.empty(Ndof, out_dt)

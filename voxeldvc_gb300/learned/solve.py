@@ -1,0 +1,83 @@
+"""DVC solve seeded by the learned initial guess.
+
+The network's displacement, resampled to the mesh nodes, replaces the coarse
+pyramid levels and the FFT shift of `multiscale_correlate_gpu`
+(engine/correlate_gpu.py:1143-1305 in the reference): only the finest level
+is solved, from that seed.  The plain multiscale solve stays the fallback:
+it runs when the registered pair's normalised residual
+    rho = mean over the live mask of (f^ - g^)^2 / 2  =  1 - ZNCC
+(f^, g^ the standardised reference and deformed values) exceeds
+`fallback_threshold` (default 0.05), when the seeded solve stops without
+meeting its GN tolerance, or when the two images differ in shape.  A
+correctly registered pair sits at the noise floor (rho ~ sigma_n^2 /
+(2 sigma_f^2), 0.005 for the benchmark textures); a pair left in a wrong
+local minimum is near 1 - ZNCC of unrelated textures.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from .. import _device as D
+from ..engine import correlate_gpu as CG
+from .seednet import SeedNet, WEIGHTS_PATH
+
+_NETS = {}
+
+
+def default_net(path=WEIGHTS_PATH):
+    """The trained network shipped with the package (loaded once per device)."""
+    key = (path, D.torch().cuda.current_device())
+    if key not in _NETS:
+        _NETS[key] = SeedNet.load(path)
+    return _NETS[key]
+
+
+def learned_seed(f_pix, g_pix, Nx, Ny, Nz, h, g_origin=(0, 0, 0), net=None):
+    """Seed U (float64 CUDA, Ndof) for the mesh from the (f, g) pair."""
+    net = net or default_net()
+    f_vox, fs = CG.pix_to_vox(f_pix, np.float32)
+    g_vox, gs = CG.pix_to_vox(g_pix, np.float32)
+    if tuple(fs) != tuple(gs):
+        raise ValueError("the learned seed needs f and g of one shape")
+    U0 = net.predict_nodes(f_vox, g_vox, fs, h, Nx, Ny, Nz)
+    if any(o != 0 for o in g_origin):
+        # the network sees g in its own array frame: u = u_array + g_origin
+        Uh = U0.cpu().numpy()
+        for c in range(3):
+            Uh[c::3] += float(g_origin[c])
+        U0 = D.to_device(Uh)
+    return U0
+
+
+def learned_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0), l0=None, net=None,
+                          fallback_threshold=0.05, scales=(2, 1, 0), fft_prealign=True, stats=None, **kwargs):
+    """Finest-level GN solve from the learned seed, with the plain
+    multiscale solve as fallback.  Same arguments and returns as
+    multiscale_correlate_gpu; `stats` (a list) receives the per-level info
+    dicts and a final {'seed': 'learned' | 'fallback', ...} entry."""
+    dtype = np.dtype(kwargs.get("dtype", np.float32))
+    levels = [] if stats is None else stats
+    t0 = time.perf_counter()
+    reason = None
+    try:
+        U0 = learned_seed(f_pix, g_pix, Nx, Ny, Nz, h, g_origin, net)
+    except ValueError as e:
+        U0, reason = None, str(e)
+    seed_s = time.perf_counter() - t0
+    if U0 is not None:
+        f_vox, fs = CG.pix_to_vox(f_pix, dtype)
+        g_vox, gs = CG.pix_to_vox(g_pix, dtype)
+        U, res, dU, info = CG._solve_level(CG._Level(f_vox, fs, g_vox, gs), Nx, Ny, Nz, h, g_origin=g_origin, l0=l0,
+                                           U0=U0, stats=levels, **kwargs)
+        rho = info.get("norm_res", float("inf"))
+        if np.isfinite(rho) and rho <= fallback_threshold and info.get("converged", False):
+            levels.append(dict(seed="learned", norm_res=rho, seed_s=seed_s))
+            return D.out(U, xp), D.out(res, xp), D.out(dU, xp)
+        reason = f"normalised residual {rho:.4f}" if rho > fallback_threshold or not np.isfinite(rho) \
+            else "GN tolerance not met"
+    U, res, dU = CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, scales=scales, g_origin=g_origin,
+                                             l0=l0, fft_prealign=fft_prealign, stats=levels, **kwargs)
+    levels.append(dict(seed="fallback", reason=reason, seed_s=seed_s))
+    return U, res, dU
