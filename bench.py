@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-layers", type=int, default=1)
+    p.add_argument("--no-forms", action="store_true",
+                   help="skip the precision / learned-seed form comparison (FP64 reference solve included)")
     p.add_argument("--only", default=None, choices=[None, "matvec"],
                    help="matvec: time only the finest-level Hessian matvec (the profiling command)")
     return p.parse_args()
@@ -267,6 +269,67 @@ def solve_kwargs(wl):
     return kw
 
 
+def compare_forms(wl, f_pix, g_pix, kw, U_plain, e2e_plain, plain_s):
+    """Plain FP32, precision form and learned seed + precision form against
+    the FP64 solve of the same inputs (the project's GPU FP64 mode, parity
+    checked against the NumPy FP64 oracle at small sizes): wall time of the
+    device-resident solve, the same through the public API with host arrays,
+    and the nodal RMS difference to the FP64 displacement."""
+    import torch
+    from voxeldvc_gb300.engine import correlate_gpu as CG
+    from voxeldvc_gb300.learned import solve as LS
+    Nx, Ny, Nz = wl.mesh
+
+    def timed(fn, reps=3):
+        fn()
+        ts, out = [], None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)), out
+
+    t64, (U64, _, _) = timed(lambda: CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, xp=torch,
+                                                                  dtype=np.float64, **kw), reps=1)
+    U64 = U64.double()
+
+    def rms(U):
+        return float(torch.sqrt(torch.mean((U.double() - U64) ** 2)).item())
+
+    out = {"reference": "GPU FP64 solve of the same inputs", "f64_s": round(t64, 4),
+           "target_rms_vx": 0.02, "plain": {"rms_vs_f64_vx": round(rms(U_plain), 6)}}
+    tm, (Um, _, _) = timed(lambda: CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, xp=torch,
+                                                                precision="mixed", **kw))
+    out["mixed"] = {"s": round(tm, 4), "rms_vs_f64_vx": round(rms(Um), 6)}
+    kwl = {k: v for k, v in kw.items() if k not in ("scales", "fft_prealign")}
+    try:
+        net = LS.default_net()
+    except (OSError, KeyError) as e:
+        out["learned_mixed"] = {"unavailable": f"no trained seed network ({e})"}
+        return out
+    stats = []
+    tl, (Ul, _, _) = timed(lambda: LS.learned_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, torch, net=net,
+                                                            precision="mixed", stats=stats, **kwl))
+    last = stats[-1]
+    gn = [s for s in stats if "gn_iters" in s]
+    out["learned_mixed"] = {"s": round(tl, 4), "rms_vs_f64_vx": round(rms(Ul), 6), "seed": last.get("seed"),
+                            "norm_res": last.get("norm_res"), "gn_iters": [s["gn_iters"] for s in gn[-1:]],
+                            "pcg_iters": [int(sum(s["pcg_iters"])) for s in gn[-1:]]}
+    # the same through the public API with host arrays (as the plain e2e)
+    f_host = f_pix.cpu().pin_memory().numpy()
+    g_host = g_pix.cpu().pin_memory().numpy()
+    te, _ = timed(lambda: LS.learned_correlate_gpu(f_host, g_host, Nx, Ny, Nz, wl.h, np, net=net,
+                                                   precision="mixed", **kwl), reps=2)
+    out["learned_mixed"]["e2e_s"] = round(te, 4)
+    if e2e_plain:
+        out["learned_mixed"]["e2e_speedup_vs_plain"] = round(e2e_plain["value"] / te, 3)
+    out["learned_mixed"]["speedup_vs_plain_device"] = round(plain_s / tl, 3)
+    out["mixed"]["speedup_vs_plain_device"] = round(plain_s / tm, 3)
+    return out
+
+
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -372,6 +435,10 @@ def gpu_arm(args):
                "h2d_bytes_per_step": int(f_host.nbytes + g_host.nbytes),
                "d2h_bytes_per_step": int(Ue.nbytes + re.nbytes + de.nbytes)}
 
+    forms = None
+    if rank == 0 and world == 1 and not args.no_forms:
+        forms = compare_forms(wl, f_pix, g_pix, kw, U, e2e, ms / 1e3)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         counts = {"gn": [s["gn_iters"] for s in level_stats], "pcg": [int(sum(s["pcg_iters"])) for s in level_stats]}
@@ -400,7 +467,7 @@ def gpu_arm(args):
                              # this launch's voxel count
                              "traffic": int(TRAFFIC_B_PER_VOXEL * nvox),
                              "algorithmic_bytes": int(alg_bytes), "ms": round(mv_ms, 4)},
-                "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+                "cpu_baseline": cpu, "e2e": e2e, "forms": forms, "clocks": clocks}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

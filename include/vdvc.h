@@ -309,7 +309,10 @@ typedef struct vdvc_gn_desc {
   const double* K_el;        /* host 24x24 (equilibrium gap)                  */
   int dynamic_mask;          /* 1: H and M follow the b mask each iteration   */
   int pcg_chunk;             /* PCG iterations per body of the graph's
-                                device-driven WHILE loop (0: 4)              */
+                                device-driven WHILE loop (0: 4); < 0: the
+                                persistent fused PCG kernel (one cooperative
+                                launch per solve) where it applies (float,
+                                h <= 2, no equilibrium gap), else 4        */
   const void* f_vox;         /* reference values, vox layout, uncentred       */
   const void* g_vox;         /* deformed image, vox layout                    */
   const void* grad;          /* (Nvox,3) eroded gradient of f                 */
@@ -361,6 +364,37 @@ int vdvc_gn_update(vdvc_gn_solver* solver, double* out8, vdvc_stream_t stream);
 int vdvc_gn_read(vdvc_gn_solver* solver, int which, void* dst, int dst_f64,
                  vdvc_stream_t stream);
 void vdvc_gn_destroy(vdvc_gn_solver* solver);
+
+/* ---- batches of independent solves ------------------------------------
+   No counterpart in the reference (it solves one pair per call): a series
+   of deformed volumes against one reference, with their own ROIs, element
+   sizes and masks, iterated in lockstep.  Each call runs one GN iteration
+   of every active problem: sampling, residual and PCG set-up on one stream
+   per problem (concurrent = 1) or all on `stream` (concurrent = 0), then
+   the PCG loops of all active problems as one CUDA graph (a device-driven
+   WHILE loop whose body holds pcg_chunk iterations of every problem), then
+   the updates, and one synchronisation.  float32 problems only; descs[i]
+   and ws[i] as for vdvc_gn_create. */
+typedef struct vdvc_gn_batch vdvc_gn_batch;
+int vdvc_gn_batch_create(const vdvc_gn_desc* descs, int n, void* const* ws,
+                         const size_t* ws_bytes, int pcg_chunk,
+                         int concurrent, vdvc_gn_batch** out);
+/* Problem i's solver (for vdvc_gn_set_U / frozen_diag / read; owned by the
+   batch: vdvc_gn_destroy on it does nothing). */
+int vdvc_gn_batch_solver(vdvc_gn_batch* batch, int i, vdvc_gn_solver** out);
+/* One GN iteration of the problems with active[i] != 0 (freeze_now may be
+   NULL).  out12: 12 doubles per problem: the 8 values of vdvc_gn_update,
+   PCG iterations, PCG relative residual, PCG status, residual status
+   (VDVC_ERR_ZERO_DIVISION when std(g) over the b mask is 0). */
+int vdvc_gn_batch_iterate(vdvc_gn_batch* batch, const int* active,
+                          const int* freeze_now, int max_iter, double tol,
+                          double* out12, vdvc_stream_t stream);
+/* Change the PCG graph's iterations per body (1..64) and the stream
+   schedule; the graph is rebuilt at the next iteration (the autotuner's
+   knobs). */
+int vdvc_gn_batch_set_schedule(vdvc_gn_batch* batch, int pcg_chunk,
+                               int concurrent);
+void vdvc_gn_batch_destroy(vdvc_gn_batch* batch);
 
 #ifdef __cplusplus
 }

@@ -127,3 +127,21 @@ def test_zero_std_raises(api):
     g = np.zeros((9, 9, 9), dtype=np.float32)  # no voxel survives g > glt
     with pytest.raises(ZeroDivisionError):
         CG.correlate_gpu(f, g, 2, 2, 2, 4, xp=np, maxiter=2, disp=False)
+
+
+def test_persistent_pcg_matches_graph(api, monkeypatch):
+    """pcg_chunk < 0 runs the h <= 2 levels on the persistent fused PCG; the
+    graph-replayed kernels give the same solve (same arithmetic, other
+    reduction grouping)."""
+    CG, G = api
+    c = load_golden("solve_multiscale.npz")
+    kw = dict(scales=(2, 1, 0), K_ref_laplacian=G.build_K_ref_laplacian(), l0=36.0, maxiter=20, eps=1e-3,
+              disp=False, dynamic_mask=True, freeze_mask_after=4, fft_prealign=True)
+    st_p = []
+    Up, _, _ = CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, stats=st_p, pcg_chunk=-1, **kw)
+    monkeypatch.setenv("VDVC_PCG", "graph")
+    st_g = []
+    Ug, _, _ = CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, stats=st_g, pcg_chunk=-1, **kw)
+    assert st_p[0]["h"] == 2
+    assert rms(Up, Ug) < 1e-4
+    assert rms(Up, c["U"]) < RMS_TOL

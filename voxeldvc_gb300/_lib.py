@@ -78,6 +78,11 @@ SIGNATURES = {
     "vdvc_gn_update": (ci, [vp, pd, vp]),
     "vdvc_gn_read": (ci, [vp, ci, vp, ci, vp]),
     "vdvc_gn_destroy": (None, [vp]),
+    "vdvc_gn_batch_create": (ci, [vp, ci, vp, vp, ci, ci, C.POINTER(vp)]),
+    "vdvc_gn_batch_solver": (ci, [vp, ci, C.POINTER(vp)]),
+    "vdvc_gn_batch_iterate": (ci, [vp, vp, vp, ci, cd, vp, vp]),
+    "vdvc_gn_batch_set_schedule": (ci, [vp, ci, ci]),
+    "vdvc_gn_batch_destroy": (None, [vp]),
     "vdvc_affine_workspace_bytes": (cz, []),
     "vdvc_affine_zncc_sums": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, pd, pd, pd, pd, vp, cz, vp]),
     "vdvc_gaussian_filter": (ci, [vp, vp, ci, ci, ci, cd, ci, cd, vp, vp, vp]),

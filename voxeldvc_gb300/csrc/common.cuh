@@ -89,6 +89,15 @@ inline size_t dtype_size(int dtype) {
   return 0;
 }
 
+// Type-exact floor / min / max: the float forms never promote to double
+// (GB300's FP64 pipe is a small fraction of its FP32 rate).
+__device__ __forceinline__ float tfloor(float x) { return floorf(x); }
+__device__ __forceinline__ double tfloor(double x) { return floor(x); }
+__device__ __forceinline__ float tmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double tmin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float tmax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double tmax(double a, double b) { return fmax(a, b); }
+
 // ---- reductions -----------------------------------------------------------
 
 // Sum of `v` over the block; result valid in thread 0.  `smem` holds
@@ -107,6 +116,26 @@ __device__ __forceinline__ double block_sum(double v, double* smem) {
   }
   return s;
 }
+
+// Sum of float partials over the block, result (float64) valid in thread 0:
+// the warp stage shuffles in FP32 and only the per-warp sums are added in
+// FP64 -- a float64 shuffle tree per warp would keep GB300's narrow FP64
+// pipe busy for microseconds per launch.  Same contract as block_sum.
+__device__ __forceinline__ double block_sum_f(float v, double* smem) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) smem[warp] = (double)v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int w = 0; w < nw; ++w) s += smem[w];
+  }
+  return s;
+}
+__device__ __forceinline__ double block_sum_f(double v, double* smem) { return block_sum(v, smem); }
 
 __device__ __forceinline__ double block_min(double v, double* smem) {
 #pragma unroll

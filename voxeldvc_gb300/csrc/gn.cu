@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <new>
 #include <type_traits>
+#include <vector>
 
 #include "ops.cuh"
 #include "pcg.cuh"
@@ -46,10 +47,14 @@ struct GnSolver {
   // device buffers (carved from the caller's workspace)
   double* U64;
   T *U32, *x, *r, *z, *p, *Ap, *Minv, *b, *w, *ru, *t1, *gvals, *res, *evA, *evD;
-  double *diag, *diag_reg;
+  T* diag;
+  double* diag_reg;  // h diag(K_lap) [+ equilibrium-gap diagonal], float64
+  T* diag_reg_t;     // the same in the solve type
   uint8_t *live, *frozen;
   double* partials;
+  size_t n_partials;
   unsigned int* ticket;
+  unsigned int* bar;
   GnScalars* sc;
   PcgState* pcg;
   Kpair<T>* kp;
@@ -86,8 +91,9 @@ static size_t carve_solver(const Mesh& m, GnSolver<T>* S, void* ws, size_t bytes
   S->w = cv.take<T>(nd);
   S->ru = cv.take<T>(nd);
   S->t1 = cv.take<T>(nd);
-  S->diag = cv.take<double>(nd);
+  S->diag = cv.take<T>(nd);
   S->diag_reg = cv.take<double>(nd);
+  S->diag_reg_t = cv.take<T>(nd);
   S->gvals = cv.take<T>(nv);
   S->res = cv.take<T>(nv);
   S->live = cv.take<uint8_t>(nv);
@@ -95,8 +101,10 @@ static size_t carve_solver(const Mesh& m, GnSolver<T>* S, void* ws, size_t bytes
   S->evA = cv.take<T>((size_t)24 * m.Ne);
   S->evD = cv.take<T>((size_t)24 * m.Ne);
   const long long nb = strip_grid_blocks(m);
-  S->partials = cv.take<double>((size_t)(nb > kReduceBlocks ? nb : kReduceBlocks) * 4);
+  S->n_partials = (size_t)(nb > kReduceBlocks ? nb : kReduceBlocks) * 4;
+  S->partials = cv.take<double>(S->n_partials);
   S->ticket = cv.take<unsigned int>(4);
+  S->bar = cv.take<unsigned int>(4);  // persistent PCG: count, generation, error flag
   S->sc = cv.take<GnScalars>(1);
   S->pcg = cv.take<PcgState>(1);
   S->kp = cv.take<Kpair<T>>(1);
@@ -114,16 +122,18 @@ __global__ void k_set_U(const double* __restrict__ U0, long long n, double* __re
   }
 }
 
-// b = sum of element vectors - ll R U ; diag = sum + ll diag_R (float64),
-// min diag -> sc->dmin.
+// b = sum of element vectors - ll R U ; diag = sum + ll diag_R ; min diag
+// -> sc->dmin.  In the solve type T: FP64 per entry would run on GB300's
+// narrow FP64 pipe.
 template <typename T>
 __global__ void __launch_bounds__(256) k_gn_gather_rhs(const Mesh m, const T* __restrict__ evA,
                                                        const T* __restrict__ evD, const T* __restrict__ ru, double ll,
-                                                       const double* __restrict__ diag_reg, T* __restrict__ b,
-                                                       double* __restrict__ diag, GnScalars* sc, GridReduce red,
+                                                       const T* __restrict__ diag_reg, T* __restrict__ b,
+                                                       T* __restrict__ diag, GnScalars* sc, GridReduce red,
                                                        bool with_diag) {
   __shared__ double s_red[8];
-  double dmin = 1.0e300;
+  const T llT = (T)ll;
+  T dmin = T(3.0e38);
   for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < m.Nnodes;
        n += (long long)gridDim.x * blockDim.x) {
     const int ni = (int)(n % m.Nnx);
@@ -144,16 +154,16 @@ __global__ void __launch_bounds__(256) k_gn_gather_rhs(const Mesh m, const T* __
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const long long dof = 3 * n + c;
-      b[dof] = ru ? (T)((double)sb[c] - ll * (double)ru[dof]) : sb[c];
+      b[dof] = ru ? sb[c] - llT * ru[dof] : sb[c];
       if (with_diag) {
-        const double dg = (double)sd[c] + (diag_reg ? ll * diag_reg[dof] : 0.0);
+        const T dg = sd[c] + (diag_reg ? llT * diag_reg[dof] : T(0));
         diag[dof] = dg;
-        dmin = fmin(dmin, dg);
+        dmin = tmin(dmin, dg);
       }
     }
   }
   if (!with_diag) return;
-  double bm = block_min(dmin, s_red);
+  double bm = block_min((double)dmin, s_red);
   // grid min through the deterministic reduction slots (values, not sums)
   __shared__ bool s_last;
   const unsigned int nb = gridDim.x;
@@ -176,26 +186,29 @@ __global__ void __launch_bounds__(256) k_gn_gather_rhs(const Mesh m, const T* __
 }
 
 template <typename T>
-__global__ void k_gn_minv(const double* __restrict__ diag, long long n, const GnScalars* sc, T* __restrict__ Minv) {
-  const double eps = 1e-5 * sc->dmin;
+__global__ void k_gn_minv(const T* __restrict__ diag, long long n, const GnScalars* sc, T* __restrict__ Minv) {
+  const T eps = (T)(1e-5 * sc->dmin);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    Minv[i] = (T)(1.0 / (diag[i] + eps));
+    Minv[i] = T(1) / (diag[i] + eps);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_gn_update(const T* __restrict__ dU, long long n, double* __restrict__ U64,
                                                    T* __restrict__ U32, GnScalars* sc, GridReduce red) {
   __shared__ double s_red[8];
-  double dd = 0.0, uu = 0.0;
+  // U is kept in float64; the norms of the convergence test are summed in T
+  // per thread (one float64 add per thread)
+  T dd = T(0), uu = T(0);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double du = (double)dU[i];
-    const double u = U64[i] + du;
+    const T du = dU[i];
+    const double u = U64[i] + (double)du;
     U64[i] = u;
-    U32[i] = (T)u;
+    const T ut = (T)u;
+    U32[i] = ut;
     dd += du * du;
-    uu += u * u;
+    uu += ut * ut;
   }
-  double mine[2] = {block_sum(dd, s_red), block_sum(uu, s_red)}, out[2];
+  double mine[2] = {block_sum_f(dd, s_red), block_sum_f(uu, s_red)}, out[2];
   if (grid_reduce_sum<2>(red, mine, out, s_red) && threadIdx.x == 0) {
     sc->norms[0] = out[0];
     sc->norms[1] = out[1];
@@ -256,6 +269,58 @@ static int apply_reg(GnSolver<T>* S, const T* v, T* out, cudaStream_t s) {
 
 // ---- one PCG iteration (captured into the graph) ----------------------------
 
+// The Hessian pass of a PCG iteration: input p_new = z + beta p, H mask, the
+// regularizer fused in its epilogue.
+template <typename T>
+static StripArgs<T> pcg_strip_args(GnSolver<T>* S) {
+  const vdvc_gn_desc& d = S->d;
+  StripArgs<T> sa{};
+  sa.m = S->m;
+  sa.v = S->z;
+  sa.p_old = S->p;
+  sa.st = S->pcg;
+  sa.grad = (const T*)d.grad;
+  // H mask: the b mask buffer (dynamic_mask) or mask0 -- fixed pointers, so
+  // the captured graph stays valid for the solver's lifetime
+  sa.mask = d.dynamic_mask ? S->frozen : d.mask0;
+  sa.evA = S->evA;
+  sa.nreg = 0;
+  // K1 is the vector Laplacian in both regularizers; pass its 8x8 block when
+  // it has the block structure of build_K_ref_laplacian
+  sa.k1_blockdiag = S->lap_blockdiag ? 1 : 0;
+  for (int q = 0; q < 64; ++q) sa.L8[q] = S->L8[q];
+  if (d.ll != 0.0 && d.reg_type == VDVC_REG_LAPLACIAN) {
+    sa.nreg = 1;
+    sa.c1 = (T)(d.ll * d.h);
+  } else if (d.ll != 0.0 && d.reg_type == VDVC_REG_EQUILIBRIUM_GAP) {
+    sa.nreg = 2;
+    sa.c1 = (T)(d.ll * d.eps_reg * d.h);
+    sa.c2 = (T)(d.ll * d.h);
+    sa.w = S->w;
+  }
+  return sa;
+}
+
+// The persistent fused PCG (one cooperative launch per solve) serves float
+// solves at h <= 2 without the equilibrium-gap stencil, when the descriptor
+// asks for it (pcg_chunk < 0) or VDVC_PCG=persistent; VDVC_PCG=graph keeps
+// the graph-replayed kernels everywhere.  Measured on GB300 at 129^3 voxels,
+// h = 2 (64^3 elements): 1.62 ms per 25-iteration solve persistent against
+// 1.26 ms graph-replayed -- the fused kernel's element phase needs 128
+// registers, which caps every phase at 16 warps per SM -- so the graph is
+// the default and the choice is left to the autotuner.
+template <typename T>
+static bool use_persistent(GnSolver<T>* S) {
+  if constexpr (!std::is_same<T, float>::value) {
+    return false;
+  } else {
+    const char* e = getenv("VDVC_PCG");
+    if (e && e[0] == 'g') return false;
+    const bool want = S->d.pcg_chunk < 0 || (e && e[0] == 'p');
+    return want && !S->mixed && S->m.h <= 2 && !(S->d.reg_type == VDVC_REG_EQUILIBRIUM_GAP && S->d.ll != 0.0);
+  }
+}
+
 template <typename T>
 static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
   const vdvc_gn_desc& d = S->d;
@@ -298,30 +363,7 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
       return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
     }
   }
-  StripArgs<T> sa{};
-  sa.m = S->m;
-  sa.v = S->z;
-  sa.p_old = S->p;
-  sa.st = S->pcg;
-  sa.grad = (const T*)d.grad;
-  // H mask: the b mask buffer (dynamic_mask) or mask0 -- fixed pointers, so
-  // the captured graph stays valid for the solver's lifetime
-  sa.mask = d.dynamic_mask ? S->frozen : d.mask0;
-  sa.evA = S->evA;
-  sa.nreg = 0;
-  // K1 is the vector Laplacian in both regularizers; pass its 8x8 block when
-  // it has the block structure of build_K_ref_laplacian
-  sa.k1_blockdiag = S->lap_blockdiag ? 1 : 0;
-  for (int q = 0; q < 64; ++q) sa.L8[q] = S->L8[q];
-  if (d.ll != 0.0 && d.reg_type == VDVC_REG_LAPLACIAN) {
-    sa.nreg = 1;
-    sa.c1 = (T)(d.ll * d.h);
-  } else if (d.ll != 0.0 && d.reg_type == VDVC_REG_EQUILIBRIUM_GAP) {
-    sa.nreg = 2;
-    sa.c1 = (T)(d.ll * d.eps_reg * d.h);
-    sa.c2 = (T)(d.ll * d.h);
-    sa.w = S->w;
-  }
+  const StripArgs<T> sa = pcg_strip_args<T>(S);
   if ((st = launch_strip<T, kModeHv | kModePcg>(sa, S->kp, s))) return st;
   if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s))) return st;
   return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
@@ -479,6 +521,11 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
       count_launch(2);
     }
   }
+  if (d->reg_type != VDVC_REG_NONE) {
+    k_copy_out<double><<<nblk(m.Ndof), 256, 0, s>>>(S->diag_reg, m.Ndof, S->diag_reg_t,
+                                                     std::is_same<T, double>::value ? 1 : 0);
+    count_launch();
+  }
   k_set_U<T><<<nblk(m.Ndof), 256, 0, s>>>(nullptr, m.Ndof, S->U64, S->U32);
   count_launch();
   if (S->mixed && (e = launch_grad_bf16((const float*)d->grad, 3 * m.Nvox, S->grad_bf16, s))) return fail(e);
@@ -513,7 +560,7 @@ static int frozen_diag(GnSolver<T>* S, cudaStream_t s) {
   }
   GridReduce red{S->partials, S->ticket};
   k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, kReduceBlocks), 256, 0, s>>>(
-      S->m, S->evD, S->evD, nullptr, S->d.ll, S->d.reg_type != VDVC_REG_NONE ? S->diag_reg : nullptr, S->t1,
+      S->m, S->evD, S->evD, nullptr, S->d.ll, S->d.reg_type != VDVC_REG_NONE ? S->diag_reg_t : nullptr, S->t1,
       S->diag, S->sc, red, true);
   VDVC_LAUNCHED();
   k_gn_minv<T><<<nblk(S->m.Ndof), 256, 0, s>>>(S->diag, S->m.Ndof, S->sc, S->Minv);
@@ -583,7 +630,7 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
   }
   GridReduce red{S->partials, S->ticket};
   k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, kReduceBlocks), 256, 0, s>>>(
-      S->m, S->evA, S->evD, reg ? S->ru : nullptr, d.ll, d.reg_type != VDVC_REG_NONE ? S->diag_reg : nullptr, S->b,
+      S->m, S->evA, S->evD, reg ? S->ru : nullptr, d.ll, d.reg_type != VDVC_REG_NONE ? S->diag_reg_t : nullptr, S->b,
       S->diag, S->sc, red, with_diag);
   VDVC_LAUNCHED();
   if (with_diag) {
@@ -608,12 +655,43 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   int st = launch_pcg_init<T>(S->b, nullptr, S->Minv, S->m.Ndof, S->r, S->z, S->p, false, S->x, S->pcg, red,
                               max_iter, tol, s);
   if (st) return st;
-  if (!S->gexec && (st = build_graph<T>(S))) return st;
-  if (max_iter > 0) VDVC_CUDA(cudaGraphLaunch(S->gexec, s));
+  bool ran = false;
+  if constexpr (std::is_same<T, float>::value) {
+    if (max_iter > 0 && use_persistent(S)) {
+      PcgPersistArgs pa{};
+      pa.sa = pcg_strip_args<T>(S);
+      pa.kp = S->kp;
+      pa.x = S->x;
+      pa.r = S->r;
+      pa.z = S->z;
+      pa.p = S->p;
+      pa.Ap = S->Ap;
+      pa.Minv = S->Minv;
+      pa.st = S->pcg;
+      pa.partials = S->partials;
+      pa.bar = S->bar;
+      pa.err = (int*)(S->bar + 2);
+      const char* sl = getenv("VDVC_BAR_SLEEP");
+      pa.sleep_ns = sl ? atoi(sl) : 0;
+      VDVC_CUDA(cudaMemsetAsync(S->bar, 0, 4 * sizeof(unsigned int), s));
+      st = launch_pcg_persistent(pa, (int)(S->n_partials / 3), s);
+      if (st == VDVC_OK) {
+        ran = true;
+      } else if (st != VDVC_ERR_UNSUPPORTED) {
+        return st;
+      }
+    }
+  }
+  if (!ran) {
+    if (!S->gexec && (st = build_graph<T>(S))) return st;
+    if (max_iter > 0) VDVC_CUDA(cudaGraphLaunch(S->gexec, s));
+  }
   VDVC_CUDA(cudaMemcpyAsync(S->h_pcg, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
   VDVC_CUDA(cudaStreamSynchronize(s));
   const PcgState& fin = S->h_pcg[0];
-  if (max_iter > 0) {
+  if (ran && fin.status == VDVC_ERR_CUDA)
+    return set_error(VDVC_ERR_CUDA, "persistent PCG: a grid barrier timed out");
+  if (max_iter > 0 && !ran) {
     // body executions = ceil(iter / chunk); each runs chunk iterations' kernels + the continue kernel
     const long long bodies = (fin.iter + S->chunk - 1) / S->chunk;
     count_launch(bodies * ((long long)S->chunk * S->kernels_per_iter + 1));
@@ -624,13 +702,21 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   return VDVC_OK;
 }
 
+// U += dU and the iteration scalars into the pinned read-back slots (no sync)
 template <typename T>
-static int update(GnSolver<T>* S, double* out8, cudaStream_t s) {
+static int update_enqueue(GnSolver<T>* S, cudaStream_t s) {
   GridReduce red{S->partials, S->ticket};
   k_gn_update<T><<<grid_blocks(S->m.Ndof, 256, kReduceBlocks), 256, 0, s>>>(S->x, S->m.Ndof, S->U64, S->U32, S->sc,
                                                                             red);
   VDVC_LAUNCHED();
   VDVC_CUDA(cudaMemcpyAsync(S->h_sc, S->sc, sizeof(GnScalars), cudaMemcpyDeviceToHost, s));
+  return VDVC_OK;
+}
+
+template <typename T>
+static int update(GnSolver<T>* S, double* out8, cudaStream_t s) {
+  int st = update_enqueue<T>(S, s);
+  if (st) return st;
   VDVC_CUDA(cudaStreamSynchronize(s));
   const GnScalars& h = *S->h_sc;
   if (out8) {
@@ -691,6 +777,189 @@ static void destroy(GnSolver<T>* S) {
   delete S;
 }
 
+// ---- batches of independent solves ------------------------------------------
+//
+// A series of deformed volumes (different ROIs, element sizes h, masks) are
+// iterated in lockstep: one GN iteration of every active problem per call.
+// Sampling, residual and PCG set-up run on one stream per problem (the small
+// problems overlap on the GPU), then the PCG loops of all active problems
+// run as ONE CUDA graph: a WHILE node whose body holds `chunk` iterations of
+// every problem as parallel branches and a continue kernel that keeps the
+// loop going while any problem's PCG state is not done (a problem that
+// converged skips its kernels).  One host synchronisation per GN iteration
+// reads every problem's scalars.  The graph is rebuilt only when the set of
+// active problems changes.
+
+__global__ void k_batch_continue(cudaGraphConditionalHandle h, PcgState* const* states, int n) {
+  if (threadIdx.x == 0) {
+    unsigned int more = 0;
+    for (int i = 0; i < n; ++i) more |= states[i]->done ? 0u : 1u;
+    cudaGraphSetConditional(h, more);
+  }
+}
+
+struct GnBatch {
+  int n = 0;
+  int chunk = 4;
+  int concurrent = 1;  // 1: problems on their own streams (parallel graph branches)
+  std::vector<GnSolver<float>*> S;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> done_ev;
+  cudaEvent_t fork_ev = nullptr;
+  cudaStream_t cap = nullptr;
+  PcgState** d_states = nullptr;  // device array of the active problems' PCG states
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<char> graph_active;
+  long long kernels_per_body = 0;
+};
+
+static void batch_free_graph(GnBatch* B) {
+  if (B->exec) cudaGraphExecDestroy(B->exec);
+  if (B->graph) cudaGraphDestroy(B->graph);
+  B->exec = nullptr;
+  B->graph = nullptr;
+}
+
+static cudaStream_t batch_stream(GnBatch* B, int i, cudaStream_t main) {
+  return B->concurrent ? B->streams[i] : main;
+}
+
+static int batch_build_graph(GnBatch* B, const std::vector<char>& active) {
+  batch_free_graph(B);
+  std::vector<PcgState*> h_states;
+  for (int i = 0; i < B->n; ++i)
+    if (active[i]) h_states.push_back(B->S[i]->pcg);
+  VDVC_CUDA(cudaMemcpy(B->d_states, h_states.data(), h_states.size() * sizeof(PcgState*), cudaMemcpyHostToDevice));
+  cudaGraph_t g = nullptr;
+  VDVC_CUDA(cudaGraphCreate(&g, 0));
+  B->graph = g;
+  cudaGraphConditionalHandle hnd;
+  VDVC_CUDA(cudaGraphConditionalHandleCreate(&hnd, g, 1u, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = hnd;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  VDVC_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  cudaStream_t cs = B->cap;
+  VDVC_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  const long long before = vdvc_launch_count();
+  int st = VDVC_OK;
+  if (cudaEventRecord(B->fork_ev, cs) != cudaSuccess) st = set_error(VDVC_ERR_CUDA, "batch fork record");
+  for (int i = 0; i < B->n && st == VDVC_OK; ++i) {
+    if (!active[i]) continue;
+    cudaStream_t ps = B->concurrent ? B->streams[i] : cs;
+    if (B->concurrent && cudaStreamWaitEvent(ps, B->fork_ev, 0) != cudaSuccess) {
+      st = set_error(VDVC_ERR_CUDA, "batch fork wait");
+      break;
+    }
+    for (int it = 0; it < B->chunk && st == VDVC_OK; ++it) st = pcg_iteration<float>(B->S[i], ps);
+    if (st == VDVC_OK && B->concurrent) {
+      if (cudaEventRecord(B->done_ev[i], ps) != cudaSuccess || cudaStreamWaitEvent(cs, B->done_ev[i], 0) != cudaSuccess)
+        st = set_error(VDVC_ERR_CUDA, "batch join");
+    }
+  }
+  const long long captured = vdvc_launch_count() - before;
+  count_launch(-captured);
+  if (st == VDVC_OK) {
+    k_batch_continue<<<1, 32, 0, cs>>>(hnd, B->d_states, (int)h_states.size());
+    if (cudaGetLastError() != cudaSuccess) st = set_error(VDVC_ERR_CUDA, "batch continue kernel capture failed");
+  }
+  cudaGraph_t body_out = nullptr;
+  cudaError_t e = cudaStreamEndCapture(cs, &body_out);
+  if (st) return st;
+  if (e != cudaSuccess) return set_error(VDVC_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+  B->kernels_per_body = captured + 1;
+  VDVC_CUDA(cudaGraphInstantiate(&B->exec, g, 0));
+  B->graph_active = active;
+  return VDVC_OK;
+}
+
+// One GN iteration of every active problem.  out: 12 doubles per problem:
+// the 8 values of vdvc_gn_update, PCG iterations, PCG residual, PCG status,
+// residual status (VDVC_ERR_ZERO_DIVISION when std(g) over the b mask is 0).
+static int batch_iterate(GnBatch* B, const int* active_in, const int* freeze_now, int max_iter, double tol,
+                         double* out, cudaStream_t s) {
+  std::vector<char> active(B->n);
+  int n_active = 0;
+  for (int i = 0; i < B->n; ++i) n_active += (active[i] = active_in[i] ? 1 : 0);
+  if (n_active == 0) return VDVC_OK;
+  int st;
+  if (max_iter > 0 && (!B->exec || active != B->graph_active) && (st = batch_build_graph(B, active))) return st;
+  // sampling, residual, b, diag and the PCG start of every active problem
+  VDVC_CUDA(cudaEventRecord(B->fork_ev, s));
+  for (int i = 0; i < B->n; ++i) {
+    if (!active[i]) continue;
+    GnSolver<float>* S = B->S[i];
+    cudaStream_t ps = batch_stream(B, i, s);
+    if (B->concurrent) VDVC_CUDA(cudaStreamWaitEvent(ps, B->fork_ev, 0));
+    if ((st = sample<float>(S, freeze_now ? freeze_now[i] : 0, ps))) return st;
+    if ((st = rhs<float>(S, ps))) return st;
+    GridReduce red{S->partials, S->ticket};
+    if ((st = launch_pcg_init<float>(S->b, nullptr, S->Minv, S->m.Ndof, S->r, S->z, S->p, false, S->x, S->pcg, red,
+                                     max_iter, tol, ps)))
+      return st;
+    if (B->concurrent) {
+      VDVC_CUDA(cudaEventRecord(B->done_ev[i], ps));
+      VDVC_CUDA(cudaStreamWaitEvent(s, B->done_ev[i], 0));
+    }
+  }
+  if (max_iter > 0) VDVC_CUDA(cudaGraphLaunch(B->exec, s));
+  VDVC_CUDA(cudaEventRecord(B->fork_ev, s));
+  for (int i = 0; i < B->n; ++i) {
+    if (!active[i]) continue;
+    GnSolver<float>* S = B->S[i];
+    cudaStream_t ps = batch_stream(B, i, s);
+    if (B->concurrent) VDVC_CUDA(cudaStreamWaitEvent(ps, B->fork_ev, 0));
+    if ((st = update_enqueue<float>(S, ps))) return st;
+    VDVC_CUDA(cudaMemcpyAsync(S->h_pcg, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, ps));
+    if (B->concurrent) {
+      VDVC_CUDA(cudaEventRecord(B->done_ev[i], ps));
+      VDVC_CUDA(cudaStreamWaitEvent(s, B->done_ev[i], 0));
+    }
+  }
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  int max_it = 0;
+  for (int i = 0; i < B->n; ++i) {
+    if (!active[i]) continue;
+    GnSolver<float>* S = B->S[i];
+    const GnScalars& h = *S->h_sc;
+    const PcgState& pc = S->h_pcg[0];
+    double* o = out + 12 * (size_t)i;
+    o[0] = h.norms[0];
+    o[1] = h.norms[1];
+    o[2] = h.dstats[0];
+    o[3] = h.dstats[1];
+    o[4] = h.dstats[2];
+    o[5] = h.gstats[3];
+    o[6] = h.gstats[0];
+    o[7] = (double)h.status;
+    o[8] = (double)pc.iter;
+    o[9] = pc.res;
+    o[10] = (double)pc.status;
+    o[11] = (double)h.status;
+    if (pc.iter > max_it) max_it = pc.iter;
+    if (h.status != VDVC_OK) VDVC_CUDA(cudaMemsetAsync(&S->sc->status, 0, sizeof(int), s));
+  }
+  if (max_iter > 0) count_launch(((max_it + B->chunk - 1) / B->chunk) * B->kernels_per_body);
+  return VDVC_OK;
+}
+
+static void batch_destroy(GnBatch* B) {
+  if (!B) return;
+  batch_free_graph(B);
+  for (auto* S : B->S) destroy<float>(S);
+  for (auto st : B->streams) cudaStreamDestroy(st);
+  for (auto ev : B->done_ev) cudaEventDestroy(ev);
+  if (B->fork_ev) cudaEventDestroy(B->fork_ev);
+  if (B->cap) cudaStreamDestroy(B->cap);
+  if (B->d_states) cudaFree(B->d_states);
+  delete B;
+}
+
 }  // namespace vdvc
 
 using namespace vdvc;
@@ -698,6 +967,12 @@ using namespace vdvc;
 struct vdvc_gn_solver {
   int dtype;
   void* impl;
+  bool borrowed = false;  // owned by a batch
+};
+
+struct vdvc_gn_batch {
+  GnBatch* impl;
+  std::vector<vdvc_gn_solver*> handles;
 };
 
 extern "C" {
@@ -775,12 +1050,95 @@ int vdvc_gn_read(vdvc_gn_solver* solver, int which, void* dst, int dst_f64, vdvc
 }
 
 void vdvc_gn_destroy(vdvc_gn_solver* solver) {
-  if (!solver) return;
+  if (!solver || solver->borrowed) return;
   if (solver->dtype == VDVC_F32)
     destroy<float>((GnSolver<float>*)solver->impl);
   else
     destroy<double>((GnSolver<double>*)solver->impl);
   delete solver;
+}
+
+int vdvc_gn_batch_create(const vdvc_gn_desc* descs, int n, void* const* ws, const size_t* ws_bytes, int pcg_chunk,
+                         int concurrent, vdvc_gn_batch** out) {
+  VDVC_CHECK_ARG(descs && ws && ws_bytes && out && n >= 1 && n <= 4096, "bad arguments");
+  for (int i = 0; i < n; ++i)
+    VDVC_CHECK_ARG(descs[i].dtype == VDVC_F32, "batched solves are float32 (problem %d)", i);
+  GnBatch* B = new (std::nothrow) GnBatch();
+  if (!B) return set_error(VDVC_ERR_ARG, "host allocation failed");
+  B->n = n;
+  B->chunk = pcg_chunk > 0 ? pcg_chunk : 4;
+  B->concurrent = concurrent ? 1 : 0;
+  auto fail = [&](int code) {
+    batch_destroy(B);
+    return code;
+  };
+  for (int i = 0; i < n; ++i) {
+    void* impl = nullptr;
+    int st = create<float>(&descs[i], ws[i], ws_bytes[i], &impl);
+    if (st) return fail(st);
+    B->S.push_back((GnSolver<float>*)impl);
+  }
+  if (cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaMalloc((void**)&B->d_states, n * sizeof(PcgState*)) != cudaSuccess)
+    return fail(set_error(VDVC_ERR_CUDA, "batch stream/event/state setup failed"));
+  for (int i = 0; i < n; ++i) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(set_error(VDVC_ERR_CUDA, "batch stream setup failed"));
+    B->streams.push_back(st);
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+      return fail(set_error(VDVC_ERR_CUDA, "batch event setup failed"));
+    B->done_ev.push_back(ev);
+  }
+  vdvc_gn_batch* h = new (std::nothrow) vdvc_gn_batch();
+  if (!h) return fail(set_error(VDVC_ERR_ARG, "host allocation failed"));
+  h->impl = B;
+  for (int i = 0; i < n; ++i) {
+    vdvc_gn_solver* sv = new (std::nothrow) vdvc_gn_solver();
+    if (!sv) {
+      for (auto* q : h->handles) delete q;
+      delete h;
+      return fail(set_error(VDVC_ERR_ARG, "host allocation failed"));
+    }
+    sv->dtype = VDVC_F32;
+    sv->impl = B->S[i];
+    sv->borrowed = true;
+    h->handles.push_back(sv);
+  }
+  *out = h;
+  return VDVC_OK;
+}
+
+int vdvc_gn_batch_solver(vdvc_gn_batch* batch, int i, vdvc_gn_solver** out) {
+  VDVC_CHECK_ARG(batch && out && i >= 0 && i < batch->impl->n, "bad arguments");
+  *out = batch->handles[i];
+  return VDVC_OK;
+}
+
+int vdvc_gn_batch_iterate(vdvc_gn_batch* batch, const int* active, const int* freeze_now, int max_iter, double tol,
+                          double* out12, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(batch && active && out12, "bad arguments");
+  return batch_iterate(batch->impl, active, freeze_now, max_iter, tol, out12, (cudaStream_t)stream);
+}
+
+int vdvc_gn_batch_set_schedule(vdvc_gn_batch* batch, int pcg_chunk, int concurrent) {
+  VDVC_CHECK_ARG(batch && pcg_chunk >= 1 && pcg_chunk <= 64, "bad arguments");
+  GnBatch* B = batch->impl;
+  if (B->chunk != pcg_chunk || B->concurrent != (concurrent ? 1 : 0)) {
+    B->chunk = pcg_chunk;
+    B->concurrent = concurrent ? 1 : 0;
+    batch_free_graph(B);
+  }
+  return VDVC_OK;
+}
+
+void vdvc_gn_batch_destroy(vdvc_gn_batch* batch) {
+  if (!batch) return;
+  for (auto* q : batch->handles) delete q;
+  batch_destroy(batch->impl);
+  delete batch;
 }
 
 }  // extern "C"

@@ -50,6 +50,21 @@ int launch_elem_fast(const StripArgs<float>& args, const Kpair<float>* kp, cudaS
 // VDVC_ERR_UNSUPPORTED when h has no specialisation.
 template <bool DG>
 int launch_rhs_fast(const StripArgs<float>& args, cudaStream_t s);
+// Persistent fused PCG for h <= 2 (elem_fast.cu): one cooperative launch runs
+// all iterations until the state says done.  partials: >= 3 * grid doubles;
+// bar: two zeroed counters; err: a zeroed flag set on a barrier timeout.
+struct PcgPersistArgs {
+  StripArgs<float> sa;  // element pass: v = z, p_old = p, evA, grad, mask, regularizer
+  const Kpair<float>* kp;
+  float *x, *r, *z, *p, *Ap;
+  const float* Minv;
+  PcgState* st;
+  double* partials;
+  unsigned int* bar;
+  int* err;
+  int sleep_ns;  // back-off of a barrier poll (0: busy poll)
+};
+int launch_pcg_persistent(const PcgPersistArgs& a, int max_blocks, cudaStream_t s);
 bool tma_enabled();
 long long strip_grid_blocks(const Mesh& m);
 

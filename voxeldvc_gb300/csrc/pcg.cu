@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(256) k_pcg_init(const T* __restrict__ b, const
                                                   T* __restrict__ x0, PcgState* st, GridReduce red, int max_iter,
                                                   double tol) {
   __shared__ double s_red[8];
-  double rz = 0.0, bb = 0.0;
+  T rz = T(0), bb = T(0);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     if (x0) x0[i] = T(0);
     const T bi = b[i];
@@ -42,10 +42,10 @@ __global__ void __launch_bounds__(256) k_pcg_init(const T* __restrict__ b, const
     r[i] = ri;
     z[i] = zi;
     p[i] = p_is_z ? zi : T(0);
-    rz += (double)ri * (double)zi;
-    bb += (double)bi * (double)bi;
+    rz += ri * zi;
+    bb += bi * bi;
   }
-  double mine[2] = {block_sum(rz, s_red), block_sum(bb, s_red)}, out[2];
+  double mine[2] = {block_sum_f(rz, s_red), block_sum_f(bb, s_red)}, out[2];
   if (grid_reduce_sum<2>(red, mine, out, s_red) && threadIdx.x == 0) {
     st->rz = out[0];
     st->r0 = out[1] + 1e-30;
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(256) k_pcg_gather(const Mesh m, const T* __res
       pap += pn * s[c];
     }
   }
-  double mine[1] = {block_sum((double)pap, s_red)}, out[1];
+  double mine[1] = {block_sum_f(pap, s_red)}, out[1];
   if (grid_reduce_sum<1>(red, mine, out, s_red) && threadIdx.x == 0) st->alpha = st->rz / (out[0] + 1e-30);
 }
 
@@ -103,10 +103,10 @@ __global__ void __launch_bounds__(256) k_pcg_alpha(const T* __restrict__ p, cons
                                                    PcgState* st, GridReduce red) {
   __shared__ double s_red[8];
   if (st->done) return;
-  double pap = 0.0;
+  T pap = T(0);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    pap += (double)p[i] * (double)Ap[i];
-  double mine[1] = {block_sum(pap, s_red)}, out[1];
+    pap += p[i] * Ap[i];
+  double mine[1] = {block_sum_f(pap, s_red)}, out[1];
   if (grid_reduce_sum<1>(red, mine, out, s_red) && threadIdx.x == 0) st->alpha = st->rz / (out[0] + 1e-30);
 }
 
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(256) k_pcg_update(const T* __restrict__ p, con
     rr += ri * ri;
     rz += ri * zi;
   }
-  double mine[2] = {block_sum((double)rr, s_red), block_sum((double)rz, s_red)}, out[2];
+  double mine[2] = {block_sum_f(rr, s_red), block_sum_f(rz, s_red)}, out[2];
   if (grid_reduce_sum<2>(red, mine, out, s_red) && threadIdx.x == 0) {
     const double res = sqrt(out[0] / st->r0);
     st->rr = out[0];

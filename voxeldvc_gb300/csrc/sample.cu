@@ -78,18 +78,18 @@ __global__ void __launch_bounds__(256) k_masked_stats<double>(const double* __re
 // (scipy.ndimage.map_coordinates order=1, mode='nearest').
 template <typename T>
 __device__ __forceinline__ T trilinear(const T* __restrict__ g, int nx, int ny, int nz, T cx, T cy, T cz) {
-  const T fx = floor(cx), fy = floor(cy), fz = floor(cz);
+  const T fx = tfloor(cx), fy = tfloor(cy), fz = tfloor(cz);
   const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
   const T tx = cx - fx, ty = cy - fy, tz = cz - fz;
-  const int ix1 = min(ix + 1, nx - 1), iy1 = min(iy + 1, ny - 1), iz1 = min(iz + 1, nz - 1);
-  // 32-bit offsets: the launcher rejects volumes of 2^32 voxels or more
+  // 32-bit offsets (the launcher rejects volumes of 2^32 voxels or more);
+  // the upper neighbour is the sample itself on the last plane of an axis
   const unsigned sy = (unsigned)nx, sz = (unsigned)nx * (unsigned)ny;
-  const unsigned b00 = (unsigned)iy * sy + (unsigned)iz * sz, b10 = (unsigned)iy1 * sy + (unsigned)iz * sz;
-  const unsigned b01 = (unsigned)iy * sy + (unsigned)iz1 * sz, b11 = (unsigned)iy1 * sy + (unsigned)iz1 * sz;
-  const T v000 = g[b00 + ix], v100 = g[b00 + ix1];
-  const T v010 = g[b10 + ix], v110 = g[b10 + ix1];
-  const T v001 = g[b01 + ix], v101 = g[b01 + ix1];
-  const T v011 = g[b11 + ix], v111 = g[b11 + ix1];
+  const unsigned o = (unsigned)ix + (unsigned)iy * sy + (unsigned)iz * sz;
+  const unsigned dx = ix < nx - 1 ? 1u : 0u, dy = iy < ny - 1 ? sy : 0u, dz = iz < nz - 1 ? sz : 0u;
+  const T v000 = __ldg(g + o), v100 = __ldg(g + o + dx);
+  const T v010 = __ldg(g + o + dy), v110 = __ldg(g + o + dy + dx);
+  const T v001 = __ldg(g + o + dz), v101 = __ldg(g + o + dz + dx);
+  const T v011 = __ldg(g + o + dz + dy), v111 = __ldg(g + o + dz + dy + dx);
   const T a00 = v000 + tx * (v100 - v000), a10 = v010 + tx * (v110 - v010);
   const T a01 = v001 + tx * (v101 - v001), a11 = v011 + tx * (v111 - v011);
   const T b0 = a00 + ty * (a10 - a00), b1 = a01 + ty * (a11 - a01);
@@ -172,12 +172,13 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 5 : 6) : 3) k_s
         } else {
           // (u + x) - g_origin, then bounds, clip and order-1 sampling
           // (engine/correlate_gpu.py:259-276)
-          T cx = (ua + vxf) - a.gx0, cy = (ub + (T)vy) - a.gy0, cz = (uc + vzf) - a.gz0;
-          const bool inb = cx >= T(0) && cx <= gxmax && cy >= T(0) && cy <= gymax && cz >= T(0) && cz <= gzmax;
-          cx = fmin(fmax(cx, T(0)), gxmax);
-          cy = fmin(fmax(cy, T(0)), gymax);
-          cz = fmin(fmax(cz, T(0)), gzmax);
-          const T gv = trilinear(a.g, a.gnx, a.gny, a.gnz, cx, cy, cz);
+          const T cx = (ua + vxf) - a.gx0, cy = (ub + (T)vy) - a.gy0, cz = (uc + vzf) - a.gz0;
+          // clipped coordinates; in bounds iff clipping changed nothing
+          // (NaN: clipped to a bound, so out of bounds as in the reference)
+          const T ccx = tmin(tmax(cx, T(0)), gxmax), ccy = tmin(tmax(cy, T(0)), gymax);
+          const T ccz = tmin(tmax(cz, T(0)), gzmax);
+          const bool inb = (ccx == cx) & (ccy == cy) & (ccz == cz);
+          const T gv = trilinear(a.g, a.gnx, a.gny, a.gnz, ccx, ccy, ccz);
           const bool m0 = a.mask0 ? (a.mask0[vv] != 0) : true;
           const bool mk = inb && m0 && (gv > a.glt);
           a.gvals[vv] = gv;

@@ -1,0 +1,177 @@
+"""Batched DVC: a series of deformed volumes against one reference, each
+with its own region of interest and element size, solved together.
+
+The reference correlates one (f, g) pair per call
+(engine/correlate_gpu.py:1143-1305, multiscale_correlate_gpu); this runs the
+same multiscale Gauss-Newton solve for every problem of a series, level by
+level, with all problems' GN iterations in lockstep through one
+`vdvc_gn_batch` (include/vdvc.h): one call per GN iteration, the PCG loops
+of all problems in one device-driven CUDA graph, one host synchronisation.
+Each problem's arithmetic is exactly that of its own multiscale solve; only
+the schedule differs.  Problems leave the lockstep as they converge.
+
+A problem is a dict: origin (x0, y0, z0) of its ROI in voxels of f, element
+size h, mesh (Nx, Ny, Nz); its ROI is f[x0 : x0 + Nx h + 1, ...] and the same
+box of its deformed image.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from .. import _device as D
+from .. import _lib
+from . import correlate_gpu as CG
+from . import autotune
+
+
+def _crop(pix, origin, size):
+    x0, y0, z0 = origin
+    sx, sy, sz = size
+    return pix[x0:x0 + sx, y0:y0 + sy, z0:z0 + sz]
+
+
+def _check_problem(p, fshape):
+    h = int(p["h"])
+    Nx, Ny, Nz = (int(v) for v in p["mesh"])
+    x0, y0, z0 = (int(v) for v in p["origin"])
+    size = (Nx * h + 1, Ny * h + 1, Nz * h + 1)
+    if min(h, Nx, Ny, Nz) < 1 or min(x0, y0, z0) < 0 or any(o + s > f for o, s, f in zip((x0, y0, z0), size, fshape)):
+        raise ValueError(f"problem {p} does not fit the reference volume {tuple(fshape)}")
+    return h, (Nx, Ny, Nz), (x0, y0, z0), size
+
+
+def batch_multiscale_correlate_gpu(f_pix, g_pixs, problems, xp, scales=(2, 1, 0), l0_factor=None,
+                                   fft_prealign=True, K_ref_laplacian=None, dynamic_mask=False,
+                                   freeze_mask_after=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
+                                   glt=0.0, tune=False, pcg_chunk=None, concurrent=None, stats=None, disp=False):
+    """Solve every problem of the series; returns a list of (U, res, dU) in
+    the layout of multiscale_correlate_gpu.  l0_factor: Laplacian length
+    l0 = l0_factor * h per problem (None: no regularizer).  Schedule: the
+    PCG graph's iterations per body and the stream layout come from
+    `pcg_chunk` / `concurrent`, or the autotuner (tune=True: measured and
+    cached, see engine/autotune.py), or defaults (4, concurrent)."""
+    if len(g_pixs) != len(problems):
+        raise ValueError("one deformed image per problem")
+    dtype = np.dtype(np.float32)
+    f_full, fshape = CG.pix_to_vox(f_pix, dtype)
+    del f_full
+    specs = [_check_problem(p, fshape) for p in problems]
+    scales = sorted(set(scales), reverse=True)
+    for h, mesh, origin, size in specs:
+        for isc in scales:
+            if h % (2 ** isc):
+                raise ValueError(f"h={h} is not divisible by 2**{isc} (scale {isc})")
+    n = len(problems)
+    U = [None] * n
+    res = [None] * n
+    dU = [None] * n
+    L = _lib.lib()
+    level_info = []
+    for iscale in scales:
+        s = 2 ** iscale
+        setups = []
+        t_setup = time.perf_counter()
+        for i, (h, mesh, origin, size) in enumerate(specs):
+            f_c, fs = CG.pix_to_vox(_crop(f_pix, origin, size), dtype)
+            g_c, gs = CG.pix_to_vox(_crop(g_pixs[i], origin, size), dtype)
+            f_i, fs_i = CG._decimate(f_c, fs, s, dtype)
+            g_i, gs_i = CG._decimate(g_c, gs, s, dtype)
+            h_i = h // s
+            U0 = None
+            if U[i] is not None:
+                U0 = (U[i] * (prev_s / s)).to(D.torch_dtype(dtype))
+            elif fft_prealign:
+                d = CG._fft_shift_vox(f_i, fs_i, g_i, gs_i, dtype)
+                nn = (mesh[0] + 1) * (mesh[1] + 1) * (mesh[2] + 1)
+                Uh = np.zeros(3 * nn, dtype=dtype)
+                Uh[0::3], Uh[1::3], Uh[2::3] = d[0], d[1], d[2]
+                U0 = D.to_device(Uh)
+            l0_i = None if l0_factor is None else l0_factor * h / s
+            ls = CG._setup_level(CG._Level(f_i, fs_i, g_i, gs_i), *mesh, h_i, glt=glt, l0=l0_i,
+                                 K_ref_laplacian=K_ref_laplacian, dynamic_mask=dynamic_mask, U0=U0,
+                                 maxiter=maxiter, disp=disp, dtype=dtype)
+            setups.append(ls)
+        t_setup = time.perf_counter() - t_setup
+        info = _solve_batch(L, setups, specs, dynamic_mask, freeze_mask_after, maxiter, eps, pcg_tol, pcg_max_iter,
+                            tune, pcg_chunk, concurrent, disp)
+        info.update(scale=iscale, setup_s=t_setup)
+        level_info.append(info)
+        for i, ls in enumerate(setups):
+            U[i], res[i], dU[i] = ls.result
+        prev_s = s
+    if stats is not None:
+        stats.extend(level_info)
+    return [(D.out(U[i], xp), D.out(res[i], xp), D.out(dU[i], xp)) for i in range(n)]
+
+
+def _solve_batch(L, setups, specs, dynamic_mask, freeze_mask_after, maxiter, eps, pcg_tol, pcg_max_iter, tune,
+                 pcg_chunk, concurrent, disp):
+    n = len(setups)
+    descs = (_lib.GnDesc * n)(*[ls.desc for ls in setups])
+    ws = (C.c_void_p * n)(*[ls.ws.data_ptr() for ls in setups])
+    wsb = (C.c_size_t * n)(*[ls.nbytes for ls in setups])
+    key = autotune.batch_key([(ls.h, specs[i][1]) for i, ls in enumerate(setups)])
+    chunk, conc = autotune.lookup(key) if (pcg_chunk is None and concurrent is None) else (None, None)
+    chunk = pcg_chunk or chunk or 4
+    conc = (1 if concurrent is None else int(bool(concurrent))) if conc is None else conc
+    batch = C.c_void_p()
+    _lib.check(L.vdvc_gn_batch_create(descs, n, ws, wsb, int(chunk), int(conc), C.byref(batch)), "batch_create")
+    st = D.stream()
+    info = {"n": n, "gn_iters": [0] * n, "pcg_iters": [[] for _ in range(n)], "h": [ls.h for ls in setups]}
+    t0 = time.perf_counter()
+    try:
+        solvers = []
+        for i, ls in enumerate(setups):
+            sv = C.c_void_p()
+            _lib.check(L.vdvc_gn_batch_solver(batch, i, C.byref(sv)), "batch_solver")
+            solvers.append(sv)
+            _lib.check(L.vdvc_gn_set_U(sv, ls.U64.data_ptr(), st), "set_U")
+            if not dynamic_mask:
+                _lib.check(L.vdvc_gn_frozen_diag(sv, st), "frozen_diag")
+        if tune and pcg_chunk is None and concurrent is None and maxiter > 0:
+            chunk, conc = autotune.tune_batch(L, batch, solvers, setups, pcg_max_iter, pcg_tol, key, st)
+        info["schedule"] = {"pcg_chunk": int(chunk), "concurrent": int(conc)}
+        active = np.ones(n, dtype=np.int32)
+        frozen = np.zeros(n, dtype=bool)
+        out = np.zeros(12 * n, dtype=np.float64)
+        errs = np.full(n, np.inf)
+        for ik in range(maxiter):
+            freeze = np.zeros(n, dtype=np.int32)
+            if freeze_mask_after is not None and ik >= freeze_mask_after:
+                freeze = ((~frozen) & (active != 0)).astype(np.int32)
+            _lib.check(L.vdvc_gn_batch_iterate(batch, active.ctypes.data, freeze.ctypes.data, int(pcg_max_iter),
+                                               float(pcg_tol), out.ctypes.data, st), "batch_iterate")
+            frozen |= freeze.astype(bool)
+            o = out.reshape(n, 12)
+            for i in np.nonzero(active)[0]:
+                if int(o[i, 11]) == _lib.ERR_ZERO_DIVISION:
+                    raise ZeroDivisionError(f"problem {i}: float division by zero (std of g over the b mask is 0)")
+                info["gn_iters"][i] = ik + 1
+                info["pcg_iters"][i].append(int(o[i, 8]))
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    errs[i] = float(np.sqrt(o[i, 0]) / np.sqrt(o[i, 1]))
+                if disp:
+                    print(f"[{i}] " + CG._gn_scalars_line(o[i], ik, errs[i], setups[i].Nvox))
+                if errs[i] < eps:
+                    active[i] = 0
+            if not active.any():
+                break
+        info["converged"] = [bool(e < eps) for e in errs]
+        info["norm_res"] = [CG._norm_res(out.reshape(n, 12)[i], setups[i].std0) for i in range(n)]
+        for i, ls in enumerate(setups):
+            f64 = int(ls.out_dt == np.float64)
+            Uo = D.empty(ls.Ndof, ls.out_dt)
+            r = D.empty(ls.Nvox, ls.out_dt)
+            d = D.empty(ls.Ndof, ls.out_dt)
+            _lib.check(L.vdvc_gn_read(solvers[i], _lib.GN_U, Uo.data_ptr(), f64, st), "read")
+            _lib.check(L.vdvc_gn_read(solvers[i], _lib.GN_RES, r.data_ptr(), f64, st), "read")
+            _lib.check(L.vdvc_gn_read(solvers[i], _lib.GN_DU, d.data_ptr(), f64, st), "read")
+            ls.result = (Uo, r, d)
+    finally:
+        L.vdvc_gn_batch_destroy(batch)
+        D.torch().cuda.current_stream().synchronize()
+    info["gn_wall_s"] = time.perf_counter() - t0
+    return info

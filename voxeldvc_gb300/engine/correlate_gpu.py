@@ -267,10 +267,19 @@ def _plane_wave(Nx, Ny, Nz, h, dtype):
     return V
 
 
-def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
-                 c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False,
-                 freeze_mask_after=None, U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
-                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=6):
+class _LevelSetup:
+    """Everything one GN solver of a level needs: the descriptor, its
+    workspaces, the device arrays it points to (kept alive here), U0 and the
+    level's scalars."""
+
+
+def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
+                 c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False, U0=None,
+                 maxiter=30, disp=True, dtype=np.float32, pcg_chunk=0, precision='plain', mixed_min_h=6):
+    """Level set-up of correlate_gpu (engine/correlate_gpu.py:905-1053):
+    gradient, masks, reference stats, regularizer and lambda calibration,
+    U0, and the solver descriptor.  Returns a _LevelSetup (ls.empty is set
+    when maxiter < 1: nothing to solve)."""
     dtype = np.dtype(dtype)
     if precision not in ('plain', 'mixed'):
         raise ValueError("precision must be 'plain' or 'mixed'")
@@ -344,8 +353,12 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
         D.to_device(U0, dtype).reshape(-1).to(D.torch().float64)
     if U64.numel() != Ndof:
         raise ValueError(f"U0 has {U64.numel()} entries, expected {Ndof}")
-    if maxiter < 1:
-        return U64.to(D.torch_dtype(out_dt)), D.zeros(Nvox, out_dt), D.zeros(Ndof, out_dt), {}
+    ls = _LevelSetup()
+    ls.h, ls.Nvox, ls.Ndof, ls.out_dt, ls.U64, ls.ll = h, Nvox, Ndof, out_dt, U64, ll
+    ls.mean0, ls.std0, ls.precision, ls.dynamic_mask = mean0, std0, precision, bool(dynamic_mask)
+    ls.empty = maxiter < 1
+    if ls.empty:
+        return ls
 
     Klap = np.ascontiguousarray(K_ref_laplacian if K_ref_laplacian is not None else np.zeros((24, 24)),
                                 dtype=np.float64)
@@ -379,6 +392,41 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
         eh_bytes = L.vdvc_eh_workspace_bytes(h, Nx, Ny, Nz)
         eh_ws = D.torch().empty(eh_bytes, dtype=D.torch().uint8, device=D.device())
         desc.eh_ws, desc.eh_ws_bytes = eh_ws.data_ptr(), eh_bytes
+    ls.desc, ls.ws, ls.eh_ws, ls.nbytes = desc, ws, eh_ws, nbytes
+    # the descriptor holds raw pointers: keep what they point to alive
+    ls.keep = (Klap, Kel, grad, mask0, interior, diag_eq, lv)
+    return ls
+
+
+def _gn_scalars_line(out8, ik, err, Nvox):
+    _, stdr = _mean_std(out8[2], out8[3], out8[4])
+    n_active = int(out8[5])
+    return ("Iter # %2d | std(res)=%2.2f gl | dU/U=%1.2e | active pts=%d/%d (%.1f%%)"
+            % (ik + 1, stdr, err, n_active, Nvox, 100 * n_active / Nvox))
+
+
+def _norm_res(out8, std0):
+    # 1 - ZNCC of the registered pair over the live mask, from the last
+    # residual: res/std0 = f^ - g^ for the standardised f^, g^ (the
+    # residual is built from the centred f, correlate_gpu.py:962, :1094)
+    c_l, s2_l = out8[2], out8[4]
+    return float(s2_l / c_l / (2.0 * std0 * std0)) if c_l > 0 else float("inf")
+
+
+def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
+                 c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False,
+                 freeze_mask_after=None, U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
+                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=6):
+    ls = _setup_level(lv, Nx, Ny, Nz, h, g_origin=g_origin, glt=glt, l0=l0, K_ref_laplacian=K_ref_laplacian,
+                      reg_exponent=reg_exponent, c_reg=c_reg, reg_type=reg_type, K_ref_elastic=K_ref_elastic,
+                      eps_reg=eps_reg, dynamic_mask=dynamic_mask, U0=U0, maxiter=maxiter, disp=disp, dtype=dtype,
+                      pcg_chunk=pcg_chunk, precision=precision, mixed_min_h=mixed_min_h)
+    out_dt, Nvox, Ndof, U64 = ls.out_dt, ls.Nvox, ls.Ndof, ls.U64
+    if ls.empty:
+        return U64.to(D.torch_dtype(out_dt)), D.zeros(Nvox, out_dt), D.zeros(Ndof, out_dt), {}
+    L = _lib.lib()
+    desc, ws, eh_ws, nbytes, ll, precision = ls.desc, ls.ws, ls.eh_ws, ls.nbytes, ls.ll, ls.precision
+
     solver = C.c_void_p()
     _lib.check(L.vdvc_gn_create(C.byref(desc), ws.data_ptr(), nbytes, C.byref(solver)), "correlate_gpu")
     info = {"gn_iters": 0, "pcg_iters": [], "ll": ll, "h": h, "precision": precision}
@@ -405,18 +453,11 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
             with np.errstate(divide='ignore', invalid='ignore'):
                 err = float(np.sqrt(np.float64(dd)) / np.sqrt(np.float64(uu)))
             if disp:
-                _, stdr = _mean_std(out8[2], out8[3], out8[4])
-                n_active = int(out8[5])
-                print("Iter # %2d | std(res)=%2.2f gl | dU/U=%1.2e | active pts=%d/%d (%.1f%%)"
-                      % (ik + 1, stdr, err, n_active, Nvox, 100 * n_active / Nvox))
+                print(_gn_scalars_line(out8, ik, err, Nvox))
             if err < eps:
                 break
         info["converged"] = bool(err < eps)
-        # 1 - ZNCC of the registered pair over the live mask, from the last
-        # residual: res/std0 = f^ - g^ for the standardised f^, g^ (the
-        # residual is built from the centred f, correlate_gpu.py:962, :1094)
-        c_l, s2_l = out8[2], out8[4]
-        info["norm_res"] = float(s2_l / c_l / (2.0 * std0 * std0)) if c_l > 0 else float("inf")
+        info["norm_res"] = _norm_res(out8, ls.std0)
         Uo = D.empty(Ndof, out_dt)
         res = D.empty(Nvox, out_dt)
         dU = D.empty(Ndof, out_dt)

@@ -36,9 +36,13 @@ def default_net(path=WEIGHTS_PATH):
 
 def learned_seed(f_pix, g_pix, Nx, Ny, Nz, h, g_origin=(0, 0, 0), net=None):
     """Seed U (float64 CUDA, Ndof) for the mesh from the (f, g) pair."""
-    net = net or default_net()
     f_vox, fs = CG.pix_to_vox(f_pix, np.float32)
     g_vox, gs = CG.pix_to_vox(g_pix, np.float32)
+    return _seed_vox(f_vox, fs, g_vox, gs, Nx, Ny, Nz, h, g_origin, net)
+
+
+def _seed_vox(f_vox, fs, g_vox, gs, Nx, Ny, Nz, h, g_origin, net):
+    net = net or default_net()
     if tuple(fs) != tuple(gs):
         raise ValueError("the learned seed needs f and g of one shape")
     U0 = net.predict_nodes(f_vox, g_vox, fs, h, Nx, Ny, Nz)
@@ -61,14 +65,21 @@ def learned_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0), l
     levels = [] if stats is None else stats
     t0 = time.perf_counter()
     reason = None
+    # one layout pass per image: the float32 copies feed both the network
+    # and (for a float32 solve) the GN level
+    f32, fs = CG.pix_to_vox(f_pix, np.float32)
+    g32, gs = CG.pix_to_vox(g_pix, np.float32)
     try:
-        U0 = learned_seed(f_pix, g_pix, Nx, Ny, Nz, h, g_origin, net)
+        U0 = _seed_vox(f32, fs, g32, gs, Nx, Ny, Nz, h, g_origin, net)
     except ValueError as e:
         U0, reason = None, str(e)
     seed_s = time.perf_counter() - t0
     if U0 is not None:
-        f_vox, fs = CG.pix_to_vox(f_pix, dtype)
-        g_vox, gs = CG.pix_to_vox(g_pix, dtype)
+        if dtype == np.float32:
+            f_vox, g_vox = f32, g32
+        else:
+            f_vox, fs = CG.pix_to_vox(f_pix, dtype)
+            g_vox, gs = CG.pix_to_vox(g_pix, dtype)
         U, res, dU, info = CG._solve_level(CG._Level(f_vox, fs, g_vox, gs), Nx, Ny, Nz, h, g_origin=g_origin, l0=l0,
                                            U0=U0, stats=levels, **kwargs)
         rho = info.get("norm_res", float("inf"))
