@@ -330,6 +330,50 @@ def compare_forms(wl, f_pix, g_pix, kw, U_plain, e2e_plain, plain_s):
     return out
 
 
+def compare_batch():
+    """The batched form on the load-series workload (16 problems, one 385^3
+    reference, uneven ROIs, h in {8, 12, 16}): the lockstep batch (cached or
+    default schedule) against the same solves one after another."""
+    import torch
+    from voxeldvc_gb300 import synth
+    from voxeldvc_gb300.engine import batch as B, correlate_gpu as CG, geometry_dvc as G
+    f_pix, gs, problems, fields = synth.series_385()
+    Kl = G.build_K_ref_laplacian()
+    kw = dict(scales=(2, 1, 0), fft_prealign=True, dynamic_mask=True, freeze_mask_after=4, maxiter=30, eps=1e-3,
+              pcg_tol=1e-6, pcg_max_iter=2000, glt=0.0)
+
+    def seq():
+        outs = []
+        for i, p in enumerate(problems):
+            h = p["h"]
+            (x0, y0, z0), (Nx, Ny, Nz) = p["origin"], p["mesh"]
+            sl = (slice(x0, x0 + Nx * h + 1), slice(y0, y0 + Ny * h + 1), slice(z0, z0 + Nz * h + 1))
+            outs.append(CG.multiscale_correlate_gpu(f_pix[sl], gs[i][sl], Nx, Ny, Nz, h, xp=torch, l0=4.5 * h,
+                                                    K_ref_laplacian=Kl, disp=False, **kw))
+        return outs
+
+    def bat(stats=None):
+        return B.batch_multiscale_correlate_gpu(f_pix, gs, problems, torch, l0_factor=4.5, K_ref_laplacian=Kl,
+                                                tune=True, stats=stats, **kw)
+
+    res = {}
+    for label, fn in (("sequential_s", seq), ("batch_s", bat)):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        res[label] = round(time.perf_counter() - t0, 4)
+    st = []
+    out = bat(st)
+    rms = [float(np.sqrt(np.mean((out[i][0].double().cpu().numpy() - synth.true_U_problem(p, fields[i])) ** 2)))
+           for i, p in enumerate(problems)]
+    res.update(problems=len(problems), hs=[p["h"] for p in problems],
+               meshes=[list(p["mesh"]) for p in problems], speedup=round(res["sequential_s"] / res["batch_s"], 3),
+               rms_vs_true_field_vx_max=round(max(rms), 5), schedule=[s["schedule"] for s in st])
+    return res
+
+
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -438,6 +482,9 @@ def gpu_arm(args):
     forms = None
     if rank == 0 and world == 1 and not args.no_forms:
         forms = compare_forms(wl, f_pix, g_pix, kw, U, e2e, ms / 1e3)
+        del f_pix, g_pix
+        torch.cuda.empty_cache()
+        forms["batch"] = compare_batch()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

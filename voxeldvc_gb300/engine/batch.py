@@ -51,8 +51,9 @@ def batch_multiscale_correlate_gpu(f_pix, g_pixs, problems, xp, scales=(2, 1, 0)
     the layout of multiscale_correlate_gpu.  l0_factor: Laplacian length
     l0 = l0_factor * h per problem (None: no regularizer).  Schedule: the
     PCG graph's iterations per body and the stream layout come from
-    `pcg_chunk` / `concurrent`, or the autotuner (tune=True: measured and
-    cached, see engine/autotune.py), or defaults (4, concurrent)."""
+    `pcg_chunk` / `concurrent`, else from the autotuner's cache, else (with
+    tune=True) are measured once per problem class and cached
+    (engine/autotune.py), else default to (4, concurrent)."""
     if len(g_pixs) != len(problems):
         raise ValueError("one deformed image per problem")
     dtype = np.dtype(np.float32)
@@ -115,6 +116,7 @@ def _solve_batch(L, setups, specs, dynamic_mask, freeze_mask_after, maxiter, eps
     wsb = (C.c_size_t * n)(*[ls.nbytes for ls in setups])
     key = autotune.batch_key([(ls.h, specs[i][1]) for i, ls in enumerate(setups)])
     chunk, conc = autotune.lookup(key) if (pcg_chunk is None and concurrent is None) else (None, None)
+    cached = chunk is not None
     chunk = pcg_chunk or chunk or 4
     conc = (1 if concurrent is None else int(bool(concurrent))) if conc is None else conc
     batch = C.c_void_p()
@@ -131,7 +133,7 @@ def _solve_batch(L, setups, specs, dynamic_mask, freeze_mask_after, maxiter, eps
             _lib.check(L.vdvc_gn_set_U(sv, ls.U64.data_ptr(), st), "set_U")
             if not dynamic_mask:
                 _lib.check(L.vdvc_gn_frozen_diag(sv, st), "frozen_diag")
-        if tune and pcg_chunk is None and concurrent is None and maxiter > 0:
+        if tune and not cached and pcg_chunk is None and concurrent is None and maxiter > 0:
             chunk, conc = autotune.tune_batch(L, batch, solvers, setups, pcg_max_iter, pcg_tol, key, st)
         info["schedule"] = {"pcg_chunk": int(chunk), "concurrent": int(conc)}
         active = np.ones(n, dtype=np.int32)

@@ -167,5 +167,46 @@ def necking_256():
     return _necking(257, 'laplacian')
 
 
+def series_385(n_steps=16, seed=3):
+    """A load series against one reference: a 385^3 reference (2000
+    cylinders), n_steps deformed images under uniaxial strain
+    eps_z = 0.2 % ... 3.2 % (Poisson contraction 0.4 eps in x and y, about the
+    volume centre, plus a 0.5 eps x 100 vx rigid drift in z), and one ROI
+    per step with edges drawn uniformly in [256, 384] voxels, snapped to
+    n h + 1 for h drawn from {8, 12, 16}, placed uniformly inside the
+    volume.  Returns (f_pix, [g_pix], problems, true fields (callables))."""
+    shape = (385, 385, 385)
+    rng = np.random.default_rng(seed)
+    f = texture(shape, 2000, seed=seed, cyl_seed=seed + 1)
+    gs, problems, fields = [], [], []
+    c = (shape[0] - 1) / 2.0
+    for k in range(n_steps):
+        ez = 0.002 * (k + 1)
+        params = [0.0, 0.0, 50.0 * ez, *np.diag([-0.4 * ez, -0.4 * ez, ez]).reshape(-1), c, c, c]
+        g = warp(f, shape, FIELD_AFFINE, params, 0.01, seed=seed + 100 + k)
+        gs.append(vox_to_pix(g, shape))
+        h = int(rng.choice([8, 12, 16]))
+        mesh, origin = [], []
+        for ax in range(3):
+            edge = int(rng.integers(256, 385))
+            n_el = max(1, (edge - 1) // h)
+            mesh.append(n_el)
+            origin.append(int(rng.integers(0, shape[ax] - (n_el * h + 1) + 1)))
+        problems.append(dict(origin=tuple(origin), h=h, mesh=tuple(mesh)))
+        fields.append((FIELD_AFFINE, params))
+    return vox_to_pix(f, shape), gs, problems, fields
+
+
+def true_U_problem(problem, field):
+    """True nodal displacement of a series problem (ROI frame)."""
+    kind, params = field
+    h = problem["h"]
+    Nx, Ny, Nz = problem["mesh"]
+    o = np.asarray(problem["origin"], np.float64)
+    nn = np.arange((Nx + 1) * (Ny + 1) * (Nz + 1))
+    X = np.stack([nn % (Nx + 1), (nn // (Nx + 1)) % (Ny + 1), nn // ((Nx + 1) * (Ny + 1))], 1) * float(h) + o
+    return field_at(kind, params, X).reshape(-1)
+
+
 WORKLOADS = {"plain_small": plain_small, "necking_512": necking_512, "necking_512_eqgap": necking_512_eqgap,
              "necking_256": necking_256}
