@@ -87,3 +87,18 @@ def test_pool_input_constant_and_shape():
     out = O.pool_input(f, g, (1.0, 2.0, 1.0, 4.0))
     assert out.shape == (3, 3, 4, 2)
     assert np.allclose(out[..., 0], 1.0) and np.allclose(out[..., 1], 1.0)
+
+
+def test_arch_layout_and_grids():
+    from voxeldvc_gb300.learned.arch import param_layout, grids, input_grid, LAYERS
+    layout, total = param_layout()
+    assert [l[0] for l in layout] == [l["name"] for l in LAYERS]
+    off = 0
+    for (name, wo, ws, bo, n_out, cin), l in zip(layout, LAYERS):
+        assert wo == off and ws == n_out * 27 * cin and bo == wo + ws
+        off = bo + n_out
+    assert total == off
+    # 513^3 voxels: input grid 129, output (node grid of h = 8) 65, coarse 33
+    assert input_grid((513, 513, 513)) == (129, 129, 129)
+    assert grids((129, 129, 129)) == ((129, 129, 129), (65, 65, 65), (33, 33, 33))
+    assert grids((65, 40, 9))[1:] == ((33, 20, 5), (17, 10, 3))
