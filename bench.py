@@ -65,8 +65,9 @@ def parse():
     p.add_argument("--cpu-sample-layers", type=int, default=1)
     p.add_argument("--no-forms", action="store_true",
                    help="skip the precision / learned-seed form comparison (FP64 reference solve included)")
-    p.add_argument("--only", default=None, choices=[None, "matvec"],
-                   help="matvec: time only the finest-level Hessian matvec (the profiling command)")
+    p.add_argument("--only", default=None, choices=[None, "matvec", "kernels"],
+                   help="matvec: time only the finest-level Hessian matvec; kernels: run each hot kernel of the "
+                        "plain, precision and learned forms a few times on the 257^3 case (the profiling commands)")
     return p.parse_args()
 
 
@@ -520,12 +521,52 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
+def kernels_only(args):
+    """Each hot kernel a few times on the 257^3 necking case (h = 8, 32^3
+    elements) and its h = 2 level (65^3 voxels after decimation by 4 ...
+    here a 129^3 h = 2 mesh of 64^3 elements): the matrix-free Hessian pass
+    (strip, h = 8; thread per element, h = 2), the precision form's element
+    Hessian formation and matvec, one GN iteration's sampling and residual
+    passes, the network's forward pass.  Prints one line per group."""
+    import torch
+    from voxeldvc_gb300 import _lib, synth
+    from voxeldvc_gb300.engine import correlate_gpu as CG, kernels_dvc as K, geometry_dvc as G
+    from voxeldvc_gb300.learned import solve as LS
+    reps = max(1, args.steps)
+    wl = synth.WORKLOADS["necking_256"]()
+    Nx, Ny, Nz = wl.mesh
+    f_pix, g_pix = wl.make()
+    f_vox, shape = CG.pix_to_vox(f_pix, np.float32)
+    grad, mask0 = CG._grad_vox(f_vox, shape, np.float32, 0.0)
+    N, w = G.build_N_stencil(wl.h)
+    v = torch.randn(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), device="cuda")
+    for _ in range(reps):
+        K.matvec_H(v, grad.view(-1, 3), mask0, N, w, wl.h, Nx, Ny, Nz, torch)
+        K.matvec_H_mixed(v, grad.view(-1, 3), mask0, N, w, wl.h, Nx, Ny, Nz, torch)
+    # h = 2 on 64^3 elements (the coarse level of the 513^3 benchmark)
+    f2 = synth.texture((129, 129, 129), 80, seed=4)
+    g2, m2 = CG._grad_vox(f2, (129, 129, 129), np.float32, 0.0)
+    N2, w2 = G.build_N_stencil(2)
+    v2 = torch.randn(3 * 65 ** 3, device="cuda")
+    for _ in range(reps):
+        K.matvec_H(v2, g2.view(-1, 3), m2, N2, w2, 2, 64, 64, 64, torch)
+    # one finest-level GN iteration (sampling, residual, b, diag, PCG)
+    CG.correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, torch, l0=36.0, K_ref_laplacian=G.build_K_ref_laplacian(),
+                     dynamic_mask=True, maxiter=reps, eps=0.0, disp=False)
+    for _ in range(reps):
+        LS.learned_seed(f_pix, g_pix, Nx, Ny, Nz, wl.h)
+    torch.cuda.synchronize()
+    print(json.dumps({"kernels": "done", "reps": reps, "workload": wl.name}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
     elif args.only == "matvec":
         matvec_only(args)
+    elif args.only == "kernels":
+        kernels_only(args)
     else:
         gpu_arm(args)
 
