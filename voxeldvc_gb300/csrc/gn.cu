@@ -343,6 +343,8 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
       EhMatvecArgs ma{};
       ma.m = S->m;
       ma.T = S->T_eh;
+      ma.pitch = eh_pitch(S->m.Ne);
+      ma.err = &S->sc->status;  // read with the GN scalars after the iteration
       ma.v = S->z;
       ma.p_old = S->p;
       ma.st = S->pcg;
@@ -454,7 +456,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   }
   if (S->mixed) {
     Carve cv(d->eh_ws, d->eh_ws_bytes);
-    S->T_eh = cv.take<float>((size_t)162 * m.Ne);
+    S->T_eh = cv.take<float>((size_t)162 * eh_pitch(m.Ne));
     S->grad_bf16 = cv.take<uint16_t>((size_t)3 * m.Nvox);
     const bool ok = std::is_same<T, float>::value;
     const bool h_ok = d->h == 1 || d->h == 2 || d->h == 3 || d->h == 4 || d->h == 6 || d->h == 8 || d->h == 12 ||
@@ -547,7 +549,7 @@ template <typename T>
 static int frozen_diag(GnSolver<T>* S, cudaStream_t s) {
   int st;
   if (S->mixed) {
-    EhFormArgs fa{S->m, S->grad_bf16, S->d.mask0, S->T_eh, (float*)S->evD};
+    EhFormArgs fa{S->m, S->grad_bf16, S->d.mask0, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne)};
     if ((st = launch_eh_form(fa, s))) return st;
     S->eh_fixed = true;
   } else {
@@ -624,7 +626,7 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
     st = launch_strip<T, kModeB | kModeRes>(a, nullptr, s);
   if (st) return st;
   if (with_diag && S->mixed) {
-    EhFormArgs fa{S->m, S->grad_bf16, S->frozen, S->T_eh, (float*)S->evD};
+    EhFormArgs fa{S->m, S->grad_bf16, S->frozen, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne)};
     if ((st = launch_eh_form(fa, s))) return st;
     if (S->frozen_set) S->eh_fixed = true;
   }

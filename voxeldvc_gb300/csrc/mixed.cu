@@ -10,13 +10,15 @@
 //   T[sx][sy][sz][kl] = sum_q w m psi_sx(qx) psi_sy(qy) psi_sz(qz) G_kl(q),
 // G = (g0g0, g0g1, g0g2, g1g1, g1g2, g2g2).  T is formed separably (per
 // voxel 18 FMAs along y, 54 per z plane, the x sum as a shared-memory
-// reduction over the element's voxel columns) and stored SoA [162][Ne].
+// reduction over the element's voxel columns) and stored tile-major
+// [Ne / 64][162][64] (see the matvec below).
 // A BF16 x BF16 product is exact in FP32, so G carries no rounding beyond
 // the BF16 gradient itself.
 #include <cuda_bf16.h>
 
 #include "ops.cuh"
 #include "pcg.cuh"
+#include "tma.cuh"
 
 namespace vdvc {
 
@@ -115,7 +117,8 @@ __global__ void __launch_bounds__(128) k_eh_form(const EhFormArgs a) {
       s += px * s_R[(e * H + q) * kRP + rest];
     }
     if (last_strip && e == nel - 1 && sx == 2) s += s_R[nthr * kRP + rest];  // column x = Nx*h: psi = (0,0,1)
-    a.T[(long long)o * m.Ne + e_base + e] = s;
+    const long long eg = e_base + e;  // tile-major: [tile][162][kEhTile]
+    a.T[((eg / kEhTile) * 162 + o) * kEhTile + (eg % kEhTile)] = s;
     // diagonal of K_e: a = (sx/2, sy/2, sz/2) with sx,sy,sz in {0,2}, kl in {00,11,22}
     const int sy = rest / 18, sz = (rest / 6) % 3, kl = rest % 6;
     if ((sx & 1) == 0 && (sy & 1) == 0 && (sz & 1) == 0 && (kl == 0 || kl == 3 || kl == 5)) {
@@ -131,89 +134,6 @@ __host__ __device__ constexpr int kl_index(int k, int l) {
   return k > l ? kl_index(l, k) : (k == 0 ? l : (k == 1 ? 2 + l : 5));
 }
 
-
-// One thread per element: out_e = K_e v_e (+ regularizer), 576 FMAs from the
-// 162 distinct entries.
-template <bool PCG>
-__global__ void __launch_bounds__(256, 3) k_eh_matvec(const EhMatvecArgs a) {
-  if constexpr (PCG) {
-    if (a.st->done) return;
-  }
-  const Mesh& m = a.m;
-  float beta = 0.f;
-  if constexpr (PCG) beta = (float)a.st->beta;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m.Ne;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int ei = (int)(e % m.Nx);
-    const long long rr = e / m.Nx;
-    const int ej = (int)(rr % m.Ny), ek = (int)(rr / m.Ny);
-    float vl[24], out[24];
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const long long node = (long long)(ei + corner_dx(b)) + (long long)(ej + corner_dy(b)) * m.Nnx +
-                             (long long)(ek + corner_dz(b)) * m.NnxNny;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float val = a.v[3 * node + c];
-        if constexpr (PCG) val += beta * a.p_old[3 * node + c];
-        vl[3 * b + c] = val;
-        out[3 * b + c] = 0.f;
-      }
-    }
-#pragma unroll
-    for (int sx = 0; sx < 3; ++sx)
-#pragma unroll
-      for (int sy = 0; sy < 3; ++sy)
-#pragma unroll
-        for (int sz = 0; sz < 3; ++sz) {
-          const int type = (sx * 3 + sy) * 3 + sz;
-          float tv[6];
-#pragma unroll
-          for (int kl = 0; kl < 6; ++kl) tv[kl] = __ldg(a.T + (long long)(type * 6 + kl) * m.Ne + e);
-#pragma unroll
-          for (int aa = 0; aa < 8; ++aa)
-#pragma unroll
-            for (int bb = 0; bb < 8; ++bb) {
-              if (corner_dx(aa) + corner_dx(bb) != sx || corner_dy(aa) + corner_dy(bb) != sy ||
-                  corner_dz(aa) + corner_dz(bb) != sz)
-                continue;
-#pragma unroll
-              for (int kk = 0; kk < 3; ++kk)
-#pragma unroll
-                for (int ll = 0; ll < 3; ++ll) out[3 * aa + kk] += tv[kl_index(kk, ll)] * vl[3 * bb + ll];
-            }
-        }
-    if (a.nreg >= 1) {
-#pragma unroll
-      for (int aa = 0; aa < 8; ++aa)
-#pragma unroll
-        for (int bb = 0; bb < 8; ++bb) {
-          const float lw = a.c1 * a.L8[aa * 8 + bb];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) out[3 * aa + c] += lw * vl[3 * bb + c];
-        }
-      if (a.nreg == 2) {
-        // the element's w values reuse the registers of v (no longer needed)
-#pragma unroll
-        for (int b = 0; b < 8; ++b) {
-          const long long node = (long long)(ei + corner_dx(b)) + (long long)(ej + corner_dy(b)) * m.Nnx +
-                                 (long long)(ek + corner_dz(b)) * m.NnxNny;
-#pragma unroll
-          for (int c = 0; c < 3; ++c) vl[3 * b + c] = a.w[3 * node + c];
-        }
-#pragma unroll 4
-        for (int r = 0; r < 24; ++r) {
-          float s = 0.f;
-#pragma unroll
-          for (int q = 0; q < 24; ++q) s += __ldg(a.K2 + r * 24 + q) * vl[q];
-          out[r] += a.c2 * s;
-        }
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < 24; ++r) a.ev[(long long)r * m.Ne + e] = out[r];
-  }
-}
 
 template <int H>
 static int launch_form(const EhFormArgs& args, cudaStream_t s) {
@@ -240,9 +160,138 @@ int launch_eh_form(const EhFormArgs& a, cudaStream_t s) {
   return set_error(VDVC_ERR_UNSUPPORTED, "element Hessians for h=%d are not built (h in {1,2,3,4,6,8,12,16})", a.m.h);
 }
 
+// ---- TMA-staged element-Hessian matvec --------------------------------------
+//
+// T is stored tile-major, [tile][162][kEhTile]: a tile's 162 entry rows of
+// kEhTile elements are one contiguous 41.5 KB span.  A block owns one tile:
+// one thread arms an mbarrier and issues a single bulk copy (cp.async.bulk)
+// of the span into shared memory while every thread loads its element's
+// nodal values; after the barrier each thread applies its element Hessian
+// from shared memory (consecutive threads, consecutive words: no bank
+// conflicts).  Five tiles in flight per SM keep the HBM stream of T deep
+// without registers holding loads.  The wait is bounded; on a timeout the
+// block raises *a.err, waits once more (bounded) for its copy and returns.
+constexpr int kTile = kEhTile;
+
+template <bool PCG>
+__global__ void __launch_bounds__(kTile) k_eh_matvec_tma(const EhMatvecArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float* sT = (float*)smem_raw;  // [162][kTile]
+  __shared__ __align__(8) uint64_t bar;
+  if constexpr (PCG) {
+    if (a.st->done) return;
+  }
+  const Mesh& m = a.m;
+  const int t = threadIdx.x;
+  const long long e0 = (long long)blockIdx.x * kTile;
+  const int n_el = (int)min((long long)kTile, m.Ne - e0);
+  constexpr uint32_t tile_bytes = 162u * kTile * sizeof(float);
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_arrive_expect_tx(&bar, tile_bytes);
+    bulk_g2s(sT, a.T + (long long)blockIdx.x * 162 * kTile, tile_bytes, &bar);
+  }
+  __syncthreads();
+  const long long e = e0 + t;
+  const bool active = t < n_el;
+  float vl[24];
+  float beta = 0.f;
+  if constexpr (PCG) beta = (float)a.st->beta;
+  int ei = 0, ej = 0, ek = 0;
+  if (active) {
+    ei = (int)(e % m.Nx);
+    const long long rr = e / m.Nx;
+    ej = (int)(rr % m.Ny);
+    ek = (int)(rr / m.Ny);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const long long node = (long long)(ei + corner_dx(b)) + (long long)(ej + corner_dy(b)) * m.Nnx +
+                             (long long)(ek + corner_dz(b)) * m.NnxNny;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float val = __ldg(a.v + 3 * node + c);
+        if constexpr (PCG) val += beta * __ldg(a.p_old + 3 * node + c);
+        vl[3 * b + c] = val;
+      }
+    }
+  }
+  if (!mbar_wait_bounded(&bar, 0)) {
+    if (t == 0) atomicExch(a.err, VDVC_ERR_CUDA);
+    mbar_wait_bounded(&bar, 0);
+    return;
+  }
+  if (!active) return;
+  float out[24];
+#pragma unroll
+  for (int r = 0; r < 24; ++r) out[r] = 0.f;
+#pragma unroll
+  for (int sx = 0; sx < 3; ++sx)
+#pragma unroll
+    for (int sy = 0; sy < 3; ++sy)
+#pragma unroll
+      for (int sz = 0; sz < 3; ++sz) {
+        const int type = (sx * 3 + sy) * 3 + sz;
+        float tv[6];
+#pragma unroll
+        for (int kl = 0; kl < 6; ++kl) tv[kl] = sT[(type * 6 + kl) * kTile + t];
+#pragma unroll
+        for (int aa = 0; aa < 8; ++aa)
+#pragma unroll
+          for (int bb = 0; bb < 8; ++bb) {
+            if (corner_dx(aa) + corner_dx(bb) != sx || corner_dy(aa) + corner_dy(bb) != sy ||
+                corner_dz(aa) + corner_dz(bb) != sz)
+              continue;
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+              for (int ll = 0; ll < 3; ++ll) out[3 * aa + kk] += tv[kl_index(kk, ll)] * vl[3 * bb + ll];
+          }
+      }
+  if (a.nreg >= 1) {
+#pragma unroll
+    for (int aa = 0; aa < 8; ++aa)
+#pragma unroll
+      for (int bb = 0; bb < 8; ++bb) {
+        const float lw = a.c1 * a.L8[aa * 8 + bb];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[3 * aa + c] += lw * vl[3 * bb + c];
+      }
+    if (a.nreg == 2) {
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const long long node = (long long)(ei + corner_dx(b)) + (long long)(ej + corner_dy(b)) * m.Nnx +
+                               (long long)(ek + corner_dz(b)) * m.NnxNny;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vl[3 * b + c] = a.w[3 * node + c];
+      }
+#pragma unroll 4
+      for (int r = 0; r < 24; ++r) {
+        float s2 = 0.f;
+#pragma unroll
+        for (int q = 0; q < 24; ++q) s2 += __ldg(a.K2 + r * 24 + q) * vl[q];
+        out[r] += a.c2 * s2;
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 24; ++r) a.ev[(long long)r * m.Ne + e] = out[r];
+}
+
+// Elements rounded up to whole tiles (the T array holds 162 * eh_pitch floats).
+long long eh_pitch(long long Ne) { return (Ne + kTile - 1) / kTile * kTile; }
+
 template <bool PCG>
 int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s) {
-  k_eh_matvec<PCG><<<grid_blocks(a.m.Ne, 256, 152 * 16), 256, 0, s>>>(a);
+  if (((uintptr_t)a.T & 15u)) return set_error(VDVC_ERR_ARG, "element Hessians misaligned");
+  const size_t smem = (size_t)162 * kTile * sizeof(float);
+  static bool attr_set = false;
+  if (!attr_set) {
+    VDVC_CUDA(cudaFuncSetAttribute(k_eh_matvec_tma<PCG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  const long long nb = (a.m.Ne + kTile - 1) / kTile;
+  k_eh_matvec_tma<PCG><<<(unsigned)nb, kTile, smem, s>>>(a);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
@@ -265,9 +314,10 @@ size_t vdvc_eh_workspace_bytes(int h, int Nx, int Ny, int Nz) {
   Mesh m;
   if (make_mesh(h, Nx, Ny, Nz, &m)) return 0;
   Carve cv(nullptr, 0);
-  cv.take<float>((size_t)162 * m.Ne);
+  cv.take<float>((size_t)162 * eh_pitch(m.Ne));
   cv.take<float>((size_t)24 * m.Ne);
   cv.take<float>((size_t)24 * m.Ne);
+  cv.take<int>(4);
   cv.take<uint16_t>((size_t)3 * m.Nvox);
   return cv.off + 256;
 }
@@ -279,22 +329,33 @@ int vdvc_matvec_H_mixed(const float* v, const float* grad, const uint8_t* mask, 
   if (st) return st;
   VDVC_CHECK_ARG(v && grad && mask && out, "null pointer");
   Carve cv(ws, ws_bytes);
-  float* T = cv.take<float>((size_t)162 * m.Ne);
+  const long long pitch = eh_pitch(m.Ne);
+  float* T = cv.take<float>((size_t)162 * pitch);
   float* evD = cv.take<float>((size_t)24 * m.Ne);
   float* ev = cv.take<float>((size_t)24 * m.Ne);
+  int* err = cv.take<int>(4);
   uint16_t* gb = cv.take<uint16_t>((size_t)3 * m.Nvox);
   if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "mixed matvec needs %zu bytes of workspace", cv.off);
   cudaStream_t s = (cudaStream_t)stream;
   if ((st = launch_grad_bf16(grad, 3 * m.Nvox, gb, s))) return st;
-  EhFormArgs fa{m, (const __nv_bfloat16*)gb, mask, T, evD};
+  EhFormArgs fa{m, (const __nv_bfloat16*)gb, mask, T, evD, pitch};
   if ((st = launch_eh_form(fa, s))) return st;
   EhMatvecArgs ma{};
   ma.m = m;
   ma.T = T;
+  ma.pitch = pitch;
+  ma.err = err;
   ma.v = v;
   ma.ev = ev;
+  VDVC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   if ((st = launch_eh_matvec<false>(ma, s))) return st;
-  return launch_gather<float>(m, ev, out, s);
+  if ((st = launch_gather<float>(m, ev, out, s))) return st;
+  // the bulk-copy waits are bounded: report a timeout (never seen in practice)
+  int h_err = 0;
+  VDVC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  if (h_err) return set_error(VDVC_ERR_CUDA, "element-Hessian tile copies timed out");
+  return VDVC_OK;
 }
 
 }  // extern "C"

@@ -107,18 +107,23 @@ template <typename T>
 int launch_masked_stats(const T* field, const uint8_t* mask, const Mesh& m, GridReduce red, double* out3,
                         cudaStream_t s);
 
-// Precision form (mixed.cu): BF16 gradient, element Hessians T[162][Ne].
+// Precision form (mixed.cu): BF16 gradient, element Hessians T stored
+// tile-major [Ne / kEhTile][162][kEhTile].
+constexpr int kEhTile = 64;
 struct EhFormArgs {
   Mesh m;
-  const void* grad;       // __nv_bfloat16  // (Nvox,3)
-  const uint8_t* mask;        // H mask
-  float* T;                   // [162][Ne]
-  float* evD;                 // [24][Ne] diagonal contributions
+  const void* grad;       // (Nvox,3) __nv_bfloat16
+  const uint8_t* mask;    // H mask
+  float* T;               // [tiles][162][kEhTile]
+  float* evD;             // [24][Ne] diagonal contributions
+  long long pitch;        // eh_pitch(Ne): elements rounded up to whole tiles
 };
 
 struct EhMatvecArgs {
   Mesh m;
-  const float* T;      // [162][Ne]
+  const float* T;      // [tiles][162][kEhTile]
+  long long pitch;     // eh_pitch(Ne): elements rounded up to whole tiles
+  int* err;            // set to VDVC_ERR_CUDA if a tile's bulk copies time out
   const float* v;      // nodal input (PCG: z)
   const float* p_old;  // PCG: p_new = z + beta p_old
   const PcgState* st;
@@ -132,6 +137,7 @@ struct EhMatvecArgs {
 };
 
 int launch_eh_form(const EhFormArgs& a, cudaStream_t s);
+long long eh_pitch(long long Ne);  // elements rounded up to whole tiles
 template <bool PCG>
 int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s);
 int launch_grad_bf16(const float* g, long long n, void* out, cudaStream_t s);
