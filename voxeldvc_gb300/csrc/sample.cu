@@ -6,6 +6,8 @@
 // The sampling kernels use the element-strip decomposition of strip.cuh so
 // the nodal field of a strip is staged once in shared memory and
 // interpolated separably per voxel column.
+#include <type_traits>
+
 #include "ops.cuh"
 
 namespace vdvc {
@@ -96,12 +98,17 @@ __device__ __forceinline__ T trilinear(const T* __restrict__ g, int nx, int ny, 
   return b0 + tz * (b1 - b0);
 }
 
-template <typename T, bool STATS, bool INTERP>
+// HH > 0: the element edge is the compile-time constant HH (the row loop is
+// unrolled four-fold and the strip shape folds into the index arithmetic);
+// HH == 0: h from the mesh.
+template <typename T, bool STATS, bool INTERP, int HH>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 5 : 6) : 3) k_sample(const SampleArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_red[4];
   const Mesh& m = a.m;
-  const int h = m.h, EX = a.EX, nthr = blockDim.x;
+  const int h = HH > 0 ? HH : m.h;
+  const int EX = HH > 0 ? (HH >= 128 ? 1 : 128 / HH) : a.EX;
+  const int nthr = blockDim.x;
   T* s_v = (T*)smem_raw;          // EX*24
   T* s_phi = s_v + (size_t)EX * 24;  // h+1
 
@@ -153,7 +160,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 5 : 6) : 3) k_s
       const int vz = k * h + qz;
       const T vzf = (T)vz;
       float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f;
-#pragma unroll 1
+#pragma unroll(HH > 0 ? 4 : 1)
       for (int qy = 0; qy < ny_e; ++qy) {
         const T fy1 = s_phi[qy];
         const int vy = j * h + qy;
@@ -223,7 +230,15 @@ int launch_sample(const SampleArgs<T>& args, cudaStream_t s) {
   const size_t smem = ((size_t)sh.EX * 24 + args.m.h + 2) * sizeof(T);
   SampleArgs<T> a = args;
   a.EX = sh.EX;
-  k_sample<T, STATS, INTERP><<<grid, sh.threads, smem, s>>>(a);
+  if constexpr (std::is_same<T, float>::value && STATS && !INTERP) {
+    switch (args.m.h) {
+      case 2: k_sample<T, STATS, INTERP, 2><<<grid, sh.threads, smem, s>>>(a); VDVC_LAUNCHED(); return VDVC_OK;
+      case 4: k_sample<T, STATS, INTERP, 4><<<grid, sh.threads, smem, s>>>(a); VDVC_LAUNCHED(); return VDVC_OK;
+      case 8: k_sample<T, STATS, INTERP, 8><<<grid, sh.threads, smem, s>>>(a); VDVC_LAUNCHED(); return VDVC_OK;
+      case 16: k_sample<T, STATS, INTERP, 16><<<grid, sh.threads, smem, s>>>(a); VDVC_LAUNCHED(); return VDVC_OK;
+    }
+  }
+  k_sample<T, STATS, INTERP, 0><<<grid, sh.threads, smem, s>>>(a);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
