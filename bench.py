@@ -471,6 +471,8 @@ def gpu_arm(args):
         f_host = f_pix.cpu().pin_memory().numpy()
         g_host = g_pix.cpu().pin_memory().numpy()
         t_e2e = []
+        # one untimed call: host result buffers are pinned once and reused
+        CG.multiscale_correlate_gpu(f_host, g_host, Nx, Ny, Nz, wl.h, xp=np, **kw)
         for _ in range(args.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()

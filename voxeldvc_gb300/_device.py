@@ -5,6 +5,8 @@ Compute never happens here; every kernel is in libvdvc.so.
 """
 from __future__ import annotations
 
+import weakref
+
 import numpy as np
 
 from . import _lib
@@ -138,9 +140,49 @@ def wants_host(xp) -> bool:
     return xp is np
 
 
+class _HostPool:
+    """Pinned host buffers for results returned as numpy arrays.
+
+    A device->host copy into freshly allocated pageable memory runs at the
+    speed of first-touch page faults (~14 GB/s measured on the GB300 machine,
+    against ~190 GB/s into mapped memory), so large results are copied into
+    pinned buffers that are reused once the array handed out for them (and
+    every view of it, which keeps it alive) is gone.  At most two buffers per
+    shape and type are kept; beyond that results use ordinary memory."""
+
+    MIN_BYTES = 1 << 20
+    PER_KEY = 2
+
+    def __init__(self):
+        self.entries = {}
+
+    def take(self, shape, dtype):
+        lst = self.entries.setdefault((tuple(shape), dtype), [])
+        for ent in lst:
+            if ent[1] is None or ent[1]() is None:
+                return ent
+        if len(lst) >= self.PER_KEY:
+            return None
+        ent = [torch().empty(tuple(shape), dtype=dtype, pin_memory=True), None]
+        lst.append(ent)
+        return ent
+
+
+host_pool = _HostPool()
+
+
 def out(t, xp):
     if wants_host(xp):
-        return t.detach().cpu().numpy()
+        t = t.detach()
+        if t.is_cuda and t.numel() * t.element_size() >= _HostPool.MIN_BYTES:
+            ent = host_pool.take(t.shape, t.dtype)
+            if ent is not None:
+                ent[0].copy_(t, non_blocking=True)
+                torch().cuda.current_stream().synchronize()
+                a = ent[0].numpy()
+                ent[1] = weakref.ref(a)
+                return a
+        return t.cpu().numpy()
     return t
 
 
