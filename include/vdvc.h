@@ -207,6 +207,29 @@ int vdvc_interp_field(const void* U, int dtype, int h, int Nx, int Ny,
                       int Nz, int channels_first, void* out,
                       vdvc_stream_t stream);
 
+/* ---- post-solve voxel stages (engine/write_output.py) ------------------- */
+/* sampling modes of vdvc_push_field (scipy.ndimage.map_coordinates) */
+enum { VDVC_MODE_NEAREST = 0, VDVC_MODE_CONSTANT = 1 };
+
+/* out(x) = field(x - u(x)) on the voxel grid (push_field_forward,
+   engine/write_output.py:571-608): field and out in vox layout
+   (nx*ny*nz) of dtype (VDVC_F32, VDVC_F64 or VDVC_U8 for label fields);
+   u_cf: the displacement at every voxel, float64 channels-first (3, nvox)
+   as vdvc_interp_field writes it; order 0 (nearest, ties upward) or 1
+   (trilinear); mode NEAREST clamps to [0, n-1], CONSTANT writes cval where
+   any coordinate is outside [0, n-1].  Coordinates in float64. */
+int vdvc_push_field(const void* field, int dtype, const double* u_cf, int nx,
+                    int ny, int nz, int order, int mode, double cval,
+                    void* out, vdvc_stream_t stream);
+
+/* *out_host = zero-normalised cross-correlation of f and g over mask
+   (compute_zncc, engine/write_output.py:658-690): float64 sums in two
+   passes (means, then centred products); NaN for an empty mask or a zero
+   denominator.  ws >= 32 KiB.  Synchronises the stream. */
+int vdvc_zncc(const void* f, const void* g, int dtype, const uint8_t* mask,
+              long long n, double* out_host, void* ws, size_t ws_bytes,
+              vdvc_stream_t stream);
+
 /* ---- reductions and pre-alignment ------------------------------------- */
 /* *out_host = sum a*b (b != NULL) or sum a, accumulated in float64;
    synchronises the stream (the xp.dot / .sum() calls of the lambda

@@ -355,6 +355,30 @@ def interp_field(U, h, Nx, Ny, Nz):
     return out
 
 
+def push_field_forward(field, U, Nx, Ny, Nz, h, order=1, mode='nearest', cval=0.0):
+    """write_output.py:571-608: field(x - u(x)) on the voxel grid, u the
+    FE-interpolated displacement, scipy map_coordinates(order, mode, cval)."""
+    from scipy.ndimage import map_coordinates
+    Nvx, Nvy, Nvz = field.shape
+    u = interp_field(np.asarray(U), h, Nx, Ny, Nz)
+    vx, vy, vz = (np.ravel(a, order='F').astype(u.dtype) for a in
+                  np.meshgrid(np.arange(Nvx), np.arange(Nvy), np.arange(Nvz), indexing='ij'))
+    coords = np.stack([vx - u[:, 0], vy - u[:, 1], vz - u[:, 2]])
+    return map_coordinates(field, coords, order=order, mode=mode, cval=cval).reshape(Nvx, Nvy, Nvz, order='F')
+
+
+def zncc(f_flat, g_flat, mask):
+    """write_output.py:658-690: zero-normalised cross-correlation over mask."""
+    f = np.asarray(f_flat, dtype=np.float64)[mask]
+    g = np.asarray(g_flat, dtype=np.float64)[mask]
+    if f.size == 0:
+        return float('nan')
+    f = f - f.mean()
+    g = g - g.mean()
+    den = np.sqrt(np.sum(f * f) * np.sum(g * g))
+    return float(np.sum(f * g) / den) if den > 0 else float('nan')
+
+
 def sample_deformed(U, g_pix, h, Nx, Ny, Nz, g_origin=(0, 0, 0), mask0=None, glt=0.0):
     """correlate_gpu.py:201-281: g at (u + x) - g_origin, clipped, order-1
     map_coordinates; mask in_bounds & mask0 & g > glt."""

@@ -223,7 +223,35 @@ def affine_cases():
                         iters=np.array(rinfo['iters']))
 
 
+def post_cases():
+    """Post-solve voxel stages (engine/write_output.py): push_field_forward
+    in both orders and modes, on float and label fields, and compute_zncc."""
+    from voxeldvc.engine import write_output as W
+    rng = np.random.default_rng(31)
+    Nx, Ny, Nz, h = 3, 2, 2, 4
+    shape = (Nx * h + 1, Ny * h + 1, Nz * h + 1)
+    f32 = _texture(shape, rng).astype(np.float32)
+    f64 = _texture(shape, rng)
+    lab = (rng.random(shape) < 0.4).astype(np.uint8) * 3
+    U = rng.standard_normal(3 * (Nx + 1) * (Ny + 1) * (Nz + 1)) * 1.7
+    d = dict(f32=f32, f64=f64, lab=lab, U=U, dims=np.array([Nx, Ny, Nz, h]))
+    for name, fld in (("f32", f32), ("f64", f64)):
+        d[f"{name}_o1_nearest"] = W.push_field_forward(fld, U, Nx, Ny, Nz, h, order=1, mode="nearest")
+        d[f"{name}_o1_constant"] = W.push_field_forward(fld, U, Nx, Ny, Nz, h, order=1, mode="constant", cval=-1.0)
+        d[f"{name}_o0_constant"] = W.push_field_forward(fld, U, Nx, Ny, Nz, h, order=0, mode="constant", cval=7.0)
+    d["lab_o0_nearest"] = W.push_field_forward(lab, U, Nx, Ny, Nz, h, order=0, mode="nearest")
+    d["lab_o0_constant"] = W.push_field_forward(lab, U, Nx, Ny, Nz, h, order=0, mode="constant", cval=5)
+    n = 5000
+    zf = rng.random(n).astype(np.float32)
+    zg = (0.7 * zf + 0.3 * rng.random(n)).astype(np.float32)
+    zm = rng.random(n) < 0.6
+    d.update(zf=zf, zg=zg, zm=zm, zncc=W.compute_zncc(zf, zg, zm),
+             zncc_empty=W.compute_zncc(zf, zg, np.zeros(n, bool)))
+    np.savez_compressed(os.path.join(OUT, "post.npz"), **d)
+
+
 if __name__ == "__main__":
+    post_cases()
     affine_cases()
     geometry()
     operators("A", 3, 2, 2, 4, seed=1)

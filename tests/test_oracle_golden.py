@@ -124,3 +124,21 @@ def test_correlate_dynamic_and_eqgap_match_reference():
     U, res, _ = O.multiscale(c["f"], c["g"], 4, 3, 2, 8, scales=(2, 1, 0), K_lap=K_lap, l0=36.0, maxiter=20,
                              eps=1e-3, dynamic_mask=True, freeze_mask_after=4, fft_prealign=True)
     assert np.abs(U - c["U"]).max() < 1e-4
+
+
+def test_post_stages_oracle():
+    """push_field_forward / compute_zncc restatements against the reference's
+    own outputs (tests/golden/post.npz)."""
+    c = load_golden("post.npz")
+    Nx, Ny, Nz, h = (int(x) for x in c["dims"])
+    for name in ("f32", "f64"):
+        for key, kw in (("o1_nearest", dict(order=1, mode="nearest")),
+                        ("o1_constant", dict(order=1, mode="constant", cval=-1.0)),
+                        ("o0_constant", dict(order=0, mode="constant", cval=7.0))):
+            out = O.push_field_forward(c[name], c["U"], Nx, Ny, Nz, h, **kw)
+            ref = c[f"{name}_{key}"]
+            assert out.dtype == ref.dtype and np.array_equal(out, ref), (name, key)
+    for key, kw in (("o0_nearest", dict(order=0, mode="nearest")), ("o0_constant", dict(order=0, mode="constant", cval=5))):
+        assert np.array_equal(O.push_field_forward(c["lab"], c["U"], Nx, Ny, Nz, h, **kw), c[f"lab_{key}"])
+    assert O.zncc(c["zf"], c["zg"], c["zm"]) == pytest.approx(float(c["zncc"]), abs=1e-15)
+    assert np.isnan(O.zncc(c["zf"], c["zg"], np.zeros_like(c["zm"])))

@@ -45,4 +45,11 @@ def test_run_writes_the_solve(tmp_path, cuda):
     grid = np.stack([U[c::3].reshape(5, 4, 3, order='F') for c in range(3)], axis=-1)
     assert np.allclose(U_rec, grid, atol=1e-12)
     assert np.load(tmp_path / "residual.npy").shape == f.shape
-    assert "dU/U=" in (tmp_path / "run_log.txt").read_text()
+    log = (tmp_path / "run_log.txt").read_text()
+    assert "dU/U=" in log
+    # post-solve stages: the pushed reference matches the oracle's push of
+    # the same displacement; the ZNCC line is logged
+    from oracle import dvc_oracle as O
+    pushed = np.load(tmp_path / "ref_forward_pushed.npy")
+    assert np.allclose(pushed, O.push_field_forward(f.astype(np.float64), U, 4, 3, 2, 8), atol=1e-9)
+    assert "ZNCC (active voxels):" in log

@@ -63,6 +63,8 @@ SIGNATURES = {
     "vdvc_sample_deformed": (ci, [vp, vp, ci, ci, ci, ci, cd, cd, cd, vp, cd, ci, ci, ci, ci, vp, vp, vp]),
     "vdvc_interp_field": (ci, [vp, ci, ci, ci, ci, ci, ci, vp, vp]),
     "vdvc_dot": (ci, [vp, vp, ci, C.c_longlong, pd, vp, cz, vp]),
+    "vdvc_push_field": (ci, [vp, ci, vp, ci, ci, ci, ci, ci, cd, vp, vp]),
+    "vdvc_zncc": (ci, [vp, vp, ci, vp, C.c_longlong, pd, vp, cz, vp]),
     "vdvc_fft_rigid_shift": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, ci, pd, vp]),
     "vdvc_pcg_workspace_bytes": (cz, []),
     "vdvc_pcg_begin": (ci, [vp, vp, vp, ci, C.c_longlong, vp, vp, vp, ci, cd, vp, cz, vp]),

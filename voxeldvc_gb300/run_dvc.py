@@ -12,6 +12,7 @@ results:
   U_local.npy          same layout, the displacement minus the affine seed
   residual.npy         (Nvx, Nvy, Nvz) final residual
   dU.npy               (Nx+1, Ny+1, Nz+1, 3) last GN update
+  ref_forward_pushed.npy  (Nvx, Nvy, Nvz) reference pushed onto the deformed grid
   run_log.txt          the run's printed output
 
 The derived post-processing fields of the reference's write_outputs (strain,
@@ -114,6 +115,17 @@ def main(argv=None):
         np.save(os.path.join(work, 'U_local.npy'), U_local)
         np.save(os.path.join(work, 'residual.npy'), res.reshape(ref.shape, order='F'))
         np.save(os.path.join(work, 'dU.npy'), _grid(dU, Nx, Ny, Nz))
+        # post-solve voxel stages (engine/write_output.py): the reference
+        # pushed onto the deformed grid, and the correlation quality over
+        # the active voxels (f and the warped g = f - res)
+        from .engine.write_output import push_reference_forward, compute_zncc
+        from .engine.correlate_gpu import compute_active_mask
+        np.save(os.path.join(work, 'ref_forward_pushed.npy'),
+                push_reference_forward(ref, U, Nx, Ny, Nz, h))
+        active = compute_active_mask(U, deformed, Nx, Ny, Nz, h, np, glt=glt)
+        f_flat = np.ravel(np.asarray(ref, dtype=np.float64), order='F')
+        zncc = compute_zncc(f_flat, f_flat - res, active)
+        print(f"  ZNCC (active voxels): {zncc:.6f}")
         for ci, name in enumerate(['ux', 'uy', 'uz']):
             comp = U_grid[..., ci]
             print(f"  {name}: mean={comp.mean():.4f}  std={comp.std():.4f}  min={comp.min():.4f}  max={comp.max():.4f}")
