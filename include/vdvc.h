@@ -230,6 +230,30 @@ int vdvc_zncc(const void* f, const void* g, int dtype, const uint8_t* mask,
               long long n, double* out_host, void* ws, size_t ws_bytes,
               vdvc_stream_t stream);
 
+/* ---- preprocess glue (preprocess.py) ----------------------------------- */
+/* out[i,j,k] (C order, nx*ny*nz) = g sampled at A (x - c) + c + t, x =
+   (i,j,k), coordinates in float32 as the reference forms them, order-1
+   interpolation, 0 outside [0, n-1] (warp_onto_ref_grid,
+   preprocess.py:233-285).  g: C-order float32 (gx, gy, gz); A: host 3x3
+   row-major; t, c: host 3-vectors. */
+int vdvc_warp_affine(const float* g, int gx, int gy, int gz, const double* A,
+                     const double* t, const double* c, int nx, int ny,
+                     int nz, float* out, vdvc_stream_t stream);
+
+/* float32 mean over B^3 blocks of a C-order volume of dtype (F32, U8, U16,
+   I16), summed in the reference's order (bin_volume,
+   preprocess.py:288-312); the shape must be divisible by B. */
+int vdvc_bin_volume(const void* vol, int dtype, int s0, int s1, int s2, int B,
+                    float* out, vdvc_stream_t stream);
+
+/* Axis projections of the valid overlap (f > glt) & (g > glt) of two C-order
+   float32 volumes (n0, n1, n2): p_a[i] = 1 where some voxel with index i on
+   axis a is valid (compute_crop's bounding-box search,
+   preprocess.py:315-367). */
+int vdvc_overlap_projections(const float* f, const float* g, int n0, int n1,
+                             int n2, double glt, uint8_t* p0, uint8_t* p1,
+                             uint8_t* p2, vdvc_stream_t stream);
+
 /* ---- reductions and pre-alignment ------------------------------------- */
 /* *out_host = sum a*b (b != NULL) or sum a, accumulated in float64;
    synchronises the stream (the xp.dot / .sum() calls of the lambda

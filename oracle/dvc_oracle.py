@@ -379,6 +379,50 @@ def zncc(f_flat, g_flat, mask):
     return float(np.sum(f * g) / den) if den > 0 else float('nan')
 
 
+def warp_onto_ref_grid(A, t, c, Nf, g):
+    """preprocess.py:233-285: g at A (x - c) + c + t on f's grid, coordinates
+    in float32 as the reference forms them, order-1, 0 outside (the
+    reference samples with cupyx's map_coordinates, scipy's semantics)."""
+    from scipy.ndimage import map_coordinates
+    A32, t32, c32 = (np.asarray(v, np.float32) for v in (A, t, c))
+    I, J, K = np.meshgrid(*[np.arange(n, dtype=np.float32) for n in Nf], indexing='ij')
+    pts = np.stack([I.ravel(), J.ravel(), K.ravel()])
+    pts_g = A32 @ (pts - c32.reshape(3, 1)) + c32.reshape(3, 1) + t32.reshape(3, 1)
+    return map_coordinates(np.asarray(g, np.float32), pts_g, order=1, mode='constant',
+                           cval=0.0).reshape(Nf).astype(np.float32)
+
+
+def bin_volume(vol, B):
+    """preprocess.py:288-312: float32 sums over the B^3 strided sub-volumes."""
+    S0, S1, S2 = vol.shape
+    out = np.zeros((S0 // B, S1 // B, S2 // B), dtype=np.float32)
+    for i in range(B):
+        for j in range(B):
+            for k in range(B):
+                out += vol[i::B, j::B, k::B]
+    out /= B ** 3
+    return out
+
+
+def compute_crop(f, g, h, glt=0.0):
+    """preprocess.py:315-367: n h + 1 crop of the valid overlap."""
+    valid = (f > glt) & (g > glt)
+    idx = [np.where(valid.any(axis=tuple(b for b in range(3) if b != a)))[0] for a in range(3)]
+    lo = np.array([i[0] for i in idx])
+    hi = np.array([i[-1] for i in idx])
+    snapped = ((hi - lo) // h) * h + 1
+    lo_out = (lo + hi) // 2 - snapped // 2
+    hi_out = lo_out + snapped
+    for a in range(3):
+        if lo_out[a] < 0:
+            hi_out[a] -= lo_out[a]
+            lo_out[a] = 0
+        if hi_out[a] > f.shape[a]:
+            lo_out[a] -= hi_out[a] - f.shape[a]
+            hi_out[a] = f.shape[a]
+    return lo_out, hi_out
+
+
 def sample_deformed(U, g_pix, h, Nx, Ny, Nz, g_origin=(0, 0, 0), mask0=None, glt=0.0):
     """correlate_gpu.py:201-281: g at (u + x) - g_origin, clipped, order-1
     map_coordinates; mask in_bounds & mask0 & g > glt."""

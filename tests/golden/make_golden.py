@@ -250,7 +250,31 @@ def post_cases():
     np.savez_compressed(os.path.join(OUT, "post.npz"), **d)
 
 
+def prep_cases():
+    """Preprocess glue (preprocess.py): bin_volume and compute_crop run from
+    the reference module, imported with stand-ins for its module-level CuPy
+    and tifffile imports (neither function uses them)."""
+    import types
+    for name in ("cupy", "tifffile"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    from voxeldvc import preprocess as P
+    rng = np.random.default_rng(41)
+    vol8 = rng.integers(0, 256, (12, 8, 16), dtype=np.uint8)
+    volf = rng.random((9, 6, 12)).astype(np.float32) * 100
+    f = _texture((40, 33, 29), rng).astype(np.float32)
+    g = _texture((40, 33, 29), rng).astype(np.float32)
+    f[:3] = 0.0
+    g[:, -5:] = 0.0
+    g[..., :2] = 0.0
+    lo, hi = P.compute_crop(f, g, 4)
+    lo2, hi2 = P.compute_crop(f, g, 8, glt=0.3)
+    np.savez_compressed(os.path.join(OUT, "prep.npz"), vol8=vol8, volf=volf, bin8_2=P.bin_volume(vol8, 2),
+                        bin8_4=P.bin_volume(vol8, 4), binf_3=P.bin_volume(volf, 3), f=f, g=g, lo=lo, hi=hi,
+                        lo2=lo2, hi2=hi2)
+
+
 if __name__ == "__main__":
+    prep_cases()
     post_cases()
     affine_cases()
     geometry()

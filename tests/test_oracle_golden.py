@@ -142,3 +142,21 @@ def test_post_stages_oracle():
         assert np.array_equal(O.push_field_forward(c["lab"], c["U"], Nx, Ny, Nz, h, **kw), c[f"lab_{key}"])
     assert O.zncc(c["zf"], c["zg"], c["zm"]) == pytest.approx(float(c["zncc"]), abs=1e-15)
     assert np.isnan(O.zncc(c["zf"], c["zg"], np.zeros_like(c["zm"])))
+
+
+def test_preprocess_oracle():
+    """bin_volume / compute_crop restatements against the reference's own
+    outputs (tests/golden/prep.npz); the warp restatement against known
+    answers (the reference's warp needs CuPy, absent here)."""
+    c = load_golden("prep.npz")
+    assert np.array_equal(O.bin_volume(c["vol8"], 2), c["bin8_2"])
+    assert np.array_equal(O.bin_volume(c["vol8"], 4), c["bin8_4"])
+    assert np.array_equal(O.bin_volume(c["volf"], 3), c["binf_3"])
+    lo, hi = O.compute_crop(c["f"], c["g"], 4)
+    assert np.array_equal(lo, c["lo"]) and np.array_equal(hi, c["hi"])
+    lo, hi = O.compute_crop(c["f"], c["g"], 8, glt=0.3)
+    assert np.array_equal(lo, c["lo2"]) and np.array_equal(hi, c["hi2"])
+    g = c["f"]
+    assert np.array_equal(O.warp_onto_ref_grid(np.eye(3), np.zeros(3), np.full(3, 7.0), g.shape, g), g)
+    w = O.warp_onto_ref_grid(np.eye(3), np.array([2.0, 0.0, -1.0]), np.zeros(3), g.shape, g)
+    assert np.array_equal(w[:-2, :, 1:], g[2:, :, :-1]) and np.all(w[-2:] == 0) and np.all(w[:, :, 0] == 0)

@@ -65,6 +65,9 @@ SIGNATURES = {
     "vdvc_dot": (ci, [vp, vp, ci, C.c_longlong, pd, vp, cz, vp]),
     "vdvc_push_field": (ci, [vp, ci, vp, ci, ci, ci, ci, ci, cd, vp, vp]),
     "vdvc_zncc": (ci, [vp, vp, ci, vp, C.c_longlong, pd, vp, cz, vp]),
+    "vdvc_warp_affine": (ci, [vp, ci, ci, ci, pd, pd, pd, ci, ci, ci, vp, vp]),
+    "vdvc_bin_volume": (ci, [vp, ci, ci, ci, ci, ci, vp, vp]),
+    "vdvc_overlap_projections": (ci, [vp, vp, ci, ci, ci, cd, vp, vp, vp, vp]),
     "vdvc_fft_rigid_shift": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, ci, pd, vp]),
     "vdvc_pcg_workspace_bytes": (cz, []),
     "vdvc_pcg_begin": (ci, [vp, vp, vp, ci, C.c_longlong, vp, vp, vp, ci, cd, vp, cz, vp]),
