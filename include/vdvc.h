@@ -254,6 +254,69 @@ int vdvc_overlap_projections(const float* f, const float* g, int n0, int n1,
                              int n2, double glt, uint8_t* p0, uint8_t* p1,
                              uint8_t* p2, vdvc_stream_t stream);
 
+/* ---- per-element (cell) output fields ------------------------------------
+   The element-scale stages of `voxeldvc run`'s outputs
+   (engine/write_output.py:256-491, engine/kernels_dvc.py:92-341).  Element
+   arrays are x-fastest (e = i + j Nx + k Nx Ny), voxel arrays x-fastest over
+   (Nx h + 1, Ny h + 1, Nz h + 1), node vectors node-major with the component
+   fastest (U[3 node + c]); an element's voxels are its (h+1)^3 block,
+   shared faces included.  All float64 unless stated. */
+
+/* Principal strains e1 >= e2 >= e3 (principal: Ne x 3) of the small-strain
+   tensor at each element centroid from the Hex8 shape-function gradients
+   scaled by 1/h (compute_principal_strains_cell, write_output.py:256-281);
+   equivalent (may be NULL): the von Mises equivalent strain
+   sqrt(2)/3 sqrt((e1-e2)^2 + (e2-e3)^2 + (e3-e1)^2)
+   (compute_equivalent_strain, :284-310). */
+int vdvc_cell_strains(const double* U, int h, int Nx, int Ny, int Nz,
+                      double* principal, double* equivalent,
+                      vdvc_stream_t stream);
+/* compute_equivalent_strain of any (n, 3) principal-strain array. */
+int vdvc_equivalent_strain(const double* principal, long long n, double* out,
+                           vdvc_stream_t stream);
+
+/* Block reductions per element over its voxels (NULL outputs are skipped):
+     material      block mean of ref > glt (compute_material_cell_mask,
+                   :313-338); ref VDVC_F32 or VDVC_F64
+     safe          no voxel of the block flagged in unsafe (uint8)
+                   (compute_safe_cell_mask, :358-381)
+     residual_std, zncc   over the block's active voxels (res != 0): the
+                   population std of res and the ZNCC of ref and ref - res,
+                   NaN below 8 active voxels or for a zero denominator
+                   (compute_correlation_quality_cell, :384-452); both are
+                   written when res != NULL. */
+int vdvc_cell_fields(const void* ref, int ref_dtype, const double* res,
+                     const uint8_t* unsafe, int h, int Nx, int Ny, int Nz,
+                     double glt, uint8_t* material, uint8_t* safe,
+                     double* residual_std, double* zncc,
+                     vdvc_stream_t stream);
+/* One-cell erosion with the 26-neighbourhood, the mesh border counting as
+   material (compute_material_cell_mask_eroded, :341-355).  in != out. */
+int vdvc_cell_erode(const uint8_t* in, int Nx, int Ny, int Nz, uint8_t* out,
+                    vdvc_stream_t stream);
+/* ||dU|| / ||U|| over each element's 24 corner DOFs, NaN where ||U|| = 0
+   (compute_gn_convergence_cell, :455-491). */
+int vdvc_cell_gn_convergence(const double* dU, const double* U, int Nx,
+                             int Ny, int Nz, double* out,
+                             vdvc_stream_t stream);
+
+/* Diagnostic masks of kernels_dvc.py:92-341 from the active voxel mask
+   (uint8) and, for the overlap-lost mask, the material mask mask0 (uint8;
+   may be NULL otherwise).  Outputs (uint8, NULL to skip):
+     unsafe_vox   (Nvox)  compute_unsafe_voxel_mask
+     unsafe_elem  (Ne)    compute_unsafe_element_mask
+     unsafe_node  (Nnode) compute_unsafe_node_mask
+     overlap_lost (Ne)    compute_overlap_lost_element_mask(frac_threshold,
+                          min_material_frac)
+   each including the outer element shell (boundary_element_mask). */
+size_t vdvc_unsafe_masks_workspace_bytes(int Nx, int Ny, int Nz);
+int vdvc_unsafe_masks(const uint8_t* active, const uint8_t* mask0, int h,
+                      int Nx, int Ny, int Nz, double frac_threshold,
+                      double min_material_frac, uint8_t* unsafe_vox,
+                      uint8_t* unsafe_elem, uint8_t* unsafe_node,
+                      uint8_t* overlap_lost, void* ws, size_t ws_bytes,
+                      vdvc_stream_t stream);
+
 /* ---- reductions and pre-alignment ------------------------------------- */
 /* *out_host = sum a*b (b != NULL) or sum a, accumulated in float64;
    synchronises the stream (the xp.dot / .sum() calls of the lambda

@@ -423,6 +423,146 @@ def compute_crop(f, g, h, glt=0.0):
     return lo_out, hi_out
 
 
+# ----------------------------------------------------------------------------
+# per-element output fields (write_output.py:256-491) and diagnostic masks
+# (kernels_dvc.py:92-341); element arrays x-fastest unless stated
+# ----------------------------------------------------------------------------
+
+def _elem_blocks(h, Nx, Ny, Nz):
+    """(Ne, (h+1)^3) flat voxel indices of every element's block."""
+    return elem_voxel_origins(np.arange(Nx * Ny * Nz), h, Nx, Ny)[:, None] + voxel_offsets(h, Nx, Ny)[None, :]
+
+
+def _x_flat(a):
+    a = np.asarray(a)
+    return a.reshape(-1, order='F') if a.ndim == 3 else a.reshape(-1)
+
+
+def _to_cells(a, Nx, Ny, Nz):
+    return np.asarray(a).reshape(Nx, Ny, Nz, order='F')
+
+
+def _corner_nodes(Nx, Ny, Nz):
+    e = np.arange(Nx * Ny * Nz)
+    n0 = e % Nx + ((e // Nx) % Ny) * (Nx + 1) + (e // (Nx * Ny)) * (Nx + 1) * (Ny + 1)
+    off = CORNER[:, 0] + CORNER[:, 1] * (Nx + 1) + CORNER[:, 2] * (Nx + 1) * (Ny + 1)
+    return n0[:, None] + off[None, :]
+
+
+def principal_strains_cell(U_grid, h):
+    """write_output.py:256-281: eigenvalues (descending) of the symmetric
+    displacement gradient at each centroid, corner weights +-1/(4h)."""
+    Nx, Ny, Nz = (n - 1 for n in U_grid.shape[:3])
+    sgn = 2.0 * CORNER - 1.0                                   # (8, 3)
+    g = np.zeros((Nx, Ny, Nz, 3, 3))
+    for a, (dx, dy, dz) in enumerate(CORNER):
+        ua = U_grid[dx:dx + Nx, dy:dy + Ny, dz:dz + Nz, :]      # (..., 3) component c
+        g += ua[..., :, None] * (sgn[a] * 0.25 / h)[None, None, None, None, :]
+    eps = 0.5 * (g + np.swapaxes(g, -1, -2))
+    return np.linalg.eigvalsh(eps)[..., ::-1]
+
+
+def equivalent_strain(ps):
+    """write_output.py:284-310."""
+    e1, e2, e3 = ps[..., 0], ps[..., 1], ps[..., 2]
+    return np.sqrt(2.0) / 3.0 * np.sqrt((e1 - e2) ** 2 + (e2 - e3) ** 2 + (e3 - e1) ** 2)
+
+
+def material_cell_mask(ref, h, Nx, Ny, Nz, glt=0.0):
+    """write_output.py:313-338: block mean of ref > glt (float64 mean)."""
+    r = _x_flat(ref).astype(np.float64)
+    return _to_cells(r[_elem_blocks(h, Nx, Ny, Nz)].mean(axis=1) > glt, Nx, Ny, Nz)
+
+
+def material_cell_mask_eroded(m):
+    """write_output.py:341-355: 26-neighbour erosion, border counts as set."""
+    p = np.pad(np.asarray(m, bool), 1, constant_values=True)
+    out = np.ones(m.shape, bool)
+    for di in range(3):
+        for dj in range(3):
+            for dk in range(3):
+                out &= p[di:di + m.shape[0], dj:dj + m.shape[1], dk:dk + m.shape[2]]
+    return out
+
+
+def safe_cell_mask(unsafe_vox, h, Nx, Ny, Nz):
+    """write_output.py:358-381: no unsafe voxel in the block."""
+    u = _x_flat(unsafe_vox).astype(bool)
+    return _to_cells(~u[_elem_blocks(h, Nx, Ny, Nz)].any(axis=1), Nx, Ny, Nz)
+
+
+def correlation_quality_cell(res, ref, h, Nx, Ny, Nz, min_active=8):
+    """write_output.py:384-452: per-block population std of res and ZNCC of
+    ref and ref - res over the active (res != 0) voxels."""
+    B = _elem_blocks(h, Nx, Ny, Nz)
+    std = np.full(len(B), np.nan)
+    zn = np.full(len(B), np.nan)
+    r_all = _x_flat(res).astype(np.float64)
+    f_all = _x_flat(ref).astype(np.float64)
+    for e, vox in enumerate(B):
+        r = r_all[vox]
+        act = r != 0.0
+        n = int(act.sum())
+        if n < min_active:
+            continue
+        r, f = r[act], f_all[vox][act]
+        std[e] = np.sqrt(max(np.mean(r * r) - np.mean(r) ** 2, 0.0))
+        fc, gc = f - f.mean(), (f - r) - (f - r).mean()
+        den = np.sqrt(np.sum(fc * fc) * np.sum(gc * gc))
+        if den > 0.0:
+            zn[e] = np.sum(fc * gc) / den
+    return _to_cells(std, Nx, Ny, Nz), _to_cells(zn, Nx, Ny, Nz)
+
+
+def gn_convergence_cell(dU, U, Nx, Ny, Nz):
+    """write_output.py:455-491: corner-DOF norm ratio, NaN where ||U|| = 0."""
+    cn = _corner_nodes(Nx, Ny, Nz)
+    d = np.asarray(dU, np.float64).reshape(-1, 3)[cn]
+    u = np.asarray(U, np.float64).reshape(-1, 3)[cn]
+    num = np.sqrt((d * d).sum(axis=(1, 2)))
+    den = np.sqrt((u * u).sum(axis=(1, 2)))
+    out = np.full(num.shape, np.nan)
+    ok = den > 0.0
+    out[ok] = num[ok] / den[ok]
+    return _to_cells(out, Nx, Ny, Nz)
+
+
+def boundary_elements(Nx, Ny, Nz):
+    """kernels_dvc.py:92-116: the outer element shell, x-fastest."""
+    e = np.arange(Nx * Ny * Nz)
+    i, j, k = e % Nx, (e // Nx) % Ny, e // (Nx * Ny)
+    return (i == 0) | (j == 0) | (k == 0) | (i == Nx - 1) | (j == Ny - 1) | (k == Nz - 1)
+
+
+def unsafe_masks(active_vox, h, Nx, Ny, Nz, mask0_vox=None, frac_threshold=0.0, min_material_frac=0.5):
+    """kernels_dvc.py:119-341 -> dict of unsafe_vox, unsafe_elem,
+    unsafe_node and (with mask0_vox) overlap_lost."""
+    act = np.asarray(active_vox, bool)
+    B = _elem_blocks(h, Nx, Ny, Nz)
+    cn = _corner_nodes(Nx, Ny, Nz)
+    Nn = (Nx + 1) * (Ny + 1) * (Nz + 1)
+    bnd = boundary_elements(Nx, Ny, Nz)
+    node_pre = np.zeros(Nn, bool)
+    node_pre[cn[(~act)[B].any(axis=1)].ravel()] = True
+    elem = node_pre[cn].any(axis=1) | bnd
+    node = node_pre.copy()
+    node[cn[bnd].ravel()] = True
+    vox = np.zeros(act.shape[0], bool)
+    vox[B[elem].ravel()] = True
+    out = dict(unsafe_vox=vox, unsafe_elem=elem, unsafe_node=node)
+    if mask0_vox is not None:
+        m0 = np.asarray(mask0_vox, bool)
+        n_mat = m0[B].sum(axis=1)
+        n_lost = (m0 & ~act)[B].sum(axis=1)
+        lost = np.zeros(len(B), bool)
+        has = n_mat > 0
+        lost[has] = n_lost[has] / n_mat[has] > frac_threshold
+        node_lost = np.zeros(Nn, bool)
+        node_lost[cn[lost].ravel()] = True
+        out["overlap_lost"] = node_lost[cn].any(axis=1) | (n_mat / B.shape[1] < min_material_frac) | bnd
+    return out
+
+
 def sample_deformed(U, g_pix, h, Nx, Ny, Nz, g_origin=(0, 0, 0), mask0=None, glt=0.0):
     """correlate_gpu.py:201-281: g at (u + x) - g_origin, clipped, order-1
     map_coordinates; mask in_bounds & mask0 & g > glt."""

@@ -273,7 +273,79 @@ def prep_cases():
                         lo2=lo2, hi2=hi2)
 
 
+def cells_cases():
+    """Per-element output fields (engine/write_output.py:256-491) and the
+    diagnostic masks (engine/kernels_dvc.py:92-341), from the reference
+    functions, on two meshes."""
+    from voxeldvc.engine import write_output as W
+    rng = np.random.default_rng(53)
+    d = {}
+    for tag, (Nx, Ny, Nz, h) in (("a", (7, 6, 5, 3)), ("b", (6, 8, 7, 2)), ("c", (10, 11, 9, 1))):
+        shape = (Nx * h + 1, Ny * h + 1, Nz * h + 1)
+        Nn = (Nx + 1) * (Ny + 1) * (Nz + 1)
+        U = rng.standard_normal(3 * Nn) * 0.3
+        U_grid = np.stack([U[c::3].reshape(Nx + 1, Ny + 1, Nz + 1, order="F") for c in range(3)], axis=-1)
+        ref = (_texture(shape, rng) * 40 + 60).astype(np.float32)
+        ref[: h + 2, : h + 1] = 0.0                      # a void corner: non-material cells
+        ref[-h - 1:, :, -h - 1:] = 80.0                  # a flat slab: zero-variance cells
+        glt = 30.0
+        active = ref > glt
+        active[:, -(h // 2 + 1):, :] = False             # lost overlap along one face
+        for _ in range(3):                               # isolated dropouts
+            active[tuple(rng.integers(h, n - h) for n in shape)] = False
+        res = np.where(active, rng.standard_normal(shape) * 3.0, 0.0)
+        res[-h - 1:, :, -h - 1:] = np.where(active[-h - 1:, :, -h - 1:], 1.5, 0.0)
+        res_flat = res.reshape(-1, order="F")
+        active_flat = res_flat != 0
+        mask0_flat = ref.reshape(-1, order="F") > glt
+        unsafe = KD.compute_unsafe_voxel_mask(active_flat, h, Nx, Ny, Nz)
+        dU = rng.standard_normal(3 * Nn) * 1e-3
+        U0 = U.copy()
+        for n in (0, 1, Nx + 1, Nx + 2, (Nx + 1) * (Ny + 1), (Nx + 1) * (Ny + 1) + 1,
+                  (Nx + 1) * (Ny + 1) + Nx + 1, (Nx + 1) * (Ny + 1) + Nx + 2):
+            U0[3 * n:3 * n + 3] = 0.0                    # element 0's corners: ||U|| = 0
+        ps = W.compute_principal_strains_cell(U_grid, h)
+        mat = W.compute_material_cell_mask(ref, h, Nx, Ny, Nz, glt=glt)
+        # no cell mean within rounding of the threshold (float32 vs float64 sums)
+        from voxeldvc.engine.kernels_dvc import get_voxel_offsets, get_elem_voxel_origins
+        vox = get_elem_voxel_origins(np.arange(Nx * Ny * Nz), h, Nx, Ny, np)[:, None] + \
+            get_voxel_offsets(h, Nx, Ny, np)[None, :]
+        means = ref.reshape(-1, order="F").astype(np.float64)[vox].mean(axis=1)
+        assert np.min(np.abs(means - glt)) > 1e-3 and np.min(np.abs(means - 70.0)) > 1e-3
+        rstd, zn = W.compute_correlation_quality_cell(res_flat, ref, h, Nx, Ny, Nz)
+        d.update({
+            f"{tag}_dims": np.array([Nx, Ny, Nz, h]), f"{tag}_U": U, f"{tag}_U_grid": U_grid, f"{tag}_ref": ref,
+            f"{tag}_glt": np.float64(glt), f"{tag}_res": res_flat, f"{tag}_mask0": mask0_flat,
+            f"{tag}_dU": dU, f"{tag}_U0": U0,
+            f"{tag}_principal": ps, f"{tag}_equivalent": W.compute_equivalent_strain(ps),
+            f"{tag}_material": mat,
+            f"{tag}_material70": W.compute_material_cell_mask(ref, h, Nx, Ny, Nz, glt=70.0), f"{tag}_material_eroded": W.compute_material_cell_mask_eroded(mat),
+            f"{tag}_unsafe_vox": unsafe, f"{tag}_safe": W.compute_safe_cell_mask(unsafe, h, Nx, Ny, Nz),
+            f"{tag}_unsafe_elem": KD.compute_unsafe_element_mask(active_flat, h, Nx, Ny, Nz),
+            f"{tag}_unsafe_node": KD.compute_unsafe_node_mask(active_flat, h, Nx, Ny, Nz),
+            f"{tag}_overlap_lost": KD.compute_overlap_lost_element_mask(active_flat, mask0_flat, h, Nx, Ny, Nz),
+            f"{tag}_overlap_lost_t": KD.compute_overlap_lost_element_mask(active_flat, mask0_flat, h, Nx, Ny, Nz,
+                                                                          frac_threshold=0.2,
+                                                                          min_material_frac=0.3),
+            f"{tag}_boundary": KD.boundary_element_mask(Nx, Ny, Nz),
+            f"{tag}_residual_std": rstd, f"{tag}_zncc": zn,
+            f"{tag}_gn": W.compute_gn_convergence_cell(dU, U0, Nx, Ny, Nz),
+        })
+        # an eroded mask with holes (interior non-material cells)
+        holes = rng.random((Nx, Ny, Nz)) > 0.15
+        d[f"{tag}_holes"] = holes
+        d[f"{tag}_holes_eroded"] = W.compute_material_cell_mask_eroded(holes)
+    ps3 = rng.standard_normal((7, 5, 3))
+    d.update(ps3=ps3, eq3=W.compute_equivalent_strain(ps3))
+    np.savez_compressed(os.path.join(OUT, "cells.npz"), **d)
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 1:  # regenerate only the named case groups
+        for name in sys.argv[1:]:
+            globals()[name]()
+        sys.exit(0)
+    cells_cases()
     prep_cases()
     post_cases()
     affine_cases()

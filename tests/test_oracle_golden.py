@@ -160,3 +160,37 @@ def test_preprocess_oracle():
     assert np.array_equal(O.warp_onto_ref_grid(np.eye(3), np.zeros(3), np.full(3, 7.0), g.shape, g), g)
     w = O.warp_onto_ref_grid(np.eye(3), np.array([2.0, 0.0, -1.0]), np.zeros(3), g.shape, g)
     assert np.array_equal(w[:-2, :, 1:], g[2:, :, :-1]) and np.all(w[-2:] == 0) and np.all(w[:, :, 0] == 0)
+
+
+def _close_nan(a, b, tol):
+    a, b = np.asarray(a), np.asarray(b)
+    return a.shape == b.shape and np.array_equal(np.isnan(a), np.isnan(b)) and \
+        np.allclose(np.nan_to_num(a), np.nan_to_num(b), rtol=tol, atol=tol)
+
+
+@pytest.mark.parametrize("tag", ["a", "b", "c"])
+def test_cell_fields_oracle(tag):
+    """Per-element strain / quality fields and the diagnostic masks against
+    the reference's own outputs (tests/golden/cells.npz)."""
+    c = load_golden("cells.npz")
+    Nx, Ny, Nz, h = (int(x) for x in c[f"{tag}_dims"])
+    g = lambda k: c[f"{tag}_{k}"]  # noqa: E731
+    ps = O.principal_strains_cell(g("U_grid"), h)
+    assert _close_nan(ps, g("principal"), 1e-13)
+    assert _close_nan(O.equivalent_strain(ps), g("equivalent"), 1e-13)
+    assert np.array_equal(O.material_cell_mask(g("ref"), h, Nx, Ny, Nz, glt=float(g("glt"))), g("material"))
+    assert np.array_equal(O.material_cell_mask(g("ref"), h, Nx, Ny, Nz, glt=70.0), g("material70"))
+    assert np.array_equal(O.material_cell_mask_eroded(g("material")), g("material_eroded"))
+    assert np.array_equal(O.material_cell_mask_eroded(g("holes")), g("holes_eroded"))
+    assert np.array_equal(O.safe_cell_mask(g("unsafe_vox"), h, Nx, Ny, Nz), g("safe"))
+    std, zn = O.correlation_quality_cell(g("res"), g("ref"), h, Nx, Ny, Nz)
+    assert _close_nan(std, g("residual_std"), 1e-12) and _close_nan(zn, g("zncc"), 1e-12)
+    assert _close_nan(O.gn_convergence_cell(g("dU"), g("U0"), Nx, Ny, Nz), g("gn"), 1e-13)
+    active = g("res") != 0
+    m = O.unsafe_masks(active, h, Nx, Ny, Nz, g("mask0"))
+    for k in ("unsafe_vox", "unsafe_elem", "unsafe_node", "overlap_lost"):
+        assert np.array_equal(m[k], g(k)), k
+    m = O.unsafe_masks(active, h, Nx, Ny, Nz, g("mask0"), frac_threshold=0.2, min_material_frac=0.3)
+    assert np.array_equal(m["overlap_lost"], g("overlap_lost_t"))
+    assert np.array_equal(O.boundary_elements(Nx, Ny, Nz), g("boundary"))
+    assert np.allclose(O.equivalent_strain(c["ps3"]), c["eq3"], rtol=1e-14, atol=0)

@@ -53,3 +53,16 @@ def test_run_writes_the_solve(tmp_path, cuda):
     pushed = np.load(tmp_path / "ref_forward_pushed.npy")
     assert np.allclose(pushed, O.push_field_forward(f.astype(np.float64), U, 4, 3, 2, 8), atol=1e-9)
     assert "ZNCC (active voxels):" in log
+    # element-scale fields: strains against the oracle, masks of the right shape
+    ps = np.load(tmp_path / "principal_strains_cell.npy")
+    assert np.allclose(ps, O.principal_strains_cell(grid, 8), rtol=0, atol=1e-14)
+    assert np.allclose(np.load(tmp_path / "equivalent_strain_cell.npy"), O.equivalent_strain(ps), rtol=1e-13)
+    res = np.load(tmp_path / "residual.npy").reshape(-1, order='F')
+    std, zn = O.correlation_quality_cell(res, f, 8, 4, 3, 2)
+    assert np.allclose(np.load(tmp_path / "zncc_cell.npy"), zn, rtol=1e-12, equal_nan=True)
+    assert np.allclose(np.load(tmp_path / "residual_std_cell.npy"), std, rtol=1e-12, equal_nan=True)
+    for name in ("material_cell_mask", "material_cell_mask_eroded", "overlap_lost_element_mask"):
+        m = np.load(tmp_path / f"{name}.npy")
+        assert m.shape == (4, 3, 2) and m.dtype == bool, name
+    assert np.load(tmp_path / "unsafe_voxel_mask.npy").shape == f.shape
+    assert "cell eq. strain:" in log and "Material cells" in log

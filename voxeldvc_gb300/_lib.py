@@ -68,6 +68,13 @@ SIGNATURES = {
     "vdvc_warp_affine": (ci, [vp, ci, ci, ci, pd, pd, pd, ci, ci, ci, vp, vp]),
     "vdvc_bin_volume": (ci, [vp, ci, ci, ci, ci, ci, vp, vp]),
     "vdvc_overlap_projections": (ci, [vp, vp, ci, ci, ci, cd, vp, vp, vp, vp]),
+    "vdvc_cell_strains": (ci, [vp, ci, ci, ci, ci, vp, vp, vp]),
+    "vdvc_equivalent_strain": (ci, [vp, C.c_longlong, vp, vp]),
+    "vdvc_cell_fields": (ci, [vp, ci, vp, vp, ci, ci, ci, ci, cd, vp, vp, vp, vp, vp]),
+    "vdvc_cell_erode": (ci, [vp, ci, ci, ci, vp, vp]),
+    "vdvc_cell_gn_convergence": (ci, [vp, vp, ci, ci, ci, vp, vp]),
+    "vdvc_unsafe_masks_workspace_bytes": (cz, [ci, ci, ci]),
+    "vdvc_unsafe_masks": (ci, [vp, vp, ci, ci, ci, ci, cd, cd, vp, vp, vp, vp, vp, cz, vp]),
     "vdvc_fft_rigid_shift": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, ci, pd, vp]),
     "vdvc_pcg_workspace_bytes": (cz, []),
     "vdvc_pcg_begin": (ci, [vp, vp, vp, ci, C.c_longlong, vp, vp, vp, ci, cd, vp, cz, vp]),

@@ -67,6 +67,66 @@ def get_elem_voxel_origins(elem_ids, h, Nx, Ny, xp):
     return _index_out(h * (i + j * Nvx + k * Nvx * Nvy), xp, elem_ids)
 
 
+# ---------------------------------------------------------------------------
+# Post-solve diagnostic masks (kernels_dvc.py:92-341), one GPU pass chain
+# (`vdvc_unsafe_masks`): element block flags -> node flags -> element flags
+# -> voxel flags.  Inputs are flat x-fastest voxel masks; outputs are host
+# bool arrays as in the reference (which runs these on the CPU).
+# ---------------------------------------------------------------------------
+
+def boundary_element_mask(Nx, Ny, Nz):
+    """(Nx*Ny*Nz,) bool, x-fastest element order: the outer element shell."""
+    i = np.arange(Nx)[None, None, :]
+    j = np.arange(Ny)[None, :, None]
+    k = np.arange(Nz)[:, None, None]
+    m = (i == 0) | (i == Nx - 1) | (j == 0) | (j == Ny - 1) | (k == 0) | (k == Nz - 1)
+    return np.broadcast_to(m, (Nz, Ny, Nx)).reshape(-1).copy()
+
+
+def _unsafe_masks(active_vox, h, Nx, Ny, Nz, mask0_vox=None, frac_threshold=0.0, min_material_frac=0.5,
+                  vox=False, elem=False, node=False, lost=False):
+    Nvox = (Nx * h + 1) * (Ny * h + 1) * (Nz * h + 1)
+    Ne, Nn = Nx * Ny * Nz, (Nx + 1) * (Ny + 1) * (Nz + 1)
+    a = D.mask_u8(active_vox).reshape(-1)
+    m0 = D.mask_u8(mask0_vox).reshape(-1) if mask0_vox is not None else None
+    if a.numel() != Nvox or (m0 is not None and m0.numel() != Nvox):
+        raise ValueError(f"voxel masks must have {Nvox} entries")
+    outs = [D.empty(n, np.uint8) if want else None for want, n in ((vox, Nvox), (elem, Ne), (node, Nn), (lost, Ne))]
+    nbytes = int(_lib.lib().vdvc_unsafe_masks_workspace_bytes(Nx, Ny, Nz))
+    ws = D.scratch.get(nbytes)
+    _lib.check(_lib.lib().vdvc_unsafe_masks(a.data_ptr(), D.ptr(m0), int(h), Nx, Ny, Nz, float(frac_threshold),
+                                            float(min_material_frac), *(D.ptr(o) for o in outs), ws.data_ptr(),
+                                            ws.numel(), D.stream()), "unsafe masks")
+    return [D.out(o.view(D.torch().bool), np) if o is not None else None for o in outs]
+
+
+def compute_unsafe_voxel_mask(active_vox, h, Nx, Ny, Nz):
+    """(Nvox,) bool: voxels of every element touching an unsafe node (a node
+    of an element holding an inactive voxel), plus the outer element shell."""
+    return _unsafe_masks(active_vox, h, Nx, Ny, Nz, vox=True)[0]
+
+
+def compute_unsafe_element_mask(active_vox, h, Nx, Ny, Nz):
+    """(Nx*Ny*Nz,) bool, x-fastest: elements touching an unsafe node, plus
+    the outer element shell."""
+    return _unsafe_masks(active_vox, h, Nx, Ny, Nz, elem=True)[1]
+
+
+def compute_unsafe_node_mask(active_vox, h, Nx, Ny, Nz):
+    """((Nx+1)*(Ny+1)*(Nz+1),) bool: nodes of elements holding an inactive
+    voxel, plus the nodes of the outer element shell."""
+    return _unsafe_masks(active_vox, h, Nx, Ny, Nz, node=True)[2]
+
+
+def compute_overlap_lost_element_mask(active_vox, mask0_vox, h, Nx, Ny, Nz, frac_threshold=0.0,
+                                      min_material_frac=0.5):
+    """(Nx*Ny*Nz,) bool, x-fastest: elements sharing a node with an element
+    whose lost material fraction exceeds frac_threshold, elements whose
+    material count fraction is below min_material_frac, and the outer
+    element shell."""
+    return _unsafe_masks(active_vox, h, Nx, Ny, Nz, mask0_vox, frac_threshold, min_material_frac, lost=True)[3]
+
+
 def auto_chunk_size(nq, max_tensor_elems=20_000_000):
     """Element-chunk size of the reference's chunked loops (kept for API
     compatibility; the kernels here do not chunk)."""

@@ -13,10 +13,15 @@ results:
   residual.npy         (Nvx, Nvy, Nvz) final residual
   dU.npy               (Nx+1, Ny+1, Nz+1, 3) last GN update
   ref_forward_pushed.npy  (Nvx, Nvy, Nvz) reference pushed onto the deformed grid
+  principal_strains_cell.npy (Nx, Ny, Nz, 3), equivalent_strain_cell.npy,
+  residual_std_cell.npy, zncc_cell.npy, gn_convergence_cell.npy,
+  material_cell_mask.npy, material_cell_mask_eroded.npy,
+  overlap_lost_element_mask.npy (Nx, Ny, Nz) per-element fields
+  unsafe_voxel_mask.npy (Nvx, Nvy, Nvz)
   run_log.txt          the run's printed output
 
-The derived post-processing fields of the reference's write_outputs (strain,
-quality and mask fields, VTK files) are a later stage and not written here.
+The reference's deformed-configuration remaps (scipy griddata) and VTK
+files are not written.
 """
 from __future__ import annotations
 
@@ -25,6 +30,7 @@ import json
 import os
 import sys
 import time
+import warnings
 
 import numpy as np
 
@@ -60,6 +66,47 @@ def mesh_dims(shape, h):
 def _grid(U, Nx, Ny, Nz):
     # node = i + j(Nx+1) + k(Nx+1)(Ny+1): Fortran order of (Nx+1, Ny+1, Nz+1)
     return np.stack([U[c::3].reshape(Nx + 1, Ny + 1, Nz + 1, order='F') for c in range(3)], axis=-1)
+
+
+def _cell_outputs(work, U, U_grid, dU, res, ref, active, Nx, Ny, Nz, h, glt):
+    """Element-scale fields of write_outputs (write_output.py:790-950) and
+    the diagnostic masks they gate with (kernels_dvc.py:92-341)."""
+    from .engine import write_output as W
+    from .engine import kernels_dvc as KD
+    Nv = ref.shape
+    mask0 = np.ravel(np.asarray(ref), order='F') > glt
+    unsafe = KD.compute_unsafe_voxel_mask(active, h, Nx, Ny, Nz)
+    safe = W.compute_safe_cell_mask(unsafe, h, Nx, Ny, Nz)
+    lost = KD.compute_overlap_lost_element_mask(active, mask0, h, Nx, Ny, Nz).reshape(Nx, Ny, Nz, order='F')
+    print(f"Unsafe voxels: {int(unsafe.sum())}/{unsafe.size} ({100 * unsafe.mean():.1f}%)")
+    print(f"Safe elements (no unsafe voxel): {int(safe.sum())}/{safe.size} ({100 * safe.mean():.1f}%)")
+    print(f"Overlap-lost elements (lost material overlap or <50% material): {int(lost.sum())}/{lost.size} "
+          f"({100 * lost.mean():.1f}%)")
+    ps = W.compute_principal_strains_cell(U_grid, h)
+    for c, name in enumerate(['e1 (max)', 'e2 (mid)', 'e3 (min)']):
+        comp = ps[..., c]
+        print(f"  cell {name}: mean={comp.mean():.5f}  std={comp.std():.5f}  min={comp.min():.5f}  "
+              f"max={comp.max():.5f}")
+    eq = W.compute_equivalent_strain(ps)
+    print(f"  cell eq. strain: mean={eq.mean():.5f}  std={eq.std():.5f}  min={eq.min():.5f}  max={eq.max():.5f}")
+    rstd, zn = W.compute_correlation_quality_cell(res, ref, h, Nx, Ny, Nz)
+    gn = W.compute_gn_convergence_cell(dU, U, Nx, Ny, Nz)
+    with warnings.catch_warnings():  # all-NaN fields print nan, as the reference's do
+        warnings.simplefilter('ignore', RuntimeWarning)
+        print(f"  cell residual std: mean={np.nanmean(rstd):.4f}  min={np.nanmin(rstd):.4f}  "
+              f"max={np.nanmax(rstd):.4f}")
+        print(f"  cell ZNCC: mean={np.nanmean(zn):.5f}  min={np.nanmin(zn):.5f}  max={np.nanmax(zn):.5f}")
+        print(f"  cell GN convergence dU/U: mean={np.nanmean(gn):.2e}  min={np.nanmin(gn):.2e}  "
+              f"max={np.nanmax(gn):.2e}")
+    mat = W.compute_material_cell_mask(ref, h, Nx, Ny, Nz, glt=glt)
+    mat_er = W.compute_material_cell_mask_eroded(mat)
+    print(f"Material cells (mean reference gray > glt): {int(mat.sum())}/{mat.size} ({100 * mat.mean():.1f}%)")
+    for name, arr in (('principal_strains_cell', ps), ('equivalent_strain_cell', eq), ('residual_std_cell', rstd),
+                      ('zncc_cell', zn), ('gn_convergence_cell', gn),
+                      ('unsafe_voxel_mask', unsafe.reshape(Nv, order='F')),
+                      ('overlap_lost_element_mask', lost), ('material_cell_mask', mat),
+                      ('material_cell_mask_eroded', mat_er)):
+        np.save(os.path.join(work, f'{name}.npy'), arr)
 
 
 def main(argv=None):
@@ -126,6 +173,7 @@ def main(argv=None):
         f_flat = np.ravel(np.asarray(ref, dtype=np.float64), order='F')
         zncc = compute_zncc(f_flat, f_flat - res, active)
         print(f"  ZNCC (active voxels): {zncc:.6f}")
+        _cell_outputs(work, U, U_grid, dU, res, ref, active, Nx, Ny, Nz, h, glt)
         for ci, name in enumerate(['ux', 'uy', 'uz']):
             comp = U_grid[..., ci]
             print(f"  {name}: mean={comp.mean():.4f}  std={comp.std():.4f}  min={comp.min():.4f}  max={comp.max():.4f}")
