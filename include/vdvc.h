@@ -222,6 +222,11 @@ int vdvc_push_field(const void* field, int dtype, const double* u_cf, int nx,
                     int ny, int nz, int order, int mode, double cval,
                     void* out, vdvc_stream_t stream);
 
+/* float64 -> dtype (VDVC_F32, VDVC_U8, VDVC_U16, VDVC_I16, VDVC_I32) with
+   scipy.ndimage's output conversion for integer fields: round half away from
+   zero, saturate (the integer-field case of push_field_forward). */
+int vdvc_cast_round(const double* in, long long n, int dtype, void* out,
+                    vdvc_stream_t stream);
 /* *out_host = zero-normalised cross-correlation of f and g over mask
    (compute_zncc, engine/write_output.py:658-690): float64 sums in two
    passes (means, then centred products); NaN for an empty mask or a zero
@@ -316,6 +321,28 @@ int vdvc_unsafe_masks(const uint8_t* active, const uint8_t* mask0, int h,
                       uint8_t* unsafe_elem, uint8_t* unsafe_node,
                       uint8_t* overlap_lost, void* ws, size_t ws_bytes,
                       vdvc_stream_t stream);
+
+/* ---- known-answer (ground-truth) harness --------------------------------
+   ground_truth/prepare_ground_truth.py and analyse_ground_truth.py.
+   Volumes are pix[x, y, z] C-order arrays, displacements (nx, ny, nz, 3)
+   channels-last, float64. */
+/* deformed(x) = ref(x - u(x)) by scipy RegularGridInterpolator (linear,
+   linear extrapolation past the edges) (make_deformed_image,
+   prepare_ground_truth.py:66-89); bit-identical to it. */
+int vdvc_gt_warp(const double* ref, const double* u_vox, int nx, int ny,
+                 int nz, double* out, vdvc_stream_t stream);
+/* out = x + u(x) inside [0, g-1] on every axis (voxel_in_bounds,
+   analyse_ground_truth.py:113-136), uint8. */
+int vdvc_gt_voxel_in_bounds(const double* u_vox, int nx, int ny, int nz,
+                            int gx, int gy, int gz, uint8_t* out,
+                            vdvc_stream_t stream);
+/* Per node (nbx, nby, nbz, C order) 1 - mean of in_bounds over the support
+   box [v-h, v+h] clamped to the image, v = crop_lo + (i, j, k) h
+   (node_oob_fraction, :139-174).  crop_lo: host, 3 values. */
+int vdvc_gt_node_oob_fraction(const uint8_t* in_bounds, int nx, int ny,
+                              int nz, int h, int nbx, int nby, int nbz,
+                              const long long* crop_lo, double* out,
+                              vdvc_stream_t stream);
 
 /* ---- reductions and pre-alignment ------------------------------------- */
 /* *out_host = sum a*b (b != NULL) or sum a, accumulated in float64;

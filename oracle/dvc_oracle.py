@@ -563,6 +563,70 @@ def unsafe_masks(active_vox, h, Nx, Ny, Nz, mask0_vox=None, frac_threshold=0.0, 
     return out
 
 
+# ----------------------------------------------------------------------------
+# known-answer harness (ground_truth/prepare_ground_truth.py,
+# ground_truth/analyse_ground_truth.py)
+# ----------------------------------------------------------------------------
+
+def gt_warp(ref, u):
+    """prepare_ground_truth.py:66-89: ref(x - u(x)), trilinear with linear
+    extrapolation (RegularGridInterpolator(fill_value=None)): per axis the
+    cell i = clip(ceil(p) - 1, 0, n - 2), weights (1 - t, t), t = p - i;
+    corner terms summed lo-before-hi with the last axis fastest."""
+    ref = np.asarray(ref, np.float64)
+    dims = ref.shape
+    grids = np.meshgrid(*(np.arange(n, dtype=np.float64) for n in dims), indexing='ij')
+    lo, w = [], []
+    for a in range(3):
+        p = grids[a] - u[..., a]
+        i = np.clip(np.ceil(p) - 1.0, 0, dims[a] - 2).astype(np.int64)
+        t = p - i
+        lo.append(i)
+        w.append((1.0 - t, t))
+    acc = np.zeros(dims)
+    for b0 in (0, 1):
+        for b1 in (0, 1):
+            for b2 in (0, 1):
+                wt = (w[0][b0] * w[1][b1]) * w[2][b2]
+                acc = acc + ref[lo[0] + b0, lo[1] + b1, lo[2] + b2] * wt
+    return acc
+
+
+def gt_uniaxial(n, strain):
+    """prepare_ground_truth.py:92-107: u_x = strain x on the (n,)*3 grid."""
+    u = np.zeros((n, n, n, 3))
+    u[..., 0] = strain * np.arange(n, dtype=np.float64)[:, None, None]
+    return u
+
+
+def gt_voxel_in_bounds(u, g_shape):
+    """analyse_ground_truth.py:113-136: x + u(x) inside [0, g - 1]."""
+    ok = np.ones(u.shape[:3], bool)
+    for a in range(3):
+        c = np.arange(u.shape[a], dtype=np.float64).reshape([-1 if b == a else 1 for b in range(3)]) + u[..., a]
+        ok &= (c >= 0) & (c <= g_shape[a] - 1)
+    return ok
+
+
+def gt_node_oob_fraction(u, h, nb, g_shape, crop_lo):
+    """analyse_ground_truth.py:139-174 via a summed-volume table of the
+    in-bounds mask: 1 - (in-bounds count / voxel count) over each node's
+    clamped support box [v - h, v + h]."""
+    inb = gt_voxel_in_bounds(u, g_shape).astype(np.int64)
+    S = np.zeros(tuple(n + 1 for n in inb.shape), np.int64)
+    S[1:, 1:, 1:] = inb.cumsum(0).cumsum(1).cumsum(2)
+    ax = []
+    for a in range(3):
+        v = crop_lo[a] + np.arange(nb[a]) * h
+        ax.append((np.maximum(v - h, 0), np.minimum(v + h, inb.shape[a] - 1) + 1))
+    A0, A1, A2 = np.meshgrid(ax[0][0], ax[1][0], ax[2][0], indexing='ij')
+    B0, B1, B2 = np.meshgrid(ax[0][1], ax[1][1], ax[2][1], indexing='ij')
+    cnt = (S[B0, B1, B2] - S[A0, B1, B2] - S[B0, A1, B2] - S[B0, B1, A2]
+           + S[A0, A1, B2] + S[A0, B1, A2] + S[B0, A1, A2] - S[A0, A1, A2])
+    tot = (B0 - A0) * (B1 - A1) * (B2 - A2)
+    return 1.0 - cnt / tot
+
+
 def sample_deformed(U, g_pix, h, Nx, Ny, Nz, g_origin=(0, 0, 0), mask0=None, glt=0.0):
     """correlate_gpu.py:201-281: g at (u + x) - g_origin, clipped, order-1
     map_coordinates; mask in_bounds & mask0 & g > glt."""

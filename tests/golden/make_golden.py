@@ -240,6 +240,10 @@ def post_cases():
         d[f"{name}_o1_constant"] = W.push_field_forward(fld, U, Nx, Ny, Nz, h, order=1, mode="constant", cval=-1.0)
         d[f"{name}_o0_constant"] = W.push_field_forward(fld, U, Nx, Ny, Nz, h, order=0, mode="constant", cval=7.0)
     d["lab_o0_nearest"] = W.push_field_forward(lab, U, Nx, Ny, Nz, h, order=0, mode="nearest")
+    # integer intensity fields at order 1: the sampler's integer output rounding
+    d["u16"] = (f64 * 3000.0).astype(np.uint16)
+    d["u16_o1_nearest"] = W.push_field_forward(d["u16"], U, Nx, Ny, Nz, h, order=1, mode="nearest")
+    d["lab_o1_nearest"] = W.push_field_forward(lab * 40, U, Nx, Ny, Nz, h, order=1, mode="nearest")
     d["lab_o0_constant"] = W.push_field_forward(lab, U, Nx, Ny, Nz, h, order=0, mode="constant", cval=5)
     n = 5000
     zf = rng.random(n).astype(np.float32)
@@ -340,11 +344,108 @@ def cells_cases():
     np.savez_compressed(os.path.join(OUT, "cells.npz"), **d)
 
 
+def gt_cases():
+    """Ground-truth harness (ground_truth/prepare_ground_truth.py,
+    analyse_ground_truth.py): the backward warp with linear extrapolation,
+    the uniaxial field, voxel recoverability, node support fractions and
+    the grid -> DOF flattening, from the reference functions."""
+    from voxeldvc.ground_truth import prepare_ground_truth as PG
+    from voxeldvc.ground_truth import analyse_ground_truth as AG
+    rng = np.random.default_rng(61)
+    n = 17
+    ref = _texture((n, n, n), rng) * 1000.0
+    u = rng.standard_normal((n, n, n, 3)) * 1.5
+    u[:3] += 2.5                                   # samples past the low x edge: extrapolation
+    u[..., -2:, 2] -= 3.0                          # and past the high z edge
+    u[5, 6, 7] = 0.0                               # an exact grid point
+    u[8, 8, 8] = (0.5, -0.25, 1.0)                 # half-integers
+    deformed = PG.make_deformed_image(ref, u)
+    uni = PG.make_uniaxial_gt(9, 0.02)
+    g_shape = (15, 19, 14)
+    inb = AG.voxel_in_bounds(u, g_shape)
+    h, nb, crop_lo = 4, (3, 4, 3), np.array([1, 0, 2])
+    oob = AG.node_oob_fraction(u, h, *nb, g_shape, crop_lo)
+    U_grid = rng.standard_normal((4, 3, 5, 3))
+    np.savez_compressed(os.path.join(OUT, "gt.npz"), ref=ref, u=u, deformed=deformed, uni=uni,
+                        g_shape=np.array(g_shape), inb=inb, h=np.int64(h), nb=np.array(nb), crop_lo=crop_lo,
+                        oob=oob, U_grid=U_grid, dofs=AG.grid_to_dofs(U_grid))
+
+
+def gt_pipeline_case(kind="z+0.01"):
+    """The known-answer pipeline run through the reference's own CPU code
+    on the seeded stand-in dataset (voxeldvc_gb300.synth.gt_stand_in):
+    prepare (make_deformed_image), preprocess (affine_prealign,
+    affine_refine_gn, compute_crop; the crop's warp onto the reference grid
+    uses the oracle's restatement, the reference's needs CuPy), run
+    (multiscale_correlate_gpu with NumPy, ext_affine seed), and the
+    analysis (node / voxel errors over the recoverable and valid sets)."""
+    import hashlib
+    import types
+    for name in ("cupy", "tifffile"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(OUT)))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(OUT))))
+    from voxeldvc_gb300.synth import gt_stand_in
+    from oracle import dvc_oracle as O
+    from voxeldvc import preprocess as P
+    from voxeldvc.ground_truth import prepare_ground_truth as PG
+    from voxeldvc.ground_truth import analyse_ground_truth as AG
+    from voxeldvc.engine import write_output as W
+    ref, U_in = gt_stand_in(kind)
+    digest = hashlib.sha256(ref.tobytes() + U_in.tobytes()).hexdigest()
+    n = ref.shape[0]
+    u_vox = U_in.astype(np.float64)[:n, :n, :n]
+    deformed = PG.make_deformed_image(ref.astype(np.float64), u_vox)
+    h, glt, l0 = 8, 0.0, 4.5 * 8
+    f_pix, g_pix = ref.astype(np.float32), deformed.astype(np.float32)
+    A, t, c, info = CG.affine_prealign(f_pix, g_pix, np, decimate=4)
+    A, t, rinfo = CG.affine_refine_gn(f_pix, g_pix, np, A, t, c)
+    g_warped = O.warp_onto_ref_grid(A, t, c, ref.shape, g_pix)
+    lo, hi = P.compute_crop(ref, g_warped, h, glt)
+    corners = np.array([[lo[0] + dx * (hi[0] - lo[0] - 1), lo[1] + dy * (hi[1] - lo[1] - 1),
+                         lo[2] + dz * (hi[2] - lo[2] - 1)] for dx in (0, 1) for dy in (0, 1) for dz in (0, 1)],
+                       dtype=np.float64)
+    cd = (corners - c) @ A.T + c + t
+    lo_def = np.maximum(np.floor(cd.min(axis=0)).astype(int) - 1, 0)
+    hi_def = np.minimum(np.ceil(cd.max(axis=0)).astype(int) + 2, np.array(deformed.shape))
+    ref_c = ref[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]]
+    def_c = deformed[lo_def[0]:hi_def[0], lo_def[1]:hi_def[1], lo_def[2]:hi_def[2]]
+    Nx, Ny, Nz = ((s - 1) // h for s in ref_c.shape)
+    U, res, dU = CG.multiscale_correlate_gpu(ref_c, def_c, Nx, Ny, Nz, h, xp=np, scales=(2, 1, 0), l0=l0, glt=glt,
+                                             K_ref_laplacian=G.build_K_ref_laplacian(), dynamic_mask=True,
+                                             fft_prealign=False, prealign_affine=False,
+                                             ext_affine=(A, t + lo - lo_def, c - lo), disp=False,
+                                             freeze_mask_after=4)
+    nb = (Nx + 1, Ny + 1, Nz + 1)
+    U_grid = np.stack([U[k::3].reshape(nb, order="F") for k in range(3)], axis=-1) + lo_def - lo
+    u_nodes = u_vox[np.ix_(*(lo[a] + np.arange(nb[a]) * h for a in range(3)))]
+    err = U_grid - u_nodes
+    oob = AG.node_oob_fraction(u_vox, h, *nb, deformed.shape, lo)
+    rec = oob <= 0
+    active = CG.compute_active_mask(U + np.tile(lo_def, len(U) // 3), def_c, Nx, Ny, Nz, h, np,
+                                    g_origin=tuple(int(x) for x in lo_def), mask0_vox=ref_c.reshape(-1, order="F") > glt,
+                                    glt=glt)
+    active = np.asarray(active)
+    lost = KD.compute_overlap_lost_element_mask(active, ref_c.reshape(-1, order="F") > glt, h, Nx, Ny, Nz)
+    node_idx = G.build_node_index(Nx, Ny, Nz)
+    en = G.element_node_ids(node_idx, Nx, Ny, Nz)
+    nm = np.zeros(node_idx.size, bool)
+    nm[en[lost].ravel()] = True
+    valid = rec & ~nm[node_idx]
+    rms = lambda m: float(np.sqrt(np.mean(err[m] ** 2)))  # noqa: E731
+    np.savez_compressed(os.path.join(OUT, f"gt_pipeline_{kind}.npz"), digest=np.array(digest), A=A, t=t, c=c,
+                        lo=lo, hi=hi, lo_def=lo_def, hi_def=hi_def, U_grid=U_grid, err=err, rec=rec,
+                        valid=valid, rms_rec=rms(rec), rms_valid=rms(valid), rms_all=rms(np.ones_like(rec)))
+    print(kind, "recoverable RMS", rms(rec), "valid RMS", rms(valid), "nodes", rec.sum(), valid.sum())
+    del W
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1:  # regenerate only the named case groups
         for name in sys.argv[1:]:
             globals()[name]()
         sys.exit(0)
+    gt_cases()
     cells_cases()
     prep_cases()
     post_cases()

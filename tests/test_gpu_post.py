@@ -50,6 +50,17 @@ def test_push_label_field_and_reference_alias(W):
         W.push_field_forward(c["f64"], c["U"], Nx, Ny, Nz, h, mode="wrap")
 
 
+def test_push_integer_fields_round_like_the_sampler(W):
+    """Order-1 pushes of integer fields round half away from zero, as the
+    reference's sampler converts to an integer output."""
+    c = load_golden("post.npz")
+    Nx, Ny, Nz, h = (int(x) for x in c["dims"])
+    out = W.push_field_forward(c["u16"], c["U"], Nx, Ny, Nz, h, order=1)
+    assert out.dtype == np.uint16 and np.array_equal(out, c["u16_o1_nearest"])
+    out = W.push_field_forward(c["lab"] * 40, c["U"], Nx, Ny, Nz, h, order=1)
+    assert out.dtype == np.uint8 and np.array_equal(out, c["lab_o1_nearest"])
+
+
 def test_compute_zncc(W):
     c = load_golden("post.npz")
     assert W.compute_zncc(c["zf"], c["zg"], c["zm"]) == pytest.approx(float(c["zncc"]), abs=1e-13)

@@ -140,6 +140,8 @@ def test_post_stages_oracle():
             assert out.dtype == ref.dtype and np.array_equal(out, ref), (name, key)
     for key, kw in (("o0_nearest", dict(order=0, mode="nearest")), ("o0_constant", dict(order=0, mode="constant", cval=5))):
         assert np.array_equal(O.push_field_forward(c["lab"], c["U"], Nx, Ny, Nz, h, **kw), c[f"lab_{key}"])
+    assert np.array_equal(O.push_field_forward(c["u16"], c["U"], Nx, Ny, Nz, h), c["u16_o1_nearest"])
+    assert np.array_equal(O.push_field_forward(c["lab"] * 40, c["U"], Nx, Ny, Nz, h), c["lab_o1_nearest"])
     assert O.zncc(c["zf"], c["zg"], c["zm"]) == pytest.approx(float(c["zncc"]), abs=1e-15)
     assert np.isnan(O.zncc(c["zf"], c["zg"], np.zeros_like(c["zm"])))
 
@@ -194,3 +196,15 @@ def test_cell_fields_oracle(tag):
     assert np.array_equal(m["overlap_lost"], g("overlap_lost_t"))
     assert np.array_equal(O.boundary_elements(Nx, Ny, Nz), g("boundary"))
     assert np.allclose(O.equivalent_strain(c["ps3"]), c["eq3"], rtol=1e-14, atol=0)
+
+
+def test_ground_truth_harness_oracle():
+    """Known-answer harness restatements against the reference's own
+    outputs (tests/golden/gt.npz)."""
+    c = load_golden("gt.npz")
+    assert np.array_equal(O.gt_warp(c["ref"], c["u"]), c["deformed"])
+    assert np.array_equal(O.gt_uniaxial(9, 0.02), c["uni"])
+    gs = tuple(int(x) for x in c["g_shape"])
+    assert np.array_equal(O.gt_voxel_in_bounds(c["u"], gs), c["inb"])
+    oob = O.gt_node_oob_fraction(c["u"], int(c["h"]), tuple(int(x) for x in c["nb"]), gs, c["crop_lo"])
+    assert np.allclose(oob, c["oob"], rtol=0, atol=1e-15)

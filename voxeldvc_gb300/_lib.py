@@ -65,6 +65,7 @@ SIGNATURES = {
     "vdvc_dot": (ci, [vp, vp, ci, C.c_longlong, pd, vp, cz, vp]),
     "vdvc_push_field": (ci, [vp, ci, vp, ci, ci, ci, ci, ci, cd, vp, vp]),
     "vdvc_zncc": (ci, [vp, vp, ci, vp, C.c_longlong, pd, vp, cz, vp]),
+    "vdvc_cast_round": (ci, [vp, C.c_longlong, ci, vp, vp]),
     "vdvc_warp_affine": (ci, [vp, ci, ci, ci, pd, pd, pd, ci, ci, ci, vp, vp]),
     "vdvc_bin_volume": (ci, [vp, ci, ci, ci, ci, ci, vp, vp]),
     "vdvc_overlap_projections": (ci, [vp, vp, ci, ci, ci, cd, vp, vp, vp, vp]),
@@ -74,6 +75,9 @@ SIGNATURES = {
     "vdvc_cell_erode": (ci, [vp, ci, ci, ci, vp, vp]),
     "vdvc_cell_gn_convergence": (ci, [vp, vp, ci, ci, ci, vp, vp]),
     "vdvc_unsafe_masks_workspace_bytes": (cz, [ci, ci, ci]),
+    "vdvc_gt_warp": (ci, [vp, vp, ci, ci, ci, vp, vp]),
+    "vdvc_gt_voxel_in_bounds": (ci, [vp, ci, ci, ci, ci, ci, ci, vp, vp]),
+    "vdvc_gt_node_oob_fraction": (ci, [vp, ci, ci, ci, ci, ci, ci, ci, C.POINTER(C.c_longlong), vp, vp]),
     "vdvc_unsafe_masks": (ci, [vp, vp, ci, ci, ci, ci, cd, cd, vp, vp, vp, vp, vp, cz, vp]),
     "vdvc_fft_rigid_shift": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, ci, pd, vp]),
     "vdvc_pcg_workspace_bytes": (cz, []),

@@ -1,15 +1,22 @@
-"""Command-line entry: `python -m voxeldvc_gb300.cli run WORK_DIR [--l0-factor F]`.
+"""Command-line entry: `python -m voxeldvc_gb300.cli COMMAND ...`.
 
-Mirrors the `run` subcommand of the reference's `voxeldvc` dispatcher
-(src/voxeldvc/cli.py); the other reference subcommands (preprocess glue,
-viewers, ground-truth tools) are not part of this package.
+Mirrors the reference's `voxeldvc` dispatcher (src/voxeldvc/cli.py) for the
+solve pipeline: preprocess, run, and the ground-truth accuracy check with
+its stages.  The viewers (napari), VTK export and format converters are not
+part of this package.
 """
 import argparse
 import importlib
 import sys
 
 _SUBCOMMANDS = {
+    "preprocess": ("voxeldvc_gb300.preprocess", "affine pre-alignment + overlap crop"),
     "run": ("voxeldvc_gb300.run_dvc", "multiscale Gauss-Newton DVC solve"),
+    "ground-truth": ("voxeldvc_gb300.run_ground_truth_pipeline", "4-stage known-ground-truth accuracy check"),
+    "prepare-ground-truth": ("voxeldvc_gb300.ground_truth.prepare_ground_truth",
+                             "generate ground-truth reference/deformed image pair"),
+    "analyse-ground-truth": ("voxeldvc_gb300.ground_truth.analyse_ground_truth",
+                             "compare recovered vs. ground-truth displacement"),
 }
 
 

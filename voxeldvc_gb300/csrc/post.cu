@@ -85,6 +85,21 @@ __global__ void __launch_bounds__(256) k_zncc(const T* __restrict__ f, const T* 
     for (int q = 0; q < 3; ++q) out3[q] = o3[q];
 }
 
+// float64 -> integer field with scipy.ndimage's output rounding (half away
+// from zero) and saturation to the type's range; float32 by round-to-nearest
+template <typename T>
+__global__ void k_cast_round(const double* __restrict__ in, long long n, double lo, double hi, T* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double r = round(in[i]);
+    out[i] = (T)fmin(fmax(r, lo), hi);
+  }
+}
+
+__global__ void k_cast_f32(const double* __restrict__ in, long long n, float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
 }  // namespace vdvc
 
 using namespace vdvc;
@@ -110,6 +125,25 @@ int vdvc_push_field(const void* field, int dtype, const double* u_cf, int nx, in
                                        cval, (uint8_t*)out);
   else
     return set_error(VDVC_ERR_ARG, "dtype %d", dtype);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_cast_round(const double* in, long long n, int dtype, void* out, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(in && out && n >= 0, "bad arguments");
+  if (n == 0) return VDVC_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = grid_blocks(n, 256, 152 * 32);
+  switch (dtype) {
+    case VDVC_F32: k_cast_f32<<<nb, 256, 0, s>>>(in, n, (float*)out); break;
+    case VDVC_U8: k_cast_round<uint8_t><<<nb, 256, 0, s>>>(in, n, 0.0, 255.0, (uint8_t*)out); break;
+    case VDVC_U16: k_cast_round<uint16_t><<<nb, 256, 0, s>>>(in, n, 0.0, 65535.0, (uint16_t*)out); break;
+    case VDVC_I16: k_cast_round<int16_t><<<nb, 256, 0, s>>>(in, n, -32768.0, 32767.0, (int16_t*)out); break;
+    case VDVC_I32:
+      k_cast_round<int32_t><<<nb, 256, 0, s>>>(in, n, -2147483648.0, 2147483647.0, (int32_t*)out);
+      break;
+    default: return set_error(VDVC_ERR_ARG, "dtype %d", dtype);
+  }
   VDVC_LAUNCHED();
   return VDVC_OK;
 }

@@ -42,6 +42,14 @@ def push_field_forward(field, U, Nx_e, Ny_e, Nz_e, h, order=1, mode='nearest', c
     out = D.empty(Nvx * Nvy * Nvz, dt)
     _lib.check(_lib.lib().vdvc_push_field(f_vox.data_ptr(), D.code_of(dt), u_cf.data_ptr(), Nvx, Nvy, Nvz, int(order),
                                           _MODES[mode], float(cval), out.data_ptr(), D.stream()), "push_field_forward")
+    if in_dt.kind in "iu" and in_dt != dt:
+        # integer fields: scipy's output conversion (round half away from zero)
+        cast = D.empty(out.numel(), np.int16 if in_dt == np.uint16 else in_dt)
+        _lib.check(_lib.lib().vdvc_cast_round(out.data_ptr(), out.numel(), D.code_of(in_dt), cast.data_ptr(),
+                                              D.stream()), "push_field_forward")
+        pushed = cast.view(Nvz, Nvy, Nvx).permute(2, 1, 0)
+        host = D.out(pushed, np) if D.wants_host(xp) else pushed
+        return host.view(np.uint16) if in_dt == np.uint16 and D.wants_host(xp) else host
     pushed = out.view(Nvz, Nvy, Nvx).permute(2, 1, 0)
     if in_dt != dt:
         pushed = pushed.to(D.torch_dtype(in_dt))

@@ -12,7 +12,10 @@ results:
   U_local.npy          same layout, the displacement minus the affine seed
   residual.npy         (Nvx, Nvy, Nvz) final residual
   dU.npy               (Nx+1, Ny+1, Nz+1, 3) last GN update
-  ref_forward_pushed.npy  (Nvx, Nvy, Nvz) reference pushed onto the deformed grid
+  ref.npy, deformed.npy  the reference crop and the deformed volume at the
+                        same index range (def_ref_aligned.npy, when present)
+  ref_forward_pushed.npy  (Nvx, Nvy, Nvz) reference pushed onto the deformed
+                        grid by the local displacement
   principal_strains_cell.npy (Nx, Ny, Nz, 3), equivalent_strain_cell.npy,
   residual_std_cell.npy, zncc_cell.npy, gn_convergence_cell.npy,
   material_cell_mask.npy, material_cell_mask_eroded.npy,
@@ -66,6 +69,11 @@ def mesh_dims(shape, h):
 def _grid(U, Nx, Ny, Nz):
     # node = i + j(Nx+1) + k(Nx+1)(Ny+1): Fortran order of (Nx+1, Ny+1, Nz+1)
     return np.stack([U[c::3].reshape(Nx + 1, Ny + 1, Nz + 1, order='F') for c in range(3)], axis=-1)
+
+
+def _dofs(U_grid):
+    # inverse of _grid: (Nx+1, Ny+1, Nz+1, 3) -> node-major flat DOFs
+    return np.ascontiguousarray(np.transpose(U_grid, (2, 1, 0, 3))).reshape(-1)
 
 
 def _cell_outputs(work, U, U_grid, dU, res, ref, active, Nx, Ny, Nz, h, glt):
@@ -162,14 +170,22 @@ def main(argv=None):
         np.save(os.path.join(work, 'U_local.npy'), U_local)
         np.save(os.path.join(work, 'residual.npy'), res.reshape(ref.shape, order='F'))
         np.save(os.path.join(work, 'dU.npy'), _grid(dU, Nx, Ny, Nz))
+        np.save(os.path.join(work, 'ref.npy'), ref)
+        aligned = os.path.join(work, 'def_ref_aligned.npy')
+        if os.path.exists(aligned):
+            np.save(os.path.join(work, 'deformed.npy'), np.load(aligned))
         # post-solve voxel stages (engine/write_output.py): the reference
         # pushed onto the deformed grid, and the correlation quality over
         # the active voxels (f and the warped g = f - res)
         from .engine.write_output import push_reference_forward, compute_zncc
         from .engine.correlate_gpu import compute_active_mask
+        # pushed with the local displacement (U minus the affine seed), as
+        # run_dvc.py:160-172 passes U_push = U_local
         np.save(os.path.join(work, 'ref_forward_pushed.npy'),
-                push_reference_forward(ref, U, Nx, Ny, Nz, h))
-        active = compute_active_mask(U, deformed, Nx, Ny, Nz, h, np, glt=glt)
+                push_reference_forward(ref, _dofs(U_local), Nx, Ny, Nz, h))
+        # mask0 & in bounds & g > glt, as write_outputs forms it (write_output.py:766-781)
+        active = compute_active_mask(U, deformed, Nx, Ny, Nz, h, np, glt=glt,
+                                     mask0_vox=np.ravel(np.asarray(ref), order='F') > glt)
         f_flat = np.ravel(np.asarray(ref, dtype=np.float64), order='F')
         zncc = compute_zncc(f_flat, f_flat - res, active)
         print(f"  ZNCC (active voxels): {zncc:.6f}")

@@ -210,3 +210,38 @@ def true_U_problem(problem, field):
 
 WORKLOADS = {"plain_small": plain_small, "necking_512": necking_512, "necking_512_eqgap": necking_512_eqgap,
              "necking_256": necking_256}
+
+
+# ---- known-answer (ground-truth) stand-ins ---------------------------------
+# Seeded substitutes for a 65^3 uint16 reference volume and its (66^3, 3)
+# float32 displacement sampled at the integer coordinates 0..65: a speckle
+# volume with mean 32112, std 6270, clipped to [15192, 58729], and a uniaxial
+# z strain eps with lateral contraction nu eps plus a smooth non-affine part.
+# "z+0.01" is +1 % tension (u_z 0 -> 0.65 vx), "z-0.05" -5 % compression
+# (u_z 0 -> -3.25 vx).  Generated with numpy / scipy on the host so the
+# oracle and the GPU pipeline see the same bytes.
+GT_KINDS = {"z+0.01": (0.01, 0.3), "z-0.05": (-0.05, 0.26)}
+
+
+def gt_stand_in(kind="z+0.01", n=65, seed=11):
+    """(ref (n, n, n) uint16, U (n+1, n+1, n+1, 3) float32)."""
+    from scipy.ndimage import gaussian_filter
+    eps, nu = GT_KINDS[kind]
+    rng = np.random.default_rng(seed)
+    t = gaussian_filter(rng.standard_normal((n, n, n)), 1.2)
+    t = (t - t.mean()) / t.std()
+    ref = np.clip(np.round(32112.0 + 6270.0 * t), 15192, 58729).astype(np.uint16)
+    g = np.arange(n + 1, dtype=np.float64)
+    X, Y, Z = np.meshgrid(g, g, g, indexing='ij')
+    U = np.empty((n + 1, n + 1, n + 1, 3))
+    x0 = 0.15 * n
+    U[..., 0] = -nu * eps * (X - x0)
+    U[..., 1] = -nu * eps * (Y - x0)
+    U[..., 2] = eps * Z
+    amp = 2.0 * abs(eps)   # smooth bumps of amplitude 2 |eps| vx, width n/5
+    for _ in range(4):
+        c = rng.random(3) * n
+        a = rng.standard_normal(3) * amp
+        w = np.exp(-((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2) / (2 * (n / 5.0) ** 2))
+        U += w[..., None] * a
+    return ref, U.astype(np.float32)
