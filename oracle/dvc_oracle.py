@@ -243,6 +243,75 @@ def matvec_h(v, grad, mask, h, Nx, Ny, Nz, chunk=None):
     return f
 
 
+def _kl(k, l):
+    k, l = min(k, l), max(k, l)
+    return (0, 1, 2, 3, 4, 5)[[(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)].index((k, l))]
+
+
+def eh_f16_elements(grad_bf16, mask, h, Nx, Ny, Nz):
+    """Element Hessians of the precision form as the tensor-core formation
+    computes them: owner-computes point sets (a shared face belongs to the
+    element beyond it), trapezoid halves on the domain faces only, operands
+    A = w m g_k g_l x 2^(13 - floor(log2 max g^2)) and P = 256 psi psi psi
+    rounded to FP16 from their FP32 values, products summed exactly (float64)
+    and unscaled.  Returns T (Ne, 27, 6): T[e, 9 sx + 3 sy + sz, kl]."""
+    H = h
+    g = np.asarray(grad_bf16, np.float32).reshape(-1, 3)
+    gm = np.float32(np.abs(g).max()) if g.size else np.float32(0)
+    g2 = np.float32(gm * gm)
+    e2 = int(np.floor(np.log2(g2))) if 0 < g2 < 3.0e38 else 0
+    e2 = max(-100, min(100, e2))
+    scaleA = np.float32(2.0 ** (13 - e2))
+    inv_h = np.float32(1) / np.float32(H)
+    q1 = np.arange(H + 1)
+    f1 = q1.astype(np.float32) * inv_h
+    f0 = np.float32(1) - f1
+    psi = np.stack([f0 * f0, f0 * f1, f1 * f1])                     # (3, H+1) float32
+    P = np.zeros((27, H + 1, H + 1, H + 1), np.float32)
+    for sx in range(3):
+        for sy in range(3):
+            for sz in range(3):
+                P[9 * sx + 3 * sy + sz] = ((np.float32(256) * psi[sx][:, None, None]) * psi[sy][None, :, None]) \
+                    * psi[sz][None, None, :]
+    P16 = P.astype(np.float16).astype(np.float64).reshape(27, -1)     # index (qx, qy, qz), qz fastest
+    Nvx, Nvy = Nx * H + 1, Ny * H + 1
+    QX, QY, QZ = (a.ravel() for a in np.meshgrid(q1, q1, q1, indexing='ij'))
+    Ne = Nx * Ny * Nz
+    T = np.zeros((Ne, 27, 6))
+    pairs = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+    for e in range(Ne):
+        i, j, k = e % Nx, (e // Nx) % Ny, e // (Nx * Ny)
+        own = ((QX < H) | (i == Nx - 1)) & ((QY < H) | (j == Ny - 1)) & ((QZ < H) | (k == Nz - 1))
+        v = i * H + QX + (j * H + QY) * Nvx + (k * H + QZ) * Nvx * Nvy
+        w = np.full(QX.shape, scaleA, np.float32)
+        w = np.where(((QX == 0) & (i == 0)) | ((QX == H) & (i == Nx - 1)), w * np.float32(0.5), w)
+        w = np.where(((QY == 0) & (j == 0)) | ((QY == H) & (j == Ny - 1)), w * np.float32(0.5), w)
+        w = np.where(((QZ == 0) & (k == 0)) | ((QZ == H) & (k == Nz - 1)), w * np.float32(0.5), w)
+        w = np.where(own & np.asarray(mask, bool)[np.where(own, v, 0)], w, np.float32(0))
+        gv = g[np.where(own, v, 0)]
+        for c, (kk, ll) in enumerate(pairs):
+            A16 = (w * (gv[:, kk] * gv[:, ll])).astype(np.float16).astype(np.float64)
+            T[e, :, c] = P16 @ A16
+    return T / (256.0 * float(scaleA))
+
+
+def eh_matvec(T, v, Nx, Ny, Nz):
+    """H v from element Hessians T (Ne, 27, 6):
+    K_e[(a,k),(b,l)] = T[e, 9 (ax+bx) + 3 (ay+by) + (az+bz), kl(k,l)]."""
+    out = np.zeros(v.shape[0])
+    for e in range(Nx * Ny * Nz):
+        d = elem_dofs(np.array([e]), Nx, Ny)[0]
+        K = np.empty((24, 24))
+        for a in range(8):
+            for b in range(8):
+                s = 9 * (CORNER[a, 0] + CORNER[b, 0]) + 3 * (CORNER[a, 1] + CORNER[b, 1]) + CORNER[a, 2] + CORNER[b, 2]
+                for k in range(3):
+                    for l in range(3):
+                        K[3 * a + k, 3 * b + l] = T[e, s, _kl(k, l)]
+        np.add.at(out, d, K @ v[d])
+    return out
+
+
 def diag_h(grad, mask, h, Nx, Ny, Nz, Ndof, chunk=None):
     """kernels_dvc.py:509-543."""
     N, w = n_stencil(h)

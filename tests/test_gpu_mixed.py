@@ -51,6 +51,31 @@ def test_mixed_matvec(api, case):
     assert rel(Hv, c["out_matvec_H_f64"]) < 1e-2
 
 
+@pytest.mark.parametrize("h,dims", [(8, (5, 3, 4)), (6, (23, 2, 3)), (8, (1, 1, 1)), (8, (4, 3, 2))])
+def test_tensor_core_formation(api, h, dims, monkeypatch):
+    """tcgen05 formation (VDVC_EH_FORM=tc) against the FP16-operand oracle
+    (ragged 21-element tiles, rows crossing mesh rows) and against the
+    CUDA-core formation."""
+    K, G = api
+    monkeypatch.setenv("VDVC_EH_FORM", "tc")
+    rng = np.random.default_rng(h + dims[0])
+    Nx, Ny, Nz = dims
+    Nvox = (Nx * h + 1) * (Ny * h + 1) * (Nz * h + 1)
+    Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    grad = (rng.standard_normal((Nvox, 3)) * 300.0).astype(np.float32)  # an intensity scale far from 1
+    mask = rng.random(Nvox) < 0.9
+    v = rng.standard_normal(Ndof).astype(np.float32)
+    N, w = G.build_N_stencil(h)
+    Hv = K.matvec_H_mixed(v, grad, mask, N, w, h, Nx, Ny, Nz, np)
+    T = O.eh_f16_elements(bf16_round(grad), mask, h, Nx, Ny, Nz)
+    assert rel(Hv, O.eh_matvec(T, v.astype(np.float64), Nx, Ny, Nz)) < 1e-5
+    monkeypatch.setenv("VDVC_EH_FORM", "cuda")
+    Hc = K.matvec_H_mixed(v, grad, mask, N, w, h, Nx, Ny, Nz, np)
+    ref16 = O.matvec_h(v.astype(np.float64), bf16_round(grad).astype(np.float64), mask, h, Nx, Ny, Nz)
+    assert rel(Hc, ref16) < 2e-6
+    assert rel(Hv, Hc) < 5e-4
+
+
 def test_mixed_matvec_random_mesh(api):
     """A mesh with several strips per row and ragged last strip (h = 4, Nx = 37)."""
     K, G = api
@@ -95,6 +120,18 @@ def test_mixed_solve_sinusoid(solve_api):
     stats = []
     U, res, _ = CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, precision="mixed", stats=stats, **kw)
     assert stats[0]["precision"] == "mixed"
+    assert rel_rms(U, c["U"]) < MIXED_REL_TOL
+
+
+@pytest.mark.parametrize("form", ["cuda", "tc"])
+def test_mixed_solve_formations(solve_api, form, monkeypatch):
+    """The precision-form solve with either element-Hessian formation (CUDA
+    cores, or tcgen05 with FP16 operands) reaches the plain solve's result."""
+    CG, G = solve_api
+    monkeypatch.setenv("VDVC_EH_FORM", form)
+    c = load_golden("solve_sinusoid.npz")
+    kw = dict(K_ref_laplacian=G.build_K_ref_laplacian(), l0=4.5 * 8, maxiter=20, eps=1e-3, disp=False)
+    U, _, _ = CG.correlate_gpu(c["f"], c["g"], 2, 2, 2, 8, xp=np, precision="mixed", **kw)
     assert rel_rms(U, c["U"]) < MIXED_REL_TOL
 
 

@@ -64,6 +64,7 @@ struct GnSolver {
   bool eh_fixed;     // T, diag and M^-1 are final (b mask frozen, or mask0)
   float* T_eh;       // [162][Ne] element Hessians
   void* grad_bf16;   // (Nvox,3) BF16
+  float* gmax;       // max |g| of grad_bf16 (the tensor-core formation's scale)
   // PCG graph
   cudaStream_t cap_stream;
   cudaGraph_t graph;
@@ -458,6 +459,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
     Carve cv(d->eh_ws, d->eh_ws_bytes);
     S->T_eh = cv.take<float>((size_t)162 * eh_pitch(m.Ne));
     S->grad_bf16 = cv.take<uint16_t>((size_t)3 * m.Nvox);
+    S->gmax = cv.take<float>(4);
     const bool ok = std::is_same<T, float>::value;
     const bool h_ok = d->h == 1 || d->h == 2 || d->h == 3 || d->h == 4 || d->h == 6 || d->h == 8 || d->h == 12 ||
                       d->h == 16;
@@ -530,7 +532,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   }
   k_set_U<T><<<nblk(m.Ndof), 256, 0, s>>>(nullptr, m.Ndof, S->U64, S->U32);
   count_launch();
-  if (S->mixed && (e = launch_grad_bf16((const float*)d->grad, 3 * m.Nvox, S->grad_bf16, s))) return fail(e);
+  if (S->mixed && (e = launch_grad_bf16((const float*)d->grad, 3 * m.Nvox, S->grad_bf16, S->gmax, s))) return fail(e);
   // sync before the graph (captured on a private stream) sees the buffers
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail(set_error(VDVC_ERR_CUDA, "solver setup sync failed"));
   *out = S;
@@ -549,7 +551,7 @@ template <typename T>
 static int frozen_diag(GnSolver<T>* S, cudaStream_t s) {
   int st;
   if (S->mixed) {
-    EhFormArgs fa{S->m, S->grad_bf16, S->d.mask0, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne)};
+    EhFormArgs fa{S->m, S->grad_bf16, S->d.mask0, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne), S->gmax, &S->sc->status};
     if ((st = launch_eh_form(fa, s))) return st;
     S->eh_fixed = true;
   } else {
@@ -626,7 +628,7 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
     st = launch_strip<T, kModeB | kModeRes>(a, nullptr, s);
   if (st) return st;
   if (with_diag && S->mixed) {
-    EhFormArgs fa{S->m, S->grad_bf16, S->frozen, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne)};
+    EhFormArgs fa{S->m, S->grad_bf16, S->frozen, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne), S->gmax, &S->sc->status};
     if ((st = launch_eh_form(fa, s))) return st;
     if (S->frozen_set) S->eh_fixed = true;
   }

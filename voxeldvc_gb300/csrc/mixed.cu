@@ -22,9 +22,17 @@
 
 namespace vdvc {
 
-__global__ void k_grad_to_bf16(const float* __restrict__ g, long long n, __nv_bfloat16* __restrict__ out) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    out[i] = __float2bfloat16_rn(g[i]);
+__global__ void k_grad_to_bf16(const float* __restrict__ g, long long n, __nv_bfloat16* __restrict__ out,
+                               unsigned int* __restrict__ amax) {
+  float mx = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(g[i]);
+    out[i] = b;
+    mx = fmaxf(mx, fabsf(__bfloat162float(b)));
+  }
+  // non-negative floats order like their bit patterns: one atomic per warp
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (amax && (threadIdx.x & 31) == 0) atomicMax(amax, __float_as_uint(mx));
 }
 
 
@@ -147,6 +155,8 @@ static int launch_form(const EhFormArgs& args, cudaStream_t s) {
 }
 
 int launch_eh_form(const EhFormArgs& a, cudaStream_t s) {
+  const int tc = launch_eh_form_tc(a, s);  // tcgen05 formation where it is built (h = 6, 8)
+  if (tc != VDVC_ERR_UNSUPPORTED) return tc;
   switch (a.m.h) {
     case 1: return launch_form<1>(a, s);
     case 2: return launch_form<2>(a, s);
@@ -298,8 +308,9 @@ int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s) {
 template int launch_eh_matvec<false>(const EhMatvecArgs&, cudaStream_t);
 template int launch_eh_matvec<true>(const EhMatvecArgs&, cudaStream_t);
 
-int launch_grad_bf16(const float* g, long long n, void* out, cudaStream_t s) {
-  k_grad_to_bf16<<<grid_blocks(n, 256, 152 * 32), 256, 0, s>>>(g, n, (__nv_bfloat16*)out);
+int launch_grad_bf16(const float* g, long long n, void* out, float* gmax, cudaStream_t s) {
+  if (gmax) VDVC_CUDA(cudaMemsetAsync(gmax, 0, sizeof(float), s));
+  k_grad_to_bf16<<<grid_blocks(n, 256, 152 * 32), 256, 0, s>>>(g, n, (__nv_bfloat16*)out, (unsigned int*)gmax);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
@@ -319,6 +330,7 @@ size_t vdvc_eh_workspace_bytes(int h, int Nx, int Ny, int Nz) {
   cv.take<float>((size_t)24 * m.Ne);
   cv.take<int>(4);
   cv.take<uint16_t>((size_t)3 * m.Nvox);
+  cv.take<float>(4);
   return cv.off + 256;
 }
 
@@ -335,10 +347,12 @@ int vdvc_matvec_H_mixed(const float* v, const float* grad, const uint8_t* mask, 
   float* ev = cv.take<float>((size_t)24 * m.Ne);
   int* err = cv.take<int>(4);
   uint16_t* gb = cv.take<uint16_t>((size_t)3 * m.Nvox);
+  float* gmax = cv.take<float>(4);
   if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "mixed matvec needs %zu bytes of workspace", cv.off);
   cudaStream_t s = (cudaStream_t)stream;
-  if ((st = launch_grad_bf16(grad, 3 * m.Nvox, gb, s))) return st;
-  EhFormArgs fa{m, (const __nv_bfloat16*)gb, mask, T, evD, pitch};
+  VDVC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  if ((st = launch_grad_bf16(grad, 3 * m.Nvox, gb, gmax, s))) return st;
+  EhFormArgs fa{m, (const __nv_bfloat16*)gb, mask, T, evD, pitch, gmax, err};
   if ((st = launch_eh_form(fa, s))) return st;
   EhMatvecArgs ma{};
   ma.m = m;
@@ -347,14 +361,13 @@ int vdvc_matvec_H_mixed(const float* v, const float* grad, const uint8_t* mask, 
   ma.err = err;
   ma.v = v;
   ma.ev = ev;
-  VDVC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   if ((st = launch_eh_matvec<false>(ma, s))) return st;
   if ((st = launch_gather<float>(m, ev, out, s))) return st;
   // the bulk-copy waits are bounded: report a timeout (never seen in practice)
   int h_err = 0;
   VDVC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
   VDVC_CUDA(cudaStreamSynchronize(s));
-  if (h_err) return set_error(VDVC_ERR_CUDA, "element-Hessian tile copies timed out");
+  if (h_err) return set_error(VDVC_ERR_CUDA, "element-Hessian waits timed out");
   return VDVC_OK;
 }
 

@@ -117,6 +117,8 @@ struct EhFormArgs {
   float* T;               // [tiles][162][kEhTile]
   float* evD;             // [24][Ne] diagonal contributions
   long long pitch;        // eh_pitch(Ne): elements rounded up to whole tiles
+  const float* gmax;      // max |g| of the BF16 gradient (device); the tensor-core formation's scale
+  int* err;               // set to VDVC_ERR_CUDA if a tensor-core formation wait times out
 };
 
 struct EhMatvecArgs {
@@ -140,7 +142,9 @@ int launch_eh_form(const EhFormArgs& a, cudaStream_t s);
 long long eh_pitch(long long Ne);  // elements rounded up to whole tiles
 template <bool PCG>
 int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s);
-int launch_grad_bf16(const float* g, long long n, void* out, cudaStream_t s);
+// BF16 copy of the gradient and, when gmax != NULL, max |g| of the copy
+int launch_grad_bf16(const float* g, long long n, void* out, float* gmax, cudaStream_t s);
+int launch_eh_form_tc(const EhFormArgs& a, cudaStream_t s);
 
 inline int grid_blocks(long long n, int threads, long long cap) {
   long long b = (n + threads - 1) / threads;
