@@ -53,7 +53,7 @@ SOLVE_COUNTS = {"necking_512": {"gn": [30, 4, 2], "pcg": [752, 84, 41]},
                 "plain_small": {"gn": [10, 5, 3], "pcg": [200, 100, 60]}}
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=3)
@@ -68,7 +68,7 @@ def parse():
     p.add_argument("--only", default=None, choices=[None, "matvec", "kernels"],
                    help="matvec: time only the finest-level Hessian matvec; kernels: run each hot kernel of the "
                         "plain, precision and learned forms a few times on the 257^3 case (the profiling commands)")
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 def matvec_only(args):
@@ -375,6 +375,19 @@ def compare_batch():
     return res
 
 
+def max_over_ranks(value, world, device):
+    """The slowest rank's value (replicas: the job ends with its last rank);
+    the process group's backend moves the tensor (NCCL on the GPU, gloo in
+    the CPU tests)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -421,10 +434,7 @@ def gpu_arm(args):
     launches = (_lib.launch_count() - n0) // max(1, args.steps)
     ms = e0.elapsed_time(e1) / args.steps
     barrier()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, "cuda")
     clocks = clk.summary()
 
     # accuracy vs the analytic field (sanity; the solve's own error)
