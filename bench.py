@@ -416,21 +416,31 @@ def gpu_arm(args):
     def step(stats=None):
         return CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, xp=torch, stats=stats, **kw)
 
-    for _ in range(args.warmup):
-        step()
+    # the per-level statistics come from the last warm-up step, so every
+    # timed step runs the same code; the host's garbage collector is held
+    # off during the timed region (the solve is host-driven per GN iteration)
+    level_stats = []
+    n_warm = max(1, args.warmup)
+    for w in range(n_warm):
+        step(level_stats if w == n_warm - 1 else None)
     torch.cuda.synchronize()
     barrier()
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     n0 = _lib.launch_count()
-    level_stats = []
-    with Clocks(local) as clk:
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for i in range(args.steps):
-            U, res, dU = step(level_stats if i == 0 else None)
-        e1.record(stream)
-        torch.cuda.synchronize()
+    import gc
+    gc.collect()
+    gc.disable()
+    try:
+        with Clocks(local) as clk:
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(args.steps):
+                U, res, dU = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+    finally:
+        gc.enable()
     launches = (_lib.launch_count() - n0) // max(1, args.steps)
     ms = e0.elapsed_time(e1) / args.steps
     barrier()
