@@ -65,7 +65,7 @@ def parse(argv=None):
     p.add_argument("--cpu-sample-layers", type=int, default=1)
     p.add_argument("--no-forms", action="store_true",
                    help="skip the precision / learned-seed form comparison (FP64 reference solve included)")
-    p.add_argument("--only", default=None, choices=[None, "matvec", "kernels"],
+    p.add_argument("--only", default=None, choices=[None, "matvec", "kernels", "ground-truth", "post"],
                    help="matvec: time only the finest-level Hessian matvec; kernels: run each hot kernel of the "
                         "plain, precision and learned forms a few times on the 257^3 case (the profiling commands)")
     return p.parse_args(argv)
@@ -581,6 +581,94 @@ def kernels_only(args):
     print(json.dumps({"kernels": "done", "reps": reps, "workload": wl.name}))
 
 
+def post_only(args):
+    """The post-solve stages of `voxeldvc run` on the 257^3 necking case after
+    one plain solve: forward push, ZNCC, active mask, per-element strain and
+    quality fields, diagnostic masks, and the ground-truth backward warp;
+    CUDA-event time per stage (median of --steps) and its algorithmic bytes."""
+    import torch
+    from voxeldvc_gb300 import synth
+    from voxeldvc_gb300.engine import correlate_gpu as CG, kernels_dvc as K, write_output as W
+    from voxeldvc_gb300.ground_truth import prepare_ground_truth as PG
+    wl = synth.WORKLOADS["necking_256"]()
+    Nx, Ny, Nz = wl.mesh
+    h = wl.h
+    f_pix, g_pix = wl.make()
+    kw = solve_kwargs(wl)
+    U, res, dU = CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp=torch, **kw)
+    nv = tuple(int(s) for s in f_pix.shape)
+    Nvox = nv[0] * nv[1] * nv[2]
+    Ne = Nx * Ny * Nz
+    U_grid = torch.stack([U[c::3].reshape(Nz + 1, Ny + 1, Nx + 1).permute(2, 1, 0) for c in range(3)], -1).double()
+    active = CG.compute_active_mask(U, g_pix, Nx, Ny, Nz, h, torch)
+    f64 = f_pix.double()
+    u_vox = torch.zeros(nv + (3,), dtype=torch.float64, device="cuda")
+    u_vox[..., 2] = 0.5
+    stages = {
+        "push_reference_forward": (lambda: W.push_reference_forward(f_pix, U, Nx, Ny, Nz, h, xp=torch),
+                                   Nvox * (4 + 24 + 4 + 4)),
+        "compute_zncc": (lambda: W.compute_zncc(f_pix.reshape(-1), g_pix.reshape(-1), active), Nvox * (8 + 8 + 1) * 2),
+        "compute_active_mask": (lambda: CG.compute_active_mask(U, g_pix, Nx, Ny, Nz, h, torch), Nvox * (4 + 1)),
+        "principal_strains_cell": (lambda: W.compute_principal_strains_cell(U_grid, h), Ne * (24 + 24)),
+        "correlation_quality_cell": (lambda: W.compute_correlation_quality_cell(res, f_pix, h, Nx, Ny, Nz),
+                                     Nvox * (8 + 4) + Ne * 16),
+        "unsafe_masks": (lambda: K.compute_unsafe_voxel_mask(active, h, Nx, Ny, Nz), Nvox * 2),
+        "gt_backward_warp": (lambda: PG.make_deformed_image(f64, u_vox, xp=torch), Nvox * (8 + 24 + 8)),
+    }
+    out = {}
+    for name, (fn, nbytes) in stages.items():
+        fn()
+        ts = []
+        for _ in range(max(3, args.steps)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = float(np.median(ts))
+        out[name] = {"ms": round(ms, 3), "algorithmic_bytes": int(nbytes), "gbs": round(nbytes / ms / 1e6, 1)}
+    print(json.dumps({"post": out, "workload": wl.name, "voxels": Nvox, "elements": Ne,
+                      "note": "host results (xp=numpy) are not requested: device tensors, no copies"}))
+
+
+def ground_truth_only(args):
+    """The known-answer pipeline (prepare -> preprocess -> run -> analyse) on
+    the seeded 65^3 stand-ins for the reference's two ground-truth datasets,
+    h = 8, l0 = 4.5 h: node RMS error over the recoverable and valid sets and
+    the wall time of each stage (the first run of a kind includes one-time
+    set-up; the second is reported)."""
+    import tempfile
+    import contextlib
+    import io
+    from voxeldvc_gb300 import synth
+    from voxeldvc_gb300 import run_ground_truth_pipeline as RG
+    from voxeldvc_gb300.ground_truth import analyse_ground_truth as AG
+    out = {}
+    for kind in synth.GT_KINDS:
+        ref, U = synth.gt_stand_in(kind)
+        with tempfile.TemporaryDirectory() as tmp:
+            np.save(os.path.join(tmp, "ref.npy"), ref)
+            np.save(os.path.join(tmp, "U.npy"), U)
+            walls = []
+            for rep in range(2):
+                work = os.path.join(tmp, f"run{rep}")
+                t0 = time.perf_counter()
+                with contextlib.redirect_stdout(io.StringIO()):
+                    RG.main(["--output-dir", work, "--gt-ref-file", os.path.join(tmp, "ref.npy"),
+                             "--gt-displacement-file", os.path.join(tmp, "U.npy")])
+                walls.append(time.perf_counter() - t0)
+            with contextlib.redirect_stdout(io.StringIO()):
+                st = AG.analyse(work, os.path.join(work, "gt_input"))
+        out[kind] = {"rms_recoverable_vx": round(st["recoverable"][1], 5), "rms_valid_vx": round(st["valid"][1], 5),
+                     "nodes_recoverable": st["recoverable"][0], "nodes_valid": st["valid"][0],
+                     "rms_voxel_valid_vx": round(st.get("voxel_valid_rms", float("nan")), 5),
+                     "pipeline_wall_s": round(walls[-1], 3)}
+    print(json.dumps({"ground_truth": out, "data": "seeded 65^3 stand-ins (synth.gt_stand_in)", "h": 8,
+                      "l0_factor": 4.5}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -589,6 +677,10 @@ def main():
         matvec_only(args)
     elif args.only == "kernels":
         kernels_only(args)
+    elif args.only == "ground-truth":
+        ground_truth_only(args)
+    elif args.only == "post":
+        post_only(args)
     else:
         gpu_arm(args)
 

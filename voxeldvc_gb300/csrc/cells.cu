@@ -83,63 +83,88 @@ __global__ void k_cell_strains(const double* __restrict__ U, int Nx, int Ny, int
 }
 
 // material mask (block mean of ref > glt), safe mask (no unsafe voxel in the
-// block), residual std and ZNCC over the block's active voxels (res != 0)
+// block), residual std and ZNCC over the block's active voxels (res != 0).
+// One warp per element: the lanes stride over the block's voxels (x fastest,
+// coalesced), float64 sums are combined by a fixed shuffle tree; the ZNCC's
+// centred second pass re-reads the block from L1.
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 template <typename TR>
-__global__ void k_cell_fields(const TR* __restrict__ ref, const double* __restrict__ res,
-                              const uint8_t* __restrict__ unsafe, int h, int Nx, int Ny, int Nz, double glt,
-                              uint8_t* __restrict__ material, uint8_t* __restrict__ safe, double* __restrict__ rstd,
-                              double* __restrict__ zncc) {
+__global__ void __launch_bounds__(256) k_cell_fields(const TR* __restrict__ ref, const double* __restrict__ res,
+                                                     const uint8_t* __restrict__ unsafe, int h, int Nx, int Ny,
+                                                     int Nz, double glt, uint8_t* __restrict__ material,
+                                                     uint8_t* __restrict__ safe, double* __restrict__ rstd,
+                                                     double* __restrict__ zncc) {
   const long long Ne = (long long)Nx * Ny * Nz;
   const long long Nvx = (long long)Nx * h + 1, NvxNvy = Nvx * ((long long)Ny * h + 1);
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < Ne; e += (long long)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  const int q1 = h + 1, nq = q1 * q1 * q1;
+  for (long long e = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); e < Ne; e += warps) {
     const int i = (int)(e % Nx);
     const long long r = e / Nx;
     const int j = (int)(r % Ny), k = (int)(r / Ny);
     const long long v0 = (long long)i * h + (long long)j * h * Nvx + (long long)k * h * NvxNvy;
     double sref = 0.0, cnt = 0.0, sr = 0.0, srr = 0.0, sf = 0.0, sg = 0.0;
     bool any_unsafe = false;
-    for (int qz = 0; qz <= h; ++qz)
-      for (int qy = 0; qy <= h; ++qy)
-        for (int qx = 0; qx <= h; ++qx) {
-          const long long v = v0 + qx + qy * Nvx + qz * NvxNvy;
-          const double f = ref ? (double)ref[v] : 0.0;
-          sref += f;
-          if (unsafe && unsafe[v]) any_unsafe = true;
-          if (res) {
-            const double rv = res[v];
-            if (rv != 0.0) {
-              cnt += 1.0;
-              sr += rv;
-              srr += rv * rv;
-              sf += f;
-              sg += f - rv;
-            }
-          }
+    for (int q = lane; q < nq; q += 32) {
+      const int qx = q % q1, qy = (q / q1) % q1, qz = q / (q1 * q1);
+      const long long v = v0 + qx + qy * Nvx + qz * NvxNvy;
+      const double f = ref ? (double)ref[v] : 0.0;
+      sref += f;
+      if (unsafe && unsafe[v]) any_unsafe = true;
+      if (res) {
+        const double rv = res[v];
+        if (rv != 0.0) {
+          cnt += 1.0;
+          sr += rv;
+          srr += rv * rv;
+          sf += f;
+          sg += f - rv;
         }
-    const double nq = (double)(h + 1) * (h + 1) * (h + 1);
-    if (material) material[e] = (sref / nq) > glt ? 1 : 0;
-    if (safe) safe[e] = any_unsafe ? 0 : 1;
+      }
+    }
+    sref = warp_sum_d(sref);
+    any_unsafe = __any_sync(0xffffffffu, any_unsafe);
+    if (lane == 0) {
+      const double nqd = (double)nq;
+      if (material) material[e] = (sref / nqd) > glt ? 1 : 0;
+      if (safe) safe[e] = any_unsafe ? 0 : 1;
+    }
     if (!res) continue;
+    cnt = warp_sum_d(cnt);
+    sr = warp_sum_d(sr);
+    srr = warp_sum_d(srr);
+    sf = warp_sum_d(sf);
+    sg = warp_sum_d(sg);
     const double dc = cnt > 1.0 ? cnt : 1.0;
-    const double mr = sr / dc;
-    const double var = srr / dc - mr * mr;
-    rstd[e] = cnt < 8.0 ? dnan() : sqrt(var > 0.0 ? var : 0.0);
     const double fm = sf / dc, gm = sg / dc;
     double num = 0.0, ff = 0.0, gg = 0.0;
-    for (int qz = 0; qz <= h; ++qz)
-      for (int qy = 0; qy <= h; ++qy)
-        for (int qx = 0; qx <= h; ++qx) {
-          const long long v = v0 + qx + qy * Nvx + qz * NvxNvy;
-          const double rv = res[v];
-          if (rv == 0.0) continue;
-          const double f = (double)ref[v];
-          const double fc = f - fm, gc = (f - rv) - gm;
-          num += fc * gc;
-          ff += fc * fc;
-          gg += gc * gc;
-        }
-    const double den = sqrt(ff * gg);
-    zncc[e] = (cnt < 8.0 || !(den > 0.0)) ? dnan() : num / den;
+    for (int q = lane; q < nq; q += 32) {
+      const int qx = q % q1, qy = (q / q1) % q1, qz = q / (q1 * q1);
+      const long long v = v0 + qx + qy * Nvx + qz * NvxNvy;
+      const double rv = res[v];
+      if (rv == 0.0) continue;
+      const double f = (double)ref[v];
+      const double fc = f - fm, gc = (f - rv) - gm;
+      num += fc * gc;
+      ff += fc * fc;
+      gg += gc * gc;
+    }
+    num = warp_sum_d(num);
+    ff = warp_sum_d(ff);
+    gg = warp_sum_d(gg);
+    if (lane == 0) {
+      const double mr = sr / dc;
+      const double var = srr / dc - mr * mr;
+      rstd[e] = cnt < 8.0 ? dnan() : sqrt(var > 0.0 ? var : 0.0);
+      const double den = sqrt(ff * gg);
+      zncc[e] = (cnt < 8.0 || !(den > 0.0)) ? dnan() : num / den;
+    }
   }
 }
 
@@ -336,12 +361,13 @@ int vdvc_cell_fields(const void* ref, int ref_dtype, const double* res, const ui
   VDVC_CHECK_ARG(!safe || unsafe, "safe needs the unsafe voxel mask");
   const long long Ne = (long long)Nx * Ny * Nz;
   cudaStream_t s = (cudaStream_t)stream;
+  const int nb = grid_blocks(Ne, 8, 152 * 16);  // 8 elements (warps) per block
   if (ref_dtype == VDVC_F32)
-    k_cell_fields<float><<<cblocks(Ne), 128, 0, s>>>((const float*)ref, res, unsafe, h, Nx, Ny, Nz, glt, material,
-                                                     safe, residual_std, zncc);
+    k_cell_fields<float><<<nb, 256, 0, s>>>((const float*)ref, res, unsafe, h, Nx, Ny, Nz, glt, material, safe,
+                                            residual_std, zncc);
   else if (ref_dtype == VDVC_F64)
-    k_cell_fields<double><<<cblocks(Ne), 128, 0, s>>>((const double*)ref, res, unsafe, h, Nx, Ny, Nz, glt, material,
-                                                      safe, residual_std, zncc);
+    k_cell_fields<double><<<nb, 256, 0, s>>>((const double*)ref, res, unsafe, h, Nx, Ny, Nz, glt, material, safe,
+                                             residual_std, zncc);
   else
     return set_error(VDVC_ERR_ARG, "ref dtype %d", ref_dtype);
   VDVC_LAUNCHED();

@@ -230,7 +230,7 @@ int launch_sample(const SampleArgs<T>& args, cudaStream_t s) {
   const size_t smem = ((size_t)sh.EX * 24 + args.m.h + 2) * sizeof(T);
   SampleArgs<T> a = args;
   a.EX = sh.EX;
-  if constexpr (std::is_same<T, float>::value && STATS && !INTERP) {
+  if constexpr (std::is_same<T, float>::value) {
     switch (args.m.h) {
       case 2: k_sample<T, STATS, INTERP, 2><<<grid, sh.threads, smem, s>>>(a); VDVC_LAUNCHED(); return VDVC_OK;
       case 4: k_sample<T, STATS, INTERP, 4><<<grid, sh.threads, smem, s>>>(a); VDVC_LAUNCHED(); return VDVC_OK;
