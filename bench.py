@@ -65,7 +65,7 @@ def parse(argv=None):
     p.add_argument("--cpu-sample-layers", type=int, default=1)
     p.add_argument("--no-forms", action="store_true",
                    help="skip the precision / learned-seed form comparison (FP64 reference solve included)")
-    p.add_argument("--only", default=None, choices=[None, "matvec", "kernels", "ground-truth", "post"],
+    p.add_argument("--only", default=None, choices=[None, "matvec", "kernels", "ground-truth", "post", "eh-form"],
                    help="matvec: time only the finest-level Hessian matvec; kernels: run each hot kernel of the "
                         "plain, precision and learned forms a few times on the 257^3 case (the profiling commands)")
     return p.parse_args(argv)
@@ -581,6 +581,45 @@ def kernels_only(args):
     print(json.dumps({"kernels": "done", "reps": reps, "workload": wl.name}))
 
 
+def eh_form_only(args):
+    """The precision form's Hessian matvec (BF16 conversion + element-Hessian
+    formation + matvec + gather) on the workload's finest level with each
+    formation: CUDA cores (default) and tcgen05 (VDVC_EH_FORM=tc); wall time
+    per call (median of --steps) and the relative difference of the results."""
+    import torch
+    from voxeldvc_gb300 import synth
+    from voxeldvc_gb300.engine import correlate_gpu as CG, kernels_dvc as K, geometry_dvc as G
+    wl = synth.WORKLOADS[args.workload]()
+    Nx, Ny, Nz = wl.mesh
+    f_pix, _ = wl.make()
+    f_vox, shape = CG.pix_to_vox(f_pix, np.float32)
+    grad, mask0 = CG._grad_vox(f_vox, shape, np.float32, 0.0)
+    N, w = G.build_N_stencil(wl.h)
+    v = torch.randn(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+    res, outs = {}, {}
+    old = os.environ.get("VDVC_EH_FORM")
+    try:
+        for form in ("cuda", "tc"):
+            os.environ["VDVC_EH_FORM"] = form
+            for _ in range(2):
+                K.matvec_H_mixed(v, grad.view(-1, 3), mask0, N, w, wl.h, Nx, Ny, Nz, torch)
+            ts = []
+            for _ in range(max(3, args.steps)):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                outs[form] = K.matvec_H_mixed(v, grad.view(-1, 3), mask0, N, w, wl.h, Nx, Ny, Nz, torch)
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            res[form] = round(float(np.median(ts)) * 1e3, 3)
+    finally:
+        if old is None:
+            os.environ.pop("VDVC_EH_FORM", None)
+        else:
+            os.environ["VDVC_EH_FORM"] = old
+    d = float(torch.linalg.norm(outs["tc"] - outs["cuda"]) / torch.linalg.norm(outs["cuda"]))
+    print(json.dumps({"eh_form_matvec_ms": res, "rel_diff_tc_vs_cuda": d, "workload": wl.name}))
+
+
 def post_only(args):
     """The post-solve stages of `voxeldvc run` on the 257^3 necking case after
     one plain solve: forward push, ZNCC, active mask, per-element strain and
@@ -681,6 +720,8 @@ def main():
         ground_truth_only(args)
     elif args.only == "post":
         post_only(args)
+    elif args.only == "eh-form":
+        eh_form_only(args)
     else:
         gpu_arm(args)
 
