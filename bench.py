@@ -62,7 +62,8 @@ def parse(argv=None):
     p.add_argument("--workload", default="necking_512")
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cpu-sample-layers", type=int, default=1)
+    p.add_argument("--cpu-sample-layers", type=int, default=None,
+                   help="element layers per CPU-baseline worker (default: the whole mesh split over the cores)")
     p.add_argument("--no-forms", action="store_true",
                    help="skip the precision / learned-seed form comparison (FP64 reference solve included)")
     p.add_argument("--only", default=None, choices=[None, "matvec", "kernels", "ground-truth", "post", "eh-form"],
@@ -174,57 +175,102 @@ def _timed(fn, *a, **k):
     return time.perf_counter() - t0
 
 
-def cpu_model(wl, counts, layers=1):
-    """Seconds of the reference path on this host's cores for one solve,
-    from the oracle's per-operation times on `layers` element layers of each
-    pyramid level (extrapolated linearly in elements) and the operation
-    counts of the solve."""
+def _cpu_slab_times(job):
+    """Per-operation seconds of the oracle on one slab of `nz` element layers
+    of every pyramid level (one worker of the CPU baseline)."""
+    Nx, Ny, h0, scales, nz, nu, seed = job
     from oracle import dvc_oracle as O
-    rng = np.random.default_rng(0)
-    Nx, Ny, Nz = wl.mesh
-    Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
-    K_lap, K_el = O.k_ref_laplacian(), O.k_ref_elastic(wl.solve.get("nu", 0.3))
-    eqgap = wl.solve["reg_type"] == "equilibrium_gap"
-    t_start = time.perf_counter()
-    # regularizer operators act on the full dof vector at every level
-    v64 = rng.standard_normal(Ndof)
-    interior = O.interior_dof_mask(Nx, Ny, Nz).astype(np.float32)
-    t_k = _timed(O.matvec_k_ref, v64, K_lap, float(wl.h), Nx, Ny, Nz)
-    t_reg = (3 if eqgap else 1) * t_k          # K P K + eps K_lap  (or K_lap)
-    t_reg_diag = (2 * 32 * t_k + t_k) if eqgap else t_k  # Hutchinson (32 probes x K P K) + diag K_lap
-    t_vec = _timed(lambda: [v64 * 1.0001 + v64 for _ in range(10)] and float(np.dot(v64, v64)))
-    levels = []
-    total = 0.0
-    scales = sorted(wl.solve["scales"], reverse=True)
-    for li, s in enumerate(scales):
-        h = wl.h // 2 ** s
-        nz = layers
+    rng = np.random.default_rng(seed)
+    K_lap = O.k_ref_laplacian()
+    out = {}
+    nd = 3 * (Nx + 1) * (Ny + 1) * (nz + 1)
+    v64 = rng.standard_normal(nd)
+    out["k"] = _timed(O.matvec_k_ref, v64, K_lap, float(h0), Nx, Ny, nz)
+    out["vec"] = _timed(lambda: [v64 * 1.0001 + v64 for _ in range(10)] and float(np.dot(v64, v64)))
+    for s in scales:
+        h = h0 // 2 ** s
         Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, nz * h + 1
         nvox = Nvx * Nvy * Nvz
         grad = rng.standard_normal((nvox, 3)).astype(np.float32)
         mask = rng.random(nvox) < 0.95
         res = rng.standard_normal(nvox)
-        nd = 3 * (Nx + 1) * (Ny + 1) * (nz + 1)
         vs = rng.standard_normal(nd)
         gimg = rng.random((Nvx, Nvy, Nvz)).astype(np.float32)
-        scale = Nz / nz
-        t_mv = _timed(O.matvec_h, vs, grad, mask, h, Nx, Ny, nz) * scale
-        t_dg = _timed(O.diag_h, grad, mask, h, Nx, Ny, nz, nd) * scale
-        t_b = _timed(O.compute_b, res, mask, grad, h, Nx, Ny, nz, nd) * scale
-        t_st = _timed(O.masked_mean_std, res, mask, h, Nx, Ny, nz) * scale
-        t_sm = _timed(O.sample_deformed, 0.3 * vs, gimg, h, Nx, Ny, nz, (0, 0, 0), mask) * scale
+        out[h] = {"mv": _timed(O.matvec_h, vs, grad, mask, h, Nx, Ny, nz),
+                  "dg": _timed(O.diag_h, grad, mask, h, Nx, Ny, nz, nd),
+                  "b": _timed(O.compute_b, res, mask, grad, h, Nx, Ny, nz, nd),
+                  "st": _timed(O.masked_mean_std, res, mask, h, Nx, Ny, nz),
+                  "sm": _timed(O.sample_deformed, 0.3 * vs, gimg, h, Nx, Ny, nz, (0, 0, 0), mask)}
+    return out
+
+
+def cpu_workers():
+    """Host cores this process may use."""
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except AttributeError:
+        return max(1, os.cpu_count() or 1)
+
+
+def cpu_model(wl, counts, layers=None, procs=None):
+    """Seconds of the reference path on this host's cores for one solve.
+    The reference's operators loop over element chunks, so the mesh splits
+    into z slabs that run on separate cores: `procs` worker processes
+    (spawned: the parent may hold a CUDA context; one BLAS/OpenMP thread
+    each) time every operation of every pyramid level on their own slabs,
+    all at once, so the times include the cores' contention for memory
+    bandwidth.  By default the slabs cover the whole mesh (Nz / procs layers
+    each) and a full-mesh operation costs the slowest worker's time; with
+    `layers` given, each worker times that many layers and the cost is
+    extrapolated linearly to Nz / procs layers.  Multiplied by the solve's
+    GN and PCG counts."""
+    import multiprocessing as mp
+    Nx, Ny, Nz = wl.mesh
+    procs = max(1, min(procs or cpu_workers(), Nz))
+    per = layers or -(-Nz // procs)
+    eqgap = wl.solve["reg_type"] == "equilibrium_gap"
+    scales = sorted(wl.solve["scales"], reverse=True)
+    jobs = [(Nx, Ny, wl.h, scales, per, wl.solve.get("nu", 0.3), p) for p in range(procs)]
+    t_start = time.perf_counter()
+    if procs > 1:
+        keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+        saved = {k: os.environ.get(k) for k in keys}
+        os.environ.update({k: "1" for k in keys})
+        try:
+            with mp.get_context("spawn").Pool(procs) as pool:
+                res = pool.map(_cpu_slab_times, jobs)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+    else:
+        res = [_cpu_slab_times(jobs[0])]
+    wall = time.perf_counter() - t_start
+    layers = per
+    scale = (Nz / procs) / per
+    slow = lambda key, lvl=None: max((r[lvl][key] if lvl else r[key]) for r in res) * scale  # noqa: E731
+    t_k = slow("k")
+    t_reg = (3 if eqgap else 1) * t_k          # K P K + eps K_lap  (or K_lap)
+    t_reg_diag = (2 * 32 * t_k + t_k) if eqgap else t_k  # Hutchinson (32 probes x K P K) + diag K_lap
+    t_vec = slow("vec")
+    levels, total = [], 0.0
+    for li, s in enumerate(scales):
+        h = wl.h // 2 ** s
+        t_mv, t_dg, t_b, t_st, t_sm = (slow(k, h) for k in ("mv", "dg", "b", "st", "sm"))
         t_pcg = t_mv + t_reg + t_vec
         t_gn = t_sm + 2 * t_st + t_b + t_reg + t_dg + t_reg_diag + t_st
         n_gn, n_pcg = counts["gn"][li], counts["pcg"][li]
         t_level = n_gn * t_gn + (n_pcg + n_gn) * t_pcg
         total += t_level
         levels.append({"h": h, "matvec_s": round(t_mv, 3), "gn_fixed_s": round(t_gn, 3), "level_s": round(t_level, 1)})
-    wall = time.perf_counter() - t_start
     return total, {"levels": levels, "reg_matvec_s": round(t_k, 3), "sample_wall_s": round(wall, 1),
-                   "sample": f"oracle per-op timing on {layers} element layer(s) of each level "
-                             f"(x{Nz // layers} to the full mesh) + one full-mesh regularizer matvec; "
-                             f"extrapolated with the solve's GN/PCG counts {counts}",
-                   "threads": 1}
+                   "sample": f"oracle per-op timing by {procs} worker processes at once, each on its own z slab "
+                             f"of {layers} element layer(s) of every level (full mesh {Nz} layers; "
+                             f"{'whole mesh covered' if layers * procs >= Nz else 'extrapolated in layers'}), "
+                             f"slowest worker per op; extrapolated with the solve's GN/PCG counts {counts}",
+                   "threads": procs}
 
 
 def reference_arm(args):
@@ -247,7 +293,7 @@ def reference_arm(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (PCG promoted to f64 as in the reference)",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": wl.name, "mesh": list(wl.mesh), "h": wl.h, "extrapolated": True},
-            "cpu_baseline": {"value": round(value, 2), "unit": "s", "cores": 1, "kind": "port",
+            "cpu_baseline": {"value": round(value, 2), "unit": "s", "cores": info["threads"], "kind": "port",
                              "sample": info["sample"]},
             "e2e": {"value": round(value, 2), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "detail": info}
@@ -513,7 +559,7 @@ def gpu_arm(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         counts = {"gn": [s["gn_iters"] for s in level_stats], "pcg": [int(sum(s["pcg_iters"])) for s in level_stats]}
         cv, cinfo = cpu_model(wl, counts, args.cpu_sample_layers)
-        cpu = {"value": round(cv, 2), "unit": "s", "cores": 1, "kind": "port", "sample": cinfo["sample"],
+        cpu = {"value": round(cv, 2), "unit": "s", "cores": cinfo["threads"], "kind": "port", "sample": cinfo["sample"],
                "detail": cinfo["levels"]}
 
     if rank == 0:

@@ -102,7 +102,7 @@ __device__ __forceinline__ T trilinear(const T* __restrict__ g, int nx, int ny, 
 // unrolled four-fold and the strip shape folds into the index arithmetic);
 // HH == 0: h from the mesh.
 template <typename T, bool STATS, bool INTERP, int HH>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 5 : 6) : 3) k_sample(const SampleArgs<T> a) {
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 6 : 6) : 3) k_sample(const SampleArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_red[4];
   const Mesh& m = a.m;
