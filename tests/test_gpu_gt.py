@@ -92,3 +92,26 @@ def test_pipeline_matches_reference_run(GT, tmp_path, kind):
     assert "valid (recoverable & unmasked)" in log
     for f in ("U_gt_vox.npy", "U_recovered_vox.npy", "voxel_valid_mask.npy", "node_oob_fraction.npy"):
         assert os.path.exists(out / f), f
+
+
+def test_sweep_runs_each_pair(GT, tmp_path):
+    """sweep-ground-truth over h in {4, 8}, l0 = 4.5 h on the tension stand-in:
+    one run directory per pair, the h = 8 row equal to the single pipeline
+    run (and so to the reference's own run), a CSV row per pair."""
+    import csv
+    from voxeldvc_gb300 import synth
+    from voxeldvc_gb300.ground_truth import sweep_ground_truth as SW
+    ref, U = synth.gt_stand_in("z+0.01")
+    np.save(tmp_path / "ref_in.npy", ref)
+    np.save(tmp_path / "U_in.npy", U)
+    root = tmp_path / "sweep"
+    assert SW.main(["--gt-ref-file", str(tmp_path / "ref_in.npy"), "--gt-displacement-file",
+                    str(tmp_path / "U_in.npy"), "--h", "4,8", "--l0-factor", "4.5", "--output-root", str(root),
+                    "--csv", str(tmp_path / "sweep.csv")]) == 0
+    rows = {int(r["h"]): r for r in csv.DictReader(open(tmp_path / "sweep.csv"))}
+    assert set(rows) == {4, 8} and all(r["status"] == "ok" for r in rows.values())
+    g = load_golden("gt_pipeline_z+0.01.npz")
+    assert abs(float(rows[8]["rms_valid"]) - float(g["rms_valid"])) < max(0.05 * float(g["rms_valid"]), 5e-4)
+    assert abs(float(rows[8]["rms"]) - float(g["rms_rec"])) < max(0.05 * float(g["rms_rec"]), 5e-4)
+    assert float(rows[4]["rms"]) < 1.0  # not diverged
+    assert (root / "h4_l0f4.5" / "U_error.npy").exists() and (root / "h8_l0f4.5" / "run_log.txt").exists()

@@ -17,6 +17,8 @@ _SUBCOMMANDS = {
                              "generate ground-truth reference/deformed image pair"),
     "analyse-ground-truth": ("voxeldvc_gb300.ground_truth.analyse_ground_truth",
                              "compare recovered vs. ground-truth displacement"),
+    "sweep-ground-truth": ("voxeldvc_gb300.ground_truth.sweep_ground_truth",
+                           "sweep h/l0_factor and score RMS vs. ground truth"),
 }
 
 
