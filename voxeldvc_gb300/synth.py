@@ -107,23 +107,66 @@ class Workload:
     params: list
     noise: float = 0.01
     solve: dict = field(default_factory=dict)
+    storage: str = "f32"  # "u16": both images quantised to 0..65535
 
     @property
     def mesh(self):
         return tuple((s - 1) // self.h for s in self.shape)
 
     def make(self):
-        """(f_pix, g_pix) float32 CUDA tensors in pix[x,y,z] layout."""
+        """(f_pix, g_pix) CUDA tensors in pix[x,y,z] layout: float32, or
+        uint16 counts (texture and noise scaled by 65535) for "u16"."""
         f = texture(self.shape, self.n_cyl)
         g = warp(f, self.shape, self.field, self.params, self.noise)
-        return vox_to_pix(f, self.shape), vox_to_pix(g, self.shape)
+        fp, gp = vox_to_pix(f, self.shape), vox_to_pix(g, self.shape)
+        if self.storage == "u16":
+            fp, gp = _to_u16(fp), _to_u16(gp)
+        return fp, gp
 
     def true_U(self):
-        """True nodal displacement (Ndof,) float64: g(x) = f(x - u(x))."""
+        """True nodal displacement (Ndof,) float64 in the correlation's sense:
+        g(x + U(x)) = f(x).  With g(y) = f(y - u(y)) that is the fixed point
+        U(x) = u(x + U(x)) (a contraction for |grad u| < 1), which differs
+        from u(x) by about |grad u| |u|."""
         Nx, Ny, Nz = self.mesh
         nn = np.arange((Nx + 1) * (Ny + 1) * (Nz + 1))
         X = np.stack([nn % (Nx + 1), (nn // (Nx + 1)) % (Ny + 1), nn // ((Nx + 1) * (Ny + 1))], 1) * float(self.h)
-        return field_at(self.field, self.params, X).reshape(-1)
+        return inverse_field(self.field, self.params, X).reshape(-1)
+
+
+def _to_u16(t):
+    """[0, 1] float32 -> uint16 counts (round to nearest, clamp); int32 where
+    this torch has no uint16 casts (the solver reads either)."""
+    T = D.torch()
+    q = (t * 65535.0).round_().clamp_(0, 65535).to(T.int32)
+    try:
+        return q.to(T.uint16)
+    except (AttributeError, RuntimeError, TypeError):
+        return q
+
+
+def large_1024(seed=5):
+    """1025^3 uint16 pair, 40000 cylinders: an affine map (3 degree rotation
+    about a seeded random axis, 20 vx translation, 0.5 % shear) composed
+    with a sinusoidal field of amplitude 1.5 vx and wavelength 128 vx, noise
+    1 % of the range; h = 8 (128^3 elements, 6,440,067 dof), 4-level
+    pyramid (scales 3, 2, 1, 0) seeded by the FFT shift and the affine
+    prealign, Laplacian regulariser l0 = 4.5 h, precision form."""
+    rng = np.random.default_rng(seed)
+    axis = rng.standard_normal(3)
+    axis /= np.linalg.norm(axis)
+    th = np.deg2rad(3.0)
+    Kx = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    R = np.eye(3) + np.sin(th) * Kx + (1 - np.cos(th)) * Kx @ Kx
+    shear = np.zeros((3, 3))
+    shear[0, 2] = 0.005
+    G = R + shear - np.eye(3)
+    t = 20.0 * axis[[1, 2, 0]] / np.linalg.norm(axis)
+    c = 512.0
+    params = [*t, *G.reshape(-1), c, c, c, 1.5, 128.0]
+    return Workload("affine_sin_1025^3_h8_u16", (1025, 1025, 1025), 8, 40000, FIELD_AFFINE_SIN, params, noise=0.01,
+                    solve=dict(reg_type='laplacian', l0=4.5 * 8, scales=(3, 2, 1, 0), prealign_affine=True,
+                               precision="mixed"), storage="u16")
 
 
 def plain_small():
@@ -197,6 +240,19 @@ def series_385(n_steps=16, seed=3):
     return vox_to_pix(f, shape), gs, problems, fields
 
 
+def inverse_field(kind, params, X, iters=60, tol=1e-10):
+    """U at points X with U = u(X + U): the displacement a correlation of
+    f against g(y) = f(y - u(y)) recovers (fixed-point iteration)."""
+    U = field_at(kind, params, X)
+    for _ in range(iters):
+        U_new = field_at(kind, params, X + U)
+        done = np.max(np.abs(U_new - U)) < tol
+        U = U_new
+        if done:
+            break
+    return U
+
+
 def true_U_problem(problem, field):
     """True nodal displacement of a series problem (ROI frame)."""
     kind, params = field
@@ -205,11 +261,11 @@ def true_U_problem(problem, field):
     o = np.asarray(problem["origin"], np.float64)
     nn = np.arange((Nx + 1) * (Ny + 1) * (Nz + 1))
     X = np.stack([nn % (Nx + 1), (nn // (Nx + 1)) % (Ny + 1), nn // ((Nx + 1) * (Ny + 1))], 1) * float(h) + o
-    return field_at(kind, params, X).reshape(-1)
+    return inverse_field(kind, params, X).reshape(-1)
 
 
 WORKLOADS = {"plain_small": plain_small, "necking_512": necking_512, "necking_512_eqgap": necking_512_eqgap,
-             "necking_256": necking_256}
+             "necking_256": necking_256, "large_1024": large_1024}
 
 
 # ---- known-answer (ground-truth) stand-ins ---------------------------------
