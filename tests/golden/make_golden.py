@@ -6,8 +6,8 @@ Run in a checkout where the reference source is available:
     PYTHONPATH=/root/reference/src python tests/golden/make_golden.py
 
 Each .npz stores the seeded inputs together with the reference outputs, so
-the tests (and the GPU machine, which has no copy of the reference) replay the
-exact same cases.  The reference cannot be imported at test time.
+the tests replay the exact same cases on machines without a copy of the
+reference.  The reference cannot be imported at test time.
 """
 from __future__ import annotations
 
