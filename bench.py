@@ -67,7 +67,7 @@ def parse(argv=None):
                    help="element layers per CPU-baseline worker (default: the whole mesh split over the cores)")
     p.add_argument("--no-forms", action="store_true",
                    help="skip the precision / learned-seed form comparison (FP64 reference solve included)")
-    p.add_argument("--only", default=None, choices=[None, "matvec", "kernels", "ground-truth", "post", "eh-form"],
+    p.add_argument("--only", default=None, choices=[None, "matvec", "kernels", "ground-truth", "post", "eh-form", "learned"],
                    help="matvec: time only the finest-level Hessian matvec; kernels: run each hot kernel of the "
                         "plain, precision and learned forms a few times on the 257^3 case (the profiling commands)")
     return p.parse_args(argv)
@@ -640,6 +640,36 @@ def kernels_only(args):
     print(json.dumps({"kernels": "done", "reps": reps, "workload": wl.name}))
 
 
+def learned_only(args):
+    """The learned seed + precision form solve of the workload, --warmup
+    untimed and --steps timed runs (device-resident inputs), with the GN
+    log of the last run: the command behind the launch-list profile of the
+    target form."""
+    import torch
+    from voxeldvc_gb300 import synth
+    from voxeldvc_gb300.learned import solve as LS
+    wl = synth.WORKLOADS[args.workload]()
+    Nx, Ny, Nz = wl.mesh
+    f_pix, g_pix = wl.make()
+    kwl = {k: v for k, v in solve_kwargs(wl).items() if k not in ("scales", "fft_prealign")}
+    net = LS.default_net()
+    ts, st = [], []
+    for i in range(args.warmup + args.steps):
+        st = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        U, _, _ = LS.learned_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, torch, net=net, precision="mixed",
+                                           stats=st, **kwl)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - t0)
+    gn = [s for s in st if "gn_iters" in s]
+    err = (U.double().cpu().numpy() - wl.true_U()).reshape(-1, 3)
+    print(json.dumps({"learned_mixed_s": round(float(np.median(ts)), 4), "workload": wl.name,
+                      "gn_iters": [s["gn_iters"] for s in gn], "pcg_iters": [s["pcg_iters"] for s in gn],
+                      "rms_vs_true_field_vx": round(float(np.sqrt(np.mean(err ** 2))), 5)}))
+
+
 def eh_form_only(args):
     """The precision form's Hessian matvec (BF16 conversion + element-Hessian
     formation + matvec + gather) on the workload's finest level with each
@@ -781,6 +811,8 @@ def main():
         post_only(args)
     elif args.only == "eh-form":
         eh_form_only(args)
+    elif args.only == "learned":
+        learned_only(args)
     else:
         gpu_arm(args)
 
