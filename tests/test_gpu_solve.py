@@ -145,3 +145,26 @@ def test_persistent_pcg_matches_graph(api, monkeypatch):
     assert st_p[0]["h"] == 2
     assert rms(Up, Ug) < 1e-4
     assert rms(Up, c["U"]) < RMS_TOL
+
+
+@pytest.mark.parametrize("h", [1, 2, 3, 4])
+@pytest.mark.parametrize("dynamic", [False, True])
+def test_small_h_gn_iterations(api, h, dynamic):
+    """Two GN iterations at element edges of 1-4 voxels, where the residual /
+    b / diag pass runs one thread per element, against the oracle: U, the
+    last residual field and the last step (FP32 vs the oracle's FP32 run)."""
+    CG, G = api
+    from scipy import ndimage
+    from oracle import dvc_oracle as O
+    n = 6 * h + 1
+    rng = np.random.default_rng(40 + h)
+    f = ndimage.gaussian_filter(rng.random((n, n, n)), 1.2).astype(np.float32)
+    f = (f - f.min()) / (f.max() - f.min()) + np.float32(0.05)
+    g = ndimage.shift(f, (0.4, -0.3, 0.25), order=1, mode='nearest').astype(np.float32)
+    kw = dict(l0=4.5 * h, maxiter=2, eps=1e-6, dynamic_mask=dynamic, freeze_mask_after=1 if dynamic else None)
+    U, res, dU = CG.correlate_gpu(f, g, 6, 6, 6, h, xp=np, K_ref_laplacian=G.build_K_ref_laplacian(), disp=False,
+                                  **kw)
+    Uo, reso, dUo = O.correlate(f, g, 6, 6, 6, h, K_lap=O.k_ref_laplacian(), **kw)
+    assert rms(U, Uo) < 1e-4
+    assert rms(dU, dUo) < 1e-4
+    assert np.abs(res - reso).max() < 1e-3

@@ -13,6 +13,8 @@
 // no contraction); b accumulates w m res N (x) grad as in compute_b_gpu
 // (:341-378), diag H accumulates w m N^2 grad_k^2 (kernels_dvc.py:509-543).
 // The displayed std(res) sums go through a deterministic grid reduction.
+#include <stdlib.h>
+
 #include "ops.cuh"
 
 namespace vdvc {
@@ -203,8 +205,156 @@ __global__ void __launch_bounds__(128, 6) k_strip_rhs_fast(const StripArgs<float
     for (int q = 0; q < 3; ++q) a.dstats[q] = out[q];
 }
 
+// Thread-per-element form of the same pass for small element edges (H <= 4),
+// where an element's few voxels cannot amortise a strip block's staging and
+// shared-memory reduction (the Hessian pass splits the same way,
+// elem_fast.cu).  Element (i,j,k) owns the voxels of elem_fast.cu; a thread
+// keeps its element's 24 b sums (and 24 diag sums) in registers, walks the
+// voxels row by row (x fastest) and writes the sums coalesced to [24][Ne].
+// Residual values are computed exactly as above; the per-element float
+// partials of the displayed sums are folded into float64 per element.
+template <int H, bool DG>
+__global__ void __launch_bounds__(256) k_elem_rhs(const StripArgs<float> a) {
+  __shared__ double s_red[8];
+  const Mesh& m = a.m;
+  float gm, ratio, mean0;
+  {
+    const double c = a.gstats[0];
+    double mean = 0.0, sd = 0.0;
+    if (c >= 1.0) {
+      mean = a.gstats[1] / c;
+      const double var = a.gstats[2] / c - mean * mean;
+      sd = sqrt(var > 0.0 ? var : 0.0);
+    }
+    if (sd == 0.0 && threadIdx.x == 0 && blockIdx.x == 0) *a.status = VDVC_ERR_ZERO_DIVISION;
+    gm = (float)mean;
+    ratio = (float)(-(a.std0 / sd));
+    mean0 = (float)a.mean0;
+  }
+  double dsum[3] = {0.0, 0.0, 0.0};
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m.Ne;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % m.Nx);
+    const long long rr = e / m.Nx;
+    const int j = (int)(rr % m.Ny), k = (int)(rr / m.Ny);
+    float o[2][2][2][3], od[2][2][2][3];
+#pragma unroll
+    for (int q = 0; q < 24; ++q) {
+      (&o[0][0][0][0])[q] = 0.f;
+      (&od[0][0][0][0])[q] = 0.f;
+    }
+    const bool x_last = (i == m.Nx - 1), y_last = (j == m.Ny - 1), z_last = (k == m.Nz - 1);
+    const float wx_first = (i == 0) ? 0.5f : 1.f;
+    const float wy_first = (j == 0) ? 0.5f : 1.f;
+    const float wz_first = (k == 0) ? 0.5f : 1.f;
+    float ds0 = 0.f, ds1 = 0.f, ds2 = 0.f;
+#pragma unroll(H <= 2 ? H + 1 : 1)
+    for (int qz = 0; qz <= H; ++qz) {
+      if (qz == H && !z_last) break;
+      const float fz1 = (float)qz / (float)H, fz0 = 1.f - fz1;
+      const float wz = (qz == 0) ? wz_first : (qz == H ? 0.5f : 1.f);
+      const int mz = (qz == 0 && k > 0) ? 2 : 1;
+#pragma unroll
+      for (int qy = 0; qy <= H; ++qy) {
+        if (qy == H && !y_last) break;
+        const float fy1 = (float)qy / (float)H, fy0 = 1.f - fy1;
+        const float wyz = wz * ((qy == 0) ? wy_first : (qy == H ? 0.5f : 1.f));
+        const int myz = mz * ((qy == 0 && j > 0) ? 2 : 1);
+        const long long vrow =
+            (long long)i * H + (long long)(j * H + qy) * m.Nvx + (long long)(k * H + qz) * m.NvxNvy;
+        float A[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+        float Dd[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+#pragma unroll
+        for (int qx = 0; qx <= H; ++qx) {
+          if (qx == H && !x_last) break;
+          const float fx1 = (float)qx / (float)H, fx0 = 1.f - fx1;
+          const float w = wyz * ((qx == 0) ? wx_first : (qx == H ? 0.5f : 1.f));
+          const long long vv = vrow + qx;
+          const float g0 = __ldg(a.grad + 3 * vv), g1 = __ldg(a.grad + 3 * vv + 1), g2 = __ldg(a.grad + 3 * vv + 2);
+          const float fv = __ldg(a.f + vv), gv = __ldg(a.gvals + vv);
+          const bool mk = __ldg(a.mask + vv) != 0, lv = __ldg(a.live + vv) != 0;
+          const float fc = rsub(fv, mean0);
+          const float rv = radd(rmul(rsub(gv, gm), ratio), fc);
+          const float r = mk ? rv : 0.f;
+          a.res_out[vv] = r;
+          if (lv) {
+            const float mf = (float)(myz * ((qx == 0 && i > 0) ? 2 : 1));
+            ds0 += mf;
+            ds1 += mf * r;
+            ds2 += mf * r * r;
+          }
+          const float rw = r * w;
+          const float t0 = rw * g0, t1 = rw * g1, t2 = rw * g2;
+          A[0][0] += fx0 * t0; A[0][1] += fx0 * t1; A[0][2] += fx0 * t2;
+          A[1][0] += fx1 * t0; A[1][1] += fx1 * t1; A[1][2] += fx1 * t2;
+          if constexpr (DG) {
+            const float w0 = w * fx0 * fx0, w1 = w * fx1 * fx1;
+            const float d0 = mk ? g0 * g0 : 0.f, d1 = mk ? g1 * g1 : 0.f, d2 = mk ? g2 * g2 : 0.f;
+            Dd[0][0] += w0 * d0; Dd[0][1] += w0 * d1; Dd[0][2] += w0 * d2;
+            Dd[1][0] += w1 * d0; Dd[1][1] += w1 * d1; Dd[1][2] += w1 * d2;
+          }
+        }
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            o[0][0][dx][c] += (fz0 * fy0) * A[dx][c];
+            o[0][1][dx][c] += (fz0 * fy1) * A[dx][c];
+            o[1][0][dx][c] += (fz1 * fy0) * A[dx][c];
+            o[1][1][dx][c] += (fz1 * fy1) * A[dx][c];
+            if constexpr (DG) {
+              od[0][0][dx][c] += (fz0 * fz0 * fy0 * fy0) * Dd[dx][c];
+              od[0][1][dx][c] += (fz0 * fz0 * fy1 * fy1) * Dd[dx][c];
+              od[1][0][dx][c] += (fz1 * fz1 * fy0 * fy0) * Dd[dx][c];
+              od[1][1][dx][c] += (fz1 * fz1 * fy1 * fy1) * Dd[dx][c];
+            }
+          }
+      }
+    }
+    dsum[0] += (double)ds0;
+    dsum[1] += (double)ds1;
+    dsum[2] += (double)ds2;
+#pragma unroll
+    for (int ca = 0; ca < 8; ++ca) {
+      const int adx = corner_dx(ca), ady = corner_dy(ca), adz = corner_dz(ca);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a.evA[(long long)(3 * ca + c) * m.Ne + e] = o[adz][ady][adx][c];
+        if constexpr (DG) a.evD[(long long)(3 * ca + c) * m.Ne + e] = od[adz][ady][adx][c];
+      }
+    }
+  }
+  double b3[3], out[3];
+  for (int q = 0; q < 3; ++q) b3[q] = block_sum(dsum[q], s_red);
+  if (grid_reduce_sum<3>(a.red, b3, out, s_red) && threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q) a.dstats[q] = out[q];
+}
+
+// Element edges up to this one take the thread-per-element form, unless
+// VDVC_HV_KERNEL=strip asks for strip kernels at every h.
+constexpr int kElemRhsMaxH = 4;
+
+static bool elem_rhs_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char* e = getenv("VDVC_HV_KERNEL");
+    on = (e && e[0] == 's') ? 0 : 1;
+  }
+  return on == 1;
+}
+
 template <int H, bool DG>
 static int launch_rh(const StripArgs<float>& args, cudaStream_t s) {
+  if constexpr (H <= kElemRhsMaxH) {
+    if (elem_rhs_enabled()) {
+      // at most kReduceBlocks blocks: the reduction partials hold that many
+      long long nb = (args.m.Ne + 255) / 256;
+      if (nb > kReduceBlocks) nb = kReduceBlocks;
+      k_elem_rhs<H, DG><<<(unsigned)nb, 256, 0, s>>>(args);
+      VDVC_LAUNCHED();
+      return VDVC_OK;
+    }
+  }
   constexpr int EX = (H >= 128) ? 1 : 128 / H;
   const int threads = (EX * H + 31) / 32 * 32;
   const size_t smem = (size_t)threads * 25 * (DG ? 2 : 1) * sizeof(float);

@@ -326,7 +326,7 @@ static int hv_kernel_choice() {
     if (e && e[0] == 't') choice = 1;
     if (e && e[0] == 'g') choice = 2;
     if (e && e[0] == 'e') choice = 3;  // thread per element wherever specialised
-    if (e && e[0] == 's') choice = 4;  // strip kernels at every h
+    if (e && e[0] == 's') choice = 4;  // strip kernels at every h (the residual pass too, rhs_fast.cu)
   }
   return choice;
 }
