@@ -6,6 +6,7 @@
 // The sampling kernels use the element-strip decomposition of strip.cuh so
 // the nodal field of a strip is staged once in shared memory and
 // interpolated separably per voxel column.
+#include <stdlib.h>
 #include <type_traits>
 
 #include "ops.cuh"
@@ -220,6 +221,128 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 6 : 6) : 3) k_s
   }
 }
 
+// Thread-per-element form of the GN sampling pass (float32, stats fused) for
+// small element edges (H <= 4), where an element's few voxels cannot
+// amortise a strip block's staging: a thread holds its element's 24 nodal
+// values, interpolates u with the strip kernel's operation order (x first,
+// then z, then y in difference form) and walks the owned voxels (the
+// ownership of elem_fast.cu).  Per-element float partials of the stats are
+// folded into float64 per element.
+template <int H>
+__global__ void __launch_bounds__(256) k_elem_sample(const SampleArgs<float> a) {
+  __shared__ double s_red[8];
+  const Mesh& m = a.m;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const float gxmax = (float)(a.gnx - 1), gymax = (float)(a.gny - 1), gzmax = (float)(a.gnz - 1);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m.Ne;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % m.Nx);
+    const long long rr = e / m.Nx;
+    const int j = (int)(rr % m.Ny), k = (int)(rr / m.Ny);
+    float uc[2][2][2][3];  // [dx][dy][dz][c]
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy) {
+        const long long n0 = (long long)i + (long long)(j + dy) * m.Nnx + (long long)(k + dz) * m.NnxNny;
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) uc[dx][dy][dz][c] = __ldg(a.U + 3 * (n0 + dx) + c);
+      }
+    const int nx_e = H + (i == m.Nx - 1), ny_e = H + (j == m.Ny - 1), nz_e = H + (k == m.Nz - 1);
+    float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f;
+#pragma unroll 1
+    for (int qx = 0; qx < nx_e; ++qx) {
+      const int x = i * H + qx;
+      const float fx1 = (float)qx / (float)H, fx0 = 1.f - fx1;
+      const int mx = (qx == 0 && i > 0) ? 2 : 1;
+      float ux[12];
+#pragma unroll
+      for (int ay = 0; ay < 2; ++ay)
+#pragma unroll
+        for (int az = 0; az < 2; ++az)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            ux[ay * 6 + az * 3 + c] = fx0 * uc[0][ay][az][c] + fx1 * uc[1][ay][az][c];
+      const float vxf = (float)x;
+#pragma unroll
+      for (int qz = 0; qz <= H; ++qz) {
+        if (qz == nz_e) break;
+        const float fz1 = (float)qz / (float)H, fz0 = 1.f - fz1;
+        const int mxz = mx * ((qz == 0 && k > 0) ? 2 : 1);
+        float u0[3], du[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          u0[c] = fz0 * ux[0 * 6 + 0 * 3 + c] + fz1 * ux[0 * 6 + 1 * 3 + c];
+          du[c] = fz0 * ux[1 * 6 + 0 * 3 + c] + fz1 * ux[1 * 6 + 1 * 3 + c] - u0[c];
+        }
+        const int vz = k * H + qz;
+        const float vzf = (float)vz;
+#pragma unroll
+        for (int qy = 0; qy <= H; ++qy) {
+          if (qy == ny_e) break;
+          const float fy1 = (float)qy / (float)H;
+          const int vy = j * H + qy;
+          const unsigned vv = (unsigned)x + (unsigned)vy * (unsigned)m.Nvx + (unsigned)vz * (unsigned)m.NvxNvy;
+          const float ua = u0[0] + fy1 * du[0], ub = u0[1] + fy1 * du[1], ucz = u0[2] + fy1 * du[2];
+          // (u + x) - g_origin, then bounds, clip and order-1 sampling
+          // (engine/correlate_gpu.py:259-276), as in k_sample
+          const float cx = (ua + vxf) - a.gx0, cy = (ub + (float)vy) - a.gy0, cz = (ucz + vzf) - a.gz0;
+          const float ccx = fminf(fmaxf(cx, 0.f), gxmax), ccy = fminf(fmaxf(cy, 0.f), gymax);
+          const float ccz = fminf(fmaxf(cz, 0.f), gzmax);
+          const bool inb = (ccx == cx) & (ccy == cy) & (ccz == cz);
+          const float gv = trilinear(a.g, a.gnx, a.gny, a.gnz, ccx, ccy, ccz);
+          const bool m0 = a.mask0 ? (a.mask0[vv] != 0) : true;
+          const bool mk = inb && m0 && (gv > a.glt);
+          a.gvals[vv] = gv;
+          a.mask_out[vv] = mk ? 1 : 0;
+          if (a.freeze_out) a.freeze_out[vv] = mk ? 1 : 0;
+          const bool bm = a.bmask_frozen ? (a.bmask_frozen[vv] != 0) : mk;
+          if (bm) {
+            const float mult = (float)(mxz * ((qy == 0 && j > 0) ? 2 : 1));
+            r0 += mult;
+            r1 += mult * gv;
+            r2 += mult * gv * gv;
+          }
+          r3 += mk ? 1.f : 0.f;
+        }
+      }
+    }
+    acc[0] += r0;
+    acc[1] += r1;
+    acc[2] += r2;
+    acc[3] += r3;
+  }
+  double b4[4], o4[4];
+  for (int q = 0; q < 4; ++q) b4[q] = block_sum(acc[q], s_red);
+  if (grid_reduce_sum<4>(a.red, b4, o4, s_red) && threadIdx.x == 0)
+    for (int q = 0; q < 4; ++q) a.stats[q] = o4[q];
+}
+
+// Element edges up to this one take the thread-per-element GN sampler,
+// unless VDVC_HV_KERNEL=strip asks for strip kernels at every h.
+constexpr int kElemSampleMaxH = 4;
+
+static bool elem_sample_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char* e = getenv("VDVC_HV_KERNEL");
+    on = (e && e[0] == 's') ? 0 : 1;
+  }
+  return on == 1;
+}
+
+template <int H>
+static int launch_elem_sample(const SampleArgs<float>& a, cudaStream_t s) {
+  // at most kReduceBlocks blocks: the reduction partials hold that many
+  long long nb = (a.m.Ne + 255) / 256;
+  if (nb > kReduceBlocks) nb = kReduceBlocks;
+  k_elem_sample<H><<<(unsigned)nb, 256, 0, s>>>(a);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
 template <typename T, bool STATS, bool INTERP>
 int launch_sample(const SampleArgs<T>& args, cudaStream_t s) {
   if (args.m.h > 128) return set_error(VDVC_ERR_UNSUPPORTED, "element edge h=%d > 128 not supported", args.m.h);
@@ -230,6 +353,16 @@ int launch_sample(const SampleArgs<T>& args, cudaStream_t s) {
   const size_t smem = ((size_t)sh.EX * 24 + args.m.h + 2) * sizeof(T);
   SampleArgs<T> a = args;
   a.EX = sh.EX;
+  if constexpr (std::is_same<T, float>::value && STATS && !INTERP) {
+    if (args.m.h <= kElemSampleMaxH && elem_sample_enabled()) {
+      switch (args.m.h) {
+        case 1: return launch_elem_sample<1>(a, s);
+        case 2: return launch_elem_sample<2>(a, s);
+        case 3: return launch_elem_sample<3>(a, s);
+        case 4: return launch_elem_sample<4>(a, s);
+      }
+    }
+  }
   if constexpr (std::is_same<T, float>::value) {
     switch (args.m.h) {
       case 2: k_sample<T, STATS, INTERP, 2><<<grid, sh.threads, smem, s>>>(a); VDVC_LAUNCHED(); return VDVC_OK;
