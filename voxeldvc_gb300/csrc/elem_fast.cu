@@ -227,6 +227,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err, unsign
 __device__ __forceinline__ double all_blocks_sum(const double* partials, int slot, unsigned int nb, double* s_red,
                                                  double* s_bc) {
   double v = 0.0;
+#pragma unroll 4
   for (unsigned int b = threadIdx.x; b < nb; b += blockDim.x) v += __ldcg(partials + (size_t)slot * nb + b);
   v = block_sum(v, s_red);
   if (threadIdx.x == 0) *s_bc = v;

@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(256) k_gn_gather_rhs(const Mesh m, const T* __
   if (s_last) {
     __threadfence();
     double v = 1.0e300;
+#pragma unroll 4
     for (unsigned int q = threadIdx.x; q < nb; q += blockDim.x) v = fmin(v, __ldcg(red.partials + q));
     v = block_min(v, s_red);
     if (threadIdx.x == 0) {
@@ -320,6 +321,13 @@ static bool use_persistent(GnSolver<T>* S) {
     const bool want = S->d.pcg_chunk < 0 || (e && e[0] == 'p');
     return want && !S->mixed && S->m.h <= 2 && !(S->d.reg_type == VDVC_REG_EQUILIBRIUM_GAP && S->d.ll != 0.0);
   }
+}
+
+// VDVC_PCG=eager: the PCG iterations are launched from the host instead of
+// the graph (a profiling mode: every kernel is a separate stream launch).
+static bool eager_pcg() {
+  const char* e = getenv("VDVC_PCG");
+  return e && e[0] == 'e';
 }
 
 template <typename T>
@@ -681,6 +689,19 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
       }
     }
   }
+  if (!ran && eager_pcg()) {
+    // the same iteration kernels launched from the host, so that a profiler
+    // sees each launch; the device state is read every 16 iterations
+    ran = true;
+    for (int it = 0; it < max_iter; ++it) {
+      if ((st = pcg_iteration<T>(S, s))) return st;
+      if ((it & 15) == 15 || it == max_iter - 1) {
+        VDVC_CUDA(cudaMemcpyAsync(S->h_pcg, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
+        VDVC_CUDA(cudaStreamSynchronize(s));
+        if (S->h_pcg->done) break;
+      }
+    }
+  }
   if (!ran) {
     if (!S->gexec && (st = build_graph<T>(S))) return st;
     if (max_iter > 0) VDVC_CUDA(cudaGraphLaunch(S->gexec, s));
@@ -690,7 +711,7 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   const PcgState& fin = S->h_pcg[0];
   if (ran && fin.status == VDVC_ERR_CUDA)
     return set_error(VDVC_ERR_CUDA, "persistent PCG: a grid barrier timed out");
-  if (max_iter > 0 && !ran) {
+  if (max_iter > 0 && !ran && S->gexec) {
     // body executions = ceil(iter / chunk); each runs chunk iterations' kernels + the continue kernel
     const long long bodies = (fin.iter + S->chunk - 1) / S->chunk;
     count_launch(bodies * ((long long)S->chunk * S->kernels_per_iter + 1));
