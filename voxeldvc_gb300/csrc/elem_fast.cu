@@ -152,7 +152,10 @@ __device__ __forceinline__ void elem_hv_body(const StripArgs<float>& a, const Kp
 }
 
 template <int H, bool PCG>
-__global__ void __launch_bounds__(256) k_elem_hv(const StripArgs<float> a, const Kpair<float>* __restrict__ kp) {
+// 128-thread blocks; at H <= 2 capped at 96 registers, 5 blocks (20 warps)
+// per SM without spills, against 16 warps at 128 registers (H >= 3 spills
+// under that cap and keeps 128).
+__global__ void __launch_bounds__(128, H <= 2 ? 5 : 4) k_elem_hv(const StripArgs<float> a, const Kpair<float>* __restrict__ kp) {
   if constexpr (PCG) {
     if (a.st->done) return;
   }
@@ -365,9 +368,9 @@ int launch_pcg_persistent(const PcgPersistArgs& a, int max_blocks, cudaStream_t 
 
 template <int H, bool PCG>
 static int launch_e(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s) {
-  const long long nb = (args.m.Ne + 255) / 256;
+  const long long nb = (args.m.Ne + 127) / 128;
   if (nb > 0x7fffffffLL) return set_error(VDVC_ERR_ARG, "too many elements");
-  k_elem_hv<H, PCG><<<(unsigned)nb, 256, 0, s>>>(args, kp);
+  k_elem_hv<H, PCG><<<(unsigned)nb, 128, 0, s>>>(args, kp);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }

@@ -135,11 +135,12 @@ __global__ void __launch_bounds__(256) k_gn_gather_rhs(const Mesh m, const T* __
   __shared__ double s_red[8];
   const T llT = (T)ll;
   T dmin = T(3.0e38);
+  // 32-bit node coordinates (the solver rejects 2^32 nodes or more)
+  const unsigned int nnx = (unsigned int)m.Nnx, nny = (unsigned int)m.Nny;
   for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < m.Nnodes;
        n += (long long)gridDim.x * blockDim.x) {
-    const int ni = (int)(n % m.Nnx);
-    const long long rr = n / m.Nnx;
-    const int nj = (int)(rr % m.Nny), nk = (int)(rr / m.Nny);
+    const unsigned int nu = (unsigned int)n, rr = nu / nnx;
+    const int ni = (int)(nu - rr * nnx), nj = (int)(rr % nny), nk = (int)(rr / nny);
     T sb[3] = {T(0), T(0), T(0)}, sd[3] = {T(0), T(0), T(0)};
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -370,13 +371,15 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
         ma.K2 = S->kp->K2;  // device address of the float K_el copy
       }
       if ((st = launch_eh_matvec<true>(ma, s))) return st;
-      if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s))) return st;
+      if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s, (long long)S->n_partials)))
+        return st;
       return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
     }
   }
   const StripArgs<T> sa = pcg_strip_args<T>(S);
   if ((st = launch_strip<T, kModeHv | kModePcg>(sa, S->kp, s))) return st;
-  if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s))) return st;
+  if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s, (long long)S->n_partials)))
+    return st;
   return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
 }
 
@@ -444,6 +447,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   if (st) return st;
   VDVC_CHECK_ARG(d->f_vox && d->g_vox && d->grad && d->mask0, "null input pointer");
   VDVC_CHECK_ARG(d->gnx >= 1 && d->gny >= 1 && d->gnz >= 1, "bad g shape");
+  if (m.Nnodes >= (1ll << 32)) return set_error(VDVC_ERR_UNSUPPORTED, "2^32 nodes or more");
   VDVC_CHECK_ARG(d->reg_type >= VDVC_REG_NONE && d->reg_type <= VDVC_REG_EQUILIBRIUM_GAP, "bad reg_type");
   if (d->reg_type != VDVC_REG_NONE) VDVC_CHECK_ARG(d->K_lap != nullptr, "K_lap required");
   if (d->reg_type == VDVC_REG_EQUILIBRIUM_GAP)
@@ -571,7 +575,7 @@ static int frozen_diag(GnSolver<T>* S, cudaStream_t s) {
     if ((st = launch_strip<T, kModeDiag>(a, nullptr, s))) return st;
   }
   GridReduce red{S->partials, S->ticket};
-  k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, kReduceBlocks), 256, 0, s>>>(
+  k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, (long long)S->n_partials), 256, 0, s>>>(
       S->m, S->evD, S->evD, nullptr, S->d.ll, S->d.reg_type != VDVC_REG_NONE ? S->diag_reg_t : nullptr, S->t1,
       S->diag, S->sc, red, true);
   VDVC_LAUNCHED();
@@ -641,7 +645,7 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
     if (S->frozen_set) S->eh_fixed = true;
   }
   GridReduce red{S->partials, S->ticket};
-  k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, kReduceBlocks), 256, 0, s>>>(
+  k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, (long long)S->n_partials), 256, 0, s>>>(
       S->m, S->evA, S->evD, reg ? S->ru : nullptr, d.ll, d.reg_type != VDVC_REG_NONE ? S->diag_reg_t : nullptr, S->b,
       S->diag, S->sc, red, with_diag);
   VDVC_LAUNCHED();

@@ -73,8 +73,9 @@ template <typename T>
 int launch_pcg_init(const T* b, const T* Ax, const T* Minv, long long n, T* r, T* z, T* p, bool p_is_z, T* x0,
                     PcgState* st, GridReduce red, int max_iter, double tol, cudaStream_t s);
 template <typename T>
+// max_blocks: blocks the reduction partials of `red` hold (kReduceBlocks at least)
 int launch_pcg_gather(const Mesh& m, const T* ev, const T* z, T* p, T* Ap, PcgState* st, GridReduce red,
-                      cudaStream_t s);
+                      cudaStream_t s, long long max_blocks = kReduceBlocks);
 template <typename T>
 int launch_pcg_update(const T* p, const T* Ap, const T* Minv, long long n, T* x, T* r, T* z, PcgState* st,
                       GridReduce red, cudaStream_t s);

@@ -70,11 +70,12 @@ __global__ void __launch_bounds__(256) k_pcg_gather(const Mesh m, const T* __res
   if (st->done) return;
   const T beta = (T)st->beta;
   T pap = T(0);
+  // 32-bit node coordinates (the launcher rejects 2^32 nodes or more)
+  const unsigned int nnx = (unsigned int)m.Nnx, nny = (unsigned int)m.Nny;
   for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < m.Nnodes;
        n += (long long)gridDim.x * blockDim.x) {
-    const int ni = (int)(n % m.Nnx);
-    const long long rr = n / m.Nnx;
-    const int nj = (int)(rr % m.Nny), nk = (int)(rr / m.Nny);
+    const unsigned int nu = (unsigned int)n, rr = nu / nnx;
+    const int ni = (int)(nu - rr * nnx), nj = (int)(rr % nny), nk = (int)(rr / nny);
     T s[3] = {T(0), T(0), T(0)};
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -189,8 +190,12 @@ int launch_pcg_init(const T* b, const T* Ax, const T* Minv, long long n, T* r, T
 
 template <typename T>
 int launch_pcg_gather(const Mesh& m, const T* ev, const T* z, T* p, T* Ap, PcgState* st, GridReduce red,
-                      cudaStream_t s) {
-  k_pcg_gather<T><<<vec_blocks(m.Nnodes), 256, 0, s>>>(m, ev, z, p, Ap, st, red);
+                      cudaStream_t s, long long max_blocks) {
+  if (m.Nnodes >= (1ll << 32)) return set_error(VDVC_ERR_UNSUPPORTED, "2^32 nodes or more");
+  // one node per thread where the partials allow it: a capped grid leaves a
+  // few threads with two nodes, which doubles the kernel's critical path
+  k_pcg_gather<T><<<grid_blocks(m.Nnodes, 256, max_blocks > kReduceBlocks ? max_blocks : kReduceBlocks), 256, 0,
+                    s>>>(m, ev, z, p, Ap, st, red);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
@@ -209,9 +214,9 @@ template int launch_pcg_init<float>(const float*, const float*, const float*, lo
 template int launch_pcg_init<double>(const double*, const double*, const double*, long long, double*, double*,
                                      double*, bool, double*, PcgState*, GridReduce, int, double, cudaStream_t);
 template int launch_pcg_gather<float>(const Mesh&, const float*, const float*, float*, float*, PcgState*, GridReduce,
-                                      cudaStream_t);
+                                      cudaStream_t, long long);
 template int launch_pcg_gather<double>(const Mesh&, const double*, const double*, double*, double*, PcgState*,
-                                       GridReduce, cudaStream_t);
+                                       GridReduce, cudaStream_t, long long);
 template int launch_pcg_update<float>(const float*, const float*, const float*, long long, float*, float*, float*,
                                       PcgState*, GridReduce, cudaStream_t);
 template int launch_pcg_update<double>(const double*, const double*, const double*, long long, double*, double*,
