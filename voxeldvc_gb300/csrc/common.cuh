@@ -187,10 +187,9 @@ __device__ bool grid_reduce_sum(const GridReduce& gr, const double (&mine)[NV], 
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
-  // Thread t sums the partials of blocks t, t + blockDim.x, ...: the loads
-  // are coalesced and, unrolled, several are in flight per thread (a
-  // contiguous range per thread serialises one L2 round trip per partial,
-  // which made this tail cost ~6 us on a 805-block grid).
+  // Thread t sums the partials of blocks t, t + blockDim.x, ... (coalesced
+  // loads, a fixed assignment, so the result does not depend on block
+  // arrival order).
   double acc[NV];
 #pragma unroll
   for (int i = 0; i < NV; ++i) acc[i] = 0.0;
