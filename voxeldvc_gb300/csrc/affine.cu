@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256) k_affine_normal(const float* __restrict__
   __threadfence();
   if (threadIdx.x < 90) {
     double t = 0.0;
-#pragma unroll 8  // same summation order; the loads of 8 blocks in flight at once
+#pragma unroll 8  // unrolled; the summation order is unchanged
     for (unsigned int b = 0; b < gridDim.x; ++b) t += __ldcg(red.partials + (size_t)b * 90 + threadIdx.x);
     out90[threadIdx.x] = t;
   }
