@@ -666,7 +666,7 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   int st = launch_pcg_init<T>(S->b, nullptr, S->Minv, S->m.Ndof, S->r, S->z, S->p, false, S->x, S->pcg, red,
                               max_iter, tol, s);
   if (st) return st;
-  bool ran = false;
+  bool ran = false, persistent = false;
   if constexpr (std::is_same<T, float>::value) {
     if (max_iter > 0 && use_persistent(S)) {
       PcgPersistArgs pa{};
@@ -687,7 +687,7 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
       VDVC_CUDA(cudaMemsetAsync(S->bar, 0, 4 * sizeof(unsigned int), s));
       st = launch_pcg_persistent(pa, (int)(S->n_partials / 3), s);
       if (st == VDVC_OK) {
-        ran = true;
+        ran = persistent = true;
       } else if (st != VDVC_ERR_UNSUPPORTED) {
         return st;
       }
@@ -713,9 +713,9 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   VDVC_CUDA(cudaMemcpyAsync(S->h_pcg, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
   VDVC_CUDA(cudaStreamSynchronize(s));
   const PcgState& fin = S->h_pcg[0];
-  if (ran && fin.status == VDVC_ERR_CUDA)
+  if (persistent && fin.status == VDVC_ERR_CUDA)
     return set_error(VDVC_ERR_CUDA, "persistent PCG: a grid barrier timed out");
-  if (max_iter > 0 && !ran && S->gexec) {
+  if (max_iter > 0 && !ran) {
     // body executions = ceil(iter / chunk); each runs chunk iterations' kernels + the continue kernel
     const long long bodies = (fin.iter + S->chunk - 1) / S->chunk;
     count_launch(bodies * ((long long)S->chunk * S->kernels_per_iter + 1));
