@@ -5,7 +5,8 @@
 // unrolled, the shape-function weights are constants, the voxel rows are
 // processed in groups whose loads (gradient, f, g(x+u) and the two masks:
 // 7 per row) are issued together, and the register budget is capped at 80
-// so that 6 blocks of 128 threads stay resident per SM.
+// so that 6 blocks of 128 threads stay resident per SM.  Element edges up
+// to 4 voxels take a thread-per-element form of the same pass (k_elem_rhs).
 //
 // Residual (engine/correlate_gpu.py:1091-1105):
 //   res = (f - mean0) - (std0/std1)(g - mean1) on the b mask, 0 elsewhere,

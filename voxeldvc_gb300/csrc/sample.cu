@@ -5,7 +5,8 @@
 //   * u(x) at every voxel (interp_field_vox).
 // The sampling kernels use the element-strip decomposition of strip.cuh so
 // the nodal field of a strip is staged once in shared memory and
-// interpolated separably per voxel column.
+// interpolated separably per voxel column; the GN form at element edges up
+// to 4 voxels runs one thread per element instead (k_elem_sample).
 #include <stdlib.h>
 #include <type_traits>
 
