@@ -608,7 +608,8 @@ def kernels_only(args):
     here a 129^3 h = 2 mesh of 64^3 elements): the matrix-free Hessian pass
     (strip, h = 8; thread per element, h = 2), the precision form's element
     Hessian formation and matvec, one GN iteration's sampling and residual
-    passes, the network's forward pass.  Prints one line per group."""
+    passes (also at the h = 4 and h = 2 levels), the network's forward
+    pass.  Prints one line per group."""
     import torch
     from voxeldvc_gb300 import _lib, synth
     from voxeldvc_gb300.engine import correlate_gpu as CG, kernels_dvc as K, geometry_dvc as G
@@ -634,6 +635,14 @@ def kernels_only(args):
     # one finest-level GN iteration (sampling, residual, b, diag, PCG)
     CG.correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, torch, l0=36.0, K_ref_laplacian=G.build_K_ref_laplacian(),
                      dynamic_mask=True, maxiter=reps, eps=0.0, disp=False)
+    # the same at the pyramid's h = 4 and h = 2 levels (images decimated by 2
+    # and 4, 32^3 elements): the thread-per-element sampling, residual and
+    # Hessian passes
+    for s in (1, 2):
+        d = 2 ** s
+        CG.correlate_gpu(f_pix[::d, ::d, ::d].contiguous(), g_pix[::d, ::d, ::d].contiguous(), Nx, Ny, Nz,
+                         wl.h // d, torch, l0=36.0 / d, K_ref_laplacian=G.build_K_ref_laplacian(),
+                         dynamic_mask=True, maxiter=reps, eps=0.0, disp=False)
     for _ in range(reps):
         LS.learned_seed(f_pix, g_pix, Nx, Ny, Nz, wl.h)
     torch.cuda.synchronize()
