@@ -94,3 +94,65 @@ def test_multiscale_rejects_bad_levels_before_device_work(scales, origin):
     with pytest.raises(ValueError):
         multiscale_correlate_gpu(f, f, 2, 2, 2, 8, xp=np, scales=scales, g_origin=origin,
                                  K_ref_laplacian=G.build_K_ref_laplacian(), l0=36.0, disp=False)
+
+
+def _owner_walk(h, Nx, Ny, Nz):
+    """The voxel walk of the thread-per-element kernels (elem_fast.cu,
+    k_elem_rhs, k_elem_sample): element (i,j,k) visits qx,qy,qz in [0, h),
+    plus q = h on the mesh's last element of an axis; weight 1/2 per axis on
+    the mesh's outer voxel planes; multiplicity 2 per axis on a voxel plane
+    shared with the lower neighbour.  Yields (element, (qx,qy,qz), voxel,
+    weight, multiplicity)."""
+    Nvx, Nvy = Nx * h + 1, Ny * h + 1
+    for k in range(Nz):
+        for j in range(Ny):
+            for i in range(Nx):
+                e = i + j * Nx + k * Nx * Ny
+                for qz in range(h + (k == Nz - 1)):
+                    for qy in range(h + (j == Ny - 1)):
+                        for qx in range(h + (i == Nx - 1)):
+                            w, mult = 1.0, 1
+                            for q, n, idx in ((qx, Nx, i), (qy, Ny, j), (qz, Nz, k)):
+                                if (q == 0 and idx == 0) or q == h:
+                                    w *= 0.5
+                                if q == 0 and idx > 0:
+                                    mult *= 2
+                            v = (i * h + qx) + (j * h + qy) * Nvx + (k * h + qz) * Nvx * Nvy
+                            yield e, (qx, qy, qz), v, w, mult
+
+
+@pytest.mark.parametrize("h", [1, 2, 3, 4])
+def test_owner_walk_equals_reference_quadrature(h):
+    """Visiting each voxel once, by its highest-index element, with the walk's
+    weights gives the same voxel -> node weights as the reference's
+    (element, stencil point) quadrature, which visits shared voxels once per
+    element (kernels_dvc.py:452-506, geometry_dvc.py:26-51); the walk's
+    multiplicities are the reference's visit counts (correlate_gpu.py:97-157)."""
+    Nx, Ny, Nz = 3, 2, 2
+    Nvox = (Nx * h + 1) * (Ny * h + 1) * (Nz * h + 1)
+    Nn = (Nx + 1) * (Ny + 1) * (Nz + 1)
+    N, w = G.build_N_stencil(h)
+    offs = K.get_voxel_offsets(h, Nx, Ny, np)
+    nodes = G.element_node_ids(G.build_node_index(Nx, Ny, Nz), Nx, Ny, Nz)
+    W_ref = np.zeros((Nvox, Nn))
+    visits = np.zeros(Nvox, np.int64)
+    for e in range(Nx * Ny * Nz):
+        v0 = K.get_elem_voxel_origins(np.array([e], np.int32), h, Nx, Ny, np)[0]
+        vox = v0 + offs
+        np.add.at(visits, vox, 1)
+        for a in range(8):
+            np.add.at(W_ref[:, nodes[e, a]], vox, w * N[:, a])
+    W_own = np.zeros((Nvox, Nn))
+    seen = np.zeros(Nvox, np.int64)
+    mults = np.zeros(Nvox, np.int64)
+    for e, (qx, qy, qz), v, wt, mult in _owner_walk(h, Nx, Ny, Nz):
+        seen[v] += 1
+        mults[v] = mult
+        fx, fy, fz = qx / h, qy / h, qz / h
+        for a in range(8):
+            dx, dy, dz = ((a + 1) >> 1) & 1, (a >> 1) & 1, (a >> 2) & 1
+            Na = (fx if dx else 1 - fx) * (fy if dy else 1 - fy) * (fz if dz else 1 - fz)
+            W_own[v, nodes[e, a]] += wt * Na
+    assert np.all(seen == 1)
+    assert np.array_equal(mults, visits)
+    assert np.allclose(W_own, W_ref, rtol=0, atol=1e-14)
