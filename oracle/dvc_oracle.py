@@ -254,7 +254,9 @@ def eh_f16_elements(grad_bf16, mask, h, Nx, Ny, Nz):
     element beyond it), trapezoid halves on the domain faces only, operands
     A = w m g_k g_l x 2^(13 - floor(log2 max g^2)) and P = 256 psi psi psi
     rounded to FP16 from their FP32 values, products summed exactly (float64)
-    and unscaled.  Returns T (Ne, 27, 6): T[e, 9 sx + 3 sy + sz, kl]."""
+    and unscaled.  Returns T (Ne, 27, 6): T[e, 9 sx + 3 sy + sz, kl].  The
+    precision form has no counterpart in the reference; T restates the
+    Hessian of kernels_dvc.py:452-506 element by element."""
     H = h
     g = np.asarray(grad_bf16, np.float32).reshape(-1, 3)
     gm = np.float32(np.abs(g).max()) if g.size else np.float32(0)
@@ -297,7 +299,8 @@ def eh_f16_elements(grad_bf16, mask, h, Nx, Ny, Nz):
 
 def eh_matvec(T, v, Nx, Ny, Nz):
     """H v from element Hessians T (Ne, 27, 6):
-    K_e[(a,k),(b,l)] = T[e, 9 (ax+bx) + 3 (ay+by) + (az+bz), kl(k,l)]."""
+    K_e[(a,k),(b,l)] = T[e, 9 (ax+bx) + 3 (ay+by) + (az+bz), kl(k,l)]; the
+    assembly of kernels_dvc.py:452-506 with stored element matrices."""
     out = np.zeros(v.shape[0])
     for e in range(Nx * Ny * Nz):
         d = elem_dofs(np.array([e]), Nx, Ny)[0]
@@ -724,6 +727,8 @@ def sample_deformed(U, g_pix, h, Nx, Ny, Nz, g_origin=(0, 0, 0), mask0=None, glt
 # ----------------------------------------------------------------------------
 
 def fft_rigid_shift(f_pix, g_pix):
+    """Integer rigid shift from the phase correlation of the common crop
+    (correlate_gpu.py:381-414)."""
     f = np.asarray(f_pix)
     g = np.asarray(g_pix)
     shp = tuple(min(a, b) for a, b in zip(f.shape, g.shape))
@@ -745,7 +750,8 @@ def fft_rigid_shift(f_pix, g_pix):
 def correlate(f_pix, g_pix, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_lap=None, reg_exponent=2,
               c_reg=1.0, reg_type='laplacian', K_el=None, eps_reg=1e-3, dynamic_mask=False, freeze_mask_after=None,
               U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000, dtype=np.float32, log=None):
-    """Returns (U, res, dU); `log` (a list) receives one dict per GN iteration."""
+    """The Gauss-Newton driver of correlate_gpu.py:828-1140 on NumPy.
+    Returns (U, res, dU); `log` (a list) receives one dict per GN iteration."""
     Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, Nz * h + 1
     Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
     Nvox = Nvx * Nvy * Nvz
