@@ -23,6 +23,7 @@ _SUBCOMMANDS = {
 
 
 def main(argv=None):
+    """Reference: cli.py:31-57."""
     argv = sys.argv[1:] if argv is None else argv
     parser = argparse.ArgumentParser(
         prog="voxeldvc",

@@ -107,7 +107,8 @@ def _grad_vox(f_vox, shape, dtype, glt=None):
 
 def image_grad_and_values(pix, xp, dtype=np.float32):
     """(f_vox (Nvox,), grad_f_vox (Nvox, 3)): values and xp.gradient of the
-    image, x-fastest voxel order."""
+    image, x-fastest voxel order.
+    Reference: engine/correlate_gpu.py:49-72."""
     dtype = np.dtype(dtype)
     f_vox, shape = pix_to_vox(pix, dtype)
     grad, _ = _grad_vox(f_vox, shape, dtype)
@@ -115,7 +116,8 @@ def image_grad_and_values(pix, xp, dtype=np.float32):
 
 
 def erode_mask0_vox(mask0_vox, Nvx, Nvy, Nvz, xp):
-    """6-neighbour erosion (minimum filter, mode 'nearest') of a voxel mask."""
+    """6-neighbour erosion (minimum filter, mode 'nearest') of a voxel mask.
+    Reference: engine/correlate_gpu.py:75-94."""
     m = D.mask_u8(mask0_vox).reshape(-1)
     if m.numel() != Nvx * Nvy * Nvz:
         raise ValueError("mask size does not match (Nvx, Nvy, Nvz)")
@@ -144,7 +146,8 @@ def _mean_std(c, s1, s2):
 
 def masked_quadpoint_mean_std(field_vox, mask_vox, h, Nx, Ny, Nz, xp, chunk_size=None):
     """Mean and population std of field_vox over the (element, stencil
-    point) array restricted to mask_vox (float64 sums)."""
+    point) array restricted to mask_vox (float64 sums).
+    Reference: engine/correlate_gpu.py:113-157."""
     dt = K._float_dtype(field_vox)
     f = D.to_device(field_vox, dt).reshape(-1)
     m = D.mask_u8(mask_vox).reshape(-1)
@@ -155,7 +158,8 @@ def masked_quadpoint_mean_std(field_vox, mask_vox, h, Nx, Ny, Nz, xp, chunk_size
 def gather_quadpoint_values(field_vox, h, Nx, Ny, Nz, xp):
     """(Ne*(h+1)^3,) per-(element, stencil point) copy of a voxel field.
     A host-side index gather kept for API compatibility (the solve itself
-    never materialises it)."""
+    never materialises it).
+    Reference: engine/correlate_gpu.py:97-110."""
     vals = np.asarray(D.out(D.to_device(field_vox), np)).reshape(-1)
     Ne = Nx * Ny * Nz
     offs = np.asarray(K.get_voxel_offsets(h, Nx, Ny, np))
@@ -165,7 +169,8 @@ def gather_quadpoint_values(field_vox, h, Nx, Ny, Nz, xp):
 
 
 def interp_field_vox(U, N_stencil, h, Nx, Ny, Nz, xp, chunk_size=200_000, channels_first=False):
-    """u(x) = sum_a N_a U_a at every voxel centre: (Nvox, 3) or (3, Nvox)."""
+    """u(x) = sum_a N_a U_a at every voxel centre: (Nvox, 3) or (3, Nvox).
+    Reference: engine/correlate_gpu.py:160-198."""
     dt = K._float_dtype(U)
     Ud = D.to_device(U, dt).reshape(-1)
     Nvox, Ndof = K._mesh_sizes(h, Nx, Ny, Nz)
@@ -193,7 +198,8 @@ def _sample(U, g_vox, gshape, h, Nx, Ny, Nz, g_origin, mask0, glt, dt):
 def sample_deformed_field(U, g_pix_x, N_stencil, h, Nx, Ny, Nz, xp, g_origin=(0, 0, 0), mask0_vox=None,
                           chunk_size=None, glt=0.0):
     """(g_vals, mask_vox): g sampled at x + u(x) (order-1, clipped) and the
-    active mask in_bounds & mask0 & g > glt."""
+    active mask in_bounds & mask0 & g > glt.
+    Reference: engine/correlate_gpu.py:201-281."""
     dt = K._float_dtype(U)
     Ud = D.to_device(U, dt).reshape(-1)
     g_vox, gshape = pix_to_vox(g_pix_x, dt)
@@ -203,14 +209,16 @@ def sample_deformed_field(U, g_pix_x, N_stencil, h, Nx, Ny, Nz, xp, g_origin=(0,
 
 
 def compute_active_mask(U, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0), mask0_vox=None, glt=0.0):
-    """Per-voxel active mask (mask0 & in_bounds(x+u) & g(x+u) > glt)."""
+    """Per-voxel active mask (mask0 & in_bounds(x+u) & g(x+u) > glt).
+    Reference: engine/correlate_gpu.py:284-338."""
     _, mask = sample_deformed_field(U, g_pix, None, h, Nx, Ny, Nz, D.torch(), g_origin=g_origin,
                                     mask0_vox=mask0_vox, glt=glt)
     return D.out(mask, xp)
 
 
 def compute_b_gpu(res_vox, mask_vox, grad_f_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, Ndof, xp, chunk_size=None):
-    """b = sum_e P_e^T sum_q w_q m_q res_q N_q (x) grad f_q."""
+    """b = sum_e P_e^T sum_q w_q m_q res_q N_q (x) grad f_q.
+    Reference: engine/correlate_gpu.py:341-378."""
     K._check_stencil(N_stencil, w_stencil, h)
     Nvox, nd = K._mesh_sizes(h, Nx, Ny, Nz)
     dt = K._float_dtype(grad_f_vox)
@@ -238,7 +246,8 @@ def _fft_shift_vox(f_vox, fshape, g_vox, gshape, dt):
 
 
 def fft_rigid_shift(f_pix, g_pix, xp):
-    """Integer voxel shift d with g(x) ~= f(x - d) by phase correlation."""
+    """Integer voxel shift d with g(x) ~= f(x - d) by phase correlation.
+    Reference: engine/correlate_gpu.py:381-414."""
     f_vox, fs = pix_to_vox(f_pix, np.float64)
     g_vox, gs = pix_to_vox(g_pix, np.float64)
     return _fft_shift_vox(f_vox, fs, g_vox, gs, np.float64)
@@ -483,7 +492,8 @@ def correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0),
                   maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
                   disp=True, dtype=np.float32, **solver_opts):
     """Matrix-free GN-PCG DVC solve of f_pix/g_pix on an (Nx,Ny,Nz) mesh of
-    edge h; returns (U, res, dU) as in the reference."""
+    edge h; returns (U, res, dU) as in the reference.
+    Reference: engine/correlate_gpu.py:828-1140."""
     dtype = np.dtype(dtype)
     f_vox, fs = pix_to_vox(f_pix, dtype)
     g_vox, gs = pix_to_vox(g_pix, dtype)
@@ -515,7 +525,8 @@ def multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, scales=(2, 1, 0),
                              **kwargs):
     """Coarse-to-fine pyramid of correlate_gpu solves (strided decimation by
     2**iscale, fixed element grid, h_i = h / 2**iscale, U carried between
-    levels); returns the finest level's (U, res, dU)."""
+    levels); returns the finest level's (U, res, dU).
+    Reference: engine/correlate_gpu.py:1143-1305."""
     scales = sorted(set(scales), reverse=True)
     dtype = np.dtype(kwargs.get('dtype', np.float32))
     disp = kwargs.get('disp', True)
@@ -642,7 +653,8 @@ def affine_prealign(f_pix, g_pix, xp, decimate=4, t0=None, angle_bound=0.3, scal
     """9-DOF (rotation, per-axis scale, translation) alignment maximising the
     ZNCC of f(x) and g(A (x - c) + c + t) on copies decimated by `decimate`;
     the cost is evaluated on the GPU, the Powell search runs on the host
-    (scipy).  Returns (A, t, c, info) in full-resolution voxel units."""
+    (scipy).  Returns (A, t, c, info) in full-resolution voxel units.
+    Reference: engine/correlate_gpu.py:451-567."""
     from scipy.optimize import minimize
     f_full, fs = pix_to_vox(f_pix, np.float32)
     g_full, gs = pix_to_vox(g_pix, np.float32)
@@ -688,7 +700,8 @@ def affine_refine_gn(f_pix, g_pix, xp, A0, t0, c, sigmas=(4.0, 2.0, 1.0, 0.0), m
     translation in the generative convention def(x) ~ ref(x - M (x - c) - t_r)
     over a Gaussian scale space; each iteration's 12x12 float64 normal
     equations are assembled on the GPU in one pass.  Returns (A, t, info) in
-    the affine_prealign convention.  `chunk_voxels` is accepted and ignored."""
+    the affine_prealign convention.  `chunk_voxels` is accepted and ignored.
+    Reference: engine/correlate_gpu.py:600-825."""
     T = D.torch()
     f, shape = pix_to_vox(f_pix, np.float32)
     g, gshape = pix_to_vox(g_pix, np.float32)

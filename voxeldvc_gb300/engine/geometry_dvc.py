@@ -123,7 +123,8 @@ def build_N_stencil(h: int):
 
 
 def build_node_index(Nx: int, Ny: int, Nz: int) -> np.ndarray:
-    """(Nx+1, Ny+1, Nz+1) array of node ids i + j(Nx+1) + k(Nx+1)(Ny+1)."""
+    """(Nx+1, Ny+1, Nz+1) array of node ids i + j(Nx+1) + k(Nx+1)(Ny+1).
+    Reference: engine/geometry_dvc.py:191-198."""
     i = np.arange(Nx + 1)[:, None, None]
     j = np.arange(Ny + 1)[None, :, None]
     k = np.arange(Nz + 1)[None, None, :]
@@ -131,7 +132,8 @@ def build_node_index(Nx: int, Ny: int, Nz: int) -> np.ndarray:
 
 
 def build_interior_dof_mask(Nx: int, Ny: int, Nz: int) -> np.ndarray:
-    """(Ndof,) bool: dofs of nodes off the outer surface of the mesh."""
+    """(Ndof,) bool: dofs of nodes off the outer surface of the mesh.
+    Reference: engine/geometry_dvc.py:201-217."""
     i = np.arange(Nx + 1)[:, None, None]
     j = np.arange(Ny + 1)[None, :, None]
     k = np.arange(Nz + 1)[None, None, :]
@@ -142,7 +144,8 @@ def build_interior_dof_mask(Nx: int, Ny: int, Nz: int) -> np.ndarray:
 
 def element_node_ids(node_idx: np.ndarray, Nx: int, Ny: int, Nz: int) -> np.ndarray:
     """(Nx*Ny*Nz, 8) node ids per element, element order x fastest, corner
-    order as documented above."""
+    order as documented above.
+    Reference: engine/geometry_dvc.py:220-239."""
     out = np.empty((Nz, Ny, Nx, 8), dtype=node_idx.dtype)
     for a, (dx, dy, dz) in enumerate(CORNERS):
         out[..., a] = np.transpose(node_idx[dx:dx + Nx, dy:dy + Ny, dz:dz + Nz], (2, 1, 0))

@@ -40,7 +40,8 @@ def _index_out(a, xp, like=None):
 
 
 def get_elem_dofs(elem_ids, Nx, Ny, xp):
-    """(chunk, 24) dof ids, node-major with the Hex8 corner order."""
+    """(chunk, 24) dof ids, node-major with the Hex8 corner order.
+    Reference: engine/kernels_dvc.py:32-61."""
     e = _host_index(elem_ids)
     i, j, k = e % Nx, (e // Nx) % Ny, e // (Nx * Ny)
     base = i + j * (Nx + 1) + k * (Nx + 1) * (Ny + 1)
@@ -52,7 +53,8 @@ def get_elem_dofs(elem_ids, Nx, Ny, xp):
 
 
 def get_voxel_offsets(h, Nx, Ny, xp):
-    """((h+1)^3,) flat voxel offsets of the stencil points (meshgrid 'ij')."""
+    """((h+1)^3,) flat voxel offsets of the stencil points (meshgrid 'ij').
+    Reference: engine/kernels_dvc.py:64-78."""
     Nvx, Nvy = Nx * h + 1, Ny * h + 1
     q = np.arange(h + 1, dtype=np.int32)
     offs = (q[:, None, None] + q[None, :, None] * Nvx + q[None, None, :] * (Nvx * Nvy)).reshape(-1)
@@ -60,7 +62,8 @@ def get_voxel_offsets(h, Nx, Ny, xp):
 
 
 def get_elem_voxel_origins(elem_ids, h, Nx, Ny, xp):
-    """Flat voxel index of each element's q = (0,0,0) voxel."""
+    """Flat voxel index of each element's q = (0,0,0) voxel.
+    Reference: engine/kernels_dvc.py:81-89."""
     e = _host_index(elem_ids)
     Nvx, Nvy = Nx * h + 1, Ny * h + 1
     i, j, k = e % Nx, (e // Nx) % Ny, e // (Nx * Ny)
@@ -75,7 +78,8 @@ def get_elem_voxel_origins(elem_ids, h, Nx, Ny, xp):
 # ---------------------------------------------------------------------------
 
 def boundary_element_mask(Nx, Ny, Nz):
-    """(Nx*Ny*Nz,) bool, x-fastest element order: the outer element shell."""
+    """(Nx*Ny*Nz,) bool, x-fastest element order: the outer element shell.
+    Reference: engine/kernels_dvc.py:92-115."""
     i = np.arange(Nx)[None, None, :]
     j = np.arange(Ny)[None, :, None]
     k = np.arange(Nz)[:, None, None]
@@ -102,19 +106,22 @@ def _unsafe_masks(active_vox, h, Nx, Ny, Nz, mask0_vox=None, frac_threshold=0.0,
 
 def compute_unsafe_voxel_mask(active_vox, h, Nx, Ny, Nz):
     """(Nvox,) bool: voxels of every element touching an unsafe node (a node
-    of an element holding an inactive voxel), plus the outer element shell."""
+    of an element holding an inactive voxel), plus the outer element shell.
+    Reference: engine/kernels_dvc.py:166-193."""
     return _unsafe_masks(active_vox, h, Nx, Ny, Nz, vox=True)[0]
 
 
 def compute_unsafe_element_mask(active_vox, h, Nx, Ny, Nz):
     """(Nx*Ny*Nz,) bool, x-fastest: elements touching an unsafe node, plus
-    the outer element shell."""
+    the outer element shell.
+    Reference: engine/kernels_dvc.py:196-213."""
     return _unsafe_masks(active_vox, h, Nx, Ny, Nz, elem=True)[1]
 
 
 def compute_unsafe_node_mask(active_vox, h, Nx, Ny, Nz):
     """((Nx+1)*(Ny+1)*(Nz+1),) bool: nodes of elements holding an inactive
-    voxel, plus the nodes of the outer element shell."""
+    voxel, plus the nodes of the outer element shell.
+    Reference: engine/kernels_dvc.py:216-233."""
     return _unsafe_masks(active_vox, h, Nx, Ny, Nz, node=True)[2]
 
 
@@ -123,13 +130,15 @@ def compute_overlap_lost_element_mask(active_vox, mask0_vox, h, Nx, Ny, Nz, frac
     """(Nx*Ny*Nz,) bool, x-fastest: elements sharing a node with an element
     whose lost material fraction exceeds frac_threshold, elements whose
     material count fraction is below min_material_frac, and the outer
-    element shell."""
+    element shell.
+    Reference: engine/kernels_dvc.py:236-341."""
     return _unsafe_masks(active_vox, h, Nx, Ny, Nz, mask0_vox, frac_threshold, min_material_frac, lost=True)[3]
 
 
 def auto_chunk_size(nq, max_tensor_elems=20_000_000):
     """Element-chunk size of the reference's chunked loops (kept for API
-    compatibility; the kernels here do not chunk)."""
+    compatibility; the kernels here do not chunk).
+    Reference: engine/kernels_dvc.py:444-449."""
     return max(1, max_tensor_elems // (nq * 24))
 
 
@@ -193,7 +202,8 @@ def _E_args(E_elem, Ne, dtype):
 # ---------------------------------------------------------------------------
 
 def matvec_K_ref(v, K_ref, E_elem, Nx, Ny, Nz, xp, chunk_size=500_000):
-    """f = sum_e E_e P_e^T K_ref P_e v (node-centric stencil, no scatter)."""
+    """f = sum_e E_e P_e^T K_ref P_e v (node-centric stencil, no scatter).
+    Reference: engine/kernels_dvc.py:349-374."""
     out_dt = D.np_dtype_of(v)
     dt = _float_dtype(v)
     vd = D.to_device(v, dt).reshape(-1)
@@ -213,7 +223,8 @@ def matvec_K_ref(v, K_ref, E_elem, Nx, Ny, Nz, xp, chunk_size=500_000):
 
 def build_diagonal_K_ref(K_ref, E_elem, Nx, Ny, Nz, Ndof, xp):
     """Diagonal of the K_ref operator (float64, like the reference's
-    np.diag of the float64 K_ref)."""
+    np.diag of the float64 K_ref).
+    Reference: engine/kernels_dvc.py:377-392."""
     Kh, Kp = _kmat(K_ref)
     dt = np.dtype(np.float64)
     Ed, Es = _E_args(E_elem, Nx * Ny * Nz, dt)
@@ -224,7 +235,8 @@ def build_diagonal_K_ref(K_ref, E_elem, Nx, Ny, Nz, Ndof, xp):
 
 
 def matvec_equilibrium_gap(v, K_ref_elastic, interior_mask, E_elem, Nx, Ny, Nz, xp, chunk_size=500_000):
-    """f = K (P_i (K v)), K = sum_e E_e P_e^T K_el P_e."""
+    """f = K (P_i (K v)), K = sum_e E_e P_e^T K_el P_e.
+    Reference: engine/kernels_dvc.py:402-417."""
     out_dt = D.np_dtype_of(v)
     dt = _float_dtype(v, interior_mask) if D.np_dtype_of(interior_mask).kind == 'f' else _float_dtype(v)
     vd = D.to_device(v, dt).reshape(-1)
@@ -285,7 +297,8 @@ def _grad_mask(grad_f_vox, mask0_vox, dt, Nvox):
 
 
 def matvec_H(v, grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, xp, chunk_size=None):
-    """f = H v = sum_e sum_q w_q m_q (v_eq . v_loc) v_eq, matrix-free."""
+    """f = H v = sum_e sum_q w_q m_q (v_eq . v_loc) v_eq, matrix-free.
+    Reference: engine/kernels_dvc.py:452-506."""
     _check_stencil(N_stencil, w_stencil, h)
     Nvox, Ndof = _mesh_sizes(h, Nx, Ny, Nz)
     out_dt = D.np_dtype_of(v)
@@ -324,7 +337,8 @@ def matvec_H_mixed(v, grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz
 
 
 def build_diagonal_H(grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, Ndof, xp, chunk_size=None):
-    """diag(H)[i] = sum over (e,q) touching dof i of w_q m_q v_eq[i]^2."""
+    """diag(H)[i] = sum over (e,q) touching dof i of w_q m_q v_eq[i]^2.
+    Reference: engine/kernels_dvc.py:509-543."""
     _check_stencil(N_stencil, w_stencil, h)
     Nvox, nd = _mesh_sizes(h, Nx, Ny, Nz)
     if nd != Ndof:
@@ -347,7 +361,8 @@ def pcg(matvec, b, M_inv, xp, x0=None, max_iter=1000, tol=1e-8, verbose=False):
     vectors.  The vector updates and the float64 dot products are libvdvc
     kernels; `matvec` is called with CUDA tensors and may return a CUDA
     tensor or anything convertible to one.  Solver objects of this package
-    bypass this loop with their fused, graph-replayed PCG."""
+    bypass this loop with their fused, graph-replayed PCG.
+    Reference: engine/kernels_dvc.py:550-583."""
     dt = _float_dtype(b, M_inv)
     bd = D.to_device(b, dt).reshape(-1)
     Md = D.to_device(M_inv, dt).reshape(-1)

@@ -25,7 +25,8 @@ def push_field_forward(field, U, Nx_e, Ny_e, Nz_e, h, order=1, mode='nearest', c
     """field_pushed(x) = field(x - u(x)) on the (Nvx, Nvy, Nvz) voxel grid.
     order 0 (nearest; for label / mask fields) or 1 (trilinear); mode
     'nearest' clamps out-of-domain lookups to the edge, 'constant' writes
-    cval there.  Returns an array of field's shape and dtype."""
+    cval there.  Returns an array of field's shape and dtype.
+    Reference: engine/write_output.py:571-608."""
     if order not in (0, 1):
         raise ValueError("order must be 0 or 1")
     if mode not in _MODES:
@@ -58,13 +59,15 @@ def push_field_forward(field, U, Nx_e, Ny_e, Nz_e, h, order=1, mode='nearest', c
 
 def push_reference_forward(ref, U, Nx_e, Ny_e, Nz_e, h, xp=np):
     """ref(x - u(x)): the reference image on the deformed image's grid
-    (order 1, mode 'nearest')."""
+    (order 1, mode 'nearest').
+    Reference: engine/write_output.py:611-622."""
     return push_field_forward(ref, U, Nx_e, Ny_e, Nz_e, h, order=1, xp=xp)
 
 
 def compute_zncc(f_flat, g_warped_flat, mask_vox, xp=np):
     """Zero-normalised cross-correlation of f and the warped g over
-    mask_vox, float64 sums; NaN for an empty mask or a zero denominator."""
+    mask_vox, float64 sums; NaN for an empty mask or a zero denominator.
+    Reference: engine/write_output.py:658-690."""
     f = D.to_device(f_flat, np.float64).reshape(-1)
     g = D.to_device(g_warped_flat, np.float64).reshape(-1)
     m = D.mask_u8(mask_vox).reshape(-1)
@@ -115,7 +118,8 @@ def _node_major(U_grid):
 def compute_principal_strains_cell(U_grid, h):
     """Principal small-strain values e1 >= e2 >= e3 at every element
     centroid, from the Hex8 shape-function gradients scaled by 1/h.
-    U_grid: (Nx+1, Ny+1, Nz+1, 3); returns (Nx, Ny, Nz, 3) float64."""
+    U_grid: (Nx+1, Ny+1, Nz+1, 3); returns (Nx, Ny, Nz, 3) float64.
+    Reference: engine/write_output.py:256-281."""
     Nx, Ny, Nz = (int(n) - 1 for n in U_grid.shape[:3])
     U = _node_major(U_grid)
     ps = D.empty(Nx * Ny * Nz * 3, np.float64)
@@ -126,7 +130,8 @@ def compute_principal_strains_cell(U_grid, h):
 
 def compute_equivalent_strain(principal_strains):
     """Von Mises equivalent strain sqrt(2)/3 sqrt((e1-e2)^2 + (e2-e3)^2 +
-    (e3-e1)^2) over the last axis; returns principal_strains.shape[:-1]."""
+    (e3-e1)^2) over the last axis; returns principal_strains.shape[:-1].
+    Reference: engine/write_output.py:284-306."""
     shape = tuple(int(s) for s in principal_strains.shape)
     if shape[-1] != 3:
         raise ValueError("the last axis must hold the three principal strains")
@@ -161,14 +166,16 @@ def _cell_call(ref, res, unsafe, h, Nx, Ny, Nz, glt=0.0, material=False, safe=Fa
 
 def compute_material_cell_mask(ref, h, Nx, Ny, Nz, glt=0.0):
     """Per-element bool mask: mean reference grey level over the element's
-    (h+1)^3 voxels > glt.  Returns (Nx, Ny, Nz)."""
+    (h+1)^3 voxels > glt.  Returns (Nx, Ny, Nz).
+    Reference: engine/write_output.py:309-333."""
     m, _, _, _ = _cell_call(ref, None, None, h, Nx, Ny, Nz, glt=glt, material=True)
     return _cell_grid(m.view(D.torch().bool), Nx, Ny, Nz)
 
 
 def compute_material_cell_mask_eroded(material_cell_mask):
     """One-cell erosion, 26-neighbourhood, the mesh border counting as
-    material (binary_erosion with border_value=1)."""
+    material (binary_erosion with border_value=1).
+    Reference: engine/write_output.py:336-349."""
     Nx, Ny, Nz = (int(n) for n in material_cell_mask.shape)
     m = _flat_x(material_cell_mask, np.uint8)
     out = D.empty(Nx * Ny * Nz, np.uint8)
@@ -179,7 +186,8 @@ def compute_material_cell_mask_eroded(material_cell_mask):
 
 def compute_safe_cell_mask(unsafe_vox, h, Nx, Ny, Nz):
     """Per-element mask, True where none of the element's (h+1)^3 voxels is
-    flagged in unsafe_vox (flat x-fastest, or an (Nvx, Nvy, Nvz) grid)."""
+    flagged in unsafe_vox (flat x-fastest, or an (Nvx, Nvy, Nvz) grid).
+    Reference: engine/write_output.py:352-377."""
     _, s, _, _ = _cell_call(None, None, unsafe_vox, h, Nx, Ny, Nz, safe=True)
     return _cell_grid(s.view(D.torch().bool), Nx, Ny, Nz)
 
@@ -188,14 +196,16 @@ def compute_correlation_quality_cell(res, ref, h, Nx, Ny, Nz):
     """(residual_std_cell, zncc_cell), both (Nx, Ny, Nz): the population std
     of res and the ZNCC of ref and ref - res over each element's active
     voxels (res != 0); NaN below 8 active voxels, and zncc NaN for a zero
-    denominator."""
+    denominator.
+    Reference: engine/write_output.py:380-447."""
     _, _, s, z = _cell_call(ref, res, None, h, Nx, Ny, Nz)
     return _cell_grid(s, Nx, Ny, Nz), _cell_grid(z, Nx, Ny, Nz)
 
 
 def compute_gn_convergence_cell(dU, U, Nx, Ny, Nz):
     """||dU|| / ||U|| over each element's 8 corner nodes (24 DOFs); NaN
-    where ||U|| = 0.  dU, U: flat node-major (Ndof,).  Returns (Nx, Ny, Nz)."""
+    where ||U|| = 0.  dU, U: flat node-major (Ndof,).  Returns (Nx, Ny, Nz).
+    Reference: engine/write_output.py:450-491."""
     d = D.to_device(dU, np.float64).reshape(-1)
     u = D.to_device(U, np.float64).reshape(-1)
     Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)

@@ -38,6 +38,7 @@ DEFAULT_GT_DIR = os.path.join(DEFAULT_WORK_DIR, 'gt_input')
 
 
 def parse_args(argv=None):
+    """Reference: ground_truth/analyse_ground_truth.py:84-91."""
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument('--work-dir', type=str, default=DEFAULT_WORK_DIR, dest='work_dir')
     p.add_argument('--gt-dir', type=str, default=DEFAULT_GT_DIR, dest='gt_dir')
@@ -45,7 +46,8 @@ def parse_args(argv=None):
 
 
 def grid_to_dofs(U_grid):
-    """(nbx, nby, nbz, 3) nodal grid -> flat node-major DOFs U[3 node + c]."""
+    """(nbx, nby, nbz, 3) nodal grid -> flat node-major DOFs U[3 node + c].
+    Reference: ground_truth/analyse_ground_truth.py:94-105."""
     return np.ascontiguousarray(np.transpose(np.asarray(U_grid), (2, 1, 0, 3))).reshape(-1)
 
 
@@ -59,7 +61,8 @@ def _in_bounds_dev(u_gt_vox, g_shape):
 
 
 def voxel_in_bounds(u_gt_vox, g_shape):
-    """(nx, ny, nz) bool: x + u_gt(x) inside the deformed image (g_origin 0)."""
+    """(nx, ny, nz) bool: x + u_gt(x) inside the deformed image (g_origin 0).
+    Reference: ground_truth/analyse_ground_truth.py:108-129."""
     out, shape = _in_bounds_dev(u_gt_vox, g_shape)
     return D.out(out.view(D.torch().bool).view(*shape), np)
 
@@ -67,7 +70,8 @@ def voxel_in_bounds(u_gt_vox, g_shape):
 def node_oob_fraction(u_gt_vox_full, h, nbfx, nbfy, nbfz, g_shape, crop_lo):
     """(nbfx, nbfy, nbfz): per node at crop_lo + (i, j, k) h, the fraction of
     its support box [v - h, v + h] (clamped to the image) whose voxels map
-    outside the deformed image under the known field."""
+    outside the deformed image under the known field.
+    Reference: ground_truth/analyse_ground_truth.py:132-165."""
     inb, (nx, ny, nz) = _in_bounds_dev(u_gt_vox_full, g_shape)
     out = D.empty(nbfx * nbfy * nbfz, np.float64)
     lo = (C.c_longlong * 3)(*(int(x) for x in crop_lo))
@@ -80,7 +84,8 @@ def load_validity_masks(work_dir, Nx_e, Ny_e, Nz_e):
     """(node_masked_out (nbx, nby, nbz), vox_masked_out (Nvx, Nvy, Nvz)) from
     the saved solver masks, or (None, None) when they are absent: voxels
     flagged in unsafe_voxel_mask.npy, and nodes of any element flagged in
-    overlap_lost_element_mask.npy."""
+    overlap_lost_element_mask.npy.
+    Reference: ground_truth/analyse_ground_truth.py:168-201."""
     elem_path = os.path.join(work_dir, 'overlap_lost_element_mask.npy')
     vox_path = os.path.join(work_dir, 'unsafe_voxel_mask.npy')
     if not (os.path.exists(elem_path) and os.path.exists(vox_path)):
@@ -203,6 +208,7 @@ def analyse(work_dir, gt_dir):
 
 
 def main(argv=None):
+    """Reference: ground_truth/analyse_ground_truth.py:204-382."""
     args = parse_args(argv)
     work_dir, gt_dir = os.path.expanduser(args.work_dir), os.path.expanduser(args.gt_dir)
     log_path = os.path.join(work_dir, 'ground_truth_comparison_log.txt')

@@ -34,7 +34,8 @@ DEFAULT_OUTPUT_DIR = os.path.join(os.path.abspath('dvc_elastic_groundtruth'), 'g
 def make_deformed_image(ref, u_gt_vox, xp=np):
     """deformed(x) = ref(x - u(x)) for ref (nx, ny, nz) and u_gt_vox
     (nx, ny, nz, 3), float64; bit-identical to the reference's
-    RegularGridInterpolator evaluation."""
+    RegularGridInterpolator evaluation.
+    Reference: ground_truth/prepare_ground_truth.py:68-90."""
     r = D.to_device(np.ascontiguousarray(ref) if not D.is_tensor(ref) else ref, np.float64)
     u = D.to_device(np.ascontiguousarray(u_gt_vox) if not D.is_tensor(u_gt_vox) else u_gt_vox, np.float64)
     nx, ny, nz = (int(s) for s in r.shape)
@@ -47,7 +48,8 @@ def make_deformed_image(ref, u_gt_vox, xp=np):
 
 
 def make_uniaxial_gt(n, strain):
-    """(n, n, n, 3) field u_x = strain * x, u_y = u_z = 0 on the integer grid."""
+    """(n, n, n, 3) field u_x = strain * x, u_y = u_z = 0 on the integer grid.
+    Reference: ground_truth/prepare_ground_truth.py:93-107."""
     u = np.zeros((n, n, n, 3), dtype=np.float64)
     u[..., 0] = strain * np.arange(n, dtype=np.float64)[:, None, None]
     return u
@@ -62,6 +64,7 @@ def gt_at_voxels(u_gt, shape):
 
 
 def parse_args(argv=None):
+    """Reference: ground_truth/prepare_ground_truth.py:110-138."""
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument('--gt-ref-file', type=str, default=DEFAULT_GT_REF_FILE, dest='gt_ref_file')
     g = p.add_mutually_exclusive_group()
@@ -73,6 +76,7 @@ def parse_args(argv=None):
 
 
 def main(argv=None):
+    """Reference: ground_truth/prepare_ground_truth.py:141-226."""
     args = parse_args(argv)
     out_dir = os.path.expanduser(args.output_dir)
     ref_file = os.path.expanduser(args.gt_ref_file)

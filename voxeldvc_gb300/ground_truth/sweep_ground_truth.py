@@ -36,6 +36,7 @@ FIELDS = ['h', 'l0_factor', 'l0', 'n_recoverable', 'n_total', 'rms', 'max_err', 
 
 
 def parse_args(argv=None):
+    """Reference: ground_truth/sweep_ground_truth.py:73-99."""
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument('--gt-ref-file', type=str, required=True, dest='gt_ref_file')
     g = p.add_mutually_exclusive_group(required=True)
@@ -49,7 +50,8 @@ def parse_args(argv=None):
 
 
 def parse_final_du_over_u(run_log_path):
-    """The last `dU/U=` value of a solve log (NaN when absent)."""
+    """The last `dU/U=` value of a solve log (NaN when absent).
+    Reference: ground_truth/sweep_ground_truth.py:102-113."""
     try:
         with open(run_log_path) as fh:
             found = _DU_RE.findall(fh.read())
@@ -66,7 +68,8 @@ def _rms_max(error, mask):
 
 
 def summarize_combo(work_dir):
-    """RMS / max error over the recoverable and valid node sets of one run."""
+    """RMS / max error over the recoverable and valid node sets of one run.
+    Reference: ground_truth/sweep_ground_truth.py:126-158."""
     error = np.load(os.path.join(work_dir, 'U_error.npy'))
     truncated = np.load(os.path.join(work_dir, 'node_truncated_mask.npy'))
     rec = ~truncated
@@ -84,6 +87,7 @@ def summarize_combo(work_dir):
 
 
 def run_sweep(h_values, l0_factors, gt_ref_file, gt_displacement_file, tensile_strain, output_root):
+    """Reference: ground_truth/sweep_ground_truth.py:161-188."""
     results = []
     for h in h_values:
         for lf in l0_factors:
@@ -115,6 +119,7 @@ def _best(results, key):
 
 
 def print_summary_table(results):
+    """Reference: ground_truth/sweep_ground_truth.py:204-236."""
     print("\n" + "=" * 104)
     print("SWEEP SUMMARY: node RMS displacement error vs. h, l0_factor "
           "(valid = fair measure; recoverable over-counts the boundary shell)")
@@ -137,6 +142,7 @@ def print_summary_table(results):
 
 
 def write_csv(path, results):
+    """Reference: ground_truth/sweep_ground_truth.py:239-248."""
     with open(path, 'w', newline='') as fh:
         w = csv.DictWriter(fh, fieldnames=FIELDS)
         w.writeheader()
@@ -146,6 +152,7 @@ def write_csv(path, results):
 
 
 def main(argv=None):
+    """Reference: ground_truth/sweep_ground_truth.py:251-262."""
     args = parse_args(argv)
     results = run_sweep([int(x) for x in args.h_values.split(',')], [float(x) for x in args.l0_factors.split(',')],
                         args.gt_ref_file, args.gt_displacement_file, args.tensile_strain,

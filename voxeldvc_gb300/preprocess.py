@@ -32,7 +32,8 @@ def warp_onto_ref_grid(A, t, c, Nf, g_gpu, xp, chunk=30):
     """g sampled on f's voxel grid at x' = A (x - c) + c + t (trilinear, 0
     outside g).  Returns a float32 numpy array of shape Nf (the reference
     returns host memory too); `chunk` is accepted and ignored -- the warp is
-    one pass."""
+    one pass.
+    Reference: preprocess.py:233-285."""
     Nf = tuple(int(n) for n in Nf)
     g = _dev_f32(g_gpu)
     gs = tuple(int(n) for n in g.shape)
@@ -50,7 +51,8 @@ def warp_onto_ref_grid(A, t, c, Nf, g_gpu, xp, chunk=30):
 
 def bin_volume(vol, B):
     """Average-bin by the integer factor B along every axis (float32); the
-    shape must be divisible by B."""
+    shape must be divisible by B.
+    Reference: preprocess.py:288-312."""
     dt = D.np_dtype_of(vol) if D.is_tensor(vol) else np.asarray(vol).dtype
     S0, S1, S2 = (int(s) for s in vol.shape)
     assert S0 % B == 0 and S1 % B == 0 and S2 % B == 0, \
@@ -67,7 +69,8 @@ def bin_volume(vol, B):
 def compute_crop(f, g_warped, h, glt=0.0):
     """n h + 1 crop of the valid overlap region (f > glt and g_warped > glt):
     bounding box by axis projections, each dimension snapped down to n h + 1
-    and re-centred, shifted into f's bounds.  Returns lo, hi (hi exclusive)."""
+    and re-centred, shifted into f's bounds.  Returns lo, hi (hi exclusive).
+    Reference: preprocess.py:315-367."""
     fd, gd = _dev_f32(f), _dev_f32(g_warped)
     n0, n1, n2 = (int(s) for s in fd.shape)
     if tuple(gd.shape) != (n0, n1, n2):
@@ -107,7 +110,8 @@ DEFAULT_H = 8
 
 
 def load_volume(filepath):
-    """.npy volume (or .tif/.tiff through tifffile where it is installed)."""
+    """.npy volume (or .tif/.tiff through tifffile where it is installed).
+    Reference: preprocess.py:72-85."""
     ext = os.path.splitext(filepath)[1].lower()
     if ext == '.npy':
         return np.load(filepath)
@@ -119,7 +123,8 @@ def load_volume(filepath):
 
 def rotation_angles_deg(A):
     """Euler angles (deg, x y z) of the rotation R of the polar
-    decomposition A = R P, and P's diagonal (the axis-aligned scale)."""
+    decomposition A = R P, and P's diagonal (the axis-aligned scale).
+    Reference: preprocess.py:199-219."""
     Us, _, Vt = np.linalg.svd(A)
     R = Us @ Vt
     if np.linalg.det(R) < 0:
@@ -132,7 +137,8 @@ def rotation_angles_deg(A):
 
 
 def normal_strains(A):
-    """diag(I - A^-1): the per-axis normal strain in the reference frame."""
+    """diag(I - A^-1): the per-axis normal strain in the reference frame.
+    Reference: preprocess.py:222-230."""
     return np.diag(np.eye(3) - np.linalg.inv(A))
 
 
@@ -183,7 +189,8 @@ def main(argv=None):
     """Same steps, outputs and affine_prealign.json keys as the reference's
     preprocess: load, bin, symmetric crop, affine prealign (+ Gauss-Newton
     refine), warp onto the reference grid, n h + 1 overlap crop, deformed
-    bounding box, save."""
+    bounding box, save.
+    Reference: preprocess.py:372-691."""
     from .engine.correlate_gpu import affine_prealign, affine_refine_gn
     args = parse_args(argv)
     if args.ref_path is None:

@@ -54,6 +54,7 @@ class _Tee:
 
 
 def parse_args(argv=None):
+    """Reference: run_dvc.py:56-62."""
     p = argparse.ArgumentParser(prog="voxeldvc run")
     p.add_argument('work_dir', type=str)
     p.add_argument('--l0-factor', type=float, default=DEFAULT_L0_FACTOR, dest='l0_factor',
@@ -118,6 +119,7 @@ def _cell_outputs(work, U, U_grid, dU, res, ref, active, Nx, Ny, Nz, h, glt):
 
 
 def main(argv=None):
+    """Reference: run_dvc.py:65-192."""
     from .engine.correlate_gpu import multiscale_correlate_gpu
     from .engine.geometry_dvc import build_K_ref_laplacian
 

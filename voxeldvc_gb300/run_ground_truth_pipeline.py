@@ -33,6 +33,7 @@ _STAGES = {
 
 
 def run_stage(module, args, in_process=True):
+    """Reference: run_ground_truth_pipeline.py:51-56."""
     print("\n" + "=" * 70)
     print("STAGE: " + " ".join([sys.executable, '-m', module] + list(args)))
     print("=" * 70)
@@ -46,6 +47,7 @@ def run_stage(module, args, in_process=True):
 
 
 def parse_args(argv=None):
+    """Reference: run_ground_truth_pipeline.py:59-84."""
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument('--gt-ref-file', type=str, default=None, dest='gt_ref_file')
     g = p.add_mutually_exclusive_group()
@@ -59,6 +61,7 @@ def parse_args(argv=None):
 
 
 def main(argv=None):
+    """Reference: run_ground_truth_pipeline.py:87-126."""
     args = parse_args(argv)
     out = os.path.abspath(args.output_dir)
     gt = os.path.join(out, 'gt_input')
