@@ -64,5 +64,10 @@ def test_run_writes_the_solve(tmp_path, cuda):
     for name in ("material_cell_mask", "material_cell_mask_eroded", "overlap_lost_element_mask"):
         m = np.load(tmp_path / f"{name}.npy")
         assert m.shape == (4, 3, 2) and m.dtype == bool, name
-    assert np.load(tmp_path / "unsafe_voxel_mask.npy").shape == f.shape
+    uv = np.load(tmp_path / "unsafe_voxel_mask.npy")
+    assert uv.shape == f.shape
+    up = np.load(tmp_path / "unsafe_voxel_mask_forward_pushed.npy")
+    assert up.dtype == bool and up.shape == f.shape
+    ref_up = O.push_field_forward(uv.astype(np.float64), U, 4, 3, 2, 8, order=0, mode='constant', cval=1.0)
+    assert np.array_equal(up, ref_up.astype(bool))
     assert "cell eq. strain:" in log and "Material cells" in log

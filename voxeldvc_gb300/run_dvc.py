@@ -116,6 +116,7 @@ def _cell_outputs(work, U, U_grid, dU, res, ref, active, Nx, Ny, Nz, h, glt):
                       ('overlap_lost_element_mask', lost), ('material_cell_mask', mat),
                       ('material_cell_mask_eroded', mat_er)):
         np.save(os.path.join(work, f'{name}.npy'), arr)
+    return unsafe.reshape(Nv, order='F')
 
 
 def main(argv=None):
@@ -191,7 +192,16 @@ def main(argv=None):
         f_flat = np.ravel(np.asarray(ref, dtype=np.float64), order='F')
         zncc = compute_zncc(f_flat, f_flat - res, active)
         print(f"  ZNCC (active voxels): {zncc:.6f}")
-        _cell_outputs(work, U, U_grid, dU, res, ref, active, Nx, Ny, Nz, h, glt)
+        unsafe_grid = _cell_outputs(work, U, U_grid, dU, res, ref, active, Nx, Ny, Nz, h, glt)
+        # the unsafe mask pushed like the reference, nearest-neighbour, and
+        # flagged unsafe where its source leaves the reference domain
+        # (write_output.py:900-911)
+        from .engine.write_output import push_field_forward
+        pushed_unsafe = np.asarray(push_field_forward(unsafe_grid.astype(np.uint8), _dofs(U_local), Nx, Ny, Nz, h,
+                                                      order=0, mode='constant', cval=1)).astype(bool)
+        print(f"Unsafe voxels (forward-pushed to deformed grid): {int(pushed_unsafe.sum())}/{pushed_unsafe.size} "
+              f"({100 * pushed_unsafe.mean():.1f}%)")
+        np.save(os.path.join(work, 'unsafe_voxel_mask_forward_pushed.npy'), pushed_unsafe)
         for ci, name in enumerate(['ux', 'uy', 'uz']):
             comp = U_grid[..., ci]
             print(f"  {name}: mean={comp.mean():.4f}  std={comp.std():.4f}  min={comp.min():.4f}  max={comp.max():.4f}")
