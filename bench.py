@@ -50,7 +50,7 @@ TRAFFIC_B_PER_VOXEL = 14.04
 SOLVE_COUNTS = {"necking_512": {"gn": [30, 4, 2], "pcg": [752, 84, 41]},
                 "necking_512_eqgap": {"gn": [30, 30, 30], "pcg": [60000, 60000, 60000]},
                 "necking_256": {"gn": [8, 6, 3], "pcg": [200, 108, 57]},
-                "plain_small": {"gn": [10, 5, 3], "pcg": [200, 100, 60]},
+                "plain_small": {"gn": [20, 7, 4], "pcg": [372, 138, 81]},
                 "large_1024": {"gn": [30, 30, 3, 2], "pcg": [2179, 1388, 140, 95]}}
 
 
@@ -64,7 +64,9 @@ def parse(argv=None):
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-layers", type=int, default=None,
-                   help="element layers per CPU-baseline worker (default: the whole mesh split over the cores)")
+                   help="element layers each CPU worker times per pyramid level (default 1)")
+    p.add_argument("--cpu-procs", type=int, default=None,
+                   help="CPU worker processes (default: every host core this process may use)")
     p.add_argument("--no-forms", action="store_true",
                    help="skip the precision / learned-seed form comparison (FP64 reference solve included)")
     p.add_argument("--only", default=None, choices=[None, "matvec", "kernels", "ground-truth", "post", "eh-form", "learned"],
@@ -167,42 +169,133 @@ class Clocks:
 
 
 # ---------------------------------------------------------------------------
-# CPU oracle leg: per-operation times on a bounded sample, extrapolated
+# CPU leg: the reference's own operators (voxelDVC engine on NumPy)
 # ---------------------------------------------------------------------------
 
-def _timed(fn, *a, **k):
+REF_DIR = os.path.join(ROOT, "baseline", "_ref")
+
+# What the CPU leg needs to know of each workload (the reference arm must not
+# load this package's native library, so it does not read voxeldvc_gb300's
+# workload table): volume edge, element edge, regularizer, l0, pyramid, the
+# seeded NumPy generator case (oracle/workload_inputs.py), the analytic field.
+CPU_WORKLOADS = {
+    "necking_512": dict(name="necking_513^3_h8", n=513, h=8, reg="laplacian", l0=36.0, scales=(2, 1, 0),
+                        case="necking_513", field="necking"),
+    "necking_256": dict(name="necking_257^3_h8", n=257, h=8, reg="laplacian", l0=36.0, scales=(2, 1, 0),
+                        case="necking_257", field="necking"),
+    "plain_small": dict(name="plain_small_129^3_h16", n=129, h=16, reg="laplacian", l0=32.0, scales=(2, 1, 0),
+                        case="plain_small", field="plain_small"),
+}
+
+
+def ref_engine():
+    """The reference's engine modules (voxelDVC src/voxeldvc/engine/*, installed
+    unmodified into baseline/_ref); they import only NumPy and SciPy."""
+    if not os.path.isdir(os.path.join(REF_DIR, "voxeldvc", "engine")):
+        raise FileNotFoundError("the reference is not installed in baseline/_ref")
+    if REF_DIR not in sys.path:
+        sys.path.insert(0, REF_DIR)
+    from voxeldvc.engine import correlate_gpu as RCG, kernels_dvc as RKD, geometry_dvc as RG
+    return RCG, RKD, RG
+
+
+def _level_field(spec, s, X, Y, Z):
+    """The workload's analytic displacement at level-s voxel coordinates, in
+    level-s voxels (the pyramid's coarse levels see u(s x) / s)."""
+    from oracle import workload_inputs as WI
+    if spec["field"] == "necking":
+        u = WI.field_necking(X * s, Y * s, Z * s, spec["n"])
+    else:
+        u = WI.field_plain_small(X * s, Y * s, Z * s)
+    return [c / s for c in u]
+
+
+def _ref_slab_job(job):
+    """Seconds of each reference operator on one z slab of one pyramid level
+    (one worker of the CPU leg): `L` element layers starting at layer z0 of
+    the level's (Nx, Ny, Nz) mesh, cut from the level's images (memory-mapped
+    .npy files written by the parent).  The operators are the reference's
+    functions called as its correlate_gpu calls them (correlate_gpu.py:
+    938-960, 1068-1128; kernels_dvc.py:349-583), on the slab's own arrays:
+    gradient and erosion, sampling of g at x + u (u = the analytic field at
+    the slab's nodes), the masked statistics, the residual, b, the diagonal,
+    the Hessian and regularizer matvecs and the PCG's vector work."""
+    tmp, s, Nx, Ny, z0, L, spec = job
+    RCG, RKD, RG = ref_engine()
+    h = spec["h"] // s
+    f = np.load(os.path.join(tmp, f"f{s}.npy"), mmap_mode="r")
+    g = np.load(os.path.join(tmp, f"g{s}.npy"), mmap_mode="r")
+    nvx, nvy, nvz = f.shape
+    v0, v1 = z0 * h, (z0 + L) * h + 1
+    t = {}
+    # per-level set-up: values, gradient (with a plane of context on each
+    # side, as in the whole image), mask0 and its erosion, grad zeroed there
+    a0, a1 = max(0, v0 - 1), min(nvz, v1 + 1)
+    f_ext = np.ascontiguousarray(f[:, :, a0:a1])
     t0 = time.perf_counter()
-    fn(*a, **k)
-    return time.perf_counter() - t0
-
-
-def _cpu_slab_times(job):
-    """Per-operation seconds of the oracle on one slab of `nz` element layers
-    of every pyramid level (one worker of the CPU baseline)."""
-    Nx, Ny, h0, scales, nz, nu, seed = job
-    from oracle import dvc_oracle as O
-    rng = np.random.default_rng(seed)
-    K_lap = O.k_ref_laplacian()
-    out = {}
-    nd = 3 * (Nx + 1) * (Ny + 1) * (nz + 1)
-    v64 = rng.standard_normal(nd)
-    out["k"] = _timed(O.matvec_k_ref, v64, K_lap, float(h0), Nx, Ny, nz)
-    out["vec"] = _timed(lambda: [v64 * 1.0001 + v64 for _ in range(10)] and float(np.dot(v64, v64)))
-    for s in scales:
-        h = h0 // 2 ** s
-        Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, nz * h + 1
-        nvox = Nvx * Nvy * Nvz
-        grad = rng.standard_normal((nvox, 3)).astype(np.float32)
-        mask = rng.random(nvox) < 0.95
-        res = rng.standard_normal(nvox)
-        vs = rng.standard_normal(nd)
-        gimg = rng.random((Nvx, Nvy, Nvz)).astype(np.float32)
-        out[h] = {"mv": _timed(O.matvec_h, vs, grad, mask, h, Nx, Ny, nz),
-                  "dg": _timed(O.diag_h, grad, mask, h, Nx, Ny, nz, nd),
-                  "b": _timed(O.compute_b, res, mask, grad, h, Nx, Ny, nz, nd),
-                  "st": _timed(O.masked_mean_std, res, mask, h, Nx, Ny, nz),
-                  "sm": _timed(O.sample_deformed, 0.3 * vs, gimg, h, Nx, Ny, nz, (0, 0, 0), mask)}
-    return out
+    f_vox, grad = RCG.image_grad_and_values(np.asarray(f_ext, dtype=np.float32), np, dtype=np.float32)
+    mask0 = f_vox > 0.0
+    gm = RCG.erode_mask0_vox(mask0, nvx, nvy, a1 - a0, np)
+    grad[~gm] = 0
+    t["grad"] = time.perf_counter() - t0
+    plane = nvx * nvy
+    lo, hi = (v0 - a0) * plane, (v1 - a0) * plane
+    f_vox, grad, mask0 = f_vox[lo:hi].copy(), grad[lo:hi].copy(), mask0[lo:hi].copy()
+    Ndof = 3 * (Nx + 1) * (Ny + 1) * (L + 1)
+    N, w = RG.build_N_stencil(h)
+    K_lap = RG.build_K_ref_laplacian()
+    # nodal U: the analytic field at the slab's nodes (level units)
+    nn = np.arange((Nx + 1) * (Ny + 1) * (L + 1))
+    X = (nn % (Nx + 1)) * float(h)
+    Y = ((nn // (Nx + 1)) % (Ny + 1)) * float(h)
+    Z = (nn // ((Nx + 1) * (Ny + 1)) + z0) * float(h)
+    U = np.empty(Ndof, np.float32)
+    for c, uc in enumerate(_level_field(spec, s, X, Y, Z)):
+        U[c::3] = uc
+    # g with a margin of planes around the slab (the deformed positions stay
+    # within it: |u_z| + 2 planes); g_origin shifts slab coordinates into it
+    m = int(np.ceil(np.max(np.abs(U[2::3])))) + 2
+    b0, b1 = max(0, v0 - m), min(nvz, v1 + m)
+    g_sl = np.ascontiguousarray(g[:, :, b0:b1])
+    origin = (0, 0, b0 - v0)
+    t0 = time.perf_counter()
+    g_vals, mvox = RCG.sample_deformed_field(U, g_sl, N, h, Nx, Ny, L, np, g_origin=origin, mask0_vox=mask0,
+                                             glt=0.0)
+    t["sample"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g_mean, std1 = RCG.masked_quadpoint_mean_std(g_vals, mvox, h, Nx, Ny, L, np)
+    t["stats"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g_vals -= g_mean
+    g_vals *= -(1.0 / max(std1, 1e-30))
+    g_vals += f_vox
+    res = g_vals
+    res[~mvox] = 0.0
+    t["res"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b = RCG.compute_b_gpu(res, mvox, grad, N, w, h, Nx, Ny, L, Ndof, np)
+    t["b"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    RKD.build_diagonal_H(grad, mvox, N, w, h, Nx, Ny, L, Ndof, np)
+    t["diag"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    RKD.build_diagonal_K_ref(K_lap, h, Nx, Ny, L, Ndof, np)
+    t["diag_reg"] = time.perf_counter() - t0
+    v = b.astype(np.float64)
+    t0 = time.perf_counter()
+    Hv = RKD.matvec_H(v, grad, mvox, N, w, h, Nx, Ny, L, np)
+    t["mv"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Rv = RKD.matvec_K_ref(v, K_lap, E_elem=h, Nx=Nx, Ny=Ny, Nz=L, xp=np)
+    t["reg"] = time.perf_counter() - t0
+    # the PCG's own vector work per iteration: the reference's pcg with an
+    # identity matvec, per iteration
+    Mi = 1.0 / (np.abs(Hv + 0.01 * Rv) + 1.0)
+    k = 8
+    t0 = time.perf_counter()
+    RKD.pcg(lambda x: x, v, Mi, np, max_iter=k, tol=0.0)
+    t["vec"] = (time.perf_counter() - t0) / (k + 1)
+    return t
 
 
 def cpu_workers():
@@ -213,91 +306,138 @@ def cpu_workers():
         return max(1, os.cpu_count() or 1)
 
 
-def cpu_model(wl, counts, layers=None, procs=None):
-    """Seconds of the reference path on this host's cores for one solve.
-    The reference's operators loop over element chunks, so the mesh splits
-    into z slabs that run on separate cores: `procs` worker processes
-    (spawned: the parent may hold a CUDA context; one BLAS/OpenMP thread
-    each) time every operation of every pyramid level on their own slabs,
-    all at once, so the times include the cores' contention for memory
-    bandwidth.  By default the slabs cover the whole mesh (Nz / procs layers
-    each) and a full-mesh operation costs the slowest worker's time; with
-    `layers` given, each worker times that many layers and the cost is
-    extrapolated linearly to Nz / procs layers.  Multiplied by the solve's
-    GN and PCG counts."""
-    import multiprocessing as mp
-    Nx, Ny, Nz = wl.mesh
-    procs = max(1, min(procs or cpu_workers(), Nz))
-    per = layers or -(-Nz // procs)
-    eqgap = wl.solve["reg_type"] == "equilibrium_gap"
-    scales = sorted(wl.solve["scales"], reverse=True)
-    jobs = [(Nx, Ny, wl.h, scales, per, wl.solve.get("nu", 0.3), p) for p in range(procs)]
-    t_start = time.perf_counter()
-    if procs > 1:
+class RefCpuLeg:
+    """The reference's own NumPy execution of the path, timed on this host's
+    cores.  The reference's operators loop over element chunks of a whole
+    mesh on one core; here every pyramid level's mesh is cut into z slabs
+    and `procs` spawned worker processes (one BLAS/OpenMP thread each) time
+    the reference functions on their own slab, all at once, so the times
+    include the cores' contention for memory bandwidth.  A worker times
+    `layers` element layers and its time is scaled to its share of the mesh
+    (Nz / procs layers); a full-mesh operation costs the slowest worker's
+    scaled time.  The solve time is assembled from the operation times with
+    the solve's GN and PCG iteration counts (labelled extrapolated)."""
+
+    def __init__(self, spec, f_pix, g_pix, procs=None, layers=1):
+        import multiprocessing as mp
+        import tempfile as tf
+        self.spec = spec
+        self.procs = procs or cpu_workers()
+        self.layers = layers
+        self.dir = tf.TemporaryDirectory(prefix="vdvc_cpu_")
+        for sc in spec["scales"]:
+            d = 2 ** sc
+            np.save(os.path.join(self.dir.name, f"f{d}.npy"), np.ascontiguousarray(f_pix[::d, ::d, ::d]))
+            np.save(os.path.join(self.dir.name, f"g{d}.npy"), np.ascontiguousarray(g_pix[::d, ::d, ::d]))
         keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
         saved = {k: os.environ.get(k) for k in keys}
         os.environ.update({k: "1" for k in keys})
         try:
-            with mp.get_context("spawn").Pool(procs) as pool:
-                res = pool.map(_cpu_slab_times, jobs)
+            self.pool = mp.get_context("spawn").Pool(self.procs)
         finally:
             for k, v in saved.items():
                 if v is None:
                     os.environ.pop(k, None)
                 else:
                     os.environ[k] = v
-    else:
-        res = [_cpu_slab_times(jobs[0])]
-    wall = time.perf_counter() - t_start
-    layers = per
-    scale = (Nz / procs) / per
-    slow = lambda key, lvl=None: max((r[lvl][key] if lvl else r[key]) for r in res) * scale  # noqa: E731
-    t_k = slow("k")
-    t_reg = (3 if eqgap else 1) * t_k          # K P K + eps K_lap  (or K_lap)
-    t_reg_diag = (2 * 32 * t_k + t_k) if eqgap else t_k  # Hutchinson (32 probes x K P K) + diag K_lap
-    t_vec = slow("vec")
-    levels, total = [], 0.0
-    for li, s in enumerate(scales):
-        h = wl.h // 2 ** s
-        t_mv, t_dg, t_b, t_st, t_sm = (slow(k, h) for k in ("mv", "dg", "b", "st", "sm"))
-        t_pcg = t_mv + t_reg + t_vec
-        t_gn = t_sm + 2 * t_st + t_b + t_reg + t_dg + t_reg_diag + t_st
-        n_gn, n_pcg = counts["gn"][li], counts["pcg"][li]
-        t_level = n_gn * t_gn + (n_pcg + n_gn) * t_pcg
-        total += t_level
-        levels.append({"h": h, "matvec_s": round(t_mv, 3), "gn_fixed_s": round(t_gn, 3), "level_s": round(t_level, 1)})
-    return total, {"levels": levels, "reg_matvec_s": round(t_k, 3), "sample_wall_s": round(wall, 1),
-                   "sample": f"oracle per-op timing by {procs} worker processes at once, each on its own z slab "
-                             f"of {layers} element layer(s) of every level (full mesh {Nz} layers; "
-                             f"{'whole mesh covered' if layers * procs >= Nz else 'extrapolated in layers'}), "
-                             f"slowest worker per op; extrapolated with the solve's GN/PCG counts {counts}",
-                   "threads": procs}
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+        self.dir.cleanup()
+
+    def sample(self, counts):
+        """One bounded sample: every level's operations on `layers` element
+        layers per worker; returns (seconds per solve, detail)."""
+        spec, n = self.spec, self.spec["n"]
+        Nel = (n - 1) // spec["h"]
+        Nx = Ny = Nz = Nel
+        procs = min(self.procs, Nz)
+        share = Nz / procs                     # layers of the mesh per core
+        jobs, where = [], []
+        for sc in sorted(spec["scales"], reverse=True):
+            d = 2 ** sc
+            for p in range(procs):
+                z0 = min(Nz - self.layers, int(p * share))
+                jobs.append((self.dir.name, d, Nx, Ny, z0, self.layers, spec))
+                where.append(d)
+        t0 = time.perf_counter()
+        res = self.pool.map(_ref_slab_job, jobs)
+        wall = time.perf_counter() - t0
+        scale = share / self.layers
+        levels, total = [], 0.0
+        for li, sc in enumerate(sorted(spec["scales"], reverse=True)):
+            d = 2 ** sc
+            rs = [r for r, w in zip(res, where) if w == d]
+            op = {k: max(r[k] for r in rs) * scale for k in rs[0]}
+            t_pcg = op["mv"] + op["reg"] + op["vec"]
+            # per GN iteration: sampling, stats of g, residual, b - ll R U,
+            # diag H + ll diag R, the displayed stats of res
+            t_gn = op["sample"] + 2 * op["stats"] + op["res"] + op["b"] + op["reg"] + op["diag"] + op["diag_reg"]
+            # per level: gradient, mask erosion, stats of f, lambda calibration
+            t_setup = op["grad"] + op["stats"] + op["mv"] + op["reg"]
+            n_gn, n_pcg = counts["gn"][li], counts["pcg"][li]
+            t_level = t_setup + n_gn * t_gn + (n_pcg + n_gn) * t_pcg
+            total += t_level
+            levels.append({"h": spec["h"] // d, "matvec_H_s": round(op["mv"], 3), "sample_s": round(op["sample"], 3),
+                           "gn_fixed_s": round(t_gn, 3), "level_s": round(t_level, 1)})
+        info = {"levels": levels, "sample_wall_s": round(wall, 2), "threads": procs,
+                "sample": f"the reference's own operators (voxelDVC engine, NumPy, from baseline/_ref) on the "
+                          f"workload's arrays: {procs} worker processes at once, each timing {self.layers} element "
+                          f"layer(s) of its own z slab of every pyramid level, scaled to its {share:g}-layer share "
+                          f"of the {Nz}-layer mesh, slowest worker per operation; solve time extrapolated with the "
+                          f"GN/PCG counts {counts}"}
+        return total, info
+
+
+def ref_counts(workload):
+    return SOLVE_COUNTS[workload]
 
 
 def reference_arm(args):
-    from voxeldvc_gb300 import synth
+    """`--impl reference`: the reference's own CPU execution of the path on
+    the host cores (rank 0 only), on the same workload, metric and units as
+    the GB300 arm.  The workload's pair is generated on the host by the
+    seeded NumPy generator (oracle/workload_inputs.py); nothing of this
+    package's GPU library is loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    wl = synth.WORKLOADS[args.workload]()
-    counts = SOLVE_COUNTS[args.workload]
-    vals = []
-    info = None
-    # the CPU leg has no warm-up effects worth discarding beyond numpy's first
-    # call; each step re-measures every operation on fresh samples
-    for _ in range(max(1, args.steps)):
-        v, info = cpu_model(wl, counts, args.cpu_sample_layers)
-        vals.append(v)
+    spec = CPU_WORKLOADS.get(args.workload)
+    base = {"metric": METRIC, "impl": "reference"}
+    if spec is None:
+        print(json.dumps(dict(base, unavailable=f"no CPU timing plan for workload {args.workload}")))
+        return
+    try:
+        ref_engine()
+    except (FileNotFoundError, ImportError) as e:
+        print(json.dumps(dict(base, unavailable=str(e))))
+        return
+    from oracle import workload_inputs as WI
+    t0 = time.perf_counter()
+    f_pix, g_pix = WI.CASES[spec["case"]]()
+    t_gen = time.perf_counter() - t0
+    counts = ref_counts(args.workload)
+    leg = RefCpuLeg(spec, f_pix, g_pix, procs=args.cpu_procs, layers=args.cpu_sample_layers or 1)
+    del f_pix, g_pix
+    vals, info = [], None
+    try:
+        for i in range(max(0, args.warmup) + max(1, args.steps)):
+            v, info = leg.sample(counts)
+            if i >= args.warmup:
+                vals.append(v)
+    finally:
+        leg.close()
     value = float(np.median(vals))
-    line = {"metric": METRIC, "value": round(value, 2), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(value * 1e3, 1), "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (PCG promoted to f64 as in the reference)",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": wl.name, "mesh": list(wl.mesh), "h": wl.h, "extrapolated": True},
-            "cpu_baseline": {"value": round(value, 2), "unit": "s", "cores": info["threads"], "kind": "port",
-                             "sample": info["sample"]},
-            "e2e": {"value": round(value, 2), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "detail": info}
+    line = dict(base, value=round(value, 2), unit="s", n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
+                ms_per_step=round(value * 1e3, 1), higher_is_better=False, scaling="weak", vs_baseline=None,
+                dtype="f32 (the reference promotes b and the PCG to f64 when l0 is set)", data="synthetic",
+                config={"workload": spec["name"], "mesh": [(spec["n"] - 1) // spec["h"]] * 3, "h": spec["h"],
+                        "reg": spec["reg"], "scales": list(spec["scales"]), "extrapolated": True},
+                cpu_baseline={"value": round(value, 2), "unit": "s", "cores": info["threads"], "kind": "reference",
+                              "sample": info["sample"]},
+                e2e={"value": round(value, 2), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                detail=dict(info, input_generation_s=round(t_gen, 1)))
     print(json.dumps(line))
 
 
@@ -368,9 +508,10 @@ def compare_forms(wl, f_pix, g_pix, kw, U_plain, e2e_plain, plain_s):
     out["learned_mixed"] = {"s": round(tl, 4), "rms_vs_f64_vx": round(rms(Ul), 6), "seed": last.get("seed"),
                             "norm_res": last.get("norm_res"), "gn_iters": [s["gn_iters"] for s in gn[-1:]],
                             "pcg_iters": [int(sum(s["pcg_iters"])) for s in gn[-1:]]}
-    # the same through the public API with host arrays (as the plain e2e)
-    f_host = f_pix.cpu().pin_memory().numpy()
-    g_host = g_pix.cpu().pin_memory().numpy()
+    # the same through the public API with host arrays (ordinary numpy
+    # arrays, as the plain e2e)
+    f_host = np.array(f_pix.cpu().numpy())
+    g_host = np.array(g_pix.cpu().numpy())
     te, _ = timed(lambda: LS.learned_correlate_gpu(f_host, g_host, Nx, Ny, Nz, wl.h, np, net=net,
                                                    precision="mixed", **kwl), reps=2)
     out["learned_mixed"]["e2e_s"] = round(te, 4)
@@ -543,11 +684,14 @@ def gpu_arm(args):
     achieved = alg_bytes / (mv_ms * 1e-3) / 1e9
     del grad, mask0, ws
 
-    # e2e through the public API with host arrays
+    # e2e through the public API with host arrays: ordinary (pageable) numpy
+    # arrays, as `voxeldvc run` hands in what np.load returned
     e2e = None
+    f_host = g_host = None
+    if rank == 0 and (args.e2e_steps > 0 or not args.no_cpu_baseline):
+        f_host = np.array(f_pix.cpu().numpy())
+        g_host = np.array(g_pix.cpu().numpy())
     if args.e2e_steps > 0 and rank == 0:
-        f_host = f_pix.cpu().pin_memory().numpy()
-        g_host = g_pix.cpu().pin_memory().numpy()
         t_e2e = []
         # one untimed call: host result buffers are pinned once and reused
         CG.multiscale_correlate_gpu(f_host, g_host, Nx, Ny, Nz, wl.h, xp=np, **kw)
@@ -569,10 +713,24 @@ def gpu_arm(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        counts = {"gn": [s["gn_iters"] for s in level_stats], "pcg": [int(sum(s["pcg_iters"])) for s in level_stats]}
-        cv, cinfo = cpu_model(wl, counts, args.cpu_sample_layers)
-        cpu = {"value": round(cv, 2), "unit": "s", "cores": cinfo["threads"], "kind": "port", "sample": cinfo["sample"],
-               "detail": cinfo["levels"]}
+        # the reference's own operators on this run's own arrays, with this
+        # solve's GN / PCG counts
+        spec = CPU_WORKLOADS.get(args.workload)
+        try:
+            if spec is None:
+                raise KeyError(f"no CPU timing plan for workload {args.workload}")
+            ref_engine()
+            counts = {"gn": [s["gn_iters"] for s in level_stats],
+                      "pcg": [int(sum(s["pcg_iters"])) for s in level_stats]}
+            leg = RefCpuLeg(spec, f_host, g_host, procs=args.cpu_procs, layers=args.cpu_sample_layers or 1)
+            try:
+                cv, cinfo = leg.sample(counts)
+            finally:
+                leg.close()
+            cpu = {"value": round(cv, 2), "unit": "s", "cores": cinfo["threads"], "kind": "reference",
+                   "sample": cinfo["sample"], "detail": cinfo["levels"]}
+        except (KeyError, FileNotFoundError, ImportError) as e:
+            cpu = {"value": None, "unit": "s", "kind": "reference", "unavailable": str(e)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(ms / 1e3, 4), "unit": "s", "n_gpus": world, "steps": args.steps,

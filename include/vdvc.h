@@ -45,7 +45,10 @@ enum {
   VDVC_ERR_ZERO_DIVISION = 6,/* a normalisation std of zero (the reference raises
                                 ZeroDivisionError at correlate_gpu.py:1095)      */
   VDVC_ERR_CUFFT = 7,        /* cuFFT plan/exec failure                          */
-  VDVC_ERR_UNSUPPORTED = 8   /* valid request this build does not implement      */
+  VDVC_ERR_UNSUPPORTED = 8,  /* valid request this build does not implement      */
+  VDVC_ERR_TIMEOUT = 9       /* a bounded device-side wait (grid barrier,
+                                mbarrier) ran out; the kernel returned without
+                                finishing and the context stays usable      */
 };
 
 /* element types for dtype / pix_dtype arguments */
@@ -135,6 +138,18 @@ int vdvc_matvec_H_noalloc(const float* v, const float* grad,
                           const uint8_t* mask, int h, int Nx, int Ny, int Nz,
                           float* out, vdvc_stream_t stream);
 size_t vdvc_matvec_H_noalloc_max_elements(void);
+
+/* ---- failure detection -------------------------------------------------- */
+/* Runs one of the library's bounded device-side waits and reports it the way
+   the production kernels do.  which = 0: the grid barrier of the fused PCG
+   iteration, expecting one block more than the launch holds, so nothing
+   releases it; 1: the mbarrier wait of the bulk-copy staging, on a barrier
+   nothing arrives at; 2 / 3: the same waits released normally.  Every wait
+   gives up after max_polls polls (1 .. 2e7).  Returns VDVC_ERR_TIMEOUT for
+   0 and 1 and VDVC_OK for 2 and 3, with every block returned and the CUDA
+   context usable; nothing faults or hangs.  Synchronises the stream.  No
+   counterpart in the reference (which has no device-side waits). */
+int vdvc_selftest_bounded_wait(int which, long long max_polls, vdvc_stream_t stream);
 
 /* Precision form of matvec_H (kernels_dvc.py:452-506): the gradient is
    rounded to BF16, the 162 distinct entries of every 24x24 element Hessian
@@ -446,10 +461,7 @@ typedef struct vdvc_gn_desc {
   const double* K_el;        /* host 24x24 (equilibrium gap)                  */
   int dynamic_mask;          /* 1: H and M follow the b mask each iteration   */
   int pcg_chunk;             /* PCG iterations per body of the graph's
-                                device-driven WHILE loop (0: 4); < 0: the
-                                persistent fused PCG kernel (one cooperative
-                                launch per solve) where it applies (float,
-                                h <= 2, no equilibrium gap), else 4        */
+                                device-driven WHILE loop (<= 0: 4)           */
   const void* f_vox;         /* reference values, vox layout, uncentred       */
   const void* g_vox;         /* deformed image, vox layout                    */
   const void* grad;          /* (Nvox,3) eroded gradient of f                 */

@@ -1,13 +1,15 @@
 """Generate the golden vectors of tests/golden/*.npz by running the
 reference's own engine code (voxelDVC, src/voxeldvc/engine/*) on NumPy.
 
-Run in a checkout where the reference source is available:
+Run it with the reference's `src` directory given explicitly:
 
-    PYTHONPATH=/root/reference/src python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference-src <voxelDVC>/src [case ...]
 
-Each .npz stores the seeded inputs together with the reference outputs, so
-the tests replay the exact same cases on machines without a copy of the
-reference.  The reference cannot be imported at test time.
+(or with VOXELDVC_REF_SRC set).  Each .npz stores the seeded inputs (or, for
+the benchmark-family solves, the digest of inputs that `oracle/workload_inputs.py`
+regenerates from seeds) together with the reference outputs, so the tests
+replay the exact same cases on machines without a copy of the reference.
+The reference cannot be imported at test time.
 """
 from __future__ import annotations
 
@@ -16,7 +18,25 @@ import sys
 
 import numpy as np
 
-REF_SRC = os.environ.get("VOXELDVC_REF_SRC", "/root/reference/src")
+
+def _reference_src():
+    for i, a in enumerate(sys.argv[1:], 1):
+        if a == "--reference-src" and i + 1 < len(sys.argv):
+            path = sys.argv[i + 1]
+            del sys.argv[i:i + 2]
+            return path
+        if a.startswith("--reference-src="):
+            del sys.argv[i]
+            return a.split("=", 1)[1]
+    path = os.environ.get("VOXELDVC_REF_SRC")
+    if not path:
+        sys.exit("make_golden.py: pass --reference-src <voxelDVC checkout>/src (or set VOXELDVC_REF_SRC)")
+    return path
+
+
+REF_SRC = _reference_src()
+if not os.path.isdir(os.path.join(REF_SRC, "voxeldvc")):
+    sys.exit(f"make_golden.py: no voxeldvc package under {REF_SRC}")
 if REF_SRC not in sys.path:
     sys.path.insert(0, REF_SRC)
 
@@ -440,10 +460,92 @@ def gt_pipeline_case(kind="z+0.01"):
     del W
 
 
+RUN_SETTINGS = dict(dynamic_mask=True, freeze_mask_after=4, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
+                    glt=0.0, fft_prealign=True, scales=(2, 1, 0))
+
+
+def baseline_solve(case="plain_small", reg="laplacian", dtype="float32", scales=""):
+    """One benchmark-family workload solved by the reference's own
+    `multiscale_correlate_gpu` on NumPy with the `voxeldvc run` settings
+    (correlate_gpu.py:1143-1305): inputs from `workload_inputs` (regenerated
+    from seeds by the tests; their digest is stored), the nodal U, per
+    pyramid level the GN iteration count, the dU/U log and the PCG
+    iteration count of every GN iteration (the reference's `pcg` calls its
+    matvec once for the initial residual and once per iteration), and the
+    CPU wall time of the solve.
+
+    case: plain_small (129^3, h = 16, Laplacian l0 = 2 h) or necking_129 /
+    necking_257 / necking_513 (h = 8, l0 = 4.5 h; reg laplacian or
+    equilibrium_gap with nu = 0.3, reg_exponent 4).  scales: pyramid levels
+    to run, e.g. "2" for the coarsest level alone (with its FFT seed),
+    default 2/1/0."""
+    import contextlib
+    import io
+    import re
+    import time
+    sys.path.insert(0, os.path.dirname(os.path.dirname(OUT)))
+    from oracle import workload_inputs as WI
+    f, g = WI.CASES[case]()
+    h = 16 if case == "plain_small" else 8
+    Nx, Ny, Nz = ((s - 1) // h for s in f.shape)
+    kw = dict(RUN_SETTINGS, K_ref_laplacian=G.build_K_ref_laplacian(), l0=(2.0 if case == "plain_small" else 4.5) * h,
+              dtype=np.dtype(dtype).type, disp=True)
+    if reg == "equilibrium_gap":
+        kw.update(reg_type="equilibrium_gap", K_ref_elastic=G.build_K_ref(0.3), reg_exponent=4)
+    if scales:
+        kw["scales"] = tuple(int(c) for c in scales.split("/"))
+    pcg_counts = []
+    real_pcg = CG.pcg
+
+    def counting_pcg(matvec, *a, **k):
+        n = [0]
+
+        def mv(v):
+            n[0] += 1
+            return matvec(v)
+        x = real_pcg(mv, *a, **k)
+        pcg_counts.append(n[0] - 1)
+        return x
+
+    CG.pcg = counting_pcg
+    buf = io.StringIO()
+    try:
+        t0 = time.perf_counter()
+        with contextlib.redirect_stdout(buf):
+            U, res, dU = CG.multiscale_correlate_gpu(f, g, Nx, Ny, Nz, h, xp=np, **kw)
+        wall = time.perf_counter() - t0
+    finally:
+        CG.pcg = real_pcg
+    log = buf.getvalue()
+    levels, errs = [], []
+    for line in log.splitlines():
+        if line.startswith("=== MULTISCALE"):
+            levels.append([])
+        m = re.search(r"dU/U=([0-9.eE+-]+|nan|inf)", line)
+        if m and levels:
+            levels[-1].append(float(m.group(1)))
+    gn = [len(lv) for lv in levels]
+    pcg, k = [], 0
+    for n in gn:
+        pcg.append(pcg_counts[k:k + n])
+        k += n
+    tag = f"{case}_{'lap' if reg == 'laplacian' else 'eqgap'}_{'f64' if dtype == 'float64' else 'f32'}"
+    if scales:
+        tag += "_s" + scales.replace("/", "")
+    np.savez_compressed(os.path.join(OUT, f"baseline_{tag}.npz"), digest=np.array(WI.digest(f, g)),
+                        dims=np.array([Nx, Ny, Nz, h]), U=U, dU=dU, res_sumsq=np.float64(np.sum(np.square(res, dtype=np.float64))),
+                        gn_iters=np.array(gn), pcg_iters=np.array(pcg_counts), du_log=np.array(sum(levels, [])),
+                        wall_s=np.float64(wall), reg=np.array(reg), l0=np.float64(kw["l0"]),
+                        scales=np.array(kw["scales"]),
+                        log=np.array(log))
+    print(tag, "wall", round(wall, 1), "s; GN", gn, "PCG", pcg, "dU/U", [lv[-1] if lv else None for lv in levels])
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 1:  # regenerate only the named case groups
-        for name in sys.argv[1:]:
-            globals()[name]()
+    if len(sys.argv) > 1:  # regenerate only the named case groups: name[:arg,arg...]
+        for spec in sys.argv[1:]:
+            name, _, rest = spec.partition(":")
+            globals()[name](*(rest.split(",") if rest else ()))
         sys.exit(0)
     gt_cases()
     cells_cases()

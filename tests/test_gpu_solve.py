@@ -129,24 +129,6 @@ def test_zero_std_raises(api):
         CG.correlate_gpu(f, g, 2, 2, 2, 4, xp=np, maxiter=2, disp=False)
 
 
-def test_persistent_pcg_matches_graph(api, monkeypatch):
-    """pcg_chunk < 0 runs the h <= 2 levels on the persistent fused PCG; the
-    graph-replayed kernels give the same solve (same arithmetic, other
-    reduction grouping)."""
-    CG, G = api
-    c = load_golden("solve_multiscale.npz")
-    kw = dict(scales=(2, 1, 0), K_ref_laplacian=G.build_K_ref_laplacian(), l0=36.0, maxiter=20, eps=1e-3,
-              disp=False, dynamic_mask=True, freeze_mask_after=4, fft_prealign=True)
-    st_p = []
-    Up, _, _ = CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, stats=st_p, pcg_chunk=-1, **kw)
-    monkeypatch.setenv("VDVC_PCG", "graph")
-    st_g = []
-    Ug, _, _ = CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, stats=st_g, pcg_chunk=-1, **kw)
-    assert st_p[0]["h"] == 2
-    assert rms(Up, Ug) < 1e-4
-    assert rms(Up, c["U"]) < RMS_TOL
-
-
 @pytest.mark.parametrize("h", [1, 2, 3, 4])
 @pytest.mark.parametrize("dynamic", [False, True])
 def test_small_h_gn_iterations(api, h, dynamic):
@@ -181,39 +163,3 @@ def test_eager_pcg_matches_graph(api, monkeypatch):
     monkeypatch.setenv("VDVC_PCG", "eager")
     Ue, _, _ = CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, **kw)
     assert np.array_equal(Ue, Ug)
-
-
-_STRIP_SOLVE = r"""
-import sys, numpy as np
-sys.path.insert(0, sys.argv[1])
-from scipy import ndimage
-from voxeldvc_gb300.engine import correlate_gpu as CG, geometry_dvc as G
-from oracle import dvc_oracle as O
-out = []
-for h in (2, 4):
-    n = 6 * h + 1
-    rng = np.random.default_rng(40 + h)
-    f = ndimage.gaussian_filter(rng.random((n, n, n)), 1.2).astype(np.float32)
-    f = (f - f.min()) / (f.max() - f.min()) + np.float32(0.05)
-    g = ndimage.shift(f, (0.4, -0.3, 0.25), order=1, mode='nearest').astype(np.float32)
-    kw = dict(l0=4.5 * h, maxiter=2, eps=1e-6, dynamic_mask=True, freeze_mask_after=1)
-    U, _, _ = CG.correlate_gpu(f, g, 6, 6, 6, h, xp=np, K_ref_laplacian=G.build_K_ref_laplacian(), disp=False, **kw)
-    Uo, _, _ = O.correlate(f, g, 6, 6, 6, h, K_lap=O.k_ref_laplacian(), **kw)
-    out.append(float(np.sqrt(np.mean((U.astype(np.float64) - Uo) ** 2))))
-print(max(out))
-"""
-
-
-def test_strip_kernels_at_small_h(api):
-    """VDVC_HV_KERNEL=strip (read once per process) keeps the strip
-    decomposition at h <= 4 for the Hessian, sampling and residual passes:
-    a fresh process solves against the oracle."""
-    import os
-    import subprocess
-    import sys
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    env = dict(os.environ, VDVC_HV_KERNEL="strip")
-    r = subprocess.run([sys.executable, "-c", _STRIP_SOLVE, root], env=env, capture_output=True, text=True,
-                       timeout=600)
-    assert r.returncode == 0, r.stderr[-2000:]
-    assert float(r.stdout.strip().splitlines()[-1]) < 1e-4

@@ -51,18 +51,25 @@ def test_reference_arm_prints_on_rank_zero_only(capsys, monkeypatch):
 
 def test_reference_arm_json_contract(capsys, monkeypatch):
     """Rank 0 of the reference arm prints one JSON line with the metric of
-    the GPU arm, the CPU baseline it measured and the end-to-end object."""
+    the GPU arm, the CPU baseline it measured -- the reference's own
+    operators, installed in baseline/_ref -- and the end-to-end object; or,
+    in a checkout without that install, its one-line `unavailable` record."""
     import json
     import bench
     monkeypatch.setenv("RANK", "0")
-    args = bench.parse(["--impl", "reference", "--workload", "plain_small", "--steps", "1", "--warmup", "0"])
+    args = bench.parse(["--impl", "reference", "--workload", "plain_small", "--steps", "1", "--warmup", "0",
+                        "--cpu-procs", "2"])
     bench.reference_arm(args)
     lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.strip()]
     assert len(lines) == 1
     d = json.loads(lines[0])
-    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "s"
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC
+    if not os.path.isdir(os.path.join(bench.REF_DIR, "voxeldvc", "engine")):
+        assert "baseline/_ref" in d["unavailable"]
+        return
+    assert d["unit"] == "s"
     assert d["higher_is_better"] is False and d["value"] > 0
     cb = d["cpu_baseline"]
-    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert cb["value"] == d["value"] and cb["kind"] == "reference" and cb["cores"] == 2 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("plain_small")

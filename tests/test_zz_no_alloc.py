@@ -63,3 +63,33 @@ def test_noalloc_rejects_meshes_beyond_its_scratch(cuda):
                                  torch.cuda.current_stream().cuda_stream)
     assert st == _lib.ERR_ARG
     assert "at most" in _lib.last_error()
+
+
+def test_noalloc_makes_no_device_allocation(cuda):
+    """After its first call on a device (which looks up the scratch array's
+    address), the entry point allocates no device memory: the device's free
+    memory is the same before and after further calls."""
+    torch = cuda
+    from voxeldvc_gb300 import _lib
+    L = _lib.lib()
+    c = load_golden("ops_D.npz")
+    Nx, Ny, Nz, h = (int(x) for x in c["dims"])
+    v = torch.from_numpy(c["v"]).cuda()
+    g = torch.from_numpy(c["grad"]).cuda()
+    m = torch.from_numpy(c["mask"]).cuda()
+    out = torch.empty_like(v)
+    s = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        st = L.vdvc_matvec_H_noalloc(v.data_ptr(), g.data_ptr(), m.data_ptr(), h, Nx, Ny, Nz, out.data_ptr(), s)
+        assert st == _lib.OK, _lib.last_error()
+
+    call()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert rel(out.cpu().numpy(), c["out_matvec_H"]) < RTOL

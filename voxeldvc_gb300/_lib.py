@@ -23,6 +23,7 @@ ERR_NONFINITE = 5
 ERR_ZERO_DIVISION = 6
 ERR_CUFFT = 7
 ERR_UNSUPPORTED = 8
+ERR_TIMEOUT = 9
 
 # element type codes
 F32, F64, U8, U16, I16, I32 = 0, 1, 2, 3, 4, 5
@@ -52,6 +53,7 @@ SIGNATURES = {
     "vdvc_matvec_H": (ci, [vp, vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_matvec_H_noalloc": (ci, [vp, vp, vp, ci, ci, ci, ci, vp, vp]),
     "vdvc_matvec_H_noalloc_max_elements": (cz, []),
+    "vdvc_selftest_bounded_wait": (ci, [ci, C.c_longlong, vp]),
     "vdvc_matvec_H_mixed": (ci, [vp, vp, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_eh_workspace_bytes": (cz, [ci, ci, ci, ci]),
     "vdvc_diag_H": (ci, [vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
@@ -159,6 +161,11 @@ class VdvcError(RuntimeError):
     """A CUDA-side failure reported by libvdvc."""
 
 
+class VdvcTimeout(VdvcError):
+    """A bounded device-side wait ran out (VDVC_ERR_TIMEOUT): the kernel
+    returned early, its results are not valid, the CUDA context is usable."""
+
+
 def lib():
     """The loaded library, with argument types set.  Raises if absent."""
     global _lib
@@ -197,6 +204,8 @@ def check(status: int, what: str = "") -> None:
         raise NotImplementedError(text)
     if status == ERR_NONFINITE:
         raise FloatingPointError(text)
+    if status == ERR_TIMEOUT:
+        raise VdvcTimeout(f"libvdvc status {status} (device-side wait timed out): {text}")
     raise VdvcError(f"libvdvc status {status} ({lib().vdvc_status_string(status).decode()}): {text}")
 
 

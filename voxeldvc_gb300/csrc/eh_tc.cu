@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(kThreads) k_eh_form_tc(const EhFormArgs a, lon
     }
   }
   if (failed) {
-    if (tid == 0) atomicExch(a.err, (int)VDVC_ERR_CUDA);
+    if (tid == 0) atomicExch(a.err, (int)VDVC_ERR_TIMEOUT);
     // let any MMA still in flight finish before the TMEM is released
     for (int b = 0; b < 2; ++b)
       if (issued[b] > 0) mbar_wait_bounded(&bar[b], (uint32_t)((issued[b] - 1) & 1));
@@ -335,11 +335,7 @@ __global__ void __launch_bounds__(kThreads) k_eh_form_tc(const EhFormArgs a, lon
 template <int H>
 int launch_tc(const EhFormArgs& a, cudaStream_t s) {
   using S = TcShape<H>;
-  static bool attr = false;
-  if (!attr) {
-    VDVC_CUDA(cudaFuncSetAttribute(k_eh_form_tc<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem));
-    attr = true;
-  }
+  if (int st = ensure_dyn_smem((const void*)k_eh_form_tc<H>, (int)S::smem)) return st;
   const long long ntiles = (a.m.Ne + kElems - 1) / kElems;
   const long long grid = ntiles < 2 * 152 ? ntiles : 2 * 152;
   k_eh_form_tc<H><<<(unsigned)grid, kThreads, S::smem, s>>>(a, ntiles);

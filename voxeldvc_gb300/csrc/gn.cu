@@ -54,11 +54,15 @@ struct GnSolver {
   double* partials;
   size_t n_partials;
   unsigned int* ticket;
-  unsigned int* bar;
+  unsigned int* bar;  // fused PCG grid barrier: count, generation, timeout flag
   GnScalars* sc;
   PcgState* pcg;
   Kpair<T>* kp;
   bool frozen_set;
+  // PCG iteration form: gather and update fused in one cooperative launch
+  // (single solves), or the two-kernel form (batches, whose problems run as
+  // concurrent graph branches and so cannot promise co-resident grids)
+  bool fused_pcg;
   // precision form
   bool mixed;
   bool eh_fixed;     // T, diag and M^-1 are final (b mask frozen, or mask0)
@@ -105,7 +109,7 @@ static size_t carve_solver(const Mesh& m, GnSolver<T>* S, void* ws, size_t bytes
   S->n_partials = (size_t)(nb > kReduceBlocks ? nb : kReduceBlocks) * 4;
   S->partials = cv.take<double>(S->n_partials);
   S->ticket = cv.take<unsigned int>(4);
-  S->bar = cv.take<unsigned int>(4);  // persistent PCG: count, generation, error flag
+  S->bar = cv.take<unsigned int>(4);  // fused PCG: count, generation, timeout flag
   S->sc = cv.take<GnScalars>(1);
   S->pcg = cv.take<PcgState>(1);
   S->kp = cv.take<Kpair<T>>(1);
@@ -304,31 +308,26 @@ static StripArgs<T> pcg_strip_args(GnSolver<T>* S) {
   return sa;
 }
 
-// The persistent fused PCG (one cooperative launch per solve) serves float
-// solves at h <= 2 without the equilibrium-gap stencil, when the descriptor
-// asks for it (pcg_chunk < 0) or VDVC_PCG=persistent; VDVC_PCG=graph keeps
-// the graph-replayed kernels everywhere.  Measured on GB300 at 129^3 voxels,
-// h = 2 (64^3 elements): 1.62 ms per 25-iteration solve persistent against
-// 1.26 ms graph-replayed -- the fused kernel's element phase needs 128
-// registers, which caps every phase at 16 warps per SM -- so the graph is
-// the default and the choice is left to the autotuner.
-template <typename T>
-static bool use_persistent(GnSolver<T>* S) {
-  if constexpr (!std::is_same<T, float>::value) {
-    return false;
-  } else {
-    const char* e = getenv("VDVC_PCG");
-    if (e && e[0] == 'g') return false;
-    const bool want = S->d.pcg_chunk < 0 || (e && e[0] == 'p');
-    return want && !S->mixed && S->m.h <= 2 && !(S->d.reg_type == VDVC_REG_EQUILIBRIUM_GAP && S->d.ll != 0.0);
-  }
-}
-
 // VDVC_PCG=eager: the PCG iterations are launched from the host instead of
 // the graph (a profiling mode: every kernel is a separate stream launch).
 static bool eager_pcg() {
   const char* e = getenv("VDVC_PCG");
   return e && e[0] == 'e';
+}
+
+// After the element pass: Ap, alpha, and the x / r / z update.
+template <typename T>
+static int pcg_gather_update(GnSolver<T>* S, cudaStream_t s) {
+  if (S->fused_pcg) {
+    // partials: [0, 1024) p.Ap per block, then 2 x 1024 for r.r and r.z
+    GridReduce red{S->partials + kReduceBlocks, S->ticket};
+    return launch_pcg_gather_update<T>(S->m, S->evA, S->Minv, S->x, S->r, S->z, S->p, S->Ap, S->pcg, S->partials,
+                                       red, S->bar, (int*)(S->bar + 2), kReduceBlocks, kBarrierSpinLimit, s);
+  }
+  GridReduce red{S->partials, S->ticket};
+  int st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s, (long long)S->n_partials);
+  if (st) return st;
+  return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
 }
 
 template <typename T>
@@ -371,16 +370,12 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
         ma.K2 = S->kp->K2;  // device address of the float K_el copy
       }
       if ((st = launch_eh_matvec<true>(ma, s))) return st;
-      if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s, (long long)S->n_partials)))
-        return st;
-      return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
+      return pcg_gather_update<T>(S, s);
     }
   }
   const StripArgs<T> sa = pcg_strip_args<T>(S);
   if ((st = launch_strip<T, kModeHv | kModePcg>(sa, S->kp, s))) return st;
-  if ((st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s, (long long)S->n_partials)))
-    return st;
-  return launch_pcg_update<T>(S->p, S->Ap, S->Minv, S->m.Ndof, S->x, S->r, S->z, S->pcg, red, s);
+  return pcg_gather_update<T>(S, s);
 }
 
 // Keeps the WHILE node of the PCG graph running until the state says done.
@@ -502,6 +497,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
     return set_error(VDVC_ERR_UNSUPPORTED, "precision form needs K_lap = one 8x8 block per component");
   }
   S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 4;
+  S->fused_pcg = true;
   cudaStream_t s = (cudaStream_t)d->stream;
   int e = VDVC_OK;
   auto fail = [&](int code) {
@@ -524,6 +520,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   }
   if (cudaMemcpyAsync(S->kp, &kh, sizeof(kh), cudaMemcpyHostToDevice, s) != cudaSuccess ||
       cudaMemsetAsync(S->ticket, 0, 4 * sizeof(unsigned int), s) != cudaSuccess ||
+      cudaMemsetAsync(S->bar, 0, 4 * sizeof(unsigned int), s) != cudaSuccess ||
       cudaMemsetAsync(S->sc, 0, sizeof(GnScalars), s) != cudaSuccess)
     return fail(set_error(VDVC_ERR_CUDA, "solver upload failed"));
   // regularizer diagonal in float64: h diag(K_lap) [+ eq. gap Hutchinson]
@@ -666,33 +663,10 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   int st = launch_pcg_init<T>(S->b, nullptr, S->Minv, S->m.Ndof, S->r, S->z, S->p, false, S->x, S->pcg, red,
                               max_iter, tol, s);
   if (st) return st;
-  bool ran = false, persistent = false;
-  if constexpr (std::is_same<T, float>::value) {
-    if (max_iter > 0 && use_persistent(S)) {
-      PcgPersistArgs pa{};
-      pa.sa = pcg_strip_args<T>(S);
-      pa.kp = S->kp;
-      pa.x = S->x;
-      pa.r = S->r;
-      pa.z = S->z;
-      pa.p = S->p;
-      pa.Ap = S->Ap;
-      pa.Minv = S->Minv;
-      pa.st = S->pcg;
-      pa.partials = S->partials;
-      pa.bar = S->bar;
-      pa.err = (int*)(S->bar + 2);
-      const char* sl = getenv("VDVC_BAR_SLEEP");
-      pa.sleep_ns = sl ? atoi(sl) : 0;
-      VDVC_CUDA(cudaMemsetAsync(S->bar, 0, 4 * sizeof(unsigned int), s));
-      st = launch_pcg_persistent(pa, (int)(S->n_partials / 3), s);
-      if (st == VDVC_OK) {
-        ran = persistent = true;
-      } else if (st != VDVC_ERR_UNSUPPORTED) {
-        return st;
-      }
-    }
-  }
+  bool ran = false;
+  // the fused iteration's barrier words start at zero (a timed-out solve
+  // leaves them mid-count)
+  VDVC_CUDA(cudaMemsetAsync(S->bar, 0, 4 * sizeof(unsigned int), s));
   if (!ran && eager_pcg()) {
     // the same iteration kernels launched from the host, so that a profiler
     // sees each launch; the device state is read every 16 iterations
@@ -713,8 +687,11 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   VDVC_CUDA(cudaMemcpyAsync(S->h_pcg, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
   VDVC_CUDA(cudaStreamSynchronize(s));
   const PcgState& fin = S->h_pcg[0];
-  if (persistent && fin.status == VDVC_ERR_CUDA)
-    return set_error(VDVC_ERR_CUDA, "persistent PCG: a grid barrier timed out");
+  if (fin.status == VDVC_ERR_TIMEOUT) {
+    VDVC_CUDA(cudaMemsetAsync(S->ticket, 0, 4 * sizeof(unsigned int), s));
+    return set_error(VDVC_ERR_TIMEOUT, "PCG: the fused iteration's grid barrier timed out after %d iterations",
+                     fin.iter);
+  }
   if (max_iter > 0 && !ran) {
     // body executions = ceil(iter / chunk); each runs chunk iterations' kernels + the continue kernel
     const long long bodies = (fin.iter + S->chunk - 1) / S->chunk;
@@ -1100,6 +1077,7 @@ int vdvc_gn_batch_create(const vdvc_gn_desc* descs, int n, void* const* ws, cons
     void* impl = nullptr;
     int st = create<float>(&descs[i], ws[i], ws_bytes[i], &impl);
     if (st) return fail(st);
+    ((GnSolver<float>*)impl)->fused_pcg = false;  // concurrent branches: no co-residency promise
     B->S.push_back((GnSolver<float>*)impl);
   }
   if (cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking) != cudaSuccess ||

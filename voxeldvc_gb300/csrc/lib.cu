@@ -4,6 +4,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <climits>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "common.cuh"
 
@@ -21,6 +24,19 @@ int set_error(int status, const char* fmt, ...) {
 }
 
 void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int ensure_dyn_smem(const void* func, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> done;  // (function, device) -> bytes set
+  int dev = 0;
+  VDVC_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = done.find({func, dev});
+  if (it != done.end() && it->second >= bytes) return VDVC_OK;
+  VDVC_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done[{func, dev}] = bytes;
+  return VDVC_OK;
+}
 
 int make_mesh(int h, int Nx, int Ny, int Nz, Mesh* m) {
   VDVC_CHECK_ARG(h >= 1 && h <= 1024, "h=%d must be in [1, 1024]", h);
@@ -63,6 +79,7 @@ const char* vdvc_status_string(int status) {
     case VDVC_ERR_ZERO_DIVISION: return "division by zero";
     case VDVC_ERR_CUFFT: return "cuFFT error";
     case VDVC_ERR_UNSUPPORTED: return "unsupported";
+    case VDVC_ERR_TIMEOUT: return "device-side wait timed out";
   }
   return "unknown status";
 }

@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kTile) k_eh_matvec_tma(const EhMatvecArgs a) {
     }
   }
   if (!mbar_wait_bounded(&bar, 0)) {
-    if (t == 0) atomicExch(a.err, VDVC_ERR_CUDA);
+    if (t == 0) atomicExch(a.err, VDVC_ERR_TIMEOUT);
     mbar_wait_bounded(&bar, 0);
     return;
   }
@@ -295,11 +295,7 @@ template <bool PCG>
 int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s) {
   if (((uintptr_t)a.T & 15u)) return set_error(VDVC_ERR_ARG, "element Hessians misaligned");
   const size_t smem = (size_t)162 * kTile * sizeof(float);
-  static bool attr_set = false;
-  if (!attr_set) {
-    VDVC_CUDA(cudaFuncSetAttribute(k_eh_matvec_tma<PCG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+  if (int st = ensure_dyn_smem((const void*)k_eh_matvec_tma<PCG>, (int)smem)) return st;
   const long long nb = (a.m.Ne + kTile - 1) / kTile;
   k_eh_matvec_tma<PCG><<<(unsigned)nb, kTile, smem, s>>>(a);
   VDVC_LAUNCHED();
@@ -367,7 +363,7 @@ int vdvc_matvec_H_mixed(const float* v, const float* grad, const uint8_t* mask, 
   int h_err = 0;
   VDVC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
   VDVC_CUDA(cudaStreamSynchronize(s));
-  if (h_err) return set_error(VDVC_ERR_CUDA, "element-Hessian waits timed out");
+  if (h_err) return set_error(VDVC_ERR_TIMEOUT, "element-Hessian matvec: a bulk-copy wait timed out");
   return VDVC_OK;
 }
 

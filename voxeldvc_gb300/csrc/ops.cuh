@@ -34,10 +34,6 @@ template <typename T, int MODE>
 int launch_strip(const StripArgs<T>& args, const Kpair<T>* kp, cudaStream_t s);
 template <typename T>
 int launch_gather(const Mesh& m, const T* ev, T* out, cudaStream_t s);
-// TMA-staged float32 Hessian pass (strip_tma.cu); needs 16-byte aligned
-// grad and mask buffers.
-template <bool PCG>
-int launch_strip_tma(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s);
 // Compile-time-h float32 Hessian pass (strip_fast.cu); VDVC_ERR_UNSUPPORTED
 // when h has no specialisation.
 template <bool PCG>
@@ -50,22 +46,6 @@ int launch_elem_fast(const StripArgs<float>& args, const Kpair<float>* kp, cudaS
 // VDVC_ERR_UNSUPPORTED when h has no specialisation.
 template <bool DG>
 int launch_rhs_fast(const StripArgs<float>& args, cudaStream_t s);
-// Persistent fused PCG for h <= 2 (elem_fast.cu): one cooperative launch runs
-// all iterations until the state says done.  partials: >= 3 * grid doubles;
-// bar: two zeroed counters; err: a zeroed flag set on a barrier timeout.
-struct PcgPersistArgs {
-  StripArgs<float> sa;  // element pass: v = z, p_old = p, evA, grad, mask, regularizer
-  const Kpair<float>* kp;
-  float *x, *r, *z, *p, *Ap;
-  const float* Minv;
-  PcgState* st;
-  double* partials;
-  unsigned int* bar;
-  int* err;
-  int sleep_ns;  // back-off of a barrier poll (0: busy poll)
-};
-int launch_pcg_persistent(const PcgPersistArgs& a, int max_blocks, cudaStream_t s);
-bool tma_enabled();
 long long strip_grid_blocks(const Mesh& m);
 
 // PCG pieces (pcg.cu).
@@ -79,6 +59,13 @@ int launch_pcg_gather(const Mesh& m, const T* ev, const T* z, T* p, T* Ap, PcgSt
 template <typename T>
 int launch_pcg_update(const T* p, const T* Ap, const T* Minv, long long n, T* x, T* r, T* z, PcgState* st,
                       GridReduce red, cudaStream_t s);
+// Gather + update fused in one cooperative launch with one grid barrier
+// (pcg.cu).  pA: max_blocks doubles; red.partials: 2 * max_blocks doubles;
+// bar: two counters and err a flag, zero before the first launch.
+template <typename T>
+int launch_pcg_gather_update(const Mesh& m, const T* ev, const T* Minv, T* x, T* r, T* z, T* p, T* Ap,
+                             PcgState* st, double* pA, GridReduce red, unsigned int* bar, int* err, int max_blocks,
+                             long long spin_limit, cudaStream_t s);
 
 // Sampling and statistics (sample.cu).
 template <typename T>

@@ -331,38 +331,27 @@ __global__ void __launch_bounds__(256) k_elem_rhs(const StripArgs<float> a) {
     for (int q = 0; q < 3; ++q) a.dstats[q] = out[q];
 }
 
-// Element edges up to this one take the thread-per-element form, unless
-// VDVC_HV_KERNEL=strip asks for strip kernels at every h.
+// Element edges up to this one take the thread-per-element form.
 constexpr int kElemRhsMaxH = 4;
-
-static bool elem_rhs_enabled() {
-  static int on = -1;
-  if (on < 0) {
-    const char* e = getenv("VDVC_HV_KERNEL");
-    on = (e && e[0] == 's') ? 0 : 1;
-  }
-  return on == 1;
-}
 
 template <int H, bool DG>
 static int launch_rh(const StripArgs<float>& args, cudaStream_t s) {
   if constexpr (H <= kElemRhsMaxH) {
-    if (elem_rhs_enabled()) {
-      // at most kReduceBlocks blocks: the reduction partials hold that many
-      long long nb = (args.m.Ne + 255) / 256;
-      if (nb > kReduceBlocks) nb = kReduceBlocks;
-      k_elem_rhs<H, DG><<<(unsigned)nb, 256, 0, s>>>(args);
-      VDVC_LAUNCHED();
-      return VDVC_OK;
-    }
+    // at most kReduceBlocks blocks: the reduction partials hold that many
+    long long nb = (args.m.Ne + 255) / 256;
+    if (nb > kReduceBlocks) nb = kReduceBlocks;
+    k_elem_rhs<H, DG><<<(unsigned)nb, 256, 0, s>>>(args);
+    VDVC_LAUNCHED();
+    return VDVC_OK;
+  } else {
+    constexpr int EX = (H >= 128) ? 1 : 128 / H;
+    const int threads = (EX * H + 31) / 32 * 32;
+    const size_t smem = (size_t)threads * 25 * (DG ? 2 : 1) * sizeof(float);
+    dim3 grid((args.m.Nx + EX - 1) / EX, args.m.Ny, args.m.Nz);
+    k_strip_rhs_fast<H, DG><<<grid, threads, smem, s>>>(args);
+    VDVC_LAUNCHED();
+    return VDVC_OK;
   }
-  constexpr int EX = (H >= 128) ? 1 : 128 / H;
-  const int threads = (EX * H + 31) / 32 * 32;
-  const size_t smem = (size_t)threads * 25 * (DG ? 2 : 1) * sizeof(float);
-  dim3 grid((args.m.Nx + EX - 1) / EX, args.m.Ny, args.m.Nz);
-  k_strip_rhs_fast<H, DG><<<grid, threads, smem, s>>>(args);
-  VDVC_LAUNCHED();
-  return VDVC_OK;
 }
 
 // VDVC_ERR_UNSUPPORTED (error text untouched) when h has no specialisation.

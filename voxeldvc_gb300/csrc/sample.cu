@@ -321,18 +321,8 @@ __global__ void __launch_bounds__(256) k_elem_sample(const SampleArgs<float> a) 
     for (int q = 0; q < 4; ++q) a.stats[q] = o4[q];
 }
 
-// Element edges up to this one take the thread-per-element GN sampler,
-// unless VDVC_HV_KERNEL=strip asks for strip kernels at every h.
+// Element edges up to this one take the thread-per-element GN sampler.
 constexpr int kElemSampleMaxH = 4;
-
-static bool elem_sample_enabled() {
-  static int on = -1;
-  if (on < 0) {
-    const char* e = getenv("VDVC_HV_KERNEL");
-    on = (e && e[0] == 's') ? 0 : 1;
-  }
-  return on == 1;
-}
 
 template <int H>
 static int launch_elem_sample(const SampleArgs<float>& a, cudaStream_t s) {
@@ -355,7 +345,7 @@ int launch_sample(const SampleArgs<T>& args, cudaStream_t s) {
   SampleArgs<T> a = args;
   a.EX = sh.EX;
   if constexpr (std::is_same<T, float>::value && STATS && !INTERP) {
-    if (args.m.h <= kElemSampleMaxH && elem_sample_enabled()) {
+    if (args.m.h <= kElemSampleMaxH) {
       switch (args.m.h) {
         case 1: return launch_elem_sample<1>(a, s);
         case 2: return launch_elem_sample<2>(a, s);

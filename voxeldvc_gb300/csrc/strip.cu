@@ -314,61 +314,30 @@ size_t strip_smem_bytes(int h, int mode, size_t tsize) {
   return n * tsize;
 }
 
-// Kernel selection for the float32 Hessian pass: VDVC_HV_KERNEL=fast (the
-// default: thread per element for h <= kElemMaxH (elem_fast.cu), else the
-// compile-time-h strip specialisation, strip_fast.cu), elem, strip, tma (bulk-copy
-// staging, strip_tma.cu) or generic (runtime h, this file).
-static int hv_kernel_choice() {
-  static int choice = -1;
-  if (choice < 0) {
-    const char* e = getenv("VDVC_HV_KERNEL");
-    choice = 0;
-    if (e && e[0] == 't') choice = 1;
-    if (e && e[0] == 'g') choice = 2;
-    if (e && e[0] == 'e') choice = 3;  // thread per element wherever specialised
-    if (e && e[0] == 's') choice = 4;  // strip kernels at every h (the residual pass too, rhs_fast.cu)
-  }
-  return choice;
-}
-
-// Default split: thread per element up to this h, strips above it.
+// Kernel selection for the float32 passes: thread per element for
+// h <= kElemMaxH (elem_fast.cu, rhs_fast.cu), else the compile-time-h strip
+// specialisations (strip_fast.cu, rhs_fast.cu); the generic strip kernel of
+// this file (runtime h) serves every other h and the float64 solve.
 constexpr int kElemMaxH = 4;
-
-bool tma_enabled() { return hv_kernel_choice() == 1; }
 
 template <typename T, int MODE>
 int launch_strip(const StripArgs<T>& args, const Kpair<T>* kp, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value && (MODE == kModeHv || MODE == (kModeHv | kModePcg))) {
     constexpr bool pcg = (MODE & kModePcg) != 0;
-    const int choice = hv_kernel_choice();
-    const bool aligned = (((uintptr_t)args.grad | (uintptr_t)args.mask) & 15) == 0;
-    if (choice == 1 && aligned) return launch_strip_tma<pcg>(args, kp, s);
-    if (choice == 3 || (choice == 0 && args.m.h <= kElemMaxH)) {
-      const int st = launch_elem_fast<pcg>(args, kp, s);
-      if (st != VDVC_ERR_UNSUPPORTED) return st;
-    }
-    if (choice == 0 || choice == 3 || choice == 4) {
-      const int st = launch_strip_fast<pcg>(args, kp, s);
-      if (st != VDVC_ERR_UNSUPPORTED) return st;
-    }
+    const int st = args.m.h <= kElemMaxH ? launch_elem_fast<pcg>(args, kp, s) : launch_strip_fast<pcg>(args, kp, s);
+    if (st != VDVC_ERR_UNSUPPORTED) return st;
   }
   if constexpr (std::is_same<T, float>::value &&
                 (MODE == (kModeB | kModeRes) || MODE == (kModeB | kModeRes | kModeDiag))) {
-    if (hv_kernel_choice() != 2) {
-      const int st = launch_rhs_fast<(MODE & kModeDiag) != 0>(args, s);
-      if (st != VDVC_ERR_UNSUPPORTED) return st;
-    }
+    const int st = launch_rhs_fast<(MODE & kModeDiag) != 0>(args, s);
+    if (st != VDVC_ERR_UNSUPPORTED) return st;
   }
   StripShape sh = strip_shape(args.m.h);
   if (args.m.h > 128) return set_error(VDVC_ERR_UNSUPPORTED, "element edge h=%d > 128 not supported", args.m.h);
   if (args.m.Ny > 65535 || args.m.Nz > 65535) return set_error(VDVC_ERR_ARG, "Ny/Nz > 65535");
   dim3 grid((args.m.Nx + sh.EX - 1) / sh.EX, args.m.Ny, args.m.Nz);
   size_t smem = strip_smem_bytes(args.m.h, MODE, sizeof(T));
-  static bool attr_set = false;
-  if (!attr_set) {
-    VDVC_CUDA(cudaFuncSetAttribute(k_strip<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    attr_set = true;
-  }
+  if (int st = ensure_dyn_smem((const void*)k_strip<T, MODE>, 96 * 1024)) return st;
   StripArgs<T> a = args;
   a.EX = sh.EX;
   k_strip<T, MODE><<<grid, sh.threads, smem, s>>>(a, kp);

@@ -203,12 +203,8 @@ static int launch_h(const StripArgs<float>& args, const Kpair<float>* kp, cudaSt
   constexpr int EX = (H >= 128) ? 1 : 128 / H;
   const int threads = (EX * H + 31) / 32 * 32;
   const size_t smem = ((size_t)threads * 25 + 24 * (EX + 1) + 1152) * sizeof(float);
-  static bool attr_set = false;
-  if (!attr_set && smem > 48 * 1024) {
-    VDVC_CUDA(cudaFuncSetAttribute(k_strip_hv_fast<H, PCG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-    attr_set = true;
-  }
+  if (smem > 48 * 1024)
+    if (int st = ensure_dyn_smem((const void*)k_strip_hv_fast<H, PCG>, (int)smem)) return st;
   dim3 grid((args.m.Nx + EX - 1) / EX, args.m.Ny, args.m.Nz);
   StripArgs<float> a = args;
   a.EX = EX;
@@ -222,10 +218,6 @@ static int launch_h(const StripArgs<float>& args, const Kpair<float>* kp, cudaSt
 template <bool PCG>
 int launch_strip_fast(const StripArgs<float>& args, const Kpair<float>* kp, cudaStream_t s) {
   switch (args.m.h) {
-    case 1: return launch_h<1, PCG>(args, kp, s);
-    case 2: return launch_h<2, PCG>(args, kp, s);
-    case 3: return launch_h<3, PCG>(args, kp, s);
-    case 4: return launch_h<4, PCG>(args, kp, s);
     case 6: return launch_h<6, PCG>(args, kp, s);
     case 8: return launch_h<8, PCG>(args, kp, s);
     case 12: return launch_h<12, PCG>(args, kp, s);

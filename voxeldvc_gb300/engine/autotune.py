@@ -6,9 +6,7 @@ single level):
     small bodies stop sooner after convergence, large bodies amortise the
     per-body continue kernel and graph-node overhead;
   * concurrent -- a batch's problems on their own streams (parallel branches
-    of one graph) or serialised on one stream;
-  * (single solves at h <= 2) the persistent fused PCG kernel instead of
-    the graph (pcg_chunk = -1).
+    of one graph) or serialised on one stream.
 Each candidate runs one GN iteration with a short PCG from the same start
 (U restored before every trial), timed on the host around a synchronised
 call; the fastest is cached under a key of GPU name + problem class in

@@ -438,7 +438,7 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
 
     solver = C.c_void_p()
     _lib.check(L.vdvc_gn_create(C.byref(desc), ws.data_ptr(), nbytes, C.byref(solver)), "correlate_gpu")
-    info = {"gn_iters": 0, "pcg_iters": [], "ll": ll, "h": h, "precision": precision}
+    info = {"gn_iters": 0, "pcg_iters": [], "pcg_status": [], "ll": ll, "h": h, "precision": precision}
     t_start = time.perf_counter()
     try:
         st = D.stream()
@@ -458,6 +458,7 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
             _lib.check(L.vdvc_gn_update(solver, C.cast(out8, _lib.pd), st), "update")
             info["gn_iters"] = ik + 1
             info["pcg_iters"].append(iters.value)
+            info["pcg_status"].append(pstat.value)
             dd, uu = out8[0], out8[1]
             with np.errstate(divide='ignore', invalid='ignore'):
                 err = float(np.sqrt(np.float64(dd)) / np.sqrt(np.float64(uu)))
