@@ -3,24 +3,29 @@
 
 Workload (default `necking_512`): the 513^3 float32 pair of a fiber-composite
 texture (5000 cylinders) under tensile necking, h = 8 (64^3 elements,
-823,875 dof), equilibrium-gap regularizer, 3-level pyramid with FFT seed,
-dynamic mask frozen after 4 iterations (the `voxeldvc run` settings).  One
+823,875 dof), Laplacian regularizer with l0 = 4.5 h (the `voxeldvc run`
+settings; the equilibrium-gap variant is `--workload necking_512_eqgap`),
+3-level pyramid with FFT seed, dynamic mask frozen after 4 iterations.  One
 step = one complete plain-FP32 multiscale GN-PCG solve to the reference's
-stopping rules.  Data are synthetic and generated on the GPU (seeded);
-the inputs (540 MB each) are larger than L2, so no flush is needed.
+stopping rules.  Data are synthetic and generated on the GPU (seeded); the
+inputs (540 MB each) are larger than L2, so no flush is needed.
 
   value   device-resident solve time (s/solve), CUDA events on the stream
-  e2e     the same solve through the public API with host numpy inputs:
-          host->device image upload and device->host read of (U, res, dU)
-          inside the timed region
+  e2e     the same solve through the public API with ordinary (pageable)
+          host numpy inputs: host->device image upload and device->host
+          read of (U, res, dU) inside the timed region
   roofline  the matrix-free Hessian matvec at the finest level, timed with
-          CUDA events right after the timed solves on the same data
-  cpu_baseline  the CPU oracle (NumPy restatement of the reference) per
-          operation on a bounded sample, extrapolated to the solve with the
-          operation counts of the GPU solve
+          CUDA events right after the timed solves on the same data;
+          `traffic` is the DRAM bytes per voxel of an ncu capture of the
+          257^3 case scaled to this launch's voxel count
+  cpu_baseline  the reference's own operators (voxelDVC's engine on NumPy,
+          installed unmodified in baseline/_ref) on slabs of this run's
+          arrays over all host cores, assembled into a solve time with this
+          solve's GN / PCG counts (labelled extrapolated)
 
-`--impl reference` times only the CPU oracle leg (the reference has no CPU
-solver of its own besides its NumPy execution) and prints the same metric.
+`--impl reference` runs only the reference's CPU leg on the same workload
+(generated by the seeded NumPy generator, without this package's GPU
+library) and prints the same metric.
 """
 from __future__ import annotations
 
@@ -39,17 +44,19 @@ sys.path.insert(0, ROOT)
 
 METRIC = "512³ h=8 DVC time to 0.02vx RMS, plain vs mixed/learned; matvec GB/s"
 
-# Operation counts of the FP32 GB300 solve of necking_512 (per level, coarse
-# to fine): GN iterations and total PCG iterations.  The CPU leg multiplies
-# its measured per-operation times by these; the GPU leg reports its own
-# counts next to them in every run.
 # DRAM bytes per voxel of one float32 matvec (k_strip_hv_fast<8> + k_gather),
 # ncu dram__bytes_read + write on the 257^3 case.
 TRAFFIC_B_PER_VOXEL = 14.04
 
+# Operation counts (per pyramid level, coarse to fine: GN iterations, total
+# PCG iterations) that the reference arm multiplies its measured operation
+# times by: those of the GB300 FP32 solve of each workload, which match the
+# reference's own solve where it was run (tests/golden/baseline_*.npz: the
+# 513^3 necking workload's coarse level takes 30 GN / 730 PCG iterations
+# there, 30 / 752 here).  The GPU arm uses the counts of its own solve.
 SOLVE_COUNTS = {"necking_512": {"gn": [30, 4, 2], "pcg": [752, 84, 41]},
                 "necking_512_eqgap": {"gn": [30, 30, 30], "pcg": [60000, 60000, 60000]},
-                "necking_256": {"gn": [8, 6, 3], "pcg": [200, 108, 57]},
+                "necking_256": {"gn": [30, 6, 3], "pcg": [732, 106, 55]},
                 "plain_small": {"gn": [20, 7, 4], "pcg": [372, 138, 81]},
                 "large_1024": {"gn": [30, 30, 3, 2], "pcg": [2179, 1388, 140, 95]}}
 
@@ -749,10 +756,9 @@ def gpu_arm(args):
                              "achieved": round(achieved, 1), "peak": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs"
                              if "hbm_gbs" in peaks else "fallback 6800", "unit": "GB/s",
                              "frac": round(achieved / peak, 4),
-                             # DRAM bytes per launch from ncu on the 257^3 case (14.04 B per
-                             # voxel, profiles/strip_hv_fast_f32_necking257.md), scaled to
-                             # this launch's voxel count
                              "traffic": int(TRAFFIC_B_PER_VOXEL * nvox),
+                             "traffic_source": f"ncu dram bytes of the 257^3 case ({TRAFFIC_B_PER_VOXEL} B per "
+                                               f"voxel) scaled to this launch's {nvox} voxels",
                              "algorithmic_bytes": int(alg_bytes), "ms": round(mv_ms, 4)},
                 "cpu_baseline": cpu, "e2e": e2e, "forms": forms, "clocks": clocks}
         print(json.dumps(line))

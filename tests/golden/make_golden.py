@@ -533,7 +533,7 @@ def baseline_solve(case="plain_small", reg="laplacian", dtype="float32", scales=
     if scales:
         tag += "_s" + scales.replace("/", "")
     np.savez_compressed(os.path.join(OUT, f"baseline_{tag}.npz"), digest=np.array(WI.digest(f, g)),
-                        dims=np.array([Nx, Ny, Nz, h]), U=U, dU=dU, res_sumsq=np.float64(np.sum(np.square(res, dtype=np.float64))),
+                        dims=np.array([Nx, Ny, Nz, h]), U=U if U.size < 200_000 else U.astype(np.float32), res_sumsq=np.float64(np.sum(np.square(res, dtype=np.float64))),
                         gn_iters=np.array(gn), pcg_iters=np.array(pcg_counts), du_log=np.array(sum(levels, [])),
                         wall_s=np.float64(wall), reg=np.array(reg), l0=np.float64(kw["l0"]),
                         scales=np.array(kw["scales"]),

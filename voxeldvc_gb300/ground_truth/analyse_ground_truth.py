@@ -207,10 +207,9 @@ def analyse(work_dir, gt_dir):
     return stats
 
 
-def main(argv=None):
-    """Reference: ground_truth/analyse_ground_truth.py:204-382."""
-    args = parse_args(argv)
-    work_dir, gt_dir = os.path.expanduser(args.work_dir), os.path.expanduser(args.gt_dir)
+def analyse_logged(work_dir, gt_dir):
+    """analyse() with its report also written to
+    <work_dir>/ground_truth_comparison_log.txt; returns analyse()'s figures."""
     log_path = os.path.join(work_dir, 'ground_truth_comparison_log.txt')
     log_file = open(log_path, 'w')
     stdout = sys.stdout
@@ -219,11 +218,18 @@ def main(argv=None):
         print("=" * 70)
         print("GROUND-TRUTH COMPARISON")
         print("=" * 70)
-        analyse(work_dir, gt_dir)
+        stats = analyse(work_dir, gt_dir)
     finally:
         sys.stdout = stdout
         log_file.close()
     print(f"Log written to {log_path}")
+    return stats
+
+
+def main(argv=None):
+    """Reference: ground_truth/analyse_ground_truth.py:204-382."""
+    args = parse_args(argv)
+    analyse_logged(os.path.expanduser(args.work_dir), os.path.expanduser(args.gt_dir))
     return 0
 
 

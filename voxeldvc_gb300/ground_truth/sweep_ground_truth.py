@@ -1,8 +1,9 @@
-"""`voxeldvc sweep-ground-truth` (ground_truth/sweep_ground_truth.py of the
-reference): the known-answer pipeline once per (h, l0_factor) pair, each in
-<output-root>/h<h>_l0f<l0_factor>/, and a table of the node RMS error over
-the recoverable and the valid node sets (read back from the U_error.npy and
-node masks the analysis stage saves) with the last dU/U of the solve log.
+"""`voxeldvc sweep-ground-truth`: the known-answer accuracy check over a grid
+of (element edge h, regularisation length factor l0_factor) pairs, as the
+reference's ground_truth/sweep_ground_truth.py offers it: each pair's run
+in <output-root>/h<h>_l0f<l0_factor>/, then a table of the node RMS and max
+error over the recoverable and the valid node sets with each solve's last
+dU/U, the best pairs, and optionally a CSV.
 
   --gt-ref-file PATH (required), --gt-displacement-file PATH | --tensile-strain S
   --h H_LIST            comma-separated element edges (default 4,8,16)
@@ -10,38 +11,167 @@ node masks the analysis stage saves) with the last dU/U of the solve log.
   --output-root DIR     (required)
   --csv PATH            also write the table as CSV
 
-A pair whose recoverable RMS exceeds 1 voxel is marked DIVERGED (an
-under-regularised solve finishes its iterations with an implausible error
-rather than raising).
+How it runs here: the known-answer input (stage 1: reference volume,
+deformed volume, true field) depends on none of the swept parameters, so it
+is prepared once in <output-root>/gt_input and every pair's directory links
+to it; each pair then runs preprocess -> solve -> analysis in this process
+(one CUDA context), and its figures come straight from the analysis stage
+rather than from re-reading the arrays it saved.  A pair that raises is
+reported as FAILED and the sweep goes on; a pair whose recoverable RMS
+exceeds 1 voxel is flagged DIVERGED (an under-regularised solve ends its
+iterations with an implausible error instead of raising).
 """
 from __future__ import annotations
 
 import argparse
 import csv
+import itertools
+import math
 import os
 import re
 import sys
+from dataclasses import dataclass, field
 
-import numpy as np
-
-from .. import run_ground_truth_pipeline
+from .. import run_ground_truth_pipeline as pipeline
 
 DEFAULT_H_SWEEP = "4,8,16"
 DEFAULT_L0_FACTOR_SWEEP = "2.25,4.5,9"
 DIVERGED_RMS_THRESHOLD = 1.0  # voxels
 
-_DU_RE = re.compile(r'dU/U=([0-9.eE+-]+)')
+# The CSV columns and the solve-log pattern are what downstream tools read.
 FIELDS = ['h', 'l0_factor', 'l0', 'n_recoverable', 'n_total', 'rms', 'max_err', 'n_valid', 'rms_valid',
           'max_err_valid', 'du_final', 'status']
+DU_PATTERN = re.compile(r'dU/U=([0-9.eE+-]+)')
+
+NAN = float('nan')
+
+
+@dataclass
+class PairOutcome:
+    """One (h, l0_factor) run: node counts and errors over the recoverable
+    and valid sets ((count, RMS, max |error|) each), the solve's last dU/U
+    and 'ok' / 'FAILED'."""
+    h: int
+    l0_factor: float
+    n_total: int = 0
+    recoverable: tuple = (0, NAN, NAN)
+    valid: tuple = (0, NAN, NAN)
+    du_final: float = NAN
+    status: str = 'ok'
+    error: str = field(default='', repr=False)
+
+    @property
+    def l0(self):
+        return self.l0_factor * self.h
+
+    @property
+    def diverged(self):
+        return self.status == 'ok' and self.recoverable[1] > DIVERGED_RMS_THRESHOLD
+
+    def row(self):
+        """The CSV / table record (FIELDS)."""
+        return dict(h=self.h, l0_factor=self.l0_factor, l0=self.l0, n_recoverable=self.recoverable[0],
+                    n_total=self.n_total, rms=self.recoverable[1], max_err=self.recoverable[2],
+                    n_valid=self.valid[0], rms_valid=self.valid[1], max_err_valid=self.valid[2],
+                    du_final=self.du_final, status=self.status)
+
+    @classmethod
+    def from_analysis(cls, h, l0_factor, figures, du_final):
+        """From analyse_ground_truth.analyse()'s figures."""
+        return cls(h=h, l0_factor=l0_factor, n_total=int(figures['all'][0]),
+                   recoverable=tuple(figures['recoverable']),
+                   valid=tuple(figures.get('valid', (0, NAN, NAN))), du_final=du_final)
+
+
+def last_du_over_u(log_text):
+    """The last `dU/U=` value a solve log printed (NaN when there is none)."""
+    hits = DU_PATTERN.findall(log_text)
+    return float(hits[-1]) if hits else NAN
+
+
+def _read_last_du(work_dir):
+    try:
+        with open(os.path.join(work_dir, 'run_log.txt')) as fh:
+            return last_du_over_u(fh.read())
+    except OSError:
+        return NAN
+
+
+def pair_dir(output_root, h, l0_factor):
+    return os.path.join(output_root, f"h{h}_l0f{l0_factor:g}")
+
+
+def run_pair(output_root, gt_dir, h, l0_factor):
+    """Stages 2-4 of one pair on the shared prepared input."""
+    work = pair_dir(output_root, h, l0_factor)
+    os.makedirs(work, exist_ok=True)
+    link = os.path.join(work, 'gt_input')
+    if not os.path.lexists(link):
+        os.symlink(os.path.relpath(gt_dir, work), link)
+    print("\n" + "#" * 70)
+    print(f"# SWEEP COMBO: h={h}  l0_factor={l0_factor:g}  (l0={l0_factor * h:g} vox)")
+    print("#" * 70)
+    figures = pipeline.solve_and_analyse(work, gt_dir, h, l0_factor)
+    return PairOutcome.from_analysis(h, l0_factor, figures, _read_last_du(work))
+
+
+def sweep(h_values, l0_factors, output_root, gt_ref_file, gt_displacement_file=None, tensile_strain=None):
+    """Prepare the known-answer input once, then run every pair."""
+    gt_dir = os.path.join(output_root, 'gt_input')
+    pipeline.prepare_input(gt_dir, gt_ref_file, gt_displacement_file, tensile_strain)
+    outcomes = []
+    for h, lf in itertools.product(h_values, l0_factors):
+        try:
+            outcomes.append(run_pair(output_root, gt_dir, h, lf))
+        except Exception as exc:  # reported in the table; the other pairs still run
+            print(f"!! combo h={h}, l0_factor={lf:g} FAILED: {exc}", file=sys.stderr)
+            outcomes.append(PairOutcome(h=h, l0_factor=lf, status='FAILED', error=str(exc)))
+    return outcomes
+
+
+def best(outcomes, figure):
+    """The non-diverged successful pair with the smallest `figure` RMS
+    ('recoverable' or 'valid'), or None."""
+    pool = [o for o in outcomes if o.status == 'ok' and not o.diverged and not math.isnan(getattr(o, figure)[1])]
+    return min(pool, key=lambda o: getattr(o, figure)[1]) if pool else None
+
+
+def summary_lines(outcomes):
+    """The summary table and the best-pair lines, as printed."""
+    rule = "=" * 104
+    lines = ["", rule, "SWEEP SUMMARY: node RMS displacement error vs. h, l0_factor "
+             "(valid = fair measure; recoverable over-counts the boundary shell)", rule,
+             f"{'h':>4} {'l0_factor':>10} {'l0(vox)':>8} {'rec.nodes':>12} {'rec RMS':>10} {'rec max':>10} "
+             f"{'val.nodes':>12} {'valid RMS':>10} {'valid max':>10} {'final dU/U':>12}  status"]
+    for o in outcomes:
+        flag = 'DIVERGED' if o.diverged else ('' if o.status == 'ok' else o.status)
+        (nr, rr, mr), (nv, rv, mv) = o.recoverable, o.valid
+        lines.append(f"{o.h:>4} {o.l0_factor:>10g} {o.l0:>8g} {f'{nr}/{o.n_total}':>12} {rr:>10.5f} {mr:>10.5f} "
+                     f"{f'{nv}/{o.n_total}':>12} {rv:>10.5f} {mv:>10.5f} {o.du_final:>12.2e}  {flag}")
+    for figure, text in (('recoverable', "\nBest by recoverable RMS (non-diverged)"),
+                         ('valid', "Best by valid RMS (non-diverged, fair measure)")):
+        b = best(outcomes, figure)
+        if b is not None:
+            lines.append(f"{text}: h={b.h}, l0_factor={b.l0_factor:g} (l0={b.l0:g} vox) -> "
+                         f"RMS={getattr(b, figure)[1]:.5f} vox")
+    return lines
+
+
+def write_csv(path, outcomes):
+    with open(path, 'w', newline='') as fh:
+        w = csv.DictWriter(fh, fieldnames=FIELDS)
+        w.writeheader()
+        w.writerows(o.row() for o in outcomes)
+    print(f"\nSaved sweep summary CSV -> {path}")
 
 
 def parse_args(argv=None):
-    """Reference: ground_truth/sweep_ground_truth.py:73-99."""
+    """The reference's options (ground_truth/sweep_ground_truth.py:73-99)."""
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument('--gt-ref-file', type=str, required=True, dest='gt_ref_file')
-    g = p.add_mutually_exclusive_group(required=True)
-    g.add_argument('--gt-displacement-file', type=str, default=None, dest='gt_displacement_file')
-    g.add_argument('--tensile-strain', type=float, default=None, dest='tensile_strain')
+    src = p.add_mutually_exclusive_group(required=True)
+    src.add_argument('--gt-displacement-file', type=str, default=None, dest='gt_displacement_file')
+    src.add_argument('--tensile-strain', type=float, default=None, dest='tensile_strain')
     p.add_argument('--h', type=str, default=DEFAULT_H_SWEEP, dest='h_values')
     p.add_argument('--l0-factor', type=str, default=DEFAULT_L0_FACTOR_SWEEP, dest='l0_factors')
     p.add_argument('--output-root', type=str, required=True, dest='output_root')
@@ -49,117 +179,14 @@ def parse_args(argv=None):
     return p.parse_args(argv)
 
 
-def parse_final_du_over_u(run_log_path):
-    """The last `dU/U=` value of a solve log (NaN when absent).
-    Reference: ground_truth/sweep_ground_truth.py:102-113."""
-    try:
-        with open(run_log_path) as fh:
-            found = _DU_RE.findall(fh.read())
-    except OSError:
-        return float('nan')
-    return float(found[-1]) if found else float('nan')
-
-
-def _rms_max(error, mask):
-    sel = error[mask]
-    if sel.size == 0:
-        return float('nan'), float('nan')
-    return float(np.sqrt(np.mean(sel ** 2))), float(np.max(np.linalg.norm(sel, axis=-1)))
-
-
-def summarize_combo(work_dir):
-    """RMS / max error over the recoverable and valid node sets of one run.
-    Reference: ground_truth/sweep_ground_truth.py:126-158."""
-    error = np.load(os.path.join(work_dir, 'U_error.npy'))
-    truncated = np.load(os.path.join(work_dir, 'node_truncated_mask.npy'))
-    rec = ~truncated
-    rms, mx = _rms_max(error, rec)
-    vpath = os.path.join(work_dir, 'node_valid_mask.npy')
-    if os.path.exists(vpath):
-        valid = np.load(vpath)
-        n_valid = int(valid.sum())
-        rms_v, mx_v = _rms_max(error, valid)
-    else:
-        n_valid, rms_v, mx_v = 0, float('nan'), float('nan')
-    return dict(n_recoverable=int(rec.sum()), n_total=int(truncated.size), rms=rms, max_err=mx, n_valid=n_valid,
-                rms_valid=rms_v, max_err_valid=mx_v,
-                du_final=parse_final_du_over_u(os.path.join(work_dir, 'run_log.txt')), status='ok')
-
-
-def run_sweep(h_values, l0_factors, gt_ref_file, gt_displacement_file, tensile_strain, output_root):
-    """Reference: ground_truth/sweep_ground_truth.py:161-188."""
-    results = []
-    for h in h_values:
-        for lf in l0_factors:
-            combo = os.path.join(output_root, f"h{h}_l0f{lf:g}")
-            args = ['--h', str(h), '--l0-factor', str(lf), '--output-dir', combo, '--gt-ref-file', gt_ref_file]
-            if gt_displacement_file is not None:
-                args += ['--gt-displacement-file', gt_displacement_file]
-            if tensile_strain is not None:
-                args += ['--tensile-strain', str(tensile_strain)]
-            print("\n" + "#" * 70)
-            print(f"# SWEEP COMBO: h={h}  l0_factor={lf:g}  (l0={lf * h:g} vox)")
-            print("#" * 70)
-            try:
-                run_ground_truth_pipeline.main(args)
-                stats = summarize_combo(combo)
-            except Exception as exc:  # a failed pair is reported, the sweep goes on
-                print(f"!! combo h={h}, l0_factor={lf:g} FAILED: {exc}", file=sys.stderr)
-                stats = dict(n_recoverable=0, n_total=0, rms=float('nan'), max_err=float('nan'), n_valid=0,
-                             rms_valid=float('nan'), max_err_valid=float('nan'), du_final=float('nan'),
-                             status='FAILED')
-            results.append(dict(h=h, l0_factor=lf, l0=lf * h, **stats))
-    return results
-
-
-def _best(results, key):
-    ok = [r for r in results if r['status'] == 'ok' and not r['rms'] > DIVERGED_RMS_THRESHOLD
-          and not np.isnan(r[key])]
-    return min(ok, key=lambda r: r[key]) if ok else None
-
-
-def print_summary_table(results):
-    """Reference: ground_truth/sweep_ground_truth.py:204-236."""
-    print("\n" + "=" * 104)
-    print("SWEEP SUMMARY: node RMS displacement error vs. h, l0_factor "
-          "(valid = fair measure; recoverable over-counts the boundary shell)")
-    print("=" * 104)
-    print(f"{'h':>4} {'l0_factor':>10} {'l0(vox)':>8} {'rec.nodes':>12} {'rec RMS':>10} {'rec max':>10} "
-          f"{'val.nodes':>12} {'valid RMS':>10} {'valid max':>10} {'final dU/U':>12}  status")
-    for r in results:
-        flag = r['status'] if r['status'] != 'ok' else ('DIVERGED' if r['rms'] > DIVERGED_RMS_THRESHOLD else '')
-        print(f"{r['h']:>4} {r['l0_factor']:>10g} {r['l0']:>8g} {str(r['n_recoverable']) + '/' + str(r['n_total']):>12} "
-              f"{r['rms']:>10.5f} {r['max_err']:>10.5f} {str(r['n_valid']) + '/' + str(r['n_total']):>12} "
-              f"{r['rms_valid']:>10.5f} {r['max_err_valid']:>10.5f} {r['du_final']:>12.2e}  {flag}")
-    b = _best(results, 'rms')
-    if b is not None:
-        print(f"\nBest by recoverable RMS (non-diverged): h={b['h']}, l0_factor={b['l0_factor']:g} "
-              f"(l0={b['l0']:g} vox) -> RMS={b['rms']:.5f} vox")
-    b = _best(results, 'rms_valid')
-    if b is not None:
-        print(f"Best by valid RMS (non-diverged, fair measure): h={b['h']}, l0_factor={b['l0_factor']:g} "
-              f"(l0={b['l0']:g} vox) -> RMS={b['rms_valid']:.5f} vox")
-
-
-def write_csv(path, results):
-    """Reference: ground_truth/sweep_ground_truth.py:239-248."""
-    with open(path, 'w', newline='') as fh:
-        w = csv.DictWriter(fh, fieldnames=FIELDS)
-        w.writeheader()
-        for r in results:
-            w.writerow({k: r[k] for k in FIELDS})
-    print(f"\nSaved sweep summary CSV -> {path}")
-
-
 def main(argv=None):
-    """Reference: ground_truth/sweep_ground_truth.py:251-262."""
     args = parse_args(argv)
-    results = run_sweep([int(x) for x in args.h_values.split(',')], [float(x) for x in args.l0_factors.split(',')],
-                        args.gt_ref_file, args.gt_displacement_file, args.tensile_strain,
-                        os.path.abspath(args.output_root))
-    print_summary_table(results)
+    outcomes = sweep([int(x) for x in args.h_values.split(',')], [float(x) for x in args.l0_factors.split(',')],
+                     os.path.abspath(args.output_root), args.gt_ref_file, args.gt_displacement_file,
+                     args.tensile_strain)
+    print("\n".join(summary_lines(outcomes)))
     if args.csv_path:
-        write_csv(args.csv_path, results)
+        write_csv(args.csv_path, outcomes)
     return 0
 
 

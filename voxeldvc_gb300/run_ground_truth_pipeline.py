@@ -13,6 +13,11 @@ run uses:
   --l0-factor F      to stage 3 (default 4.5)
   --subprocess       run each stage as `python -m` (as the reference does)
                      instead of in this process (one CUDA context)
+
+In process, `prepare_input` (stage 1) and `solve_and_analyse` (stages 2-4)
+are also callable on their own; the latter returns the analysis figures, so
+a caller running many configurations on one prepared input (the sweep)
+reads them without going back to the saved arrays.
 """
 from __future__ import annotations
 
@@ -32,11 +37,16 @@ _STAGES = {
 }
 
 
-def run_stage(module, args, in_process=True):
-    """Reference: run_ground_truth_pipeline.py:51-56."""
+def _banner(module, args):
     print("\n" + "=" * 70)
     print("STAGE: " + " ".join([sys.executable, '-m', module] + list(args)))
     print("=" * 70)
+
+
+def run_stage(module, args, in_process=True):
+    """One stage as `python -m module args` or its main() in this process.
+    Reference: run_ground_truth_pipeline.py:51-56."""
+    _banner(module, args)
     if not in_process:
         subprocess.run([sys.executable, '-m', module] + list(args), check=True)
         return
@@ -44,6 +54,33 @@ def run_stage(module, args, in_process=True):
     rc = importlib.import_module(module).main(list(args))
     if rc not in (None, 0):
         raise RuntimeError(f"stage {module} exited with {rc}")
+
+
+def prepare_input(gt_dir, gt_ref_file=None, gt_displacement_file=None, tensile_strain=None, in_process=True):
+    """Stage 1 into gt_dir (ref.npy, deformed.npy, U.npy, ...)."""
+    args = ['--output-dir', gt_dir]
+    if gt_ref_file is not None:
+        args += ['--gt-ref-file', gt_ref_file]
+    if gt_displacement_file is not None:
+        args += ['--gt-displacement-file', gt_displacement_file]
+    if tensile_strain is not None:
+        args += ['--tensile-strain', str(tensile_strain)]
+    run_stage(_STAGES['prepare'], args, in_process)
+
+
+def solve_and_analyse(work_dir, gt_dir, h=DEFAULT_H, l0_factor=DEFAULT_L0_FACTOR, in_process=True):
+    """Stages 2-4 on a prepared input; returns the analysis figures
+    ({'recoverable': (n, rms, max), 'valid': ..., 'truncated': ..., 'all':
+    ...}) in process, None with in_process=False."""
+    run_stage(_STAGES['preprocess'], [os.path.join(gt_dir, 'ref.npy'), os.path.join(gt_dir, 'deformed.npy'),
+                                      '--h', str(h), '--output-dir', work_dir], in_process)
+    run_stage(_STAGES['run'], [work_dir, '--l0-factor', str(l0_factor)], in_process)
+    if not in_process:
+        run_stage(_STAGES['analyse'], ['--work-dir', work_dir, '--gt-dir', gt_dir], False)
+        return None
+    from .ground_truth import analyse_ground_truth as AG
+    _banner(_STAGES['analyse'], ['--work-dir', work_dir, '--gt-dir', gt_dir])
+    return AG.analyse_logged(work_dir, gt_dir)
 
 
 def parse_args(argv=None):
@@ -66,18 +103,8 @@ def main(argv=None):
     out = os.path.abspath(args.output_dir)
     gt = os.path.join(out, 'gt_input')
     inproc = not args.subprocess
-    stage1 = ['--output-dir', gt]
-    if args.gt_ref_file is not None:
-        stage1 += ['--gt-ref-file', args.gt_ref_file]
-    if args.gt_displacement_file is not None:
-        stage1 += ['--gt-displacement-file', args.gt_displacement_file]
-    if args.tensile_strain is not None:
-        stage1 += ['--tensile-strain', str(args.tensile_strain)]
-    run_stage(_STAGES['prepare'], stage1, inproc)
-    run_stage(_STAGES['preprocess'], [os.path.join(gt, 'ref.npy'), os.path.join(gt, 'deformed.npy'),
-                                      '--h', str(args.h), '--output-dir', out], inproc)
-    run_stage(_STAGES['run'], [out, '--l0-factor', str(args.l0_factor)], inproc)
-    run_stage(_STAGES['analyse'], ['--work-dir', out, '--gt-dir', gt], inproc)
+    prepare_input(gt, args.gt_ref_file, args.gt_displacement_file, args.tensile_strain, inproc)
+    solve_and_analyse(out, gt, args.h, args.l0_factor, inproc)
     print("\n" + "=" * 70)
     print("✓ GROUND-TRUTH PIPELINE COMPLETE")
     print("=" * 70)
