@@ -46,9 +46,9 @@ enum {
                                 ZeroDivisionError at correlate_gpu.py:1095)      */
   VDVC_ERR_CUFFT = 7,        /* cuFFT plan/exec failure                          */
   VDVC_ERR_UNSUPPORTED = 8,  /* valid request this build does not implement      */
-  VDVC_ERR_TIMEOUT = 9       /* a bounded device-side wait (grid barrier,
-                                mbarrier) ran out; the kernel returned without
-                                finishing and the context stays usable      */
+  VDVC_ERR_TIMEOUT = 9       /* a bounded device-side wait (mbarrier) ran
+                                out; the kernel returned without finishing
+                                and the context stays usable                */
 };
 
 /* element types for dtype / pix_dtype arguments */
@@ -140,15 +140,15 @@ int vdvc_matvec_H_noalloc(const float* v, const float* grad,
 size_t vdvc_matvec_H_noalloc_max_elements(void);
 
 /* ---- failure detection -------------------------------------------------- */
-/* Runs one of the library's bounded device-side waits and reports it the way
-   the production kernels do.  which = 0: the grid barrier of the fused PCG
-   iteration, expecting one block more than the launch holds, so nothing
-   releases it; 1: the mbarrier wait of the bulk-copy staging, on a barrier
-   nothing arrives at; 2 / 3: the same waits released normally.  Every wait
-   gives up after max_polls polls (1 .. 2e7).  Returns VDVC_ERR_TIMEOUT for
-   0 and 1 and VDVC_OK for 2 and 3, with every block returned and the CUDA
-   context usable; nothing faults or hangs.  Synchronises the stream.  No
-   counterpart in the reference (which has no device-side waits). */
+/* Runs the library's bounded device-side wait -- the mbarrier wait of the
+   bulk-copy and tensor-core pipelines (element-Hessian matvec and formation,
+   tensor-core convolutions) -- and reports it the way those kernels do.
+   which = 0: on a barrier nothing arrives at, so the wait gives up after
+   max_polls polls (1 .. 2^24) and the call returns VDVC_ERR_TIMEOUT; 1: the
+   same wait released normally, VDVC_OK.  The kernel always returns and the
+   CUDA context stays usable; nothing faults or hangs.  Synchronises the
+   stream.  No counterpart in the reference (which has no device-side
+   waits). */
 int vdvc_selftest_bounded_wait(int which, long long max_polls, vdvc_stream_t stream);
 
 /* Precision form of matvec_H (kernels_dvc.py:452-506): the gradient is

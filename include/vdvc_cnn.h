@@ -38,10 +38,13 @@ typedef struct vdvc_conv_geom {
 } vdvc_conv_geom;
 
 /* out[p][n] = act( sum_{t,k} src[q(p,t)][k] * w[n][t][k] + bias[n] ),
-   on the tensor cores (mma.sync m16n8k16, BF16 x BF16 -> FP32).
+   on the tensor cores, BF16 x BF16 -> FP32: tcgen05.mma with the
+   accumulator in TMEM when the channel chunks are 16-byte aligned (source
+   channel stride and offset multiples of 8, src and w 16-byte aligned;
+   n_out <= 256), else mma.sync m16n8k16 (n_out <= 80).
    cin: a multiple of 16, or 2 (then w is [n_pad][64] with k = 2t + ci and
-   zero rows k >= 54).  Otherwise w is BF16 [n_pad][27][cin].
-   n_pad = n_out rounded up to 8 (<= 80); rows n >= n_out must be zero.
+   zero rows k >= 54, mma.sync).  Otherwise w is BF16 [n_pad][27][cin].
+   n_pad = n_out rounded up to 8; rows n >= n_out must be zero.
    bias: FP32 (n_out) or NULL.  relu: apply max(0, .).
    out_f32: store FP32 instead of BF16.  accumulate (BF16 output only):
    out += result (the input-gradient sum of two consumers). */
@@ -50,6 +53,11 @@ int vdvc_cnn_conv(const void* src, int src_cstride, int src_coff, int cin,
                   void* out, int out_f32, int out_cstride, int out_coff,
                   int accumulate, const vdvc_conv_geom* geom,
                   vdvc_stream_t stream);
+
+/* Synchronises the stream; VDVC_ERR_TIMEOUT (and clears the flag) when a
+   tensor-core convolution launched since the last call gave up one of its
+   bounded waits -- its output is then incomplete -- else VDVC_OK. */
+int vdvc_cnn_status(vdvc_stream_t stream);
 
 /* Weight gradient of a forward convolution (geom = its forward geometry):
    dw[n][t][k] (+)= sum_p dy[p][n] * x[q(p,t)][k], FP32 [n_out][27][cin],

@@ -45,6 +45,10 @@ CONV_CASES = [  # (cin, n_out, stride, source grid (x, y, z))
     (64, 16, 1, (5, 5, 5)),
     (16, 3, 1, (7, 6, 5)),
     (32, 80, 2, (5, 7, 9)),
+    # beyond the mma.sync form (n_out > 80): the tcgen05 form only, several
+    # 128-position tiles and a partial last tile
+    (64, 128, 2, (17, 9, 11)),
+    (128, 64, 1, (9, 10, 11)),
 ]
 
 
@@ -84,7 +88,7 @@ def test_conv_forward_input_grad_wgrad(env, cin, n_out, stride, src):
     assert rel(yf.cpu().numpy().reshape(ref.shape), ref_lin) < 1e-5
 
     # input gradient through the transposed weights and the adjoint geometry
-    if cin != 2 and n_out <= 64:
+    if cin != 2 and n_out <= 128:
         dy = O.bf16_round(rng.standard_normal(ref.shape))
         dyp = np.zeros(ref.shape[:3] + (npad16,))
         dyp[..., :n_out] = dy

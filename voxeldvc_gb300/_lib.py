@@ -114,6 +114,7 @@ SIGNATURES = {
     "vdvc_synth_field_grid": (ci, [ci, pd, ci, ci, ci, ci, cd, vp, vp]),
     # include/vdvc_cnn.h
     "vdvc_cnn_conv": (ci, [vp, ci, ci, ci, vp, vp, ci, ci, vp, ci, ci, ci, ci, vp, vp]),
+    "vdvc_cnn_status": (ci, [vp]),
     "vdvc_cnn_conv_wgrad": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, vp, vp, ci, vp, cz, vp]),
     "vdvc_cnn_wgrad_workspace_bytes": (cz, [ci, ci]),
     "vdvc_cnn_bias_grad": (ci, [vp, ci, ci, ci, C.c_longlong, vp, ci, vp, cz, vp]),

@@ -21,6 +21,8 @@
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <map>
+#include <mutex>
 
 #include "ops.cuh"
 #include "vdvc_cnn.h"
@@ -28,6 +30,10 @@
 namespace vdvc {
 
 typedef __nv_bfloat16 bf16;
+
+int launch_conv_tc(const void* src, int scs, int scoff, int cin, const void* w, int wrows, const float* bias,
+                   int n_out, int relu, void* out, int out_f32, int ocs, int ocoff, int accumulate,
+                   const vdvc_conv_geom* geom, int* err, cudaStream_t s);
 
 struct Geo {
   int nx, ny, nz, sx, sy, sz, a, b, c, d;
@@ -49,6 +55,26 @@ __device__ __forceinline__ long long src_index(int x, int y, int z, int t, const
   const int qx = map_src(x, tx, g, g.sx), qy = map_src(y, ty, g, g.sy), qz = map_src(z, tz, g, g.sz);
   if (qx < 0 || qy < 0 || qz < 0) return -1;
   return ((long long)qz * g.sy + qy) * g.sx + qx;
+}
+
+// Timeout flag of the tensor-core convolutions (conv_tc.cu), one per device
+// that loads the library; its address is looked up once per device.
+__device__ int g_conv_err;
+
+int conv_error_flag(int** out) {
+  static std::mutex mu;
+  static std::map<int, int*> addr;
+  int dev = 0;
+  VDVC_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = addr.find(dev);
+  if (it == addr.end()) {
+    void* p = nullptr;
+    VDVC_CUDA(cudaGetSymbolAddress(&p, g_conv_err));
+    it = addr.emplace(dev, (int*)p).first;
+  }
+  *out = it->second;
+  return VDVC_OK;
 }
 
 __device__ __forceinline__ uint32_t ld32(const bf16* p) { return __ldg((const unsigned int*)p); }
@@ -548,13 +574,25 @@ int vdvc_cnn_conv(const void* src, int src_cstride, int src_coff, int cin, const
                   const vdvc_conv_geom* geom, vdvc_stream_t stream) {
   VDVC_CHECK_ARG(src && w && out && geo_ok(geom), "bad arguments");
   VDVC_CHECK_ARG(cin == 2 || (cin >= 16 && cin % 16 == 0), "cin must be 2 or a multiple of 16 (got %d)", cin);
-  VDVC_CHECK_ARG(n_out >= 1 && n_out <= 80, "n_out must be in [1, 80]");
+  VDVC_CHECK_ARG(n_out >= 1 && n_out <= 256, "n_out must be in [1, 256]");
   VDVC_CHECK_ARG(src_cstride % 2 == 0 && src_coff % 2 == 0 && src_coff >= 0 && src_coff + cin <= src_cstride,
                  "source channel range [%d, %d) does not fit stride %d (even offsets required)", src_coff,
                  src_coff + cin, src_cstride);
   VDVC_CHECK_ARG(out_coff >= 0 && out_coff + n_out <= out_cstride, "output channel range does not fit its stride");
   VDVC_CHECK_ARG(al4(src) && al4(w), "src and w must be 4-byte aligned");
   VDVC_CHECK_ARG(!(accumulate && out_f32), "accumulate needs a BF16 output");
+  cudaStream_t s = (cudaStream_t)stream;
+  // the tensor-core form wherever the channel chunks are 16-byte aligned
+  if (cin != 2) {
+    int* err = nullptr;
+    int st = conv_error_flag(&err);
+    if (st) return st;
+    st = launch_conv_tc(src, src_cstride, src_coff, cin, w, (n_out + 7) / 8 * 8, bias, n_out, relu, out, out_f32,
+                        out_cstride, out_coff, accumulate, geom, err, s);
+    if (st != VDVC_ERR_UNSUPPORTED) return st;
+  }
+  VDVC_CHECK_ARG(n_out <= 80, "n_out must be in [1, 80] unless the layer fits the tensor-core form "
+                              "(channel strides and offsets multiples of 8, 16-byte aligned tensors)");
   const int nf = (n_out + 7) / 8;
   if (cin == 2) VDVC_CHECK_ARG(nf <= 4, "cin == 2 supports n_out <= 32");
   const Geo g = to_geo(geom);
@@ -562,7 +600,6 @@ int vdvc_cnn_conv(const void* src, int src_cstride, int src_coff, int cin, const
   const long long nb = (npos + 63) / 64;
   VDVC_CHECK_ARG(nb < 0x7fffffffLL, "grid too large");
   dim3 grid((unsigned)nb);
-  cudaStream_t s = (cudaStream_t)stream;
   const bf16* sp = (const bf16*)src;
   const bf16* wp = (const bf16*)w;
   const bool small = cin == 2;
@@ -579,6 +616,22 @@ int vdvc_cnn_conv(const void* src, int src_cstride, int src_coff, int cin, const
     case 10: launch_conv_nf<10>(small, grid, sp, src_cstride, src_coff, cin, wp, bias, n_out, relu, out, out_f32, out_cstride, out_coff, accumulate, g, s); break;
   }
   VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_cnn_status(vdvc_stream_t stream) {
+  int* err = nullptr;
+  int st = conv_error_flag(&err);
+  if (st) return st;
+  int h = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  VDVC_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  if (h) {
+    VDVC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    VDVC_CUDA(cudaStreamSynchronize(s));
+    return set_error(VDVC_ERR_TIMEOUT, "a tensor-core convolution gave up a bounded wait; its output is incomplete");
+  }
   return VDVC_OK;
 }
 

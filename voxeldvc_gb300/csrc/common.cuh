@@ -208,71 +208,6 @@ __device__ bool grid_reduce_sum(const GridReduce& gr, const double (&mine)[NV], 
   return true;
 }
 
-// ---- grid-wide barrier (cooperative launches only) ---------------------------
-//
-// Every block of the grid calls grid_barrier(); all blocks must be resident
-// (a cooperative launch guarantees it).  bar[0] counts arrivals, bar[1] is
-// the generation; both start at zero and are left consistent for the next
-// barrier.  The wait is bounded: after `spin_limit` polls a block sets *err,
-// every later or still-waiting block sees it and leaves, and the call
-// returns false in every thread of those blocks -- the kernel then skips its
-// remaining work and the host reports VDVC_ERR_TIMEOUT.  `expected` is the
-// number of arrivals that releases the barrier (gridDim for a real barrier).
-
-constexpr long long kBarrierSpinLimit = 20000000;  // polls: seconds, far beyond a healthy barrier
-
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err, unsigned int expected,
-                                             long long spin_limit) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned int* vgen = bar + 1;
-    volatile int* verr = err;
-    const unsigned int g = *vgen;
-    __threadfence();
-    int ok = 1;
-    if (atomicAdd(bar, 1u) == expected - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      long long spins = 0;
-      while (*vgen == g) {
-        if (*verr) {
-          ok = 0;
-          break;
-        }
-        if (++spins > spin_limit) {
-          atomicExch(err, 1);
-          ok = 0;
-          break;
-        }
-      }
-    }
-    __threadfence();
-    if (*verr) ok = 0;
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
-// Sum of partials[b] over b < nb in a fixed order (thread t takes b = t,
-// t + blockDim.x, ...; then the fixed block reduction), returned in every
-// thread: every block that calls it gets the same bits.
-__device__ __forceinline__ double all_blocks_sum(const double* partials, unsigned int nb, double* s_red,
-                                                 double* s_bc) {
-  double v = 0.0;
-#pragma unroll 4
-  for (unsigned int b = threadIdx.x; b < nb; b += blockDim.x) v += __ldcg(partials + b);
-  v = block_sum(v, s_red);
-  if (threadIdx.x == 0) *s_bc = v;
-  __syncthreads();
-  v = *s_bc;
-  __syncthreads();
-  return v;
-}
-
 // Scratch carving helper: successive 256-byte aligned sub-buffers of ws.
 struct Carve {
   char* base;

@@ -1,0 +1,357 @@
+// 3x3x3 gather convolution (include/vdvc_cnn.h) on the 5th-generation tensor
+// cores: tcgen05.mma kind::f16 (BF16 x BF16 -> FP32 in TMEM).
+//
+// GEMM view: D[p][n] = sum_K A[p][K] B[n][K], with p the output positions
+// (M = 128 per CTA), n the output channels (N = n_out rounded up to 16) and
+// K = (tap t, input channel c) in the order t * cin + c -- the order of the
+// packed forward weights [n_pad][27][cin] and of the input-gradient weights
+// [cin_pad][27][n_pad16], so both read unchanged.  One K-block is 64 K
+// values = eight 16-byte chunks of 8 channels; a chunk of row p is 16
+// contiguous bytes of the channels-last source at position q(p, t) (zero
+// when q falls outside the source), copied by cp.async straight into the
+// no-swizzle K-major canonical layout (8-row x 16-byte core matrices).
+// B rows past the packed rows and K past 27 * cin are zero-filled the same
+// way (src-size 0), so no extra padding is needed in global memory.
+//
+// Pipeline (128 threads, one output tile per CTA): kStages shared-memory
+// stages of (A, B); every thread copies its own A row's eight chunks and a
+// share of B for a stage, the CTA syncs, one thread issues the four K = 16
+// MMAs and commits them to the stage's mbarrier, and a stage is refilled
+// only after that mbarrier says its MMAs are done.  The epilogue reads the
+// accumulator from TMEM (each warp its 32 lanes = 32 positions), adds the
+// bias, applies ReLU and stores BF16 (optionally added to the output) or
+// FP32.  Every mbarrier wait is bounded: on a timeout the CTA sets *err,
+// skips its stores, waits (bounded) for its MMAs, frees its TMEM and
+// returns; the host reports VDVC_ERR_TIMEOUT.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "ops.cuh"
+#include "tma.cuh"
+#include "vdvc_cnn.h"
+
+namespace vdvc {
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int kThreads = 128;
+constexpr int kM = 128;
+constexpr int kStages = 4;
+constexpr uint32_t kAStage = kM * 64 * 2;  // 16 KB
+
+struct TcGeo {
+  int nx, ny, nz, sx, sy, sz, a, b, c, d;
+};
+
+__device__ __forceinline__ int tap_src(int p, int t, int a, int b, int c, int d, int S) {
+  int num = p * a + b + t * c;
+  if (num < 0) return -1;
+  if (d != 1) {
+    if (num % d) return -1;
+    num /= d;
+  }
+  return num < S ? num : -1;
+}
+
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src, uint32_t nbytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(nbytes) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void tc_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int c = 0; c < 16; ++c) v[c] = __uint_as_float(r[c]);
+}
+
+// no-swizzle K-major shared-memory descriptor (sm_100 family, version 1)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// kind::f16 instruction descriptor: FP32 D, BF16 A and B, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// byte offset of 16-byte chunk `ch` (0..7) of row `row` in a K-major tile of
+// `rows` rows: core matrix (row / 8, ch) at (ch * rows / 8 + row / 8) * 128
+__device__ __forceinline__ uint32_t chunk_off(int row, int ch, int rows) {
+  return (uint32_t)(((ch * (rows >> 3) + (row >> 3)) << 7) + ((row & 7) << 4));
+}
+
+struct ConvTcArgs {
+  const bf16* src;
+  int scs, scoff, cin;
+  const bf16* w;     // [wrows][27 * cin]
+  int wrows;         // packed weight rows (>= n_out)
+  const float* bias;
+  int n_out, NT;     // NT: n_out rounded up to 16
+  int relu, out_f32, ocs, ocoff, accumulate;
+  void* out;
+  TcGeo g;
+  int* err;
+};
+
+__global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvTcArgs A) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int NT = A.NT;
+  const uint32_t bstage = (uint32_t)NT * 128;
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + kStages * kAStage;
+  uint64_t* bars = (uint64_t*)(sB + kStages * bstage);  // kStages mbarriers
+  uint32_t* s_tmem = (uint32_t*)(bars + kStages);
+  int* s_fail = (int*)(s_tmem + 1);
+  int* s_last = s_fail + 1;  // last K-block whose MMAs were committed
+
+  const TcGeo& g = A.g;
+  const long long npos = (long long)g.nx * g.ny * g.nz;
+  const long long p = (long long)blockIdx.x * kM + tid;  // this thread's A row
+  const bool prow = p < npos;
+  int px = 0, py = 0, pz = 0;
+  if (prow) {
+    px = (int)(p % g.nx);
+    const long long r = p / g.nx;
+    py = (int)(r % g.ny);
+    pz = (int)(r / g.ny);
+  }
+  const int cpt = A.cin >> 3;           // 16-byte chunks per tap
+  const int nchunks = 27 * cpt;         // K chunks with data
+  const int nkb = (nchunks + 7) >> 3;   // K-blocks of 64
+  const long long krow = 27LL * A.cin;  // packed weight row length
+
+  uint32_t ncols = 32;
+  while ((int)ncols < NT) ncols <<= 1;
+  if (warp == 0) {
+    tc_alloc(s_tmem, ncols);
+    tc_relinquish();
+  }
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+    *s_fail = 0;
+    *s_last = -1;
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *s_tmem;
+  const uint32_t idesc = idesc_bf16(kM, NT);
+  const uint32_t aLBO = (kM / 8) * 128, bLBO = (uint32_t)(NT / 8) * 128;
+
+  // issue the copies of K-block kb into stage st
+  auto load_stage = [&](int kb, int st) {
+    const uint32_t a0 = smem_addr(sA + st * kAStage);
+    int last_t = -1;
+    long long si = -1;
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+      const int kc = kb * 8 + ch;
+      const bf16* srcp = A.src;
+      uint32_t nb = 0;
+      if (prow && kc < nchunks) {
+        const int t = kc / cpt;
+        if (t != last_t) {
+          last_t = t;
+          const int qx = tap_src(px, t % 3, g.a, g.b, g.c, g.d, g.sx);
+          const int qy = tap_src(py, (t / 3) % 3, g.a, g.b, g.c, g.d, g.sy);
+          const int qz = tap_src(pz, t / 9, g.a, g.b, g.c, g.d, g.sz);
+          si = (qx < 0 || qy < 0 || qz < 0) ? -1 : ((long long)qz * g.sy + qy) * g.sx + qx;
+        }
+        if (si >= 0) {
+          srcp = A.src + si * A.scs + A.scoff + (kc - t * cpt) * 8;
+          nb = 16;
+        }
+      }
+      cp16(a0 + chunk_off(tid, ch, kM), srcp, nb);
+    }
+    const uint32_t b0 = smem_addr(sB + st * bstage);
+    for (int q = tid; q < NT * 8; q += kThreads) {
+      const int n = q >> 3, ch = q & 7;
+      const int kc = kb * 8 + ch;
+      const bf16* srcp = A.w;
+      uint32_t nb = 0;
+      if (n < A.wrows && kc < nchunks) {
+        srcp = A.w + (long long)n * krow + (long long)kc * 8;
+        nb = 16;
+      }
+      cp16(b0 + chunk_off(n, ch, NT), srcp, nb);
+    }
+  };
+
+  bool ok = true;
+  // prologue: kStages - 1 K-blocks in flight
+  for (int kb = 0; kb < kStages - 1; ++kb) {
+    if (kb < nkb) load_stage(kb, kb);
+    cp_commit();
+  }
+  for (int kb = 0; kb < nkb; ++kb) {
+    // refill: K-block kb + kStages - 1 into the stage K-block kb - 1 used
+    const int nk = kb + kStages - 1;
+    if (nk < nkb) {
+      const int st = nk % kStages;
+      if (nk >= kStages) {
+        // that stage's previous MMAs (K-block nk - kStages) must be done
+        if (!mbar_wait_bounded(&bars[st], (uint32_t)((nk / kStages - 1) & 1))) ok = false;
+      }
+      load_stage(nk, st);
+    }
+    cp_commit();
+    cp_wait<kStages - 1>();  // this thread's copies of K-block kb have landed
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) *s_fail = 1;
+      break;
+    }
+    if (tid == 0) {
+      tc_fence_after();
+      const int st = kb % kStages;
+      const uint32_t a0 = smem_addr(sA + st * kAStage), b0 = smem_addr(sB + st * bstage);
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const uint64_t ad = smem_desc(a0 + kk * 2 * aLBO, aLBO, 128);
+        const uint64_t bd = smem_desc(b0 + kk * 2 * bLBO, bLBO, 128);
+        tc_mma(tmem, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+      }
+      tc_commit(&bars[st]);
+      *s_last = kb;
+    }
+  }
+  cp_wait<0>();
+  __syncthreads();
+  // the last commit covers every MMA issued before it
+  const int lastkb = *s_last;
+  if (lastkb < nkb - 1) ok = false;
+  if (lastkb >= 0 && !mbar_wait_bounded(&bars[lastkb % kStages], (uint32_t)((lastkb / kStages) & 1))) ok = false;
+  tc_fence_after();
+  __syncthreads();
+  const bool fail = __syncthreads_or(!ok) || *s_fail;
+  if (!fail) {
+    const long long pr = (long long)blockIdx.x * kM + warp * 32 + lane;
+    for (int c0 = 0; c0 < NT; c0 += 16) {
+      float v[16];
+      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (pr >= npos) continue;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int n = c0 + c;
+        float x = v[c];
+        if (A.bias && n < A.n_out) x += A.bias[n];
+        if (A.relu) x = fmaxf(x, 0.f);
+        v[c] = x;
+      }
+      const long long o = pr * A.ocs + A.ocoff + c0;
+      if (A.out_f32) {
+        float* op = (float*)A.out + o;
+        for (int c = 0; c < 16 && c0 + c < A.n_out; ++c) op[c] = v[c];
+      } else {
+        bf16* op = (bf16*)A.out + o;
+        for (int c = 0; c < 16 && c0 + c < A.n_out; ++c) {
+          float x = v[c];
+          if (A.accumulate) x += __bfloat162float(op[c]);
+          op[c] = __float2bfloat16_rn(x);
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(A.err, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tc_dealloc(tmem, ncols);
+  }
+}
+
+}  // namespace
+
+size_t conv_tc_smem_bytes(int n_out) {
+  const int NT = (n_out + 15) / 16 * 16;
+  return (size_t)kStages * (kAStage + (size_t)NT * 128) + kStages * 8 + 32;
+}
+
+// VDVC_ERR_UNSUPPORTED (error text untouched) when the layer does not fit
+// the tensor-core form: cin a multiple of 8 with 16-byte aligned channel
+// chunks (strides and offsets multiples of 8 channels), n_out <= 256.
+int launch_conv_tc(const void* src, int scs, int scoff, int cin, const void* w, int wrows, const float* bias,
+                   int n_out, int relu, void* out, int out_f32, int ocs, int ocoff, int accumulate,
+                   const vdvc_conv_geom* geom, int* err, cudaStream_t s) {
+  if (cin < 8 || cin % 8 || scs % 8 || scoff % 8 || n_out > 256 || wrows < n_out) return VDVC_ERR_UNSUPPORTED;
+  if (((uintptr_t)src | (uintptr_t)w) & 15) return VDVC_ERR_UNSUPPORTED;
+  ConvTcArgs a{};
+  a.src = (const bf16*)src;
+  a.scs = scs;
+  a.scoff = scoff;
+  a.cin = cin;
+  a.w = (const bf16*)w;
+  a.wrows = wrows;
+  a.bias = bias;
+  a.n_out = n_out;
+  a.NT = (n_out + 15) / 16 * 16;
+  a.relu = relu;
+  a.out_f32 = out_f32;
+  a.ocs = ocs;
+  a.ocoff = ocoff;
+  a.accumulate = accumulate;
+  a.out = out;
+  a.g = TcGeo{geom->nx, geom->ny, geom->nz, geom->sx, geom->sy, geom->sz, geom->a, geom->b, geom->c, geom->d};
+  a.err = err;
+  const long long npos = (long long)geom->nx * geom->ny * geom->nz;
+  const long long nb = (npos + kM - 1) / kM;
+  if (nb >= 0x7fffffffLL) return set_error(VDVC_ERR_ARG, "grid too large");
+  const size_t smem = conv_tc_smem_bytes(n_out);
+  if (int st = ensure_dyn_smem((const void*)k_conv_tc, (int)smem)) return st;
+  k_conv_tc<<<(unsigned)nb, kThreads, smem, s>>>(a);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+}  // namespace vdvc

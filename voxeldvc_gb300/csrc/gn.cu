@@ -54,15 +54,10 @@ struct GnSolver {
   double* partials;
   size_t n_partials;
   unsigned int* ticket;
-  unsigned int* bar;  // fused PCG grid barrier: count, generation, timeout flag
   GnScalars* sc;
   PcgState* pcg;
   Kpair<T>* kp;
   bool frozen_set;
-  // PCG iteration form: gather and update fused in one cooperative launch
-  // (single solves), or the two-kernel form (batches, whose problems run as
-  // concurrent graph branches and so cannot promise co-resident grids)
-  bool fused_pcg;
   // precision form
   bool mixed;
   bool eh_fixed;     // T, diag and M^-1 are final (b mask frozen, or mask0)
@@ -109,7 +104,6 @@ static size_t carve_solver(const Mesh& m, GnSolver<T>* S, void* ws, size_t bytes
   S->n_partials = (size_t)(nb > kReduceBlocks ? nb : kReduceBlocks) * 4;
   S->partials = cv.take<double>(S->n_partials);
   S->ticket = cv.take<unsigned int>(4);
-  S->bar = cv.take<unsigned int>(4);  // fused PCG: count, generation, timeout flag
   S->sc = cv.take<GnScalars>(1);
   S->pcg = cv.take<PcgState>(1);
   S->kp = cv.take<Kpair<T>>(1);
@@ -315,15 +309,10 @@ static bool eager_pcg() {
   return e && e[0] == 'e';
 }
 
-// After the element pass: Ap, alpha, and the x / r / z update.
+// After the element pass: p, Ap and alpha (gather), then the x / r / z
+// update with the convergence test.
 template <typename T>
 static int pcg_gather_update(GnSolver<T>* S, cudaStream_t s) {
-  if (S->fused_pcg) {
-    // partials: [0, 1024) p.Ap per block, then 2 x 1024 for r.r and r.z
-    GridReduce red{S->partials + kReduceBlocks, S->ticket};
-    return launch_pcg_gather_update<T>(S->m, S->evA, S->Minv, S->x, S->r, S->z, S->p, S->Ap, S->pcg, S->partials,
-                                       red, S->bar, (int*)(S->bar + 2), kReduceBlocks, kBarrierSpinLimit, s);
-  }
   GridReduce red{S->partials, S->ticket};
   int st = launch_pcg_gather<T>(S->m, S->evA, S->z, S->p, S->Ap, S->pcg, red, s, (long long)S->n_partials);
   if (st) return st;
@@ -497,7 +486,6 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
     return set_error(VDVC_ERR_UNSUPPORTED, "precision form needs K_lap = one 8x8 block per component");
   }
   S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 4;
-  S->fused_pcg = true;
   cudaStream_t s = (cudaStream_t)d->stream;
   int e = VDVC_OK;
   auto fail = [&](int code) {
@@ -520,7 +508,6 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   }
   if (cudaMemcpyAsync(S->kp, &kh, sizeof(kh), cudaMemcpyHostToDevice, s) != cudaSuccess ||
       cudaMemsetAsync(S->ticket, 0, 4 * sizeof(unsigned int), s) != cudaSuccess ||
-      cudaMemsetAsync(S->bar, 0, 4 * sizeof(unsigned int), s) != cudaSuccess ||
       cudaMemsetAsync(S->sc, 0, sizeof(GnScalars), s) != cudaSuccess)
     return fail(set_error(VDVC_ERR_CUDA, "solver upload failed"));
   // regularizer diagonal in float64: h diag(K_lap) [+ eq. gap Hutchinson]
@@ -664,9 +651,6 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
                               max_iter, tol, s);
   if (st) return st;
   bool ran = false;
-  // the fused iteration's barrier words start at zero (a timed-out solve
-  // leaves them mid-count)
-  VDVC_CUDA(cudaMemsetAsync(S->bar, 0, 4 * sizeof(unsigned int), s));
   if (!ran && eager_pcg()) {
     // the same iteration kernels launched from the host, so that a profiler
     // sees each launch; the device state is read every 16 iterations
@@ -687,11 +671,6 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   VDVC_CUDA(cudaMemcpyAsync(S->h_pcg, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
   VDVC_CUDA(cudaStreamSynchronize(s));
   const PcgState& fin = S->h_pcg[0];
-  if (fin.status == VDVC_ERR_TIMEOUT) {
-    VDVC_CUDA(cudaMemsetAsync(S->ticket, 0, 4 * sizeof(unsigned int), s));
-    return set_error(VDVC_ERR_TIMEOUT, "PCG: the fused iteration's grid barrier timed out after %d iterations",
-                     fin.iter);
-  }
   if (max_iter > 0 && !ran) {
     // body executions = ceil(iter / chunk); each runs chunk iterations' kernels + the continue kernel
     const long long bodies = (fin.iter + S->chunk - 1) / S->chunk;
@@ -1077,7 +1056,6 @@ int vdvc_gn_batch_create(const vdvc_gn_desc* descs, int n, void* const* ws, cons
     void* impl = nullptr;
     int st = create<float>(&descs[i], ws[i], ws_bytes[i], &impl);
     if (st) return fail(st);
-    ((GnSolver<float>*)impl)->fused_pcg = false;  // concurrent branches: no co-residency promise
     B->S.push_back((GnSolver<float>*)impl);
   }
   if (cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking) != cudaSuccess ||

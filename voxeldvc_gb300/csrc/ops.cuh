@@ -59,14 +59,6 @@ int launch_pcg_gather(const Mesh& m, const T* ev, const T* z, T* p, T* Ap, PcgSt
 template <typename T>
 int launch_pcg_update(const T* p, const T* Ap, const T* Minv, long long n, T* x, T* r, T* z, PcgState* st,
                       GridReduce red, cudaStream_t s);
-// Gather + update fused in one cooperative launch with one grid barrier
-// (pcg.cu).  pA: max_blocks doubles; red.partials: 2 * max_blocks doubles;
-// bar: two counters and err a flag, zero before the first launch.
-template <typename T>
-int launch_pcg_gather_update(const Mesh& m, const T* ev, const T* Minv, T* x, T* r, T* z, T* p, T* Ap,
-                             PcgState* st, double* pA, GridReduce red, unsigned int* bar, int* err, int max_blocks,
-                             long long spin_limit, cudaStream_t s);
-
 // Sampling and statistics (sample.cu).
 template <typename T>
 struct SampleArgs {

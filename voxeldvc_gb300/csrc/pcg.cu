@@ -98,100 +98,6 @@ __global__ void __launch_bounds__(256) k_pcg_gather(const Mesh m, const T* __res
   if (grid_reduce_sum<1>(red, mine, out, s_red) && threadIdx.x == 0) st->alpha = st->rz / (out[0] + 1e-30);
 }
 
-// Fused gather + update of one iteration (cooperative launch; one bounded
-// grid barrier instead of the gather's and the update's last-block tails and
-// a launch between them).  Each thread owns the same nodes in both phases,
-// so it reads back only its own writes across the barrier.
-//   A  p <- z + beta p ; Ap <- sum of element vectors ; block p.Ap -> pA[b]
-//   -- grid barrier --
-//   every block: alpha = rz / (sum_b pA[b] + 1e-30), identical bits
-//   B  x += alpha p ; r -= alpha Ap ; z = M r ; r.r, r.z -> last block:
-//      res, convergence, beta = r.z / (rz + 1e-30)
-// The arithmetic per entry is k_pcg_gather's and k_pcg_update's.  A barrier
-// that times out stops the solve with VDVC_ERR_TIMEOUT in the state.
-// float: 40 registers, 6 blocks (48 warps) per SM resident together
-template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 4) k_pcg_gather_update(const Mesh m, const T* __restrict__ ev,
-                                                           const T* __restrict__ Minv, T* __restrict__ x,
-                                                           T* __restrict__ r, T* __restrict__ z, T* __restrict__ p,
-                                                           T* __restrict__ Ap, PcgState* st, double* pA,
-                                                           GridReduce red, unsigned int* bar, int* err,
-                                                           long long spin_limit) {
-  __shared__ double s_red[8];
-  __shared__ double s_bc;
-  if (st->done) return;
-  const T beta = (T)st->beta;
-  const double rz_old = st->rz;
-  const unsigned int nnx = (unsigned int)m.Nnx, nny = (unsigned int)m.Nny;
-  const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  T pap = T(0);
-  for (long long n = gtid; n < m.Nnodes; n += stride) {
-    const unsigned int nu = (unsigned int)n, rr = nu / nnx;
-    const int ni = (int)(nu - rr * nnx), nj = (int)(rr % nny), nk = (int)(rr / nny);
-    T sa[3] = {T(0), T(0), T(0)};
-#pragma unroll
-    for (int a = 0; a < 8; ++a) {
-      const int ei = ni - corner_dx(a), ej = nj - corner_dy(a), ek = nk - corner_dz(a);
-      if (ei < 0 || ej < 0 || ek < 0 || ei >= m.Nx || ej >= m.Ny || ek >= m.Nz) continue;
-      const long long e = (long long)ei + (long long)ej * m.Nx + (long long)ek * m.Nx * m.Ny;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) sa[c] += ev[(long long)(3 * a + c) * m.Ne + e];
-    }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const long long d = 3 * n + c;
-      const T pn = z[d] + beta * p[d];
-      p[d] = pn;
-      Ap[d] = sa[c];
-      pap += pn * sa[c];
-    }
-  }
-  {
-    const double bs = block_sum_f(pap, s_red);
-    if (threadIdx.x == 0) pA[blockIdx.x] = bs;
-  }
-  if (!grid_barrier(bar, err, gridDim.x, spin_limit)) {
-    if (threadIdx.x == 0) {
-      st->status = VDVC_ERR_TIMEOUT;
-      st->done = 1;
-    }
-    return;
-  }
-  const double alpha = rz_old / (all_blocks_sum(pA, gridDim.x, s_red, &s_bc) + 1e-30);
-  const T af = (T)alpha;
-  T rr = T(0), rz = T(0);
-  for (long long n = gtid; n < m.Nnodes; n += stride) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const long long d = 3 * n + c;
-      x[d] = x[d] + af * p[d];
-      const T ri = r[d] - af * Ap[d];
-      const T zi = Minv[d] * ri;
-      r[d] = ri;
-      z[d] = zi;
-      rr += ri * ri;
-      rz += ri * zi;
-    }
-  }
-  double mine[2] = {block_sum_f(rr, s_red), block_sum_f(rz, s_red)}, out[2];
-  if (grid_reduce_sum<2>(red, mine, out, s_red) && threadIdx.x == 0) {
-    const double res = sqrt(out[0] / st->r0);
-    st->alpha = alpha;
-    st->rr = out[0];
-    st->res = res;
-    st->iter += 1;
-    if (!(res == res) || !isfinite(alpha)) {
-      st->status = VDVC_ERR_NONFINITE;
-      st->done = 1;
-    } else if (res < st->tol || st->iter >= st->max_iter) {
-      st->done = 1;
-    }
-    st->beta = out[1] / (rz_old + 1e-30);
-    st->rz = out[1];
-  }
-}
-
 // Generic form: alpha = rz / (p.Ap + 1e-30) for an externally computed Ap.
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_alpha(const T* __restrict__ p, const T* __restrict__ Ap, long long n,
@@ -303,40 +209,6 @@ int launch_pcg_update(const T* p, const T* Ap, const T* Minv, long long n, T* x,
   return VDVC_OK;
 }
 
-template <typename T>
-int launch_pcg_gather_update(const Mesh& m, const T* ev, const T* Minv, T* x, T* r, T* z, T* p, T* Ap,
-                             PcgState* st, double* pA, GridReduce red, unsigned int* bar, int* err, int max_blocks,
-                             long long spin_limit, cudaStream_t s) {
-  if (m.Nnodes >= (1ll << 32)) return set_error(VDVC_ERR_UNSUPPORTED, "2^32 nodes or more");
-  int dev = 0, nsm = 0, per_sm = 0;
-  VDVC_CUDA(cudaGetDevice(&dev));
-  VDVC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  VDVC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_gather_update<T>, 256, 0));
-  if (per_sm < 1) return set_error(VDVC_ERR_UNSUPPORTED, "fused PCG kernel does not fit on an SM");
-  long long grid = (m.Nnodes + 255) / 256;
-  if (grid > (long long)per_sm * nsm) grid = (long long)per_sm * nsm;  // all blocks resident
-  if (grid > max_blocks) grid = max_blocks;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(256);
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeCooperative;
-  at[0].val.cooperative = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  VDVC_CUDA(cudaLaunchKernelEx(&cfg, k_pcg_gather_update<T>, m, ev, Minv, x, r, z, p, Ap, st, pA, red, bar, err,
-                               spin_limit));
-  count_launch();
-  return VDVC_OK;
-}
-
-template int launch_pcg_gather_update<float>(const Mesh&, const float*, const float*, float*, float*, float*, float*,
-                                             float*, PcgState*, double*, GridReduce, unsigned int*, int*, int,
-                                             long long, cudaStream_t);
-template int launch_pcg_gather_update<double>(const Mesh&, const double*, const double*, double*, double*, double*,
-                                              double*, double*, PcgState*, double*, GridReduce, unsigned int*, int*,
-                                              int, long long, cudaStream_t);
 template int launch_pcg_init<float>(const float*, const float*, const float*, long long, float*, float*, float*,
                                     bool, float*, PcgState*, GridReduce, int, double, cudaStream_t);
 template int launch_pcg_init<double>(const double*, const double*, const double*, long long, double*, double*,
