@@ -52,7 +52,7 @@ TRAFFIC_B_PER_VOXEL = 14.04
 # PCG iterations) that the reference arm multiplies its measured operation
 # times by: those of the GB300 FP32 solve of each workload, which match the
 # reference's own solve where it was run (tests/golden/baseline_*.npz: the
-# 513^3 necking workload's coarse level takes 30 GN / 730 PCG iterations
+# 513^3 necking workload's coarse level takes 30 GN / 733 PCG iterations
 # there, 30 / 752 here).  The GPU arm uses the counts of its own solve.
 SOLVE_COUNTS = {"necking_512": {"gn": [30, 4, 2], "pcg": [752, 84, 41]},
                 "necking_512_eqgap": {"gn": [30, 30, 30], "pcg": [60000, 60000, 60000]},

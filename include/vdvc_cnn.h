@@ -61,8 +61,9 @@ int vdvc_cnn_status(vdvc_stream_t stream);
 
 /* Weight gradient of a forward convolution (geom = its forward geometry):
    dw[n][t][k] (+)= sum_p dy[p][n] * x[q(p,t)][k], FP32 [n_out][27][cin],
-   on the tensor cores.  The positions are split over blocks; each block's
-   partial goes to ws and a second pass sums the partials in a fixed order
+   on the tensor cores (n_out, cin <= 256; blocks of 32 output x 64 input
+   channels).  The positions are split over blocks; each block's partial
+   goes to ws and a second pass sums the partials in a fixed order
    (deterministic).  accumulate: dw += instead of dw =.
    Workspace: vdvc_cnn_wgrad_workspace_bytes(n_out, cin). */
 int vdvc_cnn_conv_wgrad(const void* dy, int dy_cstride, int dy_coff,

@@ -53,6 +53,25 @@ int vdvc_synth_warp(const float* f, int nx, int ny, int nz, int field,
                     const double* params, int n_params, double noise_sigma,
                     unsigned long long seed, float* g, vdvc_stream_t stream);
 
+/* Free-form deformation (the learned seed's training fields): the affine
+   field of VDVC_FIELD_AFFINE (affine = t[3], G[9] row-major, c[3]) plus a
+   uniform cubic B-spline displacement on an nc^3 control grid spanning the
+   volume (spacing (n - 1) / (nc - 3) per axis; the 4^3 control points of
+   the cell around x weigh in), control displacements ctrl: device FP32
+   [nc^3][3], first index fastest.  Evaluated in FP32.
+   vdvc_synth_warp_ffd: g(x) = f(x - u(x)) (trilinear, clamped) + noise.
+   vdvc_synth_ffd_inverse_grid: U with U = u(X + U) -- the displacement a
+   correlation of f against that g recovers -- at X = (i, j, k) * stride,
+   `iters` fixed-point steps, FP32 (gx*gy*gz, 3), x fastest. */
+int vdvc_synth_warp_ffd(const float* f, int nx, int ny, int nz,
+                        const double* affine, const float* ctrl, int nc,
+                        double noise_sigma, unsigned long long seed,
+                        float* g, vdvc_stream_t stream);
+int vdvc_synth_ffd_inverse_grid(const double* affine, const float* ctrl,
+                                int nc, int nx, int ny, int nz, int gx,
+                                int gy, int gz, double stride, int iters,
+                                float* out, vdvc_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,7 +101,7 @@ def test_conv_forward_input_grad_wgrad(env, cin, n_out, stride, src):
         assert np.allclose(host(dx).reshape(ref_dx.shape), ref_dx, rtol=8e-3, atol=8e-3 * np.abs(ref_dx).max())
 
     # weight and bias gradients
-    if n_out <= 32 and cin <= 64:
+    if True:  # every case: blocks of 32 x 64 channels tile the larger layers
         dy = O.bf16_round(rng.standard_normal(ref.shape))
         dw = torch.zeros(n_out * 27 * cin, dtype=torch.float32, device="cuda")
         db = torch.zeros(n_out, dtype=torch.float32, device="cuda")

@@ -111,6 +111,8 @@ SIGNATURES = {
     "vdvc_synth_workspace_bytes": (cz, [ci, ci, ci]),
     "vdvc_synth_texture": (ci, [vp, ci, ci, ci, C.c_ulonglong, cd, cd, vp, ci, cd, vp, cz, vp]),
     "vdvc_synth_warp": (ci, [vp, ci, ci, ci, ci, pd, ci, cd, C.c_ulonglong, vp, vp]),
+    "vdvc_synth_warp_ffd": (ci, [vp, ci, ci, ci, pd, vp, ci, cd, C.c_ulonglong, vp, vp]),
+    "vdvc_synth_ffd_inverse_grid": (ci, [pd, vp, ci, ci, ci, ci, ci, ci, ci, cd, ci, vp, vp]),
     "vdvc_synth_field_grid": (ci, [ci, pd, ci, ci, ci, ci, cd, vp, vp]),
     # include/vdvc_cnn.h
     "vdvc_cnn_conv": (ci, [vp, ci, ci, ci, vp, vp, ci, ci, vp, ci, ci, ci, ci, vp, vp]),

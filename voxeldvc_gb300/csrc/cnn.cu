@@ -199,6 +199,8 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ src, int 
 
 // grid (27 taps, splits), 4 warps; warp (split, w) writes its partial
 // part[(split*4 + w)][n][t][k] for n < n_out, k < cin.
+// blockIdx.z selects the block of 32 output channels x 64 input channels
+// this block computes (larger layers tile over it).
 template <int MF, int NFC>
 __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ dy, int dcs, int dcoff, int n_out,
                                                const bf16* __restrict__ x, int xcs, int xcoff, int cin, Geo g,
@@ -206,6 +208,8 @@ __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ dy, int 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gid = lane >> 2, tig = lane & 3;
   const int t = blockIdx.x, split = blockIdx.y;
+  const int kblocks = (cin + 63) / 64;
+  const int n0 = (int)(blockIdx.z / kblocks) * 32, c0 = (int)(blockIdx.z % kblocks) * 64;
   const long long npos = (long long)g.nx * g.ny * g.nz;
   const long long pbeg = (long long)split * chunk;
   const long long pend = min(npos, pbeg + chunk);
@@ -215,12 +219,12 @@ __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ dy, int 
 #pragma unroll
     for (int j = 0; j < NFC; ++j) acc[mt][j][0] = acc[mt][j][1] = acc[mt][j][2] = acc[mt][j][3] = 0.f;
 
-  for (long long k0 = pbeg + warp * 16; k0 < pend; k0 += 64) {
-    // this lane's reduction positions: k0 + 2tig + {0, 1, 8, 9}
+  for (long long p0 = pbeg + warp * 16; p0 < pend; p0 += 64) {
+    // this lane's reduction positions: p0 + 2tig + {0, 1, 8, 9}
     long long kp[4], si[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      kp[q] = k0 + tig * 2 + (q & 1) + (q >> 1) * 8;
+      kp[q] = p0 + tig * 2 + (q & 1) + (q >> 1) * 8;
       si[q] = -1;
       if (kp[q] < pend) {
         const int xx = (int)(kp[q] % g.nx);
@@ -234,7 +238,7 @@ __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ dy, int 
       uint32_t v[2][4];
 #pragma unroll
       for (int hr = 0; hr < 2; ++hr) {
-        const int n = mt * 16 + gid + 8 * hr;
+        const int n = n0 + mt * 16 + gid + 8 * hr;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
           v[hr][q] = (kp[q] < pend && n < n_out) ? ld16(dy + kp[q] * dcs + dcoff + n) : 0u;
@@ -246,7 +250,7 @@ __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ dy, int 
     }
 #pragma unroll
     for (int j = 0; j < NFC; ++j) {
-      const int k = j * 8 + gid;
+      const int k = c0 + j * 8 + gid;
       uint32_t xv[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) xv[q] = (si[q] >= 0 && k < cin) ? ld16(x + si[q] * xcs + xcoff + k) : 0u;
@@ -262,7 +266,7 @@ __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ dy, int 
     for (int j = 0; j < NFC; ++j)
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const int n = mt * 16 + gid + 8 * (e >> 1), k = j * 8 + tig * 2 + (e & 1);
+        const int n = n0 + mt * 16 + gid + 8 * (e >> 1), k = c0 + j * 8 + tig * 2 + (e & 1);
         if (n < n_out && k < cin) pw[((size_t)n * 27 + t) * cin + k] = acc[mt][j][e];
       }
 }
@@ -644,8 +648,8 @@ int vdvc_cnn_conv_wgrad(const void* dy, int dy_cstride, int dy_coff, int n_out, 
                         int x_coff, int cin, const vdvc_conv_geom* geom, float* dw, int accumulate, void* ws,
                         size_t ws_bytes, vdvc_stream_t stream) {
   VDVC_CHECK_ARG(dy && x && dw && geo_ok(geom), "bad arguments");
-  VDVC_CHECK_ARG(n_out >= 1 && n_out <= 32, "wgrad supports n_out <= 32");
-  VDVC_CHECK_ARG(cin >= 1 && cin <= 64, "wgrad supports cin <= 64");
+  VDVC_CHECK_ARG(n_out >= 1 && n_out <= 256, "wgrad supports n_out <= 256");
+  VDVC_CHECK_ARG(cin >= 1 && cin <= 256, "wgrad supports cin <= 256");
   VDVC_CHECK_ARG(dy_coff >= 0 && dy_coff + n_out <= dy_cstride && x_coff >= 0 && x_coff + cin <= x_cstride,
                  "channel ranges do not fit their strides");
   const size_t need = vdvc_cnn_wgrad_workspace_bytes(n_out, cin);
@@ -653,10 +657,10 @@ int vdvc_cnn_conv_wgrad(const void* dy, int dy_cstride, int dy_coff, int n_out, 
   const Geo g = to_geo(geom);
   const long long npos = (long long)g.nx * g.ny * g.nz;
   const long long chunk = (npos + kWgradSplits - 1) / kWgradSplits;
-  dim3 grid(27, kWgradSplits);
+  dim3 grid(27, kWgradSplits, ((n_out + 31) / 32) * ((cin + 63) / 64));
   cudaStream_t s = (cudaStream_t)stream;
   float* part = (float*)ws;
-  const int mf = (n_out + 15) / 16, nfc = (cin + 7) / 8;
+  const int mf = n_out > 16 ? 2 : 1, nfc = cin >= 64 ? 8 : (cin + 7) / 8;
   int st = (mf == 1) ? launch_wgrad_m<1>(nfc, grid, (const bf16*)dy, dy_cstride, dy_coff, n_out, (const bf16*)x,
                                          x_cstride, x_coff, cin, g, chunk, part, s)
                      : launch_wgrad_m<2>(nfc, grid, (const bf16*)dy, dy_cstride, dy_coff, n_out, (const bf16*)x,
@@ -671,16 +675,22 @@ int vdvc_cnn_conv_wgrad(const void* dy, int dy_cstride, int dy_coff, int n_out, 
 
 int vdvc_cnn_bias_grad(const void* dy, int dy_cstride, int dy_coff, int n_out, long long npos, float* db,
                        int accumulate, void* ws, size_t ws_bytes, vdvc_stream_t stream) {
-  VDVC_CHECK_ARG(dy && db && npos >= 1 && n_out >= 1 && n_out <= 32 && dy_coff >= 0 && dy_coff + n_out <= dy_cstride,
+  VDVC_CHECK_ARG(dy && db && npos >= 1 && n_out >= 1 && n_out <= 256 && dy_coff >= 0 &&
+                     dy_coff + n_out <= dy_cstride,
                  "bad arguments");
   const int nblk = 256;
-  VDVC_CHECK_ARG(ws && ws_bytes >= (size_t)nblk * n_out * sizeof(float), "bias_grad workspace too small");
+  VDVC_CHECK_ARG(ws && ws_bytes >= (size_t)nblk * 32 * sizeof(float), "bias_grad workspace too small");
   const long long chunk = (npos + nblk - 1) / nblk;
   cudaStream_t s = (cudaStream_t)stream;
-  k_bias_part<<<nblk, dim3(32, 8), 0, s>>>((const bf16*)dy, dy_cstride, dy_coff, n_out, npos, chunk, (float*)ws);
-  count_launch();
-  k_sum_parts<<<1, 32, 0, s>>>((const float*)ws, nblk, n_out, db, accumulate);
-  VDVC_LAUNCHED();
+  // groups of 32 channels, one after another through the same partials
+  for (int c0 = 0; c0 < n_out; c0 += 32) {
+    const int ng = n_out - c0 < 32 ? n_out - c0 : 32;
+    k_bias_part<<<nblk, dim3(32, 8), 0, s>>>((const bf16*)dy, dy_cstride, dy_coff + c0, ng, npos, chunk,
+                                             (float*)ws);
+    count_launch();
+    k_sum_parts<<<1, 32, 0, s>>>((const float*)ws, nblk, ng, db + c0, accumulate);
+    VDVC_LAUNCHED();
+  }
   return VDVC_OK;
 }
 
@@ -761,7 +771,7 @@ int vdvc_cnn_adam(float* w, const float* grad, float* m, float* v, long long n, 
 }
 
 int vdvc_cnn_pack_weights(const float* w, int n_out, int cin, void* wf, void* wb, vdvc_stream_t stream) {
-  VDVC_CHECK_ARG(w && wf && n_out >= 1 && n_out <= 80 && cin >= 1, "bad arguments");
+  VDVC_CHECK_ARG(w && wf && n_out >= 1 && n_out <= 256 && cin >= 1 && cin <= 256, "bad arguments");
   VDVC_CHECK_ARG(cin == 2 || cin % 16 == 0, "cin must be 2 or a multiple of 16");
   const int npad8 = (n_out + 7) / 8 * 8, npad16 = (n_out + 15) / 16 * 16, kpad8 = (cin + 7) / 8 * 8;
   const long long nf = cin == 2 ? (long long)npad8 * 64 : (long long)npad8 * 27 * cin;

@@ -179,6 +179,29 @@ __global__ void k_field_grid(FieldParams fp, int gx, int gy, int gz, double stri
   }
 }
 
+// Trilinear sample of f at (cx, cy, cz), coordinates clamped to the volume.
+__device__ __forceinline__ float sample_clamped(const float* __restrict__ f, int nx, int ny, int nz, float cx,
+                                                float cy, float cz) {
+  const float c[3] = {cx, cy, cz};
+  const int dims[3] = {nx, ny, nz};
+  int i0[3], i1[3];
+  float t[3];
+  for (int k = 0; k < 3; ++k) {
+    const float cc = fminf(fmaxf(c[k], 0.f), (float)(dims[k] - 1));
+    const float fl = floorf(cc);
+    i0[k] = (int)fl;
+    i1[k] = min(i0[k] + 1, dims[k] - 1);
+    t[k] = cc - fl;
+  }
+  auto at = [&](int xx, int yy, int zz) { return f[(long long)xx + (long long)yy * nx + (long long)zz * nx * ny]; };
+  const float a00 = at(i0[0], i0[1], i0[2]) + t[0] * (at(i1[0], i0[1], i0[2]) - at(i0[0], i0[1], i0[2]));
+  const float a10 = at(i0[0], i1[1], i0[2]) + t[0] * (at(i1[0], i1[1], i0[2]) - at(i0[0], i1[1], i0[2]));
+  const float a01 = at(i0[0], i0[1], i1[2]) + t[0] * (at(i1[0], i0[1], i1[2]) - at(i0[0], i0[1], i1[2]));
+  const float a11 = at(i0[0], i1[1], i1[2]) + t[0] * (at(i1[0], i1[1], i1[2]) - at(i0[0], i1[1], i1[2]));
+  const float b0 = a00 + t[1] * (a10 - a00), b1 = a01 + t[1] * (a11 - a01);
+  return b0 + t[2] * (b1 - b0);
+}
+
 __global__ void k_warp(const float* __restrict__ f, int nx, int ny, int nz, FieldParams fp, float sigma,
                        unsigned long long seed, float* __restrict__ g) {
   const long long n = (long long)nx * ny * nz;
@@ -188,26 +211,96 @@ __global__ void k_warp(const float* __restrict__ f, int nx, int ny, int nz, Fiel
     const int y = (int)(r % ny), z = (int)(r / ny);
     double u[3];
     field_u(fp, x, y, z, u);
-    float c[3] = {(float)(x - u[0]), (float)(y - u[1]), (float)(z - u[2])};
-    const int dims[3] = {nx, ny, nz};
-    int i0[3], i1[3];
-    float t[3];
-    for (int k = 0; k < 3; ++k) {
-      const float cc = fminf(fmaxf(c[k], 0.f), (float)(dims[k] - 1));
-      const float fl = floorf(cc);
-      i0[k] = (int)fl;
-      i1[k] = min(i0[k] + 1, dims[k] - 1);
-      t[k] = cc - fl;
-    }
-    auto at = [&](int xx, int yy, int zz) { return f[(long long)xx + (long long)yy * nx + (long long)zz * nx * ny]; };
-    const float a00 = at(i0[0], i0[1], i0[2]) + t[0] * (at(i1[0], i0[1], i0[2]) - at(i0[0], i0[1], i0[2]));
-    const float a10 = at(i0[0], i1[1], i0[2]) + t[0] * (at(i1[0], i1[1], i0[2]) - at(i0[0], i1[1], i0[2]));
-    const float a01 = at(i0[0], i0[1], i1[2]) + t[0] * (at(i1[0], i0[1], i1[2]) - at(i0[0], i0[1], i1[2]));
-    const float a11 = at(i0[0], i1[1], i1[2]) + t[0] * (at(i1[0], i1[1], i1[2]) - at(i0[0], i1[1], i1[2]));
-    const float b0 = a00 + t[1] * (a10 - a00), b1 = a01 + t[1] * (a11 - a01);
-    float val = b0 + t[2] * (b1 - b0);
+    float val = sample_clamped(f, nx, ny, nz, (float)(x - u[0]), (float)(y - u[1]), (float)(z - u[2]));
     if (sigma > 0.f) val += sigma * hash_normal(seed, (unsigned long long)v);
     g[v] = val;
+  }
+}
+
+// ---- free-form deformation: affine + cubic B-spline ---------------------------
+
+struct Ffd {
+  float G[9], t[3], c[3];  // affine part u = t + G (x - c)
+  const float* ctrl;       // [nc^3][3], first index fastest
+  int nc;
+  float inv_d[3];          // 1 / control spacing per axis
+};
+
+__device__ __forceinline__ void bspline3(float t, float (&b)[4]) {
+  const float t2 = t * t, t3 = t2 * t, s = 1.f - t;
+  b[0] = s * s * s * (1.f / 6.f);
+  b[1] = (3.f * t3 - 6.f * t2 + 4.f) * (1.f / 6.f);
+  b[2] = (-3.f * t3 + 3.f * t2 + 3.f * t + 1.f) * (1.f / 6.f);
+  b[3] = t3 * (1.f / 6.f);
+}
+
+// u(x): the affine part plus the sum over the 4^3 control points of the cell
+// around x of B(tx) B(ty) B(tz) ctrl; the cell index is clamped to
+// [0, nc - 4], so a point outside the volume sees the border cells'
+// polynomial.
+__device__ __forceinline__ void ffd_u(const Ffd& F, float x, float y, float z, float (&u)[3]) {
+  const float X[3] = {x - F.c[0], y - F.c[1], z - F.c[2]};
+  for (int k = 0; k < 3; ++k) u[k] = F.t[k] + F.G[3 * k] * X[0] + F.G[3 * k + 1] * X[1] + F.G[3 * k + 2] * X[2];
+  const float p[3] = {x, y, z};
+  int cell[3];
+  float b[3][4];
+  for (int k = 0; k < 3; ++k) {
+    const float sp = p[k] * F.inv_d[k];
+    const float fl = fminf(fmaxf(floorf(sp), 0.f), (float)(F.nc - 4));
+    cell[k] = (int)fl;
+    bspline3(sp - fl, b[k]);
+  }
+  float acc[3] = {0.f, 0.f, 0.f};
+  for (int cz = 0; cz < 4; ++cz)
+    for (int cy = 0; cy < 4; ++cy) {
+      const float wyz = b[2][cz] * b[1][cy];
+      const float* row = F.ctrl + 3 * ((long long)(cell[0]) + (long long)(cell[1] + cy) * F.nc +
+                                       (long long)(cell[2] + cz) * F.nc * F.nc);
+#pragma unroll
+      for (int cx = 0; cx < 4; ++cx) {
+        const float w = wyz * b[0][cx];
+        acc[0] += w * __ldg(row + 3 * cx);
+        acc[1] += w * __ldg(row + 3 * cx + 1);
+        acc[2] += w * __ldg(row + 3 * cx + 2);
+      }
+    }
+  for (int k = 0; k < 3; ++k) u[k] += acc[k];
+}
+
+__global__ void k_warp_ffd(const float* __restrict__ f, int nx, int ny, int nz, Ffd F, float sigma,
+                           unsigned long long seed, float* __restrict__ g) {
+  const long long n = (long long)nx * ny * nz;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(v % nx);
+    const long long r = v / nx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    float u[3];
+    ffd_u(F, (float)x, (float)y, (float)z, u);
+    float val = sample_clamped(f, nx, ny, nz, x - u[0], y - u[1], z - u[2]);
+    if (sigma > 0.f) val += sigma * hash_normal(seed, (unsigned long long)v);
+    g[v] = val;
+  }
+}
+
+// U = u(X + U) at X = (i, j, k) * stride by `iters` fixed-point steps
+__global__ void k_ffd_inverse_grid(Ffd F, int gx, int gy, int gz, float stride, int iters, float* __restrict__ out) {
+  const long long n = (long long)gx * gy * gz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % gx);
+    const long long r = i / gx;
+    const int y = (int)(r % gy), z = (int)(r / gy);
+    const float X[3] = {x * stride, y * stride, z * stride};
+    float U[3] = {0.f, 0.f, 0.f};
+    for (int it = 0; it < iters; ++it) {
+      float u[3];
+      ffd_u(F, X[0] + U[0], X[1] + U[1], X[2] + U[2], u);
+      U[0] = u[0];
+      U[1] = u[1];
+      U[2] = u[2];
+    }
+    out[3 * i] = U[0];
+    out[3 * i + 1] = U[1];
+    out[3 * i + 2] = U[2];
   }
 }
 
@@ -299,6 +392,44 @@ int vdvc_synth_warp(const float* f, int nx, int ny, int nz, int field, const dou
   if (st) return st;
   const long long n = (long long)nx * ny * nz;
   k_warp<<<gblocks(n), 256, 0, (cudaStream_t)stream>>>(f, nx, ny, nz, fp, (float)noise_sigma, seed, g);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+static int make_ffd(const double* affine, const float* ctrl, int nc, int nx, int ny, int nz, Ffd* F) {
+  VDVC_CHECK_ARG(affine && ctrl && nc >= 4 && nc <= 64, "bad free-form deformation (nc in [4, 64])");
+  VDVC_CHECK_ARG(nx >= 2 && ny >= 2 && nz >= 2, "volume too small");
+  for (int k = 0; k < 3; ++k) F->t[k] = (float)affine[k];
+  for (int k = 0; k < 9; ++k) F->G[k] = (float)affine[3 + k];
+  for (int k = 0; k < 3; ++k) F->c[k] = (float)affine[12 + k];
+  F->ctrl = ctrl;
+  F->nc = nc;
+  const int dims[3] = {nx, ny, nz};
+  for (int k = 0; k < 3; ++k) F->inv_d[k] = (float)((double)(nc - 3) / (double)(dims[k] - 1));
+  return VDVC_OK;
+}
+
+int vdvc_synth_warp_ffd(const float* f, int nx, int ny, int nz, const double* affine, const float* ctrl, int nc,
+                        double noise_sigma, unsigned long long seed, float* g, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(f && g && f != g, "bad arguments");
+  Ffd F;
+  int st = make_ffd(affine, ctrl, nc, nx, ny, nz, &F);
+  if (st) return st;
+  const long long n = (long long)nx * ny * nz;
+  k_warp_ffd<<<gblocks(n), 256, 0, (cudaStream_t)stream>>>(f, nx, ny, nz, F, (float)noise_sigma, seed, g);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_synth_ffd_inverse_grid(const double* affine, const float* ctrl, int nc, int nx, int ny, int nz, int gx,
+                                int gy, int gz, double stride, int iters, float* out, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(out && gx >= 1 && gy >= 1 && gz >= 1 && stride > 0.0 && iters >= 1 && iters <= 200,
+                 "bad arguments");
+  Ffd F;
+  int st = make_ffd(affine, ctrl, nc, nx, ny, nz, &F);
+  if (st) return st;
+  k_ffd_inverse_grid<<<gblocks((long long)gx * gy * gz), 256, 0, (cudaStream_t)stream>>>(F, gx, gy, gz,
+                                                                                         (float)stride, iters, out);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
