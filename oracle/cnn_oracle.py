@@ -139,6 +139,10 @@ def pool_input(f, g, mean_std):
 
 
 # ---- the network ---------------------------------------------------------------
+#
+# The 4-level encoder-decoder of voxeldvc_gb300/learned/arch.py:
+#   e1 -> e2a -> e2b -> e3a -> e3b -> e4a -> e4b
+#   d3 = conv([up(e4b) | e3b]),  d2 = conv([up(d3) | e2b]),  out = conv(d2)
 
 def forward(params, x, layers, bf16=False):
     """params: {name: (W, b)}; x: (Gz, Gy, Gx, 2).  Returns (pred, cache)."""
@@ -147,21 +151,23 @@ def forward(params, x, layers, bf16=False):
 
     def run(name, inp):
         l = L[name]
-        return conv(inp, P[name][0], P[name][1], l["stride"], l["relu"])
+        return _r(conv(inp, P[name][0], P[name][1], l["stride"], l["relu"]), bf16)
 
-    a0 = _r(x, bf16)
-    a1 = _r(run("c1", a0), bf16)
-    a2 = _r(run("c2", a1), bf16)
-    a3 = _r(run("c3", a2), bf16)
-    a4 = _r(run("c4", a3), bf16)
-    a5 = _r(run("c5", a4), bf16)
-    a6 = _r(run("c6", a5), bf16)
-    u6 = _r(upsample2(a6, a3.shape[:3]), bf16)
-    cat = np.concatenate([u6, a3], axis=-1)
-    a7 = _r(run("c7", cat), bf16)
-    pred = run("c8", a7)  # FP32 output on the GPU
-    cache = dict(P=P, a0=a0, a1=a1, a2=a2, a3=a3, a4=a4, a5=a5, a6=a6, cat=cat, a7=a7, pred=pred)
-    return pred, cache
+    c = dict(P=P, x=_r(x, bf16))
+    c["e1"] = run("e1", c["x"])
+    c["e2a"] = run("e2a", c["e1"])
+    c["e2b"] = run("e2b", c["e2a"])
+    c["e3a"] = run("e3a", c["e2b"])
+    c["e3b"] = run("e3b", c["e3a"])
+    c["e4a"] = run("e4a", c["e3b"])
+    c["e4b"] = run("e4b", c["e4a"])
+    c["cat3"] = np.concatenate([_r(upsample2(c["e4b"], c["e3b"].shape[:3]), bf16), c["e3b"]], axis=-1)
+    c["d3"] = run("d3", c["cat3"])
+    c["cat2"] = np.concatenate([_r(upsample2(c["d3"], c["e2b"].shape[:3]), bf16), c["e2b"]], axis=-1)
+    c["d2"] = run("d2", c["cat2"])
+    l = L["out"]
+    c["pred"] = conv(c["d2"], P["out"][0], P["out"][1], l["stride"], l["relu"])  # FP32 output on the GPU
+    return c["pred"], c
 
 
 def mse(pred, target):
@@ -170,7 +176,9 @@ def mse(pred, target):
 
 
 def backward(cache, dpred, layers, bf16=False):
-    """Gradients {name: (dW, db)} of the loss whose pred-gradient is dpred."""
+    """Gradients {name: (dW, db)} of the loss whose pred-gradient is dpred.
+    Where two gradients meet (a skip connection), the GPU stores the first
+    in BF16 and adds the second to it; the sum is rounded once more."""
     P = cache["P"]
     L = {l["name"]: l for l in layers}
     grads = {}
@@ -178,30 +186,29 @@ def backward(cache, dpred, layers, bf16=False):
     def relu_mask(d, a):
         return np.where(a > 0, d, 0.0)
 
-    def layer_back(name, dy, x_in, want_dx):
+    def back(name, dy, x_in, want_dx=True):
         l = L[name]
-        dW, db = conv_wgrad(dy, x_in, l["stride"])
-        grads[name] = (dW, db)
-        if not want_dx:
-            return None
-        return conv_input_grad(dy, P[name][0], l["stride"], x_in.shape[:3])
+        grads[name] = conv_wgrad(dy, x_in, l["stride"])
+        if want_dx:
+            return conv_input_grad(dy, P[name][0], l["stride"], x_in.shape[:3])
+        return None
 
-    d8 = _r(dpred, bf16)
-    d7 = _r(layer_back("c8", d8, cache["a7"], True), bf16)
-    d7 = relu_mask(d7, cache["a7"])
-    dcat = _r(layer_back("c7", d7, cache["cat"], True), bf16)
-    c6 = cache["a6"].shape[-1]
-    d6 = _r(upsample2_adjoint(dcat[..., :c6], cache["a6"].shape[:3]), bf16)
-    d6 = relu_mask(d6, cache["a6"])
-    d5 = relu_mask(_r(layer_back("c6", d6, cache["a5"], True), bf16), cache["a5"])
-    d4 = relu_mask(_r(layer_back("c5", d5, cache["a4"], True), bf16), cache["a4"])
-    # c3's output feeds c4 and the concatenation: the two gradients add (once
-    # rounded, as the GPU accumulates into the stored concatenation gradient)
-    d3 = _r(layer_back("c4", d4, cache["a3"], True) + dcat[..., c6:], bf16)
-    d3 = relu_mask(d3, cache["a3"])
-    d2 = relu_mask(_r(layer_back("c3", d3, cache["a2"], True), bf16), cache["a2"])
-    d1 = relu_mask(_r(layer_back("c2", d2, cache["a1"], True), bf16), cache["a1"])
-    layer_back("c1", d1, cache["a0"], False)
+    c = cache
+    dp = _r(dpred, bf16)
+    dd2 = relu_mask(_r(back("out", dp, c["d2"]), bf16), c["d2"])
+    dcat2 = _r(back("d2", dd2, c["cat2"]), bf16)
+    c3 = c["d3"].shape[-1]
+    dd3 = relu_mask(_r(upsample2_adjoint(dcat2[..., :c3], c["d3"].shape[:3]), bf16), c["d3"])
+    dcat3 = _r(back("d3", dd3, c["cat3"]), bf16)
+    c4 = c["e4b"].shape[-1]
+    de4b = relu_mask(_r(upsample2_adjoint(dcat3[..., :c4], c["e4b"].shape[:3]), bf16), c["e4b"])
+    de4a = relu_mask(_r(back("e4b", de4b, c["e4a"]), bf16), c["e4a"])
+    de3b = relu_mask(_r(back("e4a", de4a, c["e3b"]) + dcat3[..., c4:], bf16), c["e3b"])
+    de3a = relu_mask(_r(back("e3b", de3b, c["e3a"]), bf16), c["e3a"])
+    de2b = relu_mask(_r(back("e3a", de3a, c["e2b"]) + dcat2[..., c3:], bf16), c["e2b"])
+    de2a = relu_mask(_r(back("e2b", de2b, c["e2a"]), bf16), c["e2a"])
+    de1 = relu_mask(_r(back("e2a", de2a, c["e1"]), bf16), c["e1"])
+    back("e1", de1, c["x"], want_dx=False)
     return grads
 
 

@@ -56,7 +56,7 @@ def test_upsample_adjoint(n, m):
 
 
 def test_network_gradient_finite_differences():
-    G, n, m = grids((9, 9, 9))
+    G, n, m, _ = grids((9, 9, 9))
     rng = np.random.default_rng(7)
     params = O.init_params(LAYERS, seed=1)
     # non-zero biases exercise the bias gradients too
@@ -73,7 +73,7 @@ def test_network_gradient_finite_differences():
     grads = O.backward(cache, dpred, LAYERS)
     for trial in range(3):
         V = {k: (rng.standard_normal(W.shape), rng.standard_normal(b.shape)) for k, (W, b) in params.items()}
-        eps = 1e-6
+        eps = 1e-7  # small enough that no ReLU kink is crossed
         pp = {k: (W + eps * V[k][0], b + eps * V[k][1]) for k, (W, b) in params.items()}
         pm = {k: (W - eps * V[k][0], b - eps * V[k][1]) for k, (W, b) in params.items()}
         fd = (loss(pp) - loss(pm)) / (2 * eps)
@@ -98,7 +98,9 @@ def test_arch_layout_and_grids():
         assert wo == off and ws == n_out * 27 * cin and bo == wo + ws
         off = bo + n_out
     assert total == off
-    # 513^3 voxels: input grid 129, output (node grid of h = 8) 65, coarse 33
+    # 513^3 voxels: input grid 129, output (node grid of h = 8) 65, then 33, 17
     assert input_grid((513, 513, 513)) == (129, 129, 129)
-    assert grids((129, 129, 129)) == ((129, 129, 129), (65, 65, 65), (33, 33, 33))
-    assert grids((65, 40, 9))[1:] == ((33, 20, 5), (17, 10, 3))
+    assert grids((129, 129, 129)) == ((129, 129, 129), (65, 65, 65), (33, 33, 33), (17, 17, 17))
+    assert grids((65, 40, 9))[1:] == ((33, 20, 5), (17, 10, 3), (9, 5, 2))
+    # the configuration's size: about 2M parameters
+    assert 2.0e6 < total < 2.5e6

@@ -215,7 +215,7 @@ def test_network_forward_and_gradients(env):
     params = {k: (W, rng.standard_normal(b.shape) * 0.05) for k, (W, b) in params.items()}
     net = S.SeedNet(params)
     G = (17, 13, 9)
-    G, n, m = grids(G)
+    G, n, _, _ = grids(G)
     x = O.bf16_round(rng.standard_normal((G[2], G[1], G[0], 2)))
     target = rng.standard_normal((n[2], n[1], n[0], 3)).astype(np.float32)
     b = net.buffers(G)

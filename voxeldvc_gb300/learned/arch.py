@@ -1,42 +1,45 @@
 """Architecture of the learned initial guess (pure data, no device code).
 
-Input: f and g low-passed and sampled every 4 voxels, 2 channels, grid G.
-Output: the displacement (3 channels, voxels) on the stride-8 voxel grid
-n = (G - 1) // 2 + 1, which is the node grid of an h = 8 mesh.
+A 4-level 3-D convolutional encoder-decoder with 32 base channels.  Input:
+f and g low-passed and sampled every 4 voxels (2 channels, grid G0 -- 129^3
+for a 513^3 pair).  Output: the displacement (3 channels, voxels) on the
+stride-8 voxel grid G1 = (G0 - 1) // 2 + 1, which is the node grid of an
+h = 8 mesh.  Grids: G(k+1) = (G(k) - 1) // 2 + 1.
 
-    c1  2 -> 16, stride 1   grid G        ReLU
-    c2 16 -> 32, stride 2   G -> n        ReLU
-    c3 32 -> 32, stride 1   n             ReLU   (also the skip branch)
-    c4 32 -> 32, stride 2   n -> m        ReLU
-    c5 32 -> 32, stride 1   m             ReLU
-    c6 32 -> 32, stride 1   m             ReLU
-    up  linear 2x           m -> n, concatenated as [up(c6) | c3] (64 ch)
-    c7 64 -> 16, stride 1   n             ReLU
-    c8 16 ->  3, stride 1   n             (linear, FP32 output)
+    level  grid        encoder                                decoder
+    0      G0 (129^3)  e1   2 ->  32 s1
+    1      G1 ( 65^3)  e2a  32 ->  64 s2, e2b  64 ->  64      d2  (64 up + 64 skip) -> 32, out 32 -> 3
+    2      G2 ( 33^3)  e3a  64 -> 128 s2, e3b 128 -> 128      d3  (128 up + 128 skip) -> 64
+    3      G3 ( 17^3)  e4a 128 -> 128 s2, e4b 128 -> 128
 
-All convolutions are 3x3x3 with zero padding.  Receptive field of an
-output: about 41 input samples (~160 voxels) per axis.
+Every convolution is 3x3x3 with zero padding and ReLU except `out`
+(linear, FP32 output).  The decoder upsamples linearly by 2 and
+concatenates [upsampled | skip] channels.  About 2.27M parameters.
 """
 LAYERS = (
-    dict(name="c1", cin=2, cout=16, stride=1, relu=True),
-    dict(name="c2", cin=16, cout=32, stride=2, relu=True),
-    dict(name="c3", cin=32, cout=32, stride=1, relu=True),
-    dict(name="c4", cin=32, cout=32, stride=2, relu=True),
-    dict(name="c5", cin=32, cout=32, stride=1, relu=True),
-    dict(name="c6", cin=32, cout=32, stride=1, relu=True),
-    dict(name="c7", cin=64, cout=16, stride=1, relu=True),
-    dict(name="c8", cin=16, cout=3, stride=1, relu=False),
+    dict(name="e1", cin=2, cout=32, stride=1, relu=True),
+    dict(name="e2a", cin=32, cout=64, stride=2, relu=True),
+    dict(name="e2b", cin=64, cout=64, stride=1, relu=True),
+    dict(name="e3a", cin=64, cout=128, stride=2, relu=True),
+    dict(name="e3b", cin=128, cout=128, stride=1, relu=True),
+    dict(name="e4a", cin=128, cout=128, stride=2, relu=True),
+    dict(name="e4b", cin=128, cout=128, stride=1, relu=True),
+    dict(name="d3", cin=256, cout=64, stride=1, relu=True),
+    dict(name="d2", cin=128, cout=32, stride=1, relu=True),
+    dict(name="out", cin=32, cout=3, stride=1, relu=False),
 )
 LAYER = {l["name"]: l for l in LAYERS}
 OUT_STRIDE = 8   # voxels between output samples
 IN_STRIDE = 4    # voxels between input samples
+LEVELS = 4
 
 
 def grids(G):
-    """(G, n, m) per axis for an input grid G (tuple of 3)."""
-    n = tuple((g - 1) // 2 + 1 for g in G)
-    m = tuple((k - 1) // 2 + 1 for k in n)
-    return tuple(G), n, m
+    """(G0, G1, G2, G3) per axis for an input grid G (tuple of 3)."""
+    out = [tuple(int(g) for g in G)]
+    for _ in range(LEVELS - 1):
+        out.append(tuple((k - 1) // 2 + 1 for k in out[-1]))
+    return tuple(out)
 
 
 def input_grid(shape):

@@ -77,7 +77,7 @@ class SeedNet:
         for name, wo, ws, bo, n_out, cin in self.layout:
             nf = _pad(n_out, 8) * (64 if cin == 2 else 27 * cin)
             self.wf[name] = torch.zeros(nf, dtype=torch.bfloat16, device=D.device())
-            if name != "c1":
+            if cin != 2:  # the first layer needs no input gradient
                 self.wb[name] = torch.zeros(_pad(cin, 8) * 27 * _pad(n_out, 16), dtype=torch.bfloat16,
                                             device=D.device())
         self._bufs = {}
@@ -116,76 +116,103 @@ class SeedNet:
         return out
 
     def save(self, path, **meta):
+        """Weights as BF16 bit patterns (the convolutions read BF16 copies of
+        them, so nothing is lost for inference), biases FP32."""
         p = self.params_numpy()
-        arrays = {f"{k}_W": v[0] for k, v in p.items()}
+        arrays = {f"{k}_W16": _to_bf16_bits(v[0]) for k, v in p.items()}
         arrays.update({f"{k}_b": v[1] for k, v in p.items()})
         arrays.update({f"meta_{k}": np.asarray(v) for k, v in meta.items()})
-        np.savez(path, **arrays)
+        np.savez_compressed(path, **arrays)
 
     @classmethod
     def load(cls, path=WEIGHTS_PATH):
         z = np.load(path)
-        params = {l["name"]: (z[f"{l['name']}_W"], z[f"{l['name']}_b"]) for l in LAYERS}
+        params = {}
+        for l in LAYERS:
+            n = l["name"]
+            W = _from_bf16_bits(z[f"{n}_W16"]) if f"{n}_W16" in z.files else z[f"{n}_W"]
+            params[n] = (W, z[f"{n}_b"])
         net = cls(params)
         net.meta = {k[5:]: z[k] for k in z.files if k.startswith("meta_")}
         return net
 
     # ---- buffers -----------------------------------------------------------------
 
-    def buffers(self, G):
-        """Activation and gradient buffers for input grid G (cached)."""
+    # Channels-last BF16 buffers per grid level (0: input grid; 1: the output
+    # grid, stride 8 voxels; 2, 3: coarser), and gradient buffers of the
+    # same shapes.  Concatenations are one buffer: cat3 = [up(e4b) | e3b] at
+    # level 2, cat2 = [up(d3) | e2b] at level 1; the encoder writes its skip
+    # output straight into the upper channels.
+    _ACT = (("x", 0, 2), ("e1", 0, 32), ("e2a", 1, 64), ("cat2", 1, 128), ("e3a", 2, 128), ("cat3", 2, 256),
+            ("e4a", 3, 128), ("e4b", 3, 128), ("d3", 2, 64), ("d2", 1, 32))
+    _GRAD = (("dp", 1, 16), ("dd2", 1, 32), ("dcat2", 1, 128), ("dd3", 2, 64), ("dcat3", 2, 256),
+             ("de4b", 3, 128), ("de4a", 3, 128), ("de3a", 2, 128), ("de2a", 1, 64), ("de1", 0, 32))
+
+    def buffers(self, G, train=True):
+        """Activation (and, with train, gradient) buffers for input grid G
+        (cached)."""
         G = tuple(int(v) for v in G)
-        if G in self._bufs:
-            return self._bufs[G]
+        if (G, True) in self._bufs:
+            return self._bufs[(G, True)]
+        if not train and (G, False) in self._bufs:
+            return self._bufs[(G, False)]
         torch = D.torch()
-        _, n, m = grids(G)
-        bf = lambda grid, c: torch.zeros(_npos(grid) * c, dtype=torch.bfloat16, device=D.device())
-        b = dict(G=G, n=n, m=m,
-                 x=bf(G, 2), a1=bf(G, 16), a2=bf(n, 32), cat=bf(n, 64), a4=bf(m, 32), a5=bf(m, 32), a6=bf(m, 32),
-                 a7=bf(n, 16), pred=torch.zeros(_npos(n) * 8, dtype=torch.float32, device=D.device()),
-                 d8=bf(n, 16), d7=bf(n, 16), dcat=bf(n, 64), d6=bf(m, 32), d5=bf(m, 32), d4=bf(m, 32),
-                 d2=bf(n, 32), d1=bf(G, 16))
-        ws = max(_lib.lib().vdvc_cnn_wgrad_workspace_bytes(l["cout"], l["cin"]) for l in LAYERS)
+        lv = grids(G)
+        bf = lambda level, c: torch.zeros(_npos(lv[level]) * c, dtype=torch.bfloat16, device=D.device())
+        b = dict(G=G, lv=lv)
+        for name, level, c in self._ACT:
+            b[name] = bf(level, c)
+        b["pred"] = torch.zeros(_npos(lv[1]) * 8, dtype=torch.float32, device=D.device())
+        ws = 0
+        if train:
+            for name, level, c in self._GRAD:
+                b[name] = bf(level, c)
+            ws = max(_lib.lib().vdvc_cnn_wgrad_workspace_bytes(l["cout"], l["cin"]) for l in LAYERS)
         b["ws"] = torch.empty(max(ws, 1 << 16), dtype=torch.uint8, device=D.device())
         b["loss"] = torch.zeros(1, dtype=torch.float64, device=D.device())
-        self._bufs[G] = b
+        self._bufs[(G, bool(train))] = b
         return b
 
     # ---- forward / backward --------------------------------------------------------
 
-    def _conv(self, name, src, scs, scoff, cin, out, ocs, ocoff, geom, out_f32=False, relu=None):
+    def _conv(self, name, src, scs, scoff, out, ocs, ocoff, geom, out_f32=False):
         l = LAYER[name]
         _, bptr = self._wptr(name)
-        _lib.check(_lib.lib().vdvc_cnn_conv(src.data_ptr(), scs, scoff, cin, self.wf[name].data_ptr(), bptr,
-                                            l["cout"], int(l["relu"] if relu is None else relu), out.data_ptr(),
-                                            int(out_f32), ocs, ocoff, 0, C.byref(geom), D.stream()), f"conv {name}")
+        _lib.check(_lib.lib().vdvc_cnn_conv(src.data_ptr(), scs, scoff, l["cin"], self.wf[name].data_ptr(), bptr,
+                                            l["cout"], int(l["relu"]), out.data_ptr(), int(out_f32), ocs, ocoff, 0,
+                                            C.byref(geom), D.stream()), f"conv {name}")
 
-    def forward(self, G):
+    def _up(self, src, scs, scoff, m, dst, dcs, dcoff, n, nch):
+        _lib.check(_lib.lib().vdvc_cnn_upsample2(src.data_ptr(), scs, scoff, *m, dst.data_ptr(), dcs, dcoff, *n, nch,
+                                                 D.stream()), "upsample2")
+
+    def forward(self, G, train=True):
         """Run the network on buffers(G)['x']; returns the FP32 output
-        (npos(n) x 8, channels [0,3) used)."""
-        b = self.buffers(G)
-        L = _lib.lib()
-        G, n, m = b["G"], b["n"], b["m"]
-        self._conv("c1", b["x"], 2, 0, 2, b["a1"], 16, 0, fwd_geom(G, G, 1))
-        self._conv("c2", b["a1"], 16, 0, 16, b["a2"], 32, 0, fwd_geom(n, G, 2))
-        self._conv("c3", b["a2"], 32, 0, 32, b["cat"], 64, 32, fwd_geom(n, n, 1))
-        self._conv("c4", b["cat"], 64, 32, 32, b["a4"], 32, 0, fwd_geom(m, n, 2))
-        self._conv("c5", b["a4"], 32, 0, 32, b["a5"], 32, 0, fwd_geom(m, m, 1))
-        self._conv("c6", b["a5"], 32, 0, 32, b["a6"], 32, 0, fwd_geom(m, m, 1))
-        _lib.check(L.vdvc_cnn_upsample2(b["a6"].data_ptr(), 32, 0, *m, b["cat"].data_ptr(), 64, 0, *n, 32,
-                                        D.stream()), "upsample2")
-        self._conv("c7", b["cat"], 64, 0, 64, b["a7"], 16, 0, fwd_geom(n, n, 1))
-        self._conv("c8", b["a7"], 16, 0, 16, b["pred"], 8, 0, fwd_geom(n, n, 1), out_f32=True)
+        (npos(G1) x 8, channels [0,3) used)."""
+        b = self.buffers(G, train)
+        g0, g1, g2, g3 = b["lv"]
+        self._conv("e1", b["x"], 2, 0, b["e1"], 32, 0, fwd_geom(g0, g0, 1))
+        self._conv("e2a", b["e1"], 32, 0, b["e2a"], 64, 0, fwd_geom(g1, g0, 2))
+        self._conv("e2b", b["e2a"], 64, 0, b["cat2"], 128, 64, fwd_geom(g1, g1, 1))
+        self._conv("e3a", b["cat2"], 128, 64, b["e3a"], 128, 0, fwd_geom(g2, g1, 2))
+        self._conv("e3b", b["e3a"], 128, 0, b["cat3"], 256, 128, fwd_geom(g2, g2, 1))
+        self._conv("e4a", b["cat3"], 256, 128, b["e4a"], 128, 0, fwd_geom(g3, g2, 2))
+        self._conv("e4b", b["e4a"], 128, 0, b["e4b"], 128, 0, fwd_geom(g3, g3, 1))
+        self._up(b["e4b"], 128, 0, g3, b["cat3"], 256, 0, g2, 128)
+        self._conv("d3", b["cat3"], 256, 0, b["d3"], 64, 0, fwd_geom(g2, g2, 1))
+        self._up(b["d3"], 64, 0, g2, b["cat2"], 128, 0, g1, 64)
+        self._conv("d2", b["cat2"], 128, 0, b["d2"], 32, 0, fwd_geom(g1, g1, 1))
+        self._conv("out", b["d2"], 32, 0, b["pred"], 8, 0, fwd_geom(g1, g1, 1), out_f32=True)
         return b["pred"]
 
     def loss(self, G, target, want_grad=True, scale=1.0):
-        """MSE of the output against target (FP32 CUDA (npos(n), 3)); with
-        want_grad the output gradient goes to the d8 buffer.  Returns the
+        """MSE of the output against target (FP32 CUDA (npos(G1), 3)); with
+        want_grad the output gradient goes to the dp buffer.  Returns the
         device loss scalar (float64 tensor of 1)."""
-        b = self.buffers(G)
-        npos = _npos(b["n"])
+        b = self.buffers(G, want_grad)
+        npos = _npos(b["lv"][1])
         _lib.check(_lib.lib().vdvc_cnn_mse(b["pred"].data_ptr(), 8, target.data_ptr(), npos, b["loss"].data_ptr(),
-                                           b["d8"].data_ptr() if want_grad else None, 16, float(scale),
+                                           b["dp"].data_ptr() if want_grad else None, 16, float(scale),
                                            b["ws"].data_ptr(), b["ws"].numel(), D.stream()), "cnn_mse")
         return b["loss"]
 
@@ -213,40 +240,51 @@ class SeedNet:
     def _relu_bwd(self, d, a):
         _lib.check(_lib.lib().vdvc_cnn_relu_bwd(d.data_ptr(), a.data_ptr(), d.numel(), D.stream()), "relu_bwd")
 
+    def _up_bwd(self, dfine, fcs, fcoff, n, dcoarse, ccs, ccoff, m, nch):
+        _lib.check(_lib.lib().vdvc_cnn_upsample2_bwd(dfine.data_ptr(), fcs, fcoff, *n, dcoarse.data_ptr(), ccs, ccoff,
+                                                     *m, nch, D.stream()), "upsample2_bwd")
+
     def backward(self, G, accumulate=False):
         """Parameter gradients (into self.grad; added when accumulate) from
-        the output gradient in the d8 buffer."""
+        the output gradient in the dp buffer.  Where a skip connection's two
+        gradients meet, the second input gradient is added onto the first
+        in the concatenation's gradient buffer; a ReLU mask applied to a
+        whole concatenation touches only channels already consumed."""
         b = self.buffers(G)
-        L = _lib.lib()
-        G, n, m = b["G"], b["n"], b["m"]
+        g0, g1, g2, g3 = b["lv"]
         acc = accumulate
-        self._back("c8", b["d8"], 16, 0, b["a7"], 16, 0, fwd_geom(n, n, 1), b, acc)
-        self._dconv("c8", b["d8"], 16, 0, b["d7"], 16, 0, n, n)
-        self._relu_bwd(b["d7"], b["a7"])
-        self._back("c7", b["d7"], 16, 0, b["cat"], 64, 0, fwd_geom(n, n, 1), b, acc)
-        self._dconv("c7", b["d7"], 16, 0, b["dcat"], 64, 0, n, n)
-        _lib.check(L.vdvc_cnn_upsample2_bwd(b["dcat"].data_ptr(), 64, 0, *n, b["d6"].data_ptr(), 32, 0, *m, 32,
-                                            D.stream()), "upsample2_bwd")
-        self._relu_bwd(b["d6"], b["a6"])
-        self._back("c6", b["d6"], 32, 0, b["a5"], 32, 0, fwd_geom(m, m, 1), b, acc)
-        self._dconv("c6", b["d6"], 32, 0, b["d5"], 32, 0, m, m)
-        self._relu_bwd(b["d5"], b["a5"])
-        self._back("c5", b["d5"], 32, 0, b["a4"], 32, 0, fwd_geom(m, m, 1), b, acc)
-        self._dconv("c5", b["d5"], 32, 0, b["d4"], 32, 0, m, m)
-        self._relu_bwd(b["d4"], b["a4"])
-        self._back("c4", b["d4"], 32, 0, b["cat"], 64, 32, fwd_geom(m, n, 2), b, acc)
-        # c3 feeds c4 and the concatenation: add c4's input gradient onto
-        # the concatenation gradient's c3 channels
-        self._dconv("c4", b["d4"], 32, 0, b["dcat"], 64, 32, n, m, accumulate=True)
-        # ReLU mask of the whole concatenation: channels [0, 32) are spent
-        self._relu_bwd(b["dcat"], b["cat"])
-        self._back("c3", b["dcat"], 64, 32, b["a2"], 32, 0, fwd_geom(n, n, 1), b, acc)
-        self._dconv("c3", b["dcat"], 64, 32, b["d2"], 32, 0, n, n)
-        self._relu_bwd(b["d2"], b["a2"])
-        self._back("c2", b["d2"], 32, 0, b["a1"], 16, 0, fwd_geom(n, G, 2), b, acc)
-        self._dconv("c2", b["d2"], 32, 0, b["d1"], 16, 0, G, n)
-        self._relu_bwd(b["d1"], b["a1"])
-        self._back("c1", b["d1"], 16, 0, b["x"], 2, 0, fwd_geom(G, G, 1), b, acc)
+        self._back("out", b["dp"], 16, 0, b["d2"], 32, 0, fwd_geom(g1, g1, 1), b, acc)
+        self._dconv("out", b["dp"], 16, 0, b["dd2"], 32, 0, g1, g1)
+        self._relu_bwd(b["dd2"], b["d2"])
+        self._back("d2", b["dd2"], 32, 0, b["cat2"], 128, 0, fwd_geom(g1, g1, 1), b, acc)
+        self._dconv("d2", b["dd2"], 32, 0, b["dcat2"], 128, 0, g1, g1)
+        self._up_bwd(b["dcat2"], 128, 0, g1, b["dd3"], 64, 0, g2, 64)
+        self._relu_bwd(b["dd3"], b["d3"])
+        self._back("d3", b["dd3"], 64, 0, b["cat3"], 256, 0, fwd_geom(g2, g2, 1), b, acc)
+        self._dconv("d3", b["dd3"], 64, 0, b["dcat3"], 256, 0, g2, g2)
+        self._up_bwd(b["dcat3"], 256, 0, g2, b["de4b"], 128, 0, g3, 128)
+        self._relu_bwd(b["de4b"], b["e4b"])
+        self._back("e4b", b["de4b"], 128, 0, b["e4a"], 128, 0, fwd_geom(g3, g3, 1), b, acc)
+        self._dconv("e4b", b["de4b"], 128, 0, b["de4a"], 128, 0, g3, g3)
+        self._relu_bwd(b["de4a"], b["e4a"])
+        self._back("e4a", b["de4a"], 128, 0, b["cat3"], 256, 128, fwd_geom(g3, g2, 2), b, acc)
+        # e3b feeds e4a and the concatenation
+        self._dconv("e4a", b["de4a"], 128, 0, b["dcat3"], 256, 128, g2, g3, accumulate=True)
+        self._relu_bwd(b["dcat3"], b["cat3"])
+        self._back("e3b", b["dcat3"], 256, 128, b["e3a"], 128, 0, fwd_geom(g2, g2, 1), b, acc)
+        self._dconv("e3b", b["dcat3"], 256, 128, b["de3a"], 128, 0, g2, g2)
+        self._relu_bwd(b["de3a"], b["e3a"])
+        self._back("e3a", b["de3a"], 128, 0, b["cat2"], 128, 64, fwd_geom(g2, g1, 2), b, acc)
+        # e2b feeds e3a and the concatenation
+        self._dconv("e3a", b["de3a"], 128, 0, b["dcat2"], 128, 64, g1, g2, accumulate=True)
+        self._relu_bwd(b["dcat2"], b["cat2"])
+        self._back("e2b", b["dcat2"], 128, 64, b["e2a"], 64, 0, fwd_geom(g1, g1, 1), b, acc)
+        self._dconv("e2b", b["dcat2"], 128, 64, b["de2a"], 64, 0, g1, g1)
+        self._relu_bwd(b["de2a"], b["e2a"])
+        self._back("e2a", b["de2a"], 64, 0, b["e1"], 32, 0, fwd_geom(g1, g0, 2), b, acc)
+        self._dconv("e2a", b["de2a"], 64, 0, b["de1"], 32, 0, g0, g1)
+        self._relu_bwd(b["de1"], b["e1"])
+        self._back("e1", b["de1"], 32, 0, b["x"], 2, 0, fwd_geom(g0, g0, 1), b, acc)
 
     def adam(self, lr, beta1=0.9, beta2=0.999, eps=1e-8):
         self.step_count += 1
@@ -257,11 +295,11 @@ class SeedNet:
 
     # ---- inputs ------------------------------------------------------------------
 
-    def set_input(self, f_vox, g_vox, shape):
+    def set_input(self, f_vox, g_vox, shape, train=True):
         """Pool f and g (FP32 vox-layout CUDA tensors of `shape` voxels) into
         the input buffer; returns the input grid."""
         G = input_grid(shape)
-        b = self.buffers(G)
+        b = self.buffers(G, train)
         ms = np.array([*_mean_std(f_vox), *_mean_std(g_vox)], np.float64)
         _lib.check(_lib.lib().vdvc_cnn_pool_input(f_vox.data_ptr(), g_vox.data_ptr(), *shape,
                                                   ms.ctypes.data_as(_lib.pd), b["x"].data_ptr(), D.stream()),
@@ -271,13 +309,24 @@ class SeedNet:
     def predict_nodes(self, f_vox, g_vox, shape, h, Nx, Ny, Nz):
         """Seed U (float64 CUDA tensor, 3 (Nx+1)(Ny+1)(Nz+1)) for a mesh of
         edge h over a volume of `shape` voxels."""
-        G = self.set_input(f_vox, g_vox, shape)
-        pred = self.forward(G)
-        n = self.buffers(G)["n"]
+        G = self.set_input(f_vox, g_vox, shape, train=False)
+        pred = self.forward(G, train=False)
+        n = self.buffers(G, train=False)["lv"][1]
         U = D.empty(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), np.float64)
         _lib.check(_lib.lib().vdvc_cnn_seed_nodes(pred.data_ptr(), 8, *n, h, Nx, Ny, Nz, U.data_ptr(), D.stream()),
                    "cnn_seed_nodes")
         return U
+
+
+def _to_bf16_bits(a):
+    """Nearest BF16 (ties to even) of float32 a, as uint16 bit patterns."""
+    b = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) >> 16
+    return b.astype(np.uint16)
+
+
+def _from_bf16_bits(b):
+    return (np.asarray(b, np.uint32) << 16).view(np.float32)
 
 
 def _mean_std(x):
