@@ -14,10 +14,12 @@ inputs (540 MB each) are larger than L2, so no flush is needed.
   e2e     the same solve through the public API with ordinary (pageable)
           host numpy inputs: host->device image upload and device->host
           read of (U, res, dU) inside the timed region
-  roofline  the matrix-free Hessian matvec at the finest level, timed with
-          CUDA events right after the timed solves on the same data;
-          `traffic` is the DRAM bytes per voxel of an ncu capture of the
-          257^3 case scaled to this launch's voxel count
+  roofline  the finest level's Hessian matvec in the form the solve's PCG
+          applies it (element Hessians from the float32 gradient at h >= 6),
+          timed with CUDA events right after the timed solves on the same
+          data; `roofline_matrix_free` the same for the matrix-free pass (the
+          reference's formulation); `traffic` is the DRAM bytes of an ncu
+          capture of the 257^3 case scaled to this launch's size
   cpu_baseline  the reference's own operators (voxelDVC's engine on NumPy,
           installed unmodified in baseline/_ref) on slabs of this run's
           arrays over all host cores, assembled into a solve time with this
@@ -47,6 +49,11 @@ METRIC = "512³ h=8 DVC time to 0.02vx RMS, plain vs mixed/learned; matvec GB/s"
 # DRAM bytes per voxel of one float32 matvec (k_strip_hv_fast<8> + k_gather),
 # ncu dram__bytes_read + write on the 257^3 case.
 TRAFFIC_B_PER_VOXEL = 14.04
+
+# DRAM bytes per element of one element-Hessian apply (k_eh_matvec_tma +
+# k_gather), ncu dram__bytes_read + write on the 257^3 case; None until
+# captured.
+TRAFFIC_B_PER_ELEMENT_EH = None
 
 # Operation counts (per pyramid level, coarse to fine: GN iterations, total
 # PCG iterations) that the reference arm multiplies its measured operation
@@ -82,12 +89,29 @@ def parse(argv=None):
     return p.parse_args(argv)
 
 
+def _events_ms(fn, warmup, reps, stream):
+    """Mean CUDA-event time (ms) of `reps` back-to-back calls on `stream`."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / max(1, reps)
+
+
 def matvec_only(args):
     """Generate the workload's reference image, then run `--warmup` + `--steps`
-    finest-level Hessian matvecs (vdvc_matvec_H) and print their mean time."""
+    finest-level Hessian matvecs -- matrix-free (vdvc_matvec_H) and from
+    element Hessians formed once (vdvc_eh_apply) -- and print their mean
+    times."""
     import torch
     from voxeldvc_gb300 import _lib, synth
-    from voxeldvc_gb300.engine import correlate_gpu as CG
+    from voxeldvc_gb300.engine import correlate_gpu as CG, kernels_dvc as K
     wl = synth.WORKLOADS[args.workload]()
     Nx, Ny, Nz = wl.mesh
     f = synth.texture(wl.shape, wl.n_cyl)
@@ -105,19 +129,16 @@ def matvec_only(args):
         _lib.check(L.vdvc_matvec_H(v.data_ptr(), grad.data_ptr(), mask0.data_ptr(), _lib.F32, wl.h, Nx, Ny, Nz,
                                    out.data_ptr(), ws.data_ptr(), nws, s.cuda_stream))
 
-    for _ in range(args.warmup):
-        mv()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(s)
-    for _ in range(args.steps):
-        mv()
-    e1.record(s)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / max(1, args.steps)
+    ms = _events_ms(mv, args.warmup, args.steps, s)
+    eh = K.ElementHessians(grad, mask0, wl.h, Nx, Ny, Nz)
+    ms_eh = _events_ms(lambda: eh.matvec_into(v, out), args.warmup, args.steps, s)
+    eh.status()
     nvox = wl.shape[0] * wl.shape[1] * wl.shape[2]
+    ne = Nx * Ny * Nz
     print(json.dumps({"workload": wl.name, "matvec_ms": round(ms, 4),
-                      "algorithmic_GBs": round((nvox * 13 + ndof * 8) / ms / 1e6, 1)}))
+                      "algorithmic_GBs": round((nvox * 13 + ndof * 8) / ms / 1e6, 1),
+                      "eh_apply_ms": round(ms_eh, 4),
+                      "eh_apply_algorithmic_GBs": round((ne * 648 + ndof * 8) / ms_eh / 1e6, 1)}))
 
 
 # ---------------------------------------------------------------------------
@@ -492,15 +513,27 @@ def compare_forms(wl, f_pix, g_pix, kw, U_plain, e2e_plain, plain_s):
     t64, (U64, _, _) = timed(lambda: CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, xp=torch,
                                                                   dtype=np.float64, **kw), reps=1)
     U64 = U64.double()
+    from voxeldvc_gb300.engine import write_output as W
 
     def rms(U):
         return float(torch.sqrt(torch.mean((U.double() - U64) ** 2)).item())
 
+    def strains(U):
+        # principal strains at the element centroids (write_output's cell strains)
+        Ug = U.double().reshape(Nz + 1, Ny + 1, Nx + 1, 3).permute(2, 1, 0, 3)
+        return np.asarray(W.compute_principal_strains_cell(Ug, wl.h))
+
+    ps64 = strains(U64)
+
+    def strain_rms(U):
+        return float(np.sqrt(np.mean((strains(U) - ps64) ** 2)))
+
     out = {"reference": "GPU FP64 solve of the same inputs", "f64_s": round(t64, 4),
-           "target_rms_vx": 0.02, "plain": {"rms_vs_f64_vx": round(rms(U_plain), 6)}}
+           "target_rms_vx": 0.02, "strain_rms_f64": float(np.sqrt(np.mean(ps64 ** 2))),
+           "plain": {"rms_vs_f64_vx": round(rms(U_plain), 6), "strain_rms_vs_f64": strain_rms(U_plain)}}
     tm, (Um, _, _) = timed(lambda: CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, wl.h, xp=torch,
                                                                 precision="mixed", **kw))
-    out["mixed"] = {"s": round(tm, 4), "rms_vs_f64_vx": round(rms(Um), 6)}
+    out["mixed"] = {"s": round(tm, 4), "rms_vs_f64_vx": round(rms(Um), 6), "strain_rms_vs_f64": strain_rms(Um)}
     kwl = {k: v for k, v in kw.items() if k not in ("scales", "fft_prealign")}
     try:
         net = LS.default_net()
@@ -512,7 +545,8 @@ def compare_forms(wl, f_pix, g_pix, kw, U_plain, e2e_plain, plain_s):
                                                             precision="mixed", stats=stats, **kwl))
     last = stats[-1]
     gn = [s for s in stats if "gn_iters" in s]
-    out["learned_mixed"] = {"s": round(tl, 4), "rms_vs_f64_vx": round(rms(Ul), 6), "seed": last.get("seed"),
+    out["learned_mixed"] = {"s": round(tl, 4), "rms_vs_f64_vx": round(rms(Ul), 6), "strain_rms_vs_f64": strain_rms(Ul),
+                            "seed": last.get("seed"),
                             "norm_res": last.get("norm_res"), "gn_iters": [s["gn_iters"] for s in gn[-1:]],
                             "pcg_iters": [int(sum(s["pcg_iters"])) for s in gn[-1:]]}
     # the same through the public API with host arrays (ordinary numpy
@@ -657,11 +691,14 @@ def gpu_arm(args):
     inner = np.all((ijk >= 4) & (ijk <= np.array(wl.mesh) - 4), axis=1)
     rms_inner = float(np.sqrt(np.mean(err[inner] ** 2))) if inner.any() else float("nan")
 
-    # roofline: the finest-level Hessian matvec on the same data
+    # rooflines: the finest level's Hessian matvec on the same data, in the
+    # form the solve's PCG applies (element Hessians from the float32
+    # gradient at h >= 6) and matrix-free (the reference's formulation)
     grad, mask0 = CG._grad_vox(CG.pix_to_vox(f_pix, np.float32)[0], wl.shape, np.float32, 0.0)
     v = torch.randn(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), device="cuda", dtype=torch.float32)
     nvox = wl.shape[0] * wl.shape[1] * wl.shape[2]
     ndof = v.numel()
+    ne = Nx * Ny * Nz
     out = torch.empty_like(v)
     nws = _lib.lib().vdvc_workspace_bytes(_lib.F32, wl.h, Nx, Ny, Nz)
     ws = torch.empty(nws, dtype=torch.uint8, device="cuda")
@@ -671,24 +708,39 @@ def gpu_arm(args):
         _lib.check(L.vdvc_matvec_H(v.data_ptr(), grad.data_ptr(), mask0.data_ptr(), _lib.F32, wl.h, Nx, Ny, Nz,
                                    out.data_ptr(), ws.data_ptr(), nws, stream.cuda_stream))
 
-    for _ in range(5):
-        mv()
-    reps = 50
-    m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    m0.record(stream)
-    for _ in range(reps):
-        mv()
-    m1.record(stream)
-    torch.cuda.synchronize()
-    mv_ms = m0.elapsed_time(m1) / reps
+    mv_ms = _events_ms(mv, 5, 50, stream)
     alg_bytes = nvox * 13 + ndof * 8
     peaks = {}
     pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pp):
         peaks = json.load(open(pp))
     peak = peaks.get("hbm_gbs", 6800.0)
+    peak_source = "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800"
     achieved = alg_bytes / (mv_ms * 1e-3) / 1e9
+    roof_mf = {"bound": "hbm", "kernel": "matvec_H f32 matrix-free (k_strip_hv_fast + k_gather)",
+               "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_source, "unit": "GB/s",
+               "frac": round(achieved / peak, 4), "traffic": int(TRAFFIC_B_PER_VOXEL * nvox),
+               "traffic_source": f"ncu dram bytes of the 257^3 case ({TRAFFIC_B_PER_VOXEL} B per "
+                                 f"voxel) scaled to this launch's {nvox} voxels",
+               "algorithmic_bytes": int(alg_bytes), "ms": round(mv_ms, 4)}
+    roof = roof_mf
+    if level_stats and level_stats[-1].get("hessian") == "element":
+        eh = K.ElementHessians(grad, mask0, wl.h, Nx, Ny, Nz)
+        eh_ms = _events_ms(lambda: eh.matvec_into(v, out), 5, 50, stream)
+        eh.status()
+        eh_bytes = ne * 648 + ndof * 8
+        eh_ach = eh_bytes / (eh_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": "matvec_H f32 from element Hessians (k_eh_matvec_tma + k_gather), the "
+                                          "finest level's PCG operator",
+                "achieved": round(eh_ach, 1), "peak": peak, "peak_source": peak_source, "unit": "GB/s",
+                "frac": round(eh_ach / peak, 4),
+                "traffic": int(TRAFFIC_B_PER_ELEMENT_EH * ne) if TRAFFIC_B_PER_ELEMENT_EH else None,
+                "traffic_source": (f"ncu dram bytes of the 257^3 case ({TRAFFIC_B_PER_ELEMENT_EH} B per element) "
+                                   f"scaled to this launch's {ne} elements") if TRAFFIC_B_PER_ELEMENT_EH else
+                "not captured",
+                "algorithmic_bytes": int(eh_bytes), "ms": round(eh_ms, 4),
+                "formation": "once per GN iteration until the b mask freezes (k_eh_form, not in this figure)"}
+        del eh
     del grad, mask0, ws
 
     # e2e through the public API with host arrays: ordinary (pageable) numpy
@@ -752,14 +804,7 @@ def gpu_arm(args):
                           "level_gn_wall_s": [round(s["gn_wall_s"], 4) for s in level_stats],
                           "rms_vs_true_field_vx": round(rms_true, 5),
                           "rms_vs_true_field_inner_vx": round(rms_inner, 5)},
-                "roofline": {"bound": "hbm", "kernel": "matvec_H f32 (k_strip_hv_fast + k_gather)",
-                             "achieved": round(achieved, 1), "peak": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs"
-                             if "hbm_gbs" in peaks else "fallback 6800", "unit": "GB/s",
-                             "frac": round(achieved / peak, 4),
-                             "traffic": int(TRAFFIC_B_PER_VOXEL * nvox),
-                             "traffic_source": f"ncu dram bytes of the 257^3 case ({TRAFFIC_B_PER_VOXEL} B per "
-                                               f"voxel) scaled to this launch's {nvox} voxels",
-                             "algorithmic_bytes": int(alg_bytes), "ms": round(mv_ms, 4)},
+                "roofline": roof, "roofline_matrix_free": roof_mf,
                 "cpu_baseline": cpu, "e2e": e2e, "forms": forms, "clocks": clocks}
         print(json.dumps(line))
     if world > 1:

@@ -164,6 +164,29 @@ int vdvc_matvec_H_mixed(const float* v, const float* grad,
                         vdvc_stream_t stream);
 size_t vdvc_eh_workspace_bytes(int h, int Nx, int Ny, int Nz);
 
+/* The Hessian of matvec_H (kernels_dvc.py:452-506) as element Hessians,
+   formed once and applied many times -- the operator the GN solver's PCG
+   uses at element edges >= 6.  T holds the 162 distinct entries of every
+   element's 24x24 block (FP32 accumulation), tile-major, vdvc_eh_bytes()
+   bytes, 16-byte aligned.  vdvc_eh_form builds T from the float32 gradient
+   (grad_bf16 = 0: the matrix-free pass's float32 products summed in another
+   order) or from its BF16 rounding (grad_bf16 = 1: grad then points to
+   (Nvox,3) BF16 values).  vdvc_eh_apply: out = H v from T.  Both take a
+   workspace of vdvc_eh_op_workspace_bytes() bytes, zero-filled before its
+   first use; its status word records a timed-out bulk-copy wait, which
+   vdvc_eh_status reports (VDVC_ERR_TIMEOUT) and clears.  h in
+   {1,2,3,4,6,8,12,16}. */
+size_t vdvc_eh_bytes(int h, int Nx, int Ny, int Nz);
+size_t vdvc_eh_op_workspace_bytes(int h, int Nx, int Ny, int Nz);
+int vdvc_eh_form(const float* grad, int grad_bf16, const uint8_t* mask,
+                 int h, int Nx, int Ny, int Nz, float* T, void* ws,
+                 size_t ws_bytes, vdvc_stream_t stream);
+int vdvc_eh_apply(const float* T, const float* v, int h, int Nx, int Ny,
+                  int Nz, float* out, void* ws, size_t ws_bytes,
+                  vdvc_stream_t stream);
+int vdvc_eh_status(void* ws, size_t ws_bytes, int h, int Nx, int Ny, int Nz,
+                   vdvc_stream_t stream);
+
 /* out = diag(H) (build_diagonal_H, kernels_dvc.py:509-543). */
 int vdvc_diag_H(const void* grad, const uint8_t* mask, int dtype, int h,
                 int Nx, int Ny, int Nz, void* out, void* ws, size_t ws_bytes,
@@ -470,16 +493,26 @@ typedef struct vdvc_gn_desc {
   const double* diag_eqgap;  /* (Ndof) float64 Hutchinson diag of K P_i K     */
   double mean0, std0;        /* multiplicity-weighted stats of f over mask0   */
   vdvc_stream_t stream;      /* stream used for the set-up in vdvc_gn_create   */
-  int precision;             /* VDVC_PREC_PLAIN, or VDVC_PREC_MIXED: BF16
-                                gradient, element Hessians formed once per GN
-                                iteration (once per solve after the b mask
-                                freezes), FP32 element-Hessian matvecs in the
-                                PCG; dtype VDVC_F32, Laplacian K_lap          */
-  void* eh_ws;               /* VDVC_PREC_MIXED: device workspace of          */
-  size_t eh_ws_bytes;        /*   vdvc_eh_workspace_bytes(h, Nx, Ny, Nz) bytes */
+  int precision;             /* VDVC_PREC_PLAIN: matrix-free H v from the
+                                gradient every PCG step (kernels_dvc.py:
+                                452-506).  VDVC_PREC_ELEMENT: element
+                                Hessians formed from the float32 gradient
+                                once per GN iteration (once per solve after
+                                the b mask freezes), FP32 element-Hessian
+                                matvecs in the PCG -- the same float32
+                                products summed in another order.
+                                VDVC_PREC_MIXED: the same from the BF16-
+                                rounded gradient.  Both: dtype VDVC_F32,
+                                Laplacian K_lap one 8x8 block per component */
+  void* eh_ws;               /* ELEMENT / MIXED: device workspace of           */
+  size_t eh_ws_bytes;        /*   vdvc_gn_eh_workspace_bytes(precision, ...)   */
 } vdvc_gn_desc;
 
-enum { VDVC_PREC_PLAIN = 0, VDVC_PREC_MIXED = 1 };
+enum { VDVC_PREC_PLAIN = 0, VDVC_PREC_MIXED = 1, VDVC_PREC_ELEMENT = 2 };
+
+/* Bytes of vdvc_gn_desc.eh_ws for a solver of this precision and mesh (0
+   for VDVC_PREC_PLAIN or a bad mesh). */
+size_t vdvc_gn_eh_workspace_bytes(int precision, int h, int Nx, int Ny, int Nz);
 
 typedef struct vdvc_gn_solver vdvc_gn_solver;
 

@@ -31,6 +31,9 @@ F32, F64, U8, U16, I16, I32 = 0, 1, 2, 3, 4, 5
 # regularizer kinds
 REG_NONE, REG_LAPLACIAN, REG_EQUILIBRIUM_GAP = 0, 1, 2
 
+# Hessian forms of the GN solver (vdvc_gn_desc.precision)
+PREC_PLAIN, PREC_MIXED, PREC_ELEMENT = 0, 1, 2
+
 vp = C.c_void_p
 ci = C.c_int
 cd = C.c_double
@@ -56,6 +59,12 @@ SIGNATURES = {
     "vdvc_selftest_bounded_wait": (ci, [ci, C.c_longlong, vp]),
     "vdvc_matvec_H_mixed": (ci, [vp, vp, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_eh_workspace_bytes": (cz, [ci, ci, ci, ci]),
+    "vdvc_gn_eh_workspace_bytes": (cz, [ci, ci, ci, ci, ci]),
+    "vdvc_eh_bytes": (cz, [ci, ci, ci, ci]),
+    "vdvc_eh_op_workspace_bytes": (cz, [ci, ci, ci, ci]),
+    "vdvc_eh_form": (ci, [vp, ci, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
+    "vdvc_eh_apply": (ci, [vp, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
+    "vdvc_eh_status": (ci, [vp, cz, ci, ci, ci, ci, vp]),
     "vdvc_diag_H": (ci, [vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_compute_b": (ci, [vp, vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_matvec_K_ref": (ci, [vp, ci, pd, vp, cd, ci, ci, ci, vp, vp]),

@@ -13,11 +13,12 @@
 //            `chunk` iterations until the device state says done
 //   update : U += dU (float64 master copy), |dU|^2, |U|^2
 //
-// Precision form (float solver, VDVC_PREC_MIXED): the gradient is rounded to
-// BF16 once at create; rhs forms the element Hessians T[162][Ne] and the
-// diagonal from them instead of the diag strip pass; the PCG applies H from T.
-// Once the b mask is frozen (or with a fixed mask0), H, diag and M^-1 no
-// longer change and are formed only once.
+// Element-Hessian forms (float solver): rhs forms the element Hessians
+// T[162][Ne] and the diagonal from them instead of the diag strip pass, and
+// the PCG applies H from T.  Once the b mask is frozen (or with a fixed
+// mask0), H, diag and M^-1 no longer change and are formed only once.
+// VDVC_PREC_ELEMENT forms T from the float32 gradient; VDVC_PREC_MIXED (the
+// precision form) from its BF16 rounding, made once at create.
 #include <cstdlib>
 #include <new>
 #include <type_traits>
@@ -58,11 +59,12 @@ struct GnSolver {
   PcgState* pcg;
   Kpair<T>* kp;
   bool frozen_set;
-  // precision form
-  bool mixed;
+  // element-Hessian forms
+  bool eh;           // the PCG applies H from element Hessians
+  bool eh_bf16;      // ... formed from the BF16 gradient (precision form)
   bool eh_fixed;     // T, diag and M^-1 are final (b mask frozen, or mask0)
   float* T_eh;       // [162][Ne] element Hessians
-  void* grad_bf16;   // (Nvox,3) BF16
+  void* grad_bf16;   // (Nvox,3) BF16 (precision form only)
   float* gmax;       // max |g| of grad_bf16 (the tensor-core formation's scale)
   // PCG graph
   cudaStream_t cap_stream;
@@ -337,7 +339,7 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
     if ((st = launch_kref_apply<T>(a, S->Kel, s))) return st;
   }
   if constexpr (std::is_same<T, float>::value) {
-    if (S->mixed) {
+    if (S->eh) {
       EhMatvecArgs ma{};
       ma.m = S->m;
       ma.T = S->T_eh;
@@ -446,24 +448,26 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
     return set_error(VDVC_ERR_WORKSPACE, "solver needs %zu bytes of workspace (got %zu)", need, ws_bytes);
   }
   carve_solver<T>(m, S, ws, ws_bytes);
-  S->mixed = d->precision == VDVC_PREC_MIXED;
-  if (d->precision != VDVC_PREC_PLAIN && !S->mixed) {
+  S->eh = d->precision == VDVC_PREC_MIXED || d->precision == VDVC_PREC_ELEMENT;
+  S->eh_bf16 = d->precision == VDVC_PREC_MIXED;
+  if (d->precision != VDVC_PREC_PLAIN && !S->eh) {
     delete S;
     return set_error(VDVC_ERR_ARG, "precision %d", d->precision);
   }
-  if (S->mixed) {
+  if (S->eh) {
     Carve cv(d->eh_ws, d->eh_ws_bytes);
     S->T_eh = cv.take<float>((size_t)162 * eh_pitch(m.Ne));
-    S->grad_bf16 = cv.take<uint16_t>((size_t)3 * m.Nvox);
     S->gmax = cv.take<float>(4);
+    S->grad_bf16 = S->eh_bf16 ? cv.take<uint16_t>((size_t)3 * m.Nvox) : nullptr;
     const bool ok = std::is_same<T, float>::value;
     const bool h_ok = d->h == 1 || d->h == 2 || d->h == 3 || d->h == 4 || d->h == 6 || d->h == 8 || d->h == 12 ||
                       d->h == 16;
     if (!ok || !h_ok || !d->eh_ws || !cv.fits()) {
       delete S;
-      if (!ok) return set_error(VDVC_ERR_ARG, "the precision form is a float32 solve");
-      if (!h_ok) return set_error(VDVC_ERR_UNSUPPORTED, "precision form for h=%d (h in {1,2,3,4,6,8,12,16})", d->h);
-      return set_error(VDVC_ERR_WORKSPACE, "precision form needs eh_ws of vdvc_eh_workspace_bytes bytes");
+      if (!ok) return set_error(VDVC_ERR_ARG, "the element-Hessian forms are float32 solves");
+      if (!h_ok)
+        return set_error(VDVC_ERR_UNSUPPORTED, "element Hessians for h=%d (h in {1,2,3,4,6,8,12,16})", d->h);
+      return set_error(VDVC_ERR_WORKSPACE, "element-Hessian form needs eh_ws of vdvc_gn_eh_workspace_bytes bytes");
     }
   }
   if (d->K_lap) load_K(d->K_lap, &S->Klap);
@@ -481,9 +485,9 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
     }
   for (int a = 0; a < 8; ++a)
     for (int b = 0; b < 8; ++b) S->L8[a * 8 + b] = (float)S->Klap.k[(3 * a) * 24 + 3 * b];
-  if (S->mixed && d->reg_type != VDVC_REG_NONE && !S->lap_blockdiag) {
+  if (S->eh && d->reg_type != VDVC_REG_NONE && !S->lap_blockdiag) {
     delete S;
-    return set_error(VDVC_ERR_UNSUPPORTED, "precision form needs K_lap = one 8x8 block per component");
+    return set_error(VDVC_ERR_UNSUPPORTED, "element-Hessian form needs K_lap = one 8x8 block per component");
   }
   S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 4;
   cudaStream_t s = (cudaStream_t)d->stream;
@@ -528,7 +532,7 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   }
   k_set_U<T><<<nblk(m.Ndof), 256, 0, s>>>(nullptr, m.Ndof, S->U64, S->U32);
   count_launch();
-  if (S->mixed && (e = launch_grad_bf16((const float*)d->grad, 3 * m.Nvox, S->grad_bf16, S->gmax, s))) return fail(e);
+  if (S->eh_bf16 && (e = launch_grad_bf16((const float*)d->grad, 3 * m.Nvox, S->grad_bf16, S->gmax, s))) return fail(e);
   // sync before the graph (captured on a private stream) sees the buffers
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail(set_error(VDVC_ERR_CUDA, "solver setup sync failed"));
   *out = S;
@@ -542,13 +546,21 @@ static int set_U(GnSolver<T>* S, const double* U0, cudaStream_t s) {
   return VDVC_OK;
 }
 
+// Element-Hessian formation over `mask` from the solver's gradient (float32,
+// or its BF16 rounding in the precision form).
+template <typename T>
+static EhFormArgs eh_form_args(GnSolver<T>* S, const uint8_t* mask) {
+  EhFormArgs fa{S->m, S->eh_bf16 ? S->grad_bf16 : S->d.grad, mask, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne),
+                S->eh_bf16 ? S->gmax : nullptr, &S->sc->status, S->eh_bf16 ? 0 : 1};
+  return fa;
+}
+
 // Frozen-H preconditioner (dynamic_mask == 0): diag H over mask0, built once.
 template <typename T>
 static int frozen_diag(GnSolver<T>* S, cudaStream_t s) {
   int st;
-  if (S->mixed) {
-    EhFormArgs fa{S->m, S->grad_bf16, S->d.mask0, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne), S->gmax, &S->sc->status};
-    if ((st = launch_eh_form(fa, s))) return st;
+  if (S->eh) {
+    if ((st = launch_eh_form(eh_form_args(S, S->d.mask0), s))) return st;
     S->eh_fixed = true;
   } else {
     StripArgs<T> a{};
@@ -615,17 +627,16 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
   a.status = &S->sc->status;
   a.evA = S->evA;
   a.evD = S->evD;
-  // diag H from the strip pass (plain), from the element Hessians (mixed), or
+  // diag H from the strip pass (matrix-free), from the element Hessians, or
   // not at all once it is final
   const bool with_diag = d.dynamic_mask && !S->eh_fixed;
-  if (with_diag && !S->mixed)
+  if (with_diag && !S->eh)
     st = launch_strip<T, kModeB | kModeRes | kModeDiag>(a, nullptr, s);
   else
     st = launch_strip<T, kModeB | kModeRes>(a, nullptr, s);
   if (st) return st;
-  if (with_diag && S->mixed) {
-    EhFormArgs fa{S->m, S->grad_bf16, S->frozen, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne), S->gmax, &S->sc->status};
-    if ((st = launch_eh_form(fa, s))) return st;
+  if (with_diag && S->eh) {
+    if ((st = launch_eh_form(eh_form_args(S, S->frozen), s))) return st;
     if (S->frozen_set) S->eh_fixed = true;
   }
   GridReduce red{S->partials, S->ticket};

@@ -1,6 +1,8 @@
-// Precision form of the Hessian: BF16 image gradient, element Hessians
-// formed once per Gauss-Newton iteration with FP32 accumulation, FP32
-// element-Hessian matvecs in the PCG.
+// Element-Hessian form of the Hessian: element Hessians formed once per
+// Gauss-Newton iteration with FP32 accumulation, FP32 element-Hessian
+// matvecs in the PCG.  The gradient is either the float32 gradient itself
+// (VDVC_PREC_ELEMENT: the plain solve's arithmetic in another summation
+// order) or its BF16 rounding (VDVC_PREC_MIXED, the precision form).
 //
 // Element Hessian structure.  With owner-computes quadrature (strip.cuh),
 //   K_e[(a,k),(b,l)] = sum_q w_q m_q N_a(q) N_b(q) g_k(q) g_l(q),
@@ -13,7 +15,8 @@
 // reduction over the element's voxel columns) and stored tile-major
 // [Ne / 64][162][64] (see the matvec below).
 // A BF16 x BF16 product is exact in FP32, so G carries no rounding beyond
-// the BF16 gradient itself.
+// the BF16 gradient itself; from the float32 gradient G is rounded once, as
+// the matrix-free pass rounds its products.
 #include <cuda_bf16.h>
 
 #include "ops.cuh"
@@ -38,7 +41,10 @@ __global__ void k_grad_to_bf16(const float* __restrict__ g, long long n, __nv_bf
 
 constexpr int kRP = 55;  // shared-memory pitch of a column's 54 partial sums (odd: no bank conflicts)
 
-template <int H>
+__device__ __forceinline__ float grad_comp(const __nv_bfloat16* g, long long i) { return __bfloat162float(g[i]); }
+__device__ __forceinline__ float grad_comp(const float* g, long long i) { return __ldg(g + i); }
+
+template <int H, typename GT>
 __global__ void __launch_bounds__(128) k_eh_form(const EhFormArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int EX = (H >= 128) ? 1 : 128 / H;
@@ -82,10 +88,10 @@ __global__ void __launch_bounds__(128) k_eh_form(const EhFormArgs a) {
       for (int qy = 0; qy <= H; ++qy) {
         if (qy == H && !y_last) break;
         const long long v = v0 + (long long)qy * row_stride;
-        const __nv_bfloat16* gb = (const __nv_bfloat16*)a.grad + 3 * v;
-        const float g0 = __bfloat162float(gb[0]);
-        const float g1 = __bfloat162float(gb[1]);
-        const float g2 = __bfloat162float(gb[2]);
+        const GT* gb = (const GT*)a.grad + 3 * v;
+        const float g0 = grad_comp(gb, 0);
+        const float g1 = grad_comp(gb, 1);
+        const float g2 = grad_comp(gb, 2);
         float W = a.mask[v] ? 1.f : 0.f;
         if (qy == 0) W *= wy_first;
         if (qy == H) W *= 0.5f;
@@ -149,14 +155,19 @@ static int launch_form(const EhFormArgs& args, cudaStream_t s) {
   const int threads = (EX * H + 31) / 32 * 32;
   const size_t smem = (size_t)(threads + 1) * kRP * sizeof(float);
   dim3 grid((args.m.Nx + EX - 1) / EX, args.m.Ny, args.m.Nz);
-  k_eh_form<H><<<grid, threads, smem, s>>>(args);
+  if (args.grad_f32)
+    k_eh_form<H, float><<<grid, threads, smem, s>>>(args);
+  else
+    k_eh_form<H, __nv_bfloat16><<<grid, threads, smem, s>>>(args);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
 
 int launch_eh_form(const EhFormArgs& a, cudaStream_t s) {
-  const int tc = launch_eh_form_tc(a, s);  // tcgen05 formation where it is built (h = 6, 8)
-  if (tc != VDVC_ERR_UNSUPPORTED) return tc;
+  if (!a.grad_f32) {
+    const int tc = launch_eh_form_tc(a, s);  // tcgen05 formation where it is built (h = 6, 8)
+    if (tc != VDVC_ERR_UNSUPPORTED) return tc;
+  }
   switch (a.m.h) {
     case 1: return launch_form<1>(a, s);
     case 2: return launch_form<2>(a, s);
@@ -330,6 +341,96 @@ size_t vdvc_eh_workspace_bytes(int h, int Nx, int Ny, int Nz) {
   return cv.off + 256;
 }
 
+size_t vdvc_gn_eh_workspace_bytes(int precision, int h, int Nx, int Ny, int Nz) {
+  Mesh m;
+  if (make_mesh(h, Nx, Ny, Nz, &m)) return 0;
+  if (precision != VDVC_PREC_MIXED && precision != VDVC_PREC_ELEMENT) return 0;
+  // the solver's carve order: T, gmax, [BF16 gradient]
+  Carve cv(nullptr, 0);
+  cv.take<float>((size_t)162 * eh_pitch(m.Ne));
+  cv.take<float>(4);
+  if (precision == VDVC_PREC_MIXED) cv.take<uint16_t>((size_t)3 * m.Nvox);
+  return cv.off + 256;
+}
+
+size_t vdvc_eh_bytes(int h, int Nx, int Ny, int Nz) {
+  Mesh m;
+  if (make_mesh(h, Nx, Ny, Nz, &m)) return 0;
+  return (size_t)162 * eh_pitch(m.Ne) * sizeof(float);
+}
+
+size_t vdvc_eh_op_workspace_bytes(int h, int Nx, int Ny, int Nz) {
+  Mesh m;
+  if (make_mesh(h, Nx, Ny, Nz, &m)) return 0;
+  Carve cv(nullptr, 0);
+  cv.take<float>((size_t)24 * m.Ne);
+  cv.take<int>(4);
+  cv.take<float>(4);
+  return cv.off + 256;
+}
+
+int vdvc_eh_form(const float* grad, int grad_bf16, const uint8_t* mask, int h, int Nx, int Ny, int Nz, float* T,
+                 void* ws, size_t ws_bytes, vdvc_stream_t stream) {
+  Mesh m;
+  int st = make_mesh(h, Nx, Ny, Nz, &m);
+  if (st) return st;
+  VDVC_CHECK_ARG(grad && mask && T, "null pointer");
+  VDVC_CHECK_ARG(grad_bf16 == 0 || grad_bf16 == 1, "grad_bf16 must be 0 or 1");
+  VDVC_CHECK_ARG(((uintptr_t)T & 15u) == 0, "T must be 16-byte aligned");
+  Carve cv(ws, ws_bytes);
+  float* evD = cv.take<float>((size_t)24 * m.Ne);
+  int* err = cv.take<int>(4);
+  float* gmax = cv.take<float>(4);
+  if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "eh_form needs %zu bytes of workspace", cv.off);
+  cudaStream_t s = (cudaStream_t)stream;
+  VDVC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  if (grad_bf16) VDVC_CUDA(cudaMemsetAsync(gmax, 0, sizeof(float), s));
+  // the tensor-core formation needs max |g|, which only the solver's BF16
+  // conversion records: this entry takes the CUDA-core formation
+  EhFormArgs fa{m, grad, mask, T, evD, eh_pitch(m.Ne), nullptr, err, grad_bf16 ? 0 : 1};
+  return launch_eh_form(fa, s);
+}
+
+int vdvc_eh_apply(const float* T, const float* v, int h, int Nx, int Ny, int Nz, float* out, void* ws,
+                  size_t ws_bytes, vdvc_stream_t stream) {
+  Mesh m;
+  int st = make_mesh(h, Nx, Ny, Nz, &m);
+  if (st) return st;
+  VDVC_CHECK_ARG(T && v && out, "null pointer");
+  VDVC_CHECK_ARG(((uintptr_t)T & 15u) == 0, "T must be 16-byte aligned");
+  Carve cv(ws, ws_bytes);
+  float* ev = cv.take<float>((size_t)24 * m.Ne);
+  int* err = cv.take<int>(4);
+  if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "eh_apply needs %zu bytes of workspace", cv.off);
+  cudaStream_t s = (cudaStream_t)stream;
+  EhMatvecArgs ma{};
+  ma.m = m;
+  ma.T = T;
+  ma.pitch = eh_pitch(m.Ne);
+  ma.err = err;
+  ma.v = v;
+  ma.ev = ev;
+  if ((st = launch_eh_matvec<false>(ma, s))) return st;
+  return launch_gather<float>(m, ev, out, s);
+}
+
+int vdvc_eh_status(void* ws, size_t ws_bytes, int h, int Nx, int Ny, int Nz, vdvc_stream_t stream) {
+  Mesh m;
+  int st = make_mesh(h, Nx, Ny, Nz, &m);
+  if (st) return st;
+  Carve cv(ws, ws_bytes);
+  cv.take<float>((size_t)24 * m.Ne);
+  int* err = cv.take<int>(4);
+  if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "workspace of %zu bytes expected", cv.off);
+  int h_err = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  VDVC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  VDVC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  if (h_err) return set_error(VDVC_ERR_TIMEOUT, "element-Hessian matvec: a bulk-copy wait timed out");
+  return VDVC_OK;
+}
+
 int vdvc_matvec_H_mixed(const float* v, const float* grad, const uint8_t* mask, int h, int Nx, int Ny, int Nz,
                         float* out, void* ws, size_t ws_bytes, vdvc_stream_t stream) {
   Mesh m;
@@ -348,7 +449,7 @@ int vdvc_matvec_H_mixed(const float* v, const float* grad, const uint8_t* mask, 
   cudaStream_t s = (cudaStream_t)stream;
   VDVC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   if ((st = launch_grad_bf16(grad, 3 * m.Nvox, gb, gmax, s))) return st;
-  EhFormArgs fa{m, (const __nv_bfloat16*)gb, mask, T, evD, pitch, gmax, err};
+  EhFormArgs fa{m, (const __nv_bfloat16*)gb, mask, T, evD, pitch, gmax, err, 0};
   if ((st = launch_eh_form(fa, s))) return st;
   EhMatvecArgs ma{};
   ma.m = m;

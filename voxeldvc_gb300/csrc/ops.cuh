@@ -92,13 +92,14 @@ int launch_masked_stats(const T* field, const uint8_t* mask, const Mesh& m, Grid
 constexpr int kEhTile = 64;
 struct EhFormArgs {
   Mesh m;
-  const void* grad;       // (Nvox,3) __nv_bfloat16
+  const void* grad;       // (Nvox,3) __nv_bfloat16, or float when grad_f32
   const uint8_t* mask;    // H mask
   float* T;               // [tiles][162][kEhTile]
   float* evD;             // [24][Ne] diagonal contributions
   long long pitch;        // eh_pitch(Ne): elements rounded up to whole tiles
   const float* gmax;      // max |g| of the BF16 gradient (device); the tensor-core formation's scale
   int* err;               // set to VDVC_ERR_CUDA if a tensor-core formation wait times out
+  int grad_f32;           // 1: grad is the float32 gradient itself (no BF16 rounding)
 };
 
 struct EhMatvecArgs {

@@ -282,23 +282,56 @@ class _LevelSetup:
     level's scalars."""
 
 
+# Element edges the element-Hessian kernels are built for, and the smallest
+# edge at which a float32 plain solve takes them by default.
+ELEMENT_H = frozenset((1, 2, 3, 4, 6, 8, 12, 16))
+ELEMENT_MIN_H = 6
+
+
+def _lap_blockdiag(K):
+    """K (24x24, dof 3a+c) = one 8x8 block L8 on each displacement
+    component, K[3a+c][3b+c'] = (c == c') L8[a][b], exactly."""
+    K = np.asarray(K, dtype=np.float64)
+    L8 = K[0::3, 0::3]
+    ref = np.kron(L8, np.eye(3))
+    return K.shape == (24, 24) and bool(np.array_equal(K, ref))
+
+
 def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
                  c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False, U0=None,
-                 maxiter=30, disp=True, dtype=np.float32, pcg_chunk=0, precision='plain', mixed_min_h=6):
+                 maxiter=30, disp=True, dtype=np.float32, pcg_chunk=0, precision='plain', mixed_min_h=6,
+                 hessian='auto'):
     """Level set-up of correlate_gpu (engine/correlate_gpu.py:905-1053):
     gradient, masks, reference stats, regularizer and lambda calibration,
     U0, and the solver descriptor.  Returns a _LevelSetup (ls.empty is set
-    when maxiter < 1: nothing to solve)."""
+    when maxiter < 1: nothing to solve).
+
+    hessian: how a float32 plain solve applies H in its PCG -- 'matrix_free'
+    (from the gradient every step, as kernels_dvc.matvec_H), 'element'
+    (element Hessians formed from the same float32 gradient once per GN
+    iteration: the same float32 products summed in another order) or 'auto'
+    (element Hessians at h >= ELEMENT_MIN_H, where an element's 162 stored
+    entries weigh less than its voxels' gradient and mask, 13 B x h^3)."""
     dtype = np.dtype(dtype)
     if precision not in ('plain', 'mixed'):
         raise ValueError("precision must be 'plain' or 'mixed'")
     if precision == 'mixed' and dtype != np.float32:
         raise ValueError("precision='mixed' is a float32 solve (BF16 gradient, FP32 element Hessians)")
-    # The element-Hessian form pays where an element's 162 stored entries
+    if hessian not in ('auto', 'matrix_free', 'element'):
+        raise ValueError("hessian must be 'auto', 'matrix_free' or 'element'")
+    # The element-Hessian forms pay where an element's 162 stored entries
     # weigh less than its voxels' gradient and mask (13 B x h^3): h >= 6.
     # Below that the matrix-free FP32 pass moves less data and is kept.
     if precision == 'mixed' and h < mixed_min_h:
         precision = 'plain'
+    element = False
+    if precision == 'plain' and dtype == np.float32 and h in ELEMENT_H and hessian != 'matrix_free':
+        lap_ok = l0 is None or K_ref_laplacian is None or _lap_blockdiag(K_ref_laplacian)
+        if hessian == 'element' and not lap_ok:
+            raise ValueError("hessian='element' needs K_ref_laplacian = one 8x8 block per displacement component")
+        element = lap_ok and (hessian == 'element' or h >= ELEMENT_MIN_H)
+    elif hessian == 'element':
+        raise ValueError(f"hessian='element' is a float32 plain solve with h in {sorted(ELEMENT_H)}")
 
     Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, Nz * h + 1
     Ndof = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
@@ -365,6 +398,7 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     ls = _LevelSetup()
     ls.h, ls.Nvox, ls.Ndof, ls.out_dt, ls.U64, ls.ll = h, Nvox, Ndof, out_dt, U64, ll
     ls.mean0, ls.std0, ls.precision, ls.dynamic_mask = mean0, std0, precision, bool(dynamic_mask)
+    ls.hessian = 'element' if (element or precision == 'mixed') else 'matrix_free'
     ls.empty = maxiter < 1
     if ls.empty:
         return ls
@@ -396,9 +430,9 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     nbytes = L.vdvc_gn_workspace_bytes(desc.dtype, h, Nx, Ny, Nz)
     ws = D.torch().empty(nbytes, dtype=D.torch().uint8, device=D.device())
     eh_ws = None
-    if precision == 'mixed':
-        desc.precision = 1
-        eh_bytes = L.vdvc_eh_workspace_bytes(h, Nx, Ny, Nz)
+    if precision == 'mixed' or element:
+        desc.precision = _lib.PREC_MIXED if precision == 'mixed' else _lib.PREC_ELEMENT
+        eh_bytes = L.vdvc_gn_eh_workspace_bytes(desc.precision, h, Nx, Ny, Nz)
         eh_ws = D.torch().empty(eh_bytes, dtype=D.torch().uint8, device=D.device())
         desc.eh_ws, desc.eh_ws_bytes = eh_ws.data_ptr(), eh_bytes
     ls.desc, ls.ws, ls.eh_ws, ls.nbytes = desc, ws, eh_ws, nbytes
@@ -425,11 +459,12 @@ def _norm_res(out8, std0):
 def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
                  c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False,
                  freeze_mask_after=None, U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
-                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=6):
+                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=6,
+                 hessian='auto'):
     ls = _setup_level(lv, Nx, Ny, Nz, h, g_origin=g_origin, glt=glt, l0=l0, K_ref_laplacian=K_ref_laplacian,
                       reg_exponent=reg_exponent, c_reg=c_reg, reg_type=reg_type, K_ref_elastic=K_ref_elastic,
                       eps_reg=eps_reg, dynamic_mask=dynamic_mask, U0=U0, maxiter=maxiter, disp=disp, dtype=dtype,
-                      pcg_chunk=pcg_chunk, precision=precision, mixed_min_h=mixed_min_h)
+                      pcg_chunk=pcg_chunk, precision=precision, mixed_min_h=mixed_min_h, hessian=hessian)
     out_dt, Nvox, Ndof, U64 = ls.out_dt, ls.Nvox, ls.Ndof, ls.U64
     if ls.empty:
         return U64.to(D.torch_dtype(out_dt)), D.zeros(Nvox, out_dt), D.zeros(Ndof, out_dt), {}
@@ -438,7 +473,8 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
 
     solver = C.c_void_p()
     _lib.check(L.vdvc_gn_create(C.byref(desc), ws.data_ptr(), nbytes, C.byref(solver)), "correlate_gpu")
-    info = {"gn_iters": 0, "pcg_iters": [], "pcg_status": [], "ll": ll, "h": h, "precision": precision}
+    info = {"gn_iters": 0, "pcg_iters": [], "pcg_status": [], "du": [], "ll": ll, "h": h, "precision": precision,
+            "hessian": ls.hessian}
     t_start = time.perf_counter()
     try:
         st = D.stream()
@@ -462,6 +498,7 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
             dd, uu = out8[0], out8[1]
             with np.errstate(divide='ignore', invalid='ignore'):
                 err = float(np.sqrt(np.float64(dd)) / np.sqrt(np.float64(uu)))
+            info["du"].append(err)
             if disp:
                 print(_gn_scalars_line(out8, ik, err, Nvox))
             if err < eps:

@@ -336,6 +336,56 @@ def matvec_H_mixed(v, grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz
     return D.out(out, xp)
 
 
+class ElementHessians:
+    """The operator of matvec_H held as element Hessians (the 162 distinct
+    entries of each element's 24x24 block, FP32 accumulation): formed once
+    from the float32 gradient -- or from its BF16 rounding with bf16=True --
+    and applied many times, as the GN solver's PCG does at element edges
+    >= 6.  The reference applies H matrix-free on every call
+    (engine/kernels_dvc.py:452-506); the float32 form sums the same float32
+    products in another order."""
+
+    def __init__(self, grad_f_vox, mask0_vox, h, Nx, Ny, Nz, bf16=False):
+        torch = D.torch()
+        Nvox, self.Ndof = _mesh_sizes(h, Nx, Ny, Nz)
+        self.mesh = (h, Nx, Ny, Nz)
+        L = _lib.lib()
+        nT = L.vdvc_eh_bytes(h, Nx, Ny, Nz)
+        nw = L.vdvc_eh_op_workspace_bytes(h, Nx, Ny, Nz)
+        if nT == 0 or nw == 0:
+            _lib.check(_lib.ERR_ARG, "element-Hessian size query")
+        g, m = _grad_mask(grad_f_vox, mask0_vox, np.dtype(np.float32), Nvox)
+        if bf16:
+            g = g.to(torch.bfloat16)
+        self.T = torch.empty(nT // 4, dtype=torch.float32, device=D.device())
+        self.ws = torch.zeros(nw, dtype=torch.uint8, device=D.device())
+        _lib.check(L.vdvc_eh_form(g.data_ptr(), int(bool(bf16)), m.data_ptr(), h, Nx, Ny, Nz, self.T.data_ptr(),
+                                  self.ws.data_ptr(), nw, D.stream()), "ElementHessians")
+        self._keep = g
+
+    def matvec_into(self, v, out):
+        """out = H v for float32 CUDA tensors of Ndof entries (no checks,
+        no allocation: the timing path)."""
+        h, Nx, Ny, Nz = self.mesh
+        _lib.check(_lib.lib().vdvc_eh_apply(self.T.data_ptr(), v.data_ptr(), h, Nx, Ny, Nz, out.data_ptr(),
+                                            self.ws.data_ptr(), self.ws.numel(), D.stream()), "ElementHessians")
+
+    def matvec(self, v, xp):
+        vd = D.to_device(v, np.dtype(np.float32)).reshape(-1).contiguous()
+        if vd.numel() != self.Ndof:
+            raise ValueError(f"v has {vd.numel()} entries, expected Ndof={self.Ndof}")
+        out = D.empty(self.Ndof, np.dtype(np.float32))
+        self.matvec_into(vd, out)
+        self.status()
+        return D.out(out, xp)
+
+    def status(self):
+        """Raises VdvcTimeout if a bulk-copy wait of an apply timed out."""
+        h, Nx, Ny, Nz = self.mesh
+        _lib.check(_lib.lib().vdvc_eh_status(self.ws.data_ptr(), self.ws.numel(), h, Nx, Ny, Nz, D.stream()),
+                   "ElementHessians")
+
+
 def build_diagonal_H(grad_f_vox, mask0_vox, N_stencil, w_stencil, h, Nx, Ny, Nz, Ndof, xp, chunk_size=None):
     """diag(H)[i] = sum over (e,q) touching dof i of w_q m_q v_eq[i]^2.
     Reference: engine/kernels_dvc.py:509-543."""
