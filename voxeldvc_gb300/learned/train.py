@@ -117,7 +117,12 @@ def validate(net, maker, n_pairs=16):
     return float(np.mean(err)), float(np.mean(mag))
 
 
-def train(pairs=20000, batch=4, lr=1e-3, seed=0, log_every=100, out=WEIGHTS_PATH, log=print):
+def train(pairs=20000, batch=4, lr=3e-4, seed=0, log_every=100, out=WEIGHTS_PATH, log=print, clip=1.0):
+    """Adam over `pairs` on-the-fly pairs in batches of `batch`: linear
+    warm-up over the first thirtieth of the steps, then a cosine decay; the
+    batch gradient is clipped to an L2 norm of `clip` (fields of up to ~40
+    vx make single batches' gradients vary by orders of magnitude, and
+    without the clip the network settles on predicting zero)."""
     torch = D.torch()
     net = SeedNet(seed=seed)
     maker = PairMaker()
@@ -134,6 +139,9 @@ def train(pairs=20000, batch=4, lr=1e-3, seed=0, log_every=100, out=WEIGHTS_PATH
             net.forward(G)
             loss = net.loss(G, target, scale=1.0 / batch)
             net.backward(G, accumulate=bi > 0)
+        if clip:
+            gn = torch.linalg.vector_norm(net.grad)
+            net.grad.mul_(torch.clamp(clip / (gn + 1e-12), max=1.0))
         net.adam(max(lr_t, lr * 1e-3))
         if step % log_every == 0 or step == steps:
             _lib.check(_lib.lib().vdvc_cnn_status(D.stream()), "tensor-core convolutions")
@@ -145,7 +153,7 @@ def train(pairs=20000, batch=4, lr=1e-3, seed=0, log_every=100, out=WEIGHTS_PATH
     val_rms, val_mag = validate(net, maker)
     log(f"held-out RMS error {val_rms:.3f} vx (field RMS {val_mag:.3f} vx); training {train_s:.0f} s")
     if out:
-        net.save(out, pairs=steps * batch, batch=batch, lr=lr, size=SIZE, seed=seed, train_seconds=train_s,
+        net.save(out, pairs=steps * batch, batch=batch, lr=lr, clip=clip, size=SIZE, seed=seed, train_seconds=train_s,
                  val_rms=val_rms, val_field_rms=val_mag, history=np.asarray(history, np.float64))
     return net, dict(val_rms=val_rms, val_field_rms=val_mag, train_seconds=train_s, pairs=steps * batch,
                      history=history)
@@ -155,12 +163,13 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--pairs", type=int, default=20000)
     ap.add_argument("--batch", type=int, default=4)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=3e-4)
+    ap.add_argument("--clip", type=float, default=1.0, help="L2 norm the batch gradient is clipped to (0: none)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--log-every", type=int, default=100)
     ap.add_argument("--out", default=WEIGHTS_PATH)
     a = ap.parse_args(argv)
-    _, info = train(a.pairs, a.batch, a.lr, a.seed, a.log_every, a.out)
+    _, info = train(a.pairs, a.batch, a.lr, a.seed, a.log_every, a.out, clip=a.clip)
     print(json.dumps({k: v for k, v in info.items() if k != "history"}))
 
 
