@@ -75,7 +75,7 @@ def parse(argv=None):
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="necking_512")
-    p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-layers", type=int, default=None,
                    help="element layers each CPU worker times per pyramid level (default 1)")
@@ -759,7 +759,7 @@ def gpu_arm(args):
             t0 = time.perf_counter()
             Ue, re, de = CG.multiscale_correlate_gpu(f_host, g_host, Nx, Ny, Nz, wl.h, xp=np, **kw)
             t_e2e.append(time.perf_counter() - t0)
-        e2e = {"value": round(float(np.median(t_e2e)), 4), "unit": "s",
+        e2e = {"value": round(float(np.median(t_e2e)), 4), "unit": "s", "samples_s": [round(t, 4) for t in t_e2e],
                "h2d_bytes_per_step": int(f_host.nbytes + g_host.nbytes),
                "d2h_bytes_per_step": int(Ue.nbytes + re.nbytes + de.nbytes)}
 

@@ -65,9 +65,12 @@ def test_element_form_against_golden_and_matrix_free(api, name):
     assert rms(Ue, c[key]) < RMS_TOL
     assert rms(Ue, Um) < SAME_TOL
     # the same GN path: iteration counts per level, PCG counts within one
+    # (within 5 % on the equilibrium-gap system, whose PCG runs hundreds of
+    # iterations on a stiff operator and moves with the last bits of alpha)
     assert [s["gn_iters"] for s in se] == [s["gn_iters"] for s in sm]
     for a, b in zip(se, sm):
-        assert all(abs(x - y) <= 1 for x, y in zip(a["pcg_iters"], b["pcg_iters"]))
+        assert all(abs(x - y) <= max(1, 0.05 * y) for x, y in zip(a["pcg_iters"], b["pcg_iters"])), \
+            (a["pcg_iters"], b["pcg_iters"])
 
 
 @pytest.mark.parametrize("h", [1, 2, 3, 4])

@@ -288,12 +288,18 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvTcArgs A) {
         v[c] = x;
       }
       const long long o = pr * A.ocs + A.ocoff + c0;
+      // fixed trip counts with a predicate: a data-dependent bound would
+      // index v[] at run time and move it to local memory
       if (A.out_f32) {
         float* op = (float*)A.out + o;
-        for (int c = 0; c < 16 && c0 + c < A.n_out; ++c) op[c] = v[c];
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (c0 + c < A.n_out) op[c] = v[c];
       } else {
         bf16* op = (bf16*)A.out + o;
-        for (int c = 0; c < 16 && c0 + c < A.n_out; ++c) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          if (c0 + c >= A.n_out) continue;
           float x = v[c];
           if (A.accumulate) x += __bfloat162float(op[c]);
           op[c] = __float2bfloat16_rn(x);

@@ -143,9 +143,12 @@ __global__ void __launch_bounds__(128) k_eh_form(const EhFormArgs a) {
   }
 }
 
-// kl index of the unordered component pair (k,l)
+// kl index of the unordered component pair (k,l): (0,0) 0, (0,1) 1,
+// (0,2) 2, (1,1) 3, (1,2) 4, (2,2) 5.  Not recursive, so that it folds to a
+// constant in unrolled loops (a runtime index into a register array would
+// move the array to local memory).
 __host__ __device__ constexpr int kl_index(int k, int l) {
-  return k > l ? kl_index(l, k) : (k == 0 ? l : (k == 1 ? 2 + l : 5));
+  return k <= l ? (k == 0 ? l : (k == 1 ? 2 + l : 5)) : (l == 0 ? k : (l == 1 ? 2 + k : 5));
 }
 
 
@@ -286,7 +289,8 @@ __global__ void __launch_bounds__(kTile) k_eh_matvec_tma(const EhMatvecArgs a) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) vl[3 * b + c] = a.w[3 * node + c];
       }
-#pragma unroll 4
+      // fully unrolled: a runtime row index would put out[] in local memory
+#pragma unroll
       for (int r = 0; r < 24; ++r) {
         float s2 = 0.f;
 #pragma unroll
