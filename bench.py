@@ -50,10 +50,10 @@ METRIC = "512³ h=8 DVC time to 0.02vx RMS, plain vs mixed/learned; matvec GB/s"
 # ncu dram__bytes_read + write on the 257^3 case.
 TRAFFIC_B_PER_VOXEL = 14.04
 
-# DRAM bytes per element of one element-Hessian apply (k_eh_matvec_tma +
-# k_gather), ncu dram__bytes_read + write on the 257^3 case; None until
-# captured.
-TRAFFIC_B_PER_ELEMENT_EH = None
+# DRAM bytes per element of one element-Hessian apply, ncu dram__bytes_read
+# + write of k_eh_matvec_tma on the 513^3 case itself (the gather's element-
+# vector reads hit L2).
+TRAFFIC_B_PER_ELEMENT_EH = 709.8
 
 # Operation counts (per pyramid level, coarse to fine: GN iterations, total
 # PCG iterations) that the reference arm multiplies its measured operation
@@ -735,8 +735,8 @@ def gpu_arm(args):
                 "achieved": round(eh_ach, 1), "peak": peak, "peak_source": peak_source, "unit": "GB/s",
                 "frac": round(eh_ach / peak, 4),
                 "traffic": int(TRAFFIC_B_PER_ELEMENT_EH * ne) if TRAFFIC_B_PER_ELEMENT_EH else None,
-                "traffic_source": (f"ncu dram bytes of the 257^3 case ({TRAFFIC_B_PER_ELEMENT_EH} B per element) "
-                                   f"scaled to this launch's {ne} elements") if TRAFFIC_B_PER_ELEMENT_EH else
+                "traffic_source": (f"ncu dram bytes of k_eh_matvec_tma on the 513^3 case ({TRAFFIC_B_PER_ELEMENT_EH} "
+                                   f"B per element) times this launch's {ne} elements") if TRAFFIC_B_PER_ELEMENT_EH else
                 "not captured",
                 "algorithmic_bytes": int(eh_bytes), "ms": round(eh_ms, 4),
                 "formation": "once per GN iteration until the b mask freezes (k_eh_form, not in this figure)"}
