@@ -603,7 +603,9 @@ def compare_batch():
            for i, p in enumerate(problems)]
     res.update(problems=len(problems), hs=[p["h"] for p in problems],
                meshes=[list(p["mesh"]) for p in problems], speedup=round(res["sequential_s"] / res["batch_s"], 3),
-               rms_vs_true_field_vx_max=round(max(rms), 5), schedule=[s["schedule"] for s in st])
+               rms_vs_true_field_vx_max=round(max(rms), 5), schedule=[s["schedule"] for s in st],
+               level_setup_s=[round(s["setup_s"], 4) for s in st], level_gn_wall_s=[round(s["gn_wall_s"], 4) for s in st],
+               level_gn_iters_max=[max(s["gn_iters"]) for s in st])
     return res
 
 
@@ -889,6 +891,7 @@ def learned_only(args):
     err = (U.double().cpu().numpy() - wl.true_U()).reshape(-1, 3)
     print(json.dumps({"learned_mixed_s": round(float(np.median(ts)), 4), "workload": wl.name,
                       "gn_iters": [s["gn_iters"] for s in gn], "pcg_iters": [s["pcg_iters"] for s in gn],
+                      "du": [[float(f"{d:.3e}") for d in s["du"]] for s in gn], "seed": st[-1].get("seed"),
                       "rms_vs_true_field_vx": round(float(np.sqrt(np.mean(err ** 2))), 5)}))
 
 

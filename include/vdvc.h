@@ -76,6 +76,13 @@ const char* vdvc_last_error(void);
 /* Number of kernels this library has enqueued since load (graph nodes
    count once per replay). */
 long long vdvc_launch_count(void);
+/* 1 when kernels on `device` read ordinary (pageable, not registered) host
+   memory in place through the host's page tables --
+   cudaDevAttrPageableMemoryAccess and ...UsesHostPageTables, e.g. a Grace
+   host over NVLink-C2C -- else 0.  Where it is 1,
+   vdvc_pix_to_vox accepts a host pointer as `pix` (the transpose then reads
+   the host array itself instead of a staged device copy). */
+int vdvc_device_reads_pageable(int device);
 
 /* ---- scratch size query -------------------------------------------- */
 /* Bytes of scratch that any single operator call below needs for this mesh

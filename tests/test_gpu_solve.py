@@ -102,6 +102,23 @@ def test_device_arrays_in_and_out(api, cuda):
     assert rms(U.cpu().numpy(), c["U"]) < RMS_TOL
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.uint16, np.uint8])
+def test_host_array_layout(api, cuda, dtype):
+    """pix_to_vox of a host array large enough for the in-place read (where
+    the device reads pageable host memory) against the same array staged as
+    a device tensor: identical vox layout and values."""
+    torch = cuda
+    CG, G = api
+    rng = np.random.default_rng(5)
+    a = (rng.random((97, 83, 71)) * 200).astype(dtype)
+    assert a.nbytes >= CG._DIRECT_MIN_BYTES or dtype == np.uint8
+    v_host, s_host = CG.pix_to_vox(a, np.float32)
+    v_dev, s_dev = CG.pix_to_vox(torch.from_numpy(a.astype(np.float64)).cuda(), np.float32)
+    assert s_host == s_dev == a.shape
+    assert torch.equal(v_host, v_dev)
+    assert np.array_equal(v_host.cpu().numpy(), a.transpose(2, 1, 0).reshape(-1).astype(np.float32))
+
+
 def test_error_paths(api):
     CG, G = api
     c = load_golden("solve_sinusoid.npz")

@@ -59,6 +59,7 @@ SIGNATURES = {
     "vdvc_selftest_bounded_wait": (ci, [ci, C.c_longlong, vp]),
     "vdvc_matvec_H_mixed": (ci, [vp, vp, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_eh_workspace_bytes": (cz, [ci, ci, ci, ci]),
+    "vdvc_device_reads_pageable": (ci, [ci]),
     "vdvc_gn_eh_workspace_bytes": (cz, [ci, ci, ci, ci, ci]),
     "vdvc_eh_bytes": (cz, [ci, ci, ci, ci]),
     "vdvc_eh_op_workspace_bytes": (cz, [ci, ci, ci, ci]),

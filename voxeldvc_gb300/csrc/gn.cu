@@ -778,8 +778,15 @@ static void destroy(GnSolver<T>* S) {
 // every problem as parallel branches and a continue kernel that keeps the
 // loop going while any problem's PCG state is not done (a problem that
 // converged skips its kernels).  One host synchronisation per GN iteration
-// reads every problem's scalars.  The graph is rebuilt only when the set of
-// active problems changes.
+// reads every problem's scalars.  The graph holds every problem of the
+// batch and is built once per schedule: a problem that left the lockstep
+// keeps its PCG state at done, so its captured kernels return at once
+// (rebuilding the graph whenever a problem converged cost a capture and an
+// instantiation per convergence, more than the early returns).
+
+__global__ void k_pcg_mark_done(PcgState* st) {
+  if (threadIdx.x == 0) st->done = 1;
+}
 
 __global__ void k_batch_continue(cudaGraphConditionalHandle h, PcgState* const* states, int n) {
   if (threadIdx.x == 0) {
@@ -879,7 +886,13 @@ static int batch_iterate(GnBatch* B, const int* active_in, const int* freeze_now
   for (int i = 0; i < B->n; ++i) n_active += (active[i] = active_in[i] ? 1 : 0);
   if (n_active == 0) return VDVC_OK;
   int st;
-  if (max_iter > 0 && (!B->exec || active != B->graph_active) && (st = batch_build_graph(B, active))) return st;
+  if (max_iter > 0 && !B->exec && (st = batch_build_graph(B, std::vector<char>(B->n, 1)))) return st;
+  // problems outside the lockstep: their captured PCG kernels must return at once
+  for (int i = 0; i < B->n; ++i)
+    if (!active[i]) {
+      k_pcg_mark_done<<<1, 32, 0, s>>>(B->S[i]->pcg);
+      VDVC_LAUNCHED();
+    }
   // sampling, residual, b, diag and the PCG start of every active problem
   VDVC_CUDA(cudaEventRecord(B->fork_ev, s));
   for (int i = 0; i < B->n; ++i) {

@@ -88,4 +88,16 @@ const char* vdvc_last_error(void) { return vdvc::g_last_error; }
 
 long long vdvc_launch_count(void) { return vdvc::g_launches.load(); }
 
+int vdvc_device_reads_pageable(int device) {
+  // pageable access through the host's own page tables (address translation
+  // services): the device reads host pages in place, without migrating them
+  int pageable = 0, host_tables = 0;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return (pageable && host_tables) ? 1 : 0;
+}
+
 }  // extern "C"

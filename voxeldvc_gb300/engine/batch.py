@@ -57,8 +57,9 @@ def batch_multiscale_correlate_gpu(f_pix, g_pixs, problems, xp, scales=(2, 1, 0)
     if len(g_pixs) != len(problems):
         raise ValueError("one deformed image per problem")
     dtype = np.dtype(np.float32)
-    f_full, fshape = CG.pix_to_vox(f_pix, dtype)
-    del f_full
+    fshape = tuple(int(v) for v in f_pix.shape)
+    if len(fshape) != 3:
+        raise ValueError(f"expected a 3-D reference volume, got shape {fshape}")
     specs = [_check_problem(p, fshape) for p in problems]
     scales = sorted(set(scales), reverse=True)
     for h, mesh, origin, size in specs:
@@ -71,13 +72,17 @@ def batch_multiscale_correlate_gpu(f_pix, g_pixs, problems, xp, scales=(2, 1, 0)
     dU = [None] * n
     L = _lib.lib()
     level_info = []
+    # each problem's ROI of f and of its g in vox layout, once for all levels
+    t_setup = time.perf_counter()
+    rois = [(CG.pix_to_vox(_crop(f_pix, origin, size), dtype), CG.pix_to_vox(_crop(g_pixs[i], origin, size), dtype))
+            for i, (h, mesh, origin, size) in enumerate(specs)]
+    t_layout = time.perf_counter() - t_setup
     for iscale in scales:
         s = 2 ** iscale
         setups = []
         t_setup = time.perf_counter()
         for i, (h, mesh, origin, size) in enumerate(specs):
-            f_c, fs = CG.pix_to_vox(_crop(f_pix, origin, size), dtype)
-            g_c, gs = CG.pix_to_vox(_crop(g_pixs[i], origin, size), dtype)
+            (f_c, fs), (g_c, gs) = rois[i]
             f_i, fs_i = CG._decimate(f_c, fs, s, dtype)
             g_i, gs_i = CG._decimate(g_c, gs, s, dtype)
             h_i = h // s
@@ -98,7 +103,7 @@ def batch_multiscale_correlate_gpu(f_pix, g_pixs, problems, xp, scales=(2, 1, 0)
         t_setup = time.perf_counter() - t_setup
         info = _solve_batch(L, setups, specs, dynamic_mask, freeze_mask_after, maxiter, eps, pcg_tol, pcg_max_iter,
                             tune, pcg_chunk, concurrent, disp)
-        info.update(scale=iscale, setup_s=t_setup)
+        info.update(scale=iscale, setup_s=t_setup, layout_s=t_layout if iscale == scales[0] else 0.0)
         level_info.append(info)
         for i, ls in enumerate(setups):
             U[i], res[i], dU[i] = ls.result

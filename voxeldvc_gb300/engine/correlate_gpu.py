@@ -53,9 +53,35 @@ def _pix_code_and_tensor(pix):
     return raw, D.code_of(a.dtype), shape
 
 
+# Host arrays at least this large are read by the transpose kernel in place
+# where the device reads pageable host memory (no staged copy).
+_DIRECT_MIN_BYTES = 1 << 20
+_direct = {}
+
+
+def _host_direct():
+    dev = D.torch().cuda.current_device()
+    if dev not in _direct:
+        _direct[dev] = bool(_lib.lib().vdvc_device_reads_pageable(dev))
+    return _direct[dev]
+
+
 def pix_to_vox(pix, dtype=np.float32):
     """Device copy of pix[x,y,z] in vox layout (x fastest), cast to dtype.
-    Returns (tensor (Nvox,), shape)."""
+    Returns (tensor (Nvox,), shape).  A large host array is read in place by
+    the transpose kernel where the device reads pageable host memory
+    (vdvc_device_reads_pageable), else staged through a device copy."""
+    if not D.is_tensor(pix):
+        a = np.asarray(pix)
+        if (a.ndim == 3 and a.nbytes >= _DIRECT_MIN_BYTES and a.flags.c_contiguous and
+                a.dtype in (np.float32, np.float64, np.uint8, np.uint16, np.int16, np.int32) and _host_direct()):
+            nx, ny, nz = a.shape
+            out = D.empty(nx * ny * nz, dtype)
+            _lib.check(_lib.lib().vdvc_pix_to_vox(a.ctypes.data, D.code_of(a.dtype), nx, ny, nz, out.data_ptr(),
+                                                  D.code_of(dtype), D.stream()), "pix_to_vox")
+            # the kernel reads `a`: finish before the caller may free or change it
+            D.torch().cuda.current_stream().synchronize()
+            return out, (nx, ny, nz)
     t, code, shape = _pix_code_and_tensor(pix)
     if len(shape) != 3:
         raise ValueError(f"expected a 3-D volume, got shape {shape}")
