@@ -105,6 +105,12 @@ int vdvc_cnn_upsample2_bwd(const void* dfine, int f_cstride, int fcoff,
 int vdvc_cnn_pool_input(const float* f_vox, const float* g_vox, int nx,
                         int ny, int nz, const double* mean_std, void* out,
                         vdvc_stream_t stream);
+/* The same of the pair mirrored along the axes of `flip` (bit 0 x, 1 y,
+   2 z): the input of a mirrored network pass (test-time averaging). */
+int vdvc_cnn_pool_input_mirrored(const float* f_vox, const float* g_vox,
+                                 int nx, int ny, int nz,
+                                 const double* mean_std, int flip, void* out,
+                                 vdvc_stream_t stream);
 
 /* Mean squared error of pred (FP32, channels [0,3) of stride pred_cstride)
    against target (FP32 [npos][3]); *loss (device double) = mean; dpred
@@ -134,6 +140,14 @@ int vdvc_cnn_pack_weights(const float* w, int n_out, int cin, void* wf,
 int vdvc_cnn_seed_nodes(const float* pred, int pred_cstride, int px, int py,
                         int pz, int h, int Nx, int Ny, int Nz, double* U,
                         vdvc_stream_t stream);
+/* The same with U = (accumulate ? U : 0) + weight * sample, where pred is
+   the output of the pass mirrored along the axes of `flip`: read at the
+   mirrored positions, the mirrored components negated.  Mirroring an axis
+   needs the mesh to span the output grid along it, (p - 1) * 8 = N h. */
+int vdvc_cnn_seed_nodes_acc(const float* pred, int pred_cstride, int px,
+                            int py, int pz, int h, int Nx, int Ny, int Nz,
+                            int flip, double weight, int accumulate,
+                            double* U, vdvc_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -206,6 +206,58 @@ def test_pool_input_mse_adam_seed(env):
     assert np.allclose(U.cpu().numpy(), ref, atol=1e-5)
 
 
+def test_mirrored_pool_and_seed(env):
+    """The mirrored input pooling equals the pooling of the mirrored images,
+    and a mirrored pass's output accumulated into the seed equals the
+    unmirrored field it stands for (averaging two equal predictions gives
+    the prediction back)."""
+    torch, L, S = env
+    lib = L.lib()
+    rng = np.random.default_rng(4)
+    nx, ny, nz = 17, 13, 9
+    f = rng.random((nz, ny, nx)).astype(np.float32)
+    g = rng.random((nz, ny, nx)).astype(np.float32)
+    ms = np.array([0.4, 0.3, 0.6, 0.2])
+    gx, gy, gz = (nx - 1) // 4 + 1, (ny - 1) // 4 + 1, (nz - 1) // 4 + 1
+    fd, gd = torch.from_numpy(f.reshape(-1)).cuda(), torch.from_numpy(g.reshape(-1)).cuda()
+    for flip in (1, 2, 3, 5, 7):
+        axes = tuple(2 - k for k in range(3) if (flip >> k) & 1)  # numpy axes of x, y, z in (z, y, x)
+        fm = torch.from_numpy(np.ascontiguousarray(np.flip(f, axes)).reshape(-1)).cuda()
+        gm = torch.from_numpy(np.ascontiguousarray(np.flip(g, axes)).reshape(-1)).cuda()
+        a = torch.zeros(gx * gy * gz * 2, dtype=torch.bfloat16, device="cuda")
+        b = torch.zeros_like(a)
+        L.check(lib.vdvc_cnn_pool_input_mirrored(fd.data_ptr(), gd.data_ptr(), nx, ny, nz, ms.ctypes.data_as(L.pd),
+                                                 flip, a.data_ptr(), stream(torch)))
+        L.check(lib.vdvc_cnn_pool_input(fm.data_ptr(), gm.data_ptr(), nx, ny, nz, ms.ctypes.data_as(L.pd),
+                                        b.data_ptr(), stream(torch)))
+        assert torch.equal(a, b), flip
+    # seed: pred0 on the output grid of a 33 x 25 x 17 volume meshed at h = 4
+    px, py, pz = 5, 4, 3
+    h, Nx, Ny, Nz = 4, 8, 6, 4
+    pr = rng.standard_normal((pz, py, px, 8)).astype(np.float32)
+    n = 3 * (Nx + 1) * (Ny + 1) * (Nz + 1)
+    U1 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    U2 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    p0 = torch.from_numpy(pr.reshape(-1)).cuda()
+    L.check(lib.vdvc_cnn_seed_nodes(p0.data_ptr(), 8, px, py, pz, h, Nx, Ny, Nz, U1.data_ptr(), stream(torch)))
+    for flip in (1, 2, 3, 4, 7):
+        axes = tuple(2 - k for k in range(3) if (flip >> k) & 1)
+        pm = np.flip(pr, axes).copy()
+        for k in range(3):
+            if (flip >> k) & 1:
+                pm[..., k] = -pm[..., k]
+        pmd = torch.from_numpy(pm.reshape(-1)).cuda()
+        L.check(lib.vdvc_cnn_seed_nodes_acc(p0.data_ptr(), 8, px, py, pz, h, Nx, Ny, Nz, 0, 0.5, 0, U2.data_ptr(),
+                                            stream(torch)))
+        L.check(lib.vdvc_cnn_seed_nodes_acc(pmd.data_ptr(), 8, px, py, pz, h, Nx, Ny, Nz, flip, 0.5, 1,
+                                            U2.data_ptr(), stream(torch)))
+        assert torch.allclose(U1, U2, atol=1e-6), flip
+    # a mesh that does not span the output grid cannot be mirrored
+    with pytest.raises(Exception):
+        L.check(lib.vdvc_cnn_seed_nodes_acc(p0.data_ptr(), 8, px, py, pz, h, Nx - 1, Ny, Nz, 1, 1.0, 0,
+                                            U2.data_ptr(), stream(torch)))
+
+
 def test_network_forward_and_gradients(env):
     """The whole network on the GPU vs the oracle with BF16 emulation."""
     torch, L, S = env

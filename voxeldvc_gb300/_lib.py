@@ -134,10 +134,12 @@ SIGNATURES = {
     "vdvc_cnn_upsample2": (ci, [vp, ci, ci, ci, ci, ci, vp, ci, ci, ci, ci, ci, ci, vp]),
     "vdvc_cnn_upsample2_bwd": (ci, [vp, ci, ci, ci, ci, ci, vp, ci, ci, ci, ci, ci, ci, vp]),
     "vdvc_cnn_pool_input": (ci, [vp, vp, ci, ci, ci, pd, vp, vp]),
+    "vdvc_cnn_pool_input_mirrored": (ci, [vp, vp, ci, ci, ci, pd, ci, vp, vp]),
     "vdvc_cnn_mse": (ci, [vp, ci, vp, C.c_longlong, vp, vp, ci, cd, vp, cz, vp]),
     "vdvc_cnn_adam": (ci, [vp, vp, vp, vp, C.c_longlong, cd, cd, cd, cd, ci, vp]),
     "vdvc_cnn_pack_weights": (ci, [vp, ci, ci, vp, vp, vp]),
     "vdvc_cnn_seed_nodes": (ci, [vp, ci, ci, ci, ci, ci, ci, ci, ci, vp, vp]),
+    "vdvc_cnn_seed_nodes_acc": (ci, [vp, ci, ci, ci, ci, ci, ci, ci, ci, ci, cd, ci, vp, vp]),
 }
 
 

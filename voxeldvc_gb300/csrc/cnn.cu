@@ -393,8 +393,10 @@ __global__ void k_upsample2_bwd(const bf16* __restrict__ df, int fcs, int fcoff,
   }
 }
 
+// flip (bit 0 x, 1 y, 2 z): pool the image mirrored along those axes.
 __global__ void k_pool_input(const float* __restrict__ f, const float* __restrict__ gimg, int nx, int ny, int nz,
-                             int gx, int gy, int gz, float mf, float isf, float mg, float isg, bf16* __restrict__ out) {
+                             int gx, int gy, int gz, float mf, float isf, float mg, float isg, int flip,
+                             bf16* __restrict__ out) {
   const long long n = (long long)gx * gy * gz;
   const float tw[5] = {1.f, 2.f, 2.f, 2.f, 1.f};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -409,13 +411,15 @@ __global__ void k_pool_input(const float* __restrict__ f, const float* __restric
         const int vy = 4 * y + dyy;
         if (vy < 0 || vy >= ny) continue;
         const float wzy = tw[dz + 2] * tw[dyy + 2];
-        const long long row = ((long long)vz * ny + vy) * nx;
+        const int sz = (flip & 4) ? nz - 1 - vz : vz, sy = (flip & 2) ? ny - 1 - vy : vy;
+        const long long row = ((long long)sz * ny + sy) * nx;
         for (int dx = -2; dx <= 2; ++dx) {
           const int vx = 4 * x + dx;
           if (vx < 0 || vx >= nx) continue;
+          const int sx = (flip & 1) ? nx - 1 - vx : vx;
           const float wgt = wzy * tw[dx + 2];
-          sf += wgt * f[row + vx];
-          sg += wgt * gimg[row + vx];
+          sf += wgt * f[row + sx];
+          sg += wgt * gimg[row + sx];
           sw += wgt;
         }
       }
@@ -486,15 +490,20 @@ __global__ void k_pack(const float* __restrict__ w, int n_out, int cin, int npad
   }
 }
 
+// flip (bit 0 x, 1 y, 2 z): pred is the network's output for the pair
+// mirrored along those axes; it is read at the mirrored positions with the
+// mirrored components negated.  U = (accumulate ? U : 0) + weight * sample.
 __global__ void k_seed_nodes(const float* __restrict__ pred, int pcs, int px, int py, int pz, int h, int Nnx, int Nny,
-                             int Nnz, double* __restrict__ U) {
+                             int Nnz, int flip, double weight, int accumulate, double* __restrict__ U) {
   const long long n = (long long)Nnx * Nny * Nnz;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int ni = (int)(i % Nnx);
     const long long rr = i / Nnx;
     const int nj = (int)(rr % Nny), nk = (int)(rr / Nny);
-    const double c[3] = {ni * (double)h / 8.0, nj * (double)h / 8.0, nk * (double)h / 8.0};
     const int dims[3] = {px, py, pz};
+    double c[3] = {ni * (double)h / 8.0, nj * (double)h / 8.0, nk * (double)h / 8.0};
+    for (int k = 0; k < 3; ++k)
+      if (flip & (1 << k)) c[k] = (double)(dims[k] - 1) - c[k];
     int lo[3], hi[3];
     double t[3];
     for (int k = 0; k < 3; ++k) {
@@ -510,7 +519,8 @@ __global__ void k_seed_nodes(const float* __restrict__ pred, int pcs, int px, in
         const double wgt = ((a & 1) ? t[0] : 1.0 - t[0]) * ((a & 2) ? t[1] : 1.0 - t[1]) * ((a & 4) ? t[2] : 1.0 - t[2]);
         if (wgt != 0.0) v += wgt * (double)pred[(((long long)Z * py + Y) * px + X) * pcs + ch];
       }
-      U[3 * i + ch] = v;
+      if (flip & (1 << ch)) v = -v;
+      U[3 * i + ch] = (accumulate ? U[3 * i + ch] : 0.0) + weight * v;
     }
   }
 }
@@ -732,13 +742,19 @@ int vdvc_cnn_upsample2_bwd(const void* dfine, int f_cstride, int fcoff, int nx, 
 
 int vdvc_cnn_pool_input(const float* f_vox, const float* g_vox, int nx, int ny, int nz, const double* mean_std,
                         void* out, vdvc_stream_t stream) {
+  return vdvc_cnn_pool_input_mirrored(f_vox, g_vox, nx, ny, nz, mean_std, 0, out, stream);
+}
+
+int vdvc_cnn_pool_input_mirrored(const float* f_vox, const float* g_vox, int nx, int ny, int nz,
+                                 const double* mean_std, int flip, void* out, vdvc_stream_t stream) {
   VDVC_CHECK_ARG(f_vox && g_vox && out && mean_std && nx >= 1 && ny >= 1 && nz >= 1, "bad arguments");
+  VDVC_CHECK_ARG(flip >= 0 && flip <= 7, "flip is a bit mask of the axes x (1), y (2), z (4)");
   VDVC_CHECK_ARG(mean_std[1] > 0.0 && mean_std[3] > 0.0, "image std must be positive");
   const int gx = (nx - 1) / 4 + 1, gy = (ny - 1) / 4 + 1, gz = (nz - 1) / 4 + 1;
   const long long n = (long long)gx * gy * gz;
   k_pool_input<<<eblocks(n), 256, 0, (cudaStream_t)stream>>>(f_vox, g_vox, nx, ny, nz, gx, gy, gz, (float)mean_std[0],
                                                              (float)(1.0 / mean_std[1]), (float)mean_std[2],
-                                                             (float)(1.0 / mean_std[3]), (bf16*)out);
+                                                             (float)(1.0 / mean_std[3]), flip, (bf16*)out);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
@@ -783,11 +799,21 @@ int vdvc_cnn_pack_weights(const float* w, int n_out, int cin, void* wf, void* wb
 
 int vdvc_cnn_seed_nodes(const float* pred, int pred_cstride, int px, int py, int pz, int h, int Nx, int Ny, int Nz,
                         double* U, vdvc_stream_t stream) {
+  return vdvc_cnn_seed_nodes_acc(pred, pred_cstride, px, py, pz, h, Nx, Ny, Nz, 0, 1.0, 0, U, stream);
+}
+
+int vdvc_cnn_seed_nodes_acc(const float* pred, int pred_cstride, int px, int py, int pz, int h, int Nx, int Ny,
+                            int Nz, int flip, double weight, int accumulate, double* U, vdvc_stream_t stream) {
   VDVC_CHECK_ARG(pred && U && pred_cstride >= 3 && px >= 1 && py >= 1 && pz >= 1 && h >= 1, "bad arguments");
   VDVC_CHECK_ARG(Nx >= 1 && Ny >= 1 && Nz >= 1, "bad mesh");
+  VDVC_CHECK_ARG(flip >= 0 && flip <= 7, "flip is a bit mask of the axes x (1), y (2), z (4)");
+  const int N[3] = {Nx, Ny, Nz}, P[3] = {px, py, pz};
+  for (int k = 0; k < 3; ++k)
+    VDVC_CHECK_ARG(!(flip & (1 << k)) || (long long)(P[k] - 1) * 8 == (long long)N[k] * h,
+                   "a mirrored seed needs the mesh to span the output grid along each mirrored axis");
   const long long n = (long long)(Nx + 1) * (Ny + 1) * (Nz + 1);
   k_seed_nodes<<<eblocks(n), 256, 0, (cudaStream_t)stream>>>(pred, pred_cstride, px, py, pz, h, Nx + 1, Ny + 1, Nz + 1,
-                                                             U);
+                                                             flip, weight, accumulate, U);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }

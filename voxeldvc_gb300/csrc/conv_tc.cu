@@ -38,7 +38,7 @@ typedef __nv_bfloat16 bf16;
 
 constexpr int kThreads = 128;
 constexpr int kM = 128;
-constexpr int kStages = 4;
+constexpr int kStages = 3;  // 3 stages: 8 % faster network than 4 (more CTAs per SM), same as 2 within 3 %
 constexpr uint32_t kAStage = kM * 64 * 2;  // 16 KB
 
 struct TcGeo {

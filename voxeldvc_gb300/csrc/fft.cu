@@ -7,7 +7,10 @@
 // numpy's argmax returns the first maximum in C order of pix[x,y,z]
 // (x slowest); the arg-max kernel breaks ties the same way.
 #include <cstdint>
+#include <mutex>
+#include <new>
 #include <type_traits>
+#include <vector>
 #include <cufft.h>
 
 #include "ops.cuh"
@@ -123,6 +126,119 @@ __global__ void __launch_bounds__(256) k_dot(const T* __restrict__ a, const T* _
   if (grid_reduce_sum<1>(red, mine, o, s_red) && threadIdx.x == 0) *out = o[0];
 }
 
+// cuFFT plans and work buffers of the phase correlation, cached per
+// (device, shape): creating a plan pair costs milliseconds (a workspace
+// allocation and the plan build), against well under a millisecond for the
+// transforms of a pyramid's coarsest level.  A plan is taken out of the
+// cache for the duration of a call (never shared by two calls at once) and
+// put back after the call's stream has finished with it.
+struct FftPlan {
+  int dev, sx, sy, sz;
+  cufftHandle pf, pi;
+  double *fr, *gr;
+  cufftDoubleComplex *Fc, *Gc;
+  ArgMax *partial, *result;
+  unsigned int* ticket;
+  size_t bytes;
+  unsigned long long stamp;
+};
+
+static std::mutex g_fft_mu;
+static std::vector<FftPlan*> g_fft_cache;
+static unsigned long long g_fft_clock = 0;
+constexpr size_t kFftCacheBytes = (size_t)4 << 30;
+constexpr size_t kFftCacheEntries = 32;
+
+static void fft_destroy(FftPlan* P) {
+  if (!P) return;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != P->dev) cudaSetDevice(P->dev);
+  if (P->pf) cufftDestroy(P->pf);
+  if (P->pi) cufftDestroy(P->pi);
+  cudaFree(P->fr);
+  cudaFree(P->gr);
+  cudaFree(P->Fc);
+  cudaFree(P->Gc);
+  cudaFree(P->partial);
+  cudaFree(P->result);
+  cudaFree(P->ticket);
+  if (cur != P->dev) cudaSetDevice(cur);
+  delete P;
+}
+
+static int fft_acquire(int sx, int sy, int sz, FftPlan** out) {
+  int dev = 0;
+  VDVC_CUDA(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> lk(g_fft_mu);
+    for (size_t i = 0; i < g_fft_cache.size(); ++i) {
+      FftPlan* P = g_fft_cache[i];
+      if (P->dev == dev && P->sx == sx && P->sy == sy && P->sz == sz) {
+        g_fft_cache.erase(g_fft_cache.begin() + i);
+        *out = P;
+        return VDVC_OK;
+      }
+    }
+  }
+  const long long n = (long long)sx * sy * sz;
+  const long long nc = (long long)sz * sy * (sx / 2 + 1);
+  FftPlan* P = new (std::nothrow) FftPlan{};
+  if (!P) return set_error(VDVC_ERR_ARG, "host allocation failed");
+  P->dev = dev;
+  P->sx = sx;
+  P->sy = sy;
+  P->sz = sz;
+  P->bytes = (size_t)(2 * n) * sizeof(double) + (size_t)(2 * nc) * sizeof(cufftDoubleComplex);
+  if (cudaMalloc((void**)&P->fr, n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&P->gr, n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&P->Fc, nc * sizeof(cufftDoubleComplex)) != cudaSuccess ||
+      cudaMalloc((void**)&P->Gc, nc * sizeof(cufftDoubleComplex)) != cudaSuccess ||
+      cudaMalloc((void**)&P->partial, kReduceBlocks * sizeof(ArgMax)) != cudaSuccess ||
+      cudaMalloc((void**)&P->result, sizeof(ArgMax)) != cudaSuccess ||
+      cudaMalloc((void**)&P->ticket, sizeof(unsigned int)) != cudaSuccess) {
+    cudaGetLastError();
+    fft_destroy(P);
+    return set_error(VDVC_ERR_CUDA, "fft_rigid_shift: device allocation failed");
+  }
+  if (cufftPlan3d(&P->pf, sz, sy, sx, CUFFT_D2Z) != CUFFT_SUCCESS) {
+    P->pf = 0;
+    fft_destroy(P);
+    return set_error(VDVC_ERR_CUFFT, "fft_rigid_shift: plan creation failed");
+  }
+  if (cufftPlan3d(&P->pi, sz, sy, sx, CUFFT_Z2D) != CUFFT_SUCCESS) {
+    P->pi = 0;
+    fft_destroy(P);
+    return set_error(VDVC_ERR_CUFFT, "fft_rigid_shift: plan creation failed");
+  }
+  *out = P;
+  return VDVC_OK;
+}
+
+static void fft_release(FftPlan* P, bool reuse) {
+  if (!reuse) {
+    fft_destroy(P);
+    return;
+  }
+  std::vector<FftPlan*> evicted;
+  {
+    std::lock_guard<std::mutex> lk(g_fft_mu);
+    P->stamp = ++g_fft_clock;
+    g_fft_cache.push_back(P);
+    size_t total = 0;
+    for (FftPlan* q : g_fft_cache) total += q->bytes;
+    while (g_fft_cache.size() > 1 && (total > kFftCacheBytes || g_fft_cache.size() > kFftCacheEntries)) {
+      size_t oldest = 0;
+      for (size_t i = 1; i < g_fft_cache.size(); ++i)
+        if (g_fft_cache[i]->stamp < g_fft_cache[oldest]->stamp) oldest = i;
+      total -= g_fft_cache[oldest]->bytes;
+      evicted.push_back(g_fft_cache[oldest]);
+      g_fft_cache.erase(g_fft_cache.begin() + oldest);
+    }
+  }
+  for (FftPlan* q : evicted) fft_destroy(q);
+}
+
 }  // namespace vdvc
 
 using namespace vdvc;
@@ -167,63 +283,46 @@ int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz, const voi
                          int dtype, double* d_out3, vdvc_stream_t stream) {
   VDVC_CHECK_ARG(f_vox && g_vox && d_out3, "null pointer");
   VDVC_CHECK_ARG(fnx >= 1 && fny >= 1 && fnz >= 1 && gnx >= 1 && gny >= 1 && gnz >= 1, "bad shapes");
+  VDVC_CHECK_ARG(dtype == VDVC_F32 || dtype == VDVC_F64, "dtype %d", dtype);
   const int sx = fnx < gnx ? fnx : gnx, sy = fny < gny ? fny : gny, sz = fnz < gnz ? fnz : gnz;
   const long long n = (long long)sx * sy * sz;
   const long long nc = (long long)sz * sy * (sx / 2 + 1);
   cudaStream_t s = (cudaStream_t)stream;
-  int st = VDVC_OK;
-  double *fr = nullptr, *gr = nullptr;
-  cufftDoubleComplex *Fc = nullptr, *Gc = nullptr;
-  ArgMax *partial = nullptr, *result = nullptr;
-  unsigned int* ticket = nullptr;
-  cufftHandle pf = 0, pi = 0;
-  bool have_pf = false, have_pi = false;
-  ArgMax host;
+  FftPlan* P = nullptr;
+  int st = fft_acquire(sx, sy, sz, &P);
+  if (st) return st;
   const int nb = grid_blocks(n, 256, kReduceBlocks);
-  if (cudaMallocAsync((void**)&fr, n * sizeof(double), s) != cudaSuccess ||
-      cudaMallocAsync((void**)&gr, n * sizeof(double), s) != cudaSuccess ||
-      cudaMallocAsync((void**)&Fc, nc * sizeof(cufftDoubleComplex), s) != cudaSuccess ||
-      cudaMallocAsync((void**)&Gc, nc * sizeof(cufftDoubleComplex), s) != cudaSuccess ||
-      cudaMallocAsync((void**)&partial, kReduceBlocks * sizeof(ArgMax), s) != cudaSuccess ||
-      cudaMallocAsync((void**)&result, sizeof(ArgMax), s) != cudaSuccess ||
-      cudaMallocAsync((void**)&ticket, sizeof(unsigned int), s) != cudaSuccess) {
-    st = set_error(VDVC_ERR_CUDA, "fft_rigid_shift: device allocation failed");
-    goto cleanup;
-  }
-  if (cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s) != cudaSuccess) {
-    st = set_error(VDVC_ERR_CUDA, "memset");
-    goto cleanup;
-  }
-  if (dtype == VDVC_F32) {
-    k_crop_to_f64<float><<<nb, 256, 0, s>>>((const float*)f_vox, fnx, fny, sx, sy, sz, fr);
-    k_crop_to_f64<float><<<nb, 256, 0, s>>>((const float*)g_vox, gnx, gny, sx, sy, sz, gr);
-  } else if (dtype == VDVC_F64) {
-    k_crop_to_f64<double><<<nb, 256, 0, s>>>((const double*)f_vox, fnx, fny, sx, sy, sz, fr);
-    k_crop_to_f64<double><<<nb, 256, 0, s>>>((const double*)g_vox, gnx, gny, sx, sy, sz, gr);
+  ArgMax host;
+  bool ok = cudaMemsetAsync(P->ticket, 0, sizeof(unsigned int), s) == cudaSuccess;
+  if (ok) {
+    if (dtype == VDVC_F32) {
+      k_crop_to_f64<float><<<nb, 256, 0, s>>>((const float*)f_vox, fnx, fny, sx, sy, sz, P->fr);
+      k_crop_to_f64<float><<<nb, 256, 0, s>>>((const float*)g_vox, gnx, gny, sx, sy, sz, P->gr);
+    } else {
+      k_crop_to_f64<double><<<nb, 256, 0, s>>>((const double*)f_vox, fnx, fny, sx, sy, sz, P->fr);
+      k_crop_to_f64<double><<<nb, 256, 0, s>>>((const double*)g_vox, gnx, gny, sx, sy, sz, P->gr);
+    }
+    count_launch(2);
+    ok = cufftSetStream(P->pf, s) == CUFFT_SUCCESS && cufftSetStream(P->pi, s) == CUFFT_SUCCESS &&
+         cufftExecD2Z(P->pf, P->fr, P->Fc) == CUFFT_SUCCESS && cufftExecD2Z(P->pf, P->gr, P->Gc) == CUFFT_SUCCESS;
+    if (!ok) st = set_error(VDVC_ERR_CUFFT, "fft_rigid_shift: forward transforms failed");
   } else {
-    st = set_error(VDVC_ERR_ARG, "dtype %d", dtype);
-    goto cleanup;
+    st = set_error(VDVC_ERR_CUDA, "memset");
   }
-  count_launch(2);
-  VDVC_CUFFT(cufftPlan3d(&pf, sz, sy, sx, CUFFT_D2Z));
-  have_pf = true;
-  VDVC_CUFFT(cufftPlan3d(&pi, sz, sy, sx, CUFFT_Z2D));
-  have_pi = true;
-  VDVC_CUFFT(cufftSetStream(pf, s));
-  VDVC_CUFFT(cufftSetStream(pi, s));
-  VDVC_CUFFT(cufftExecD2Z(pf, fr, Fc));
-  VDVC_CUFFT(cufftExecD2Z(pf, gr, Gc));
-  k_cross_power<<<grid_blocks(nc, 256, 152 * 16), 256, 0, s>>>(Fc, Gc, nc);
-  count_launch();
-  VDVC_CUFFT(cufftExecZ2D(pi, Fc, fr));
-  k_argmax<<<nb, 256, 0, s>>>(fr, sx, sy, sz, partial, ticket, result);
-  count_launch();
-  if (cudaMemcpyAsync(&host, result, sizeof(ArgMax), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess) {
-    st = set_error(VDVC_ERR_CUDA, "fft_rigid_shift: %s", cudaGetErrorString(cudaGetLastError()));
-    goto cleanup;
+  if (ok) {
+    k_cross_power<<<grid_blocks(nc, 256, 152 * 16), 256, 0, s>>>(P->Fc, P->Gc, nc);
+    count_launch();
+    ok = cufftExecZ2D(P->pi, P->Fc, P->fr) == CUFFT_SUCCESS;
+    if (!ok) st = set_error(VDVC_ERR_CUFFT, "fft_rigid_shift: inverse transform failed");
   }
-  {
+  if (ok) {
+    k_argmax<<<nb, 256, 0, s>>>(P->fr, sx, sy, sz, P->partial, P->ticket, P->result);
+    count_launch();
+    ok = cudaMemcpyAsync(&host, P->result, sizeof(ArgMax), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+         cudaStreamSynchronize(s) == cudaSuccess;
+    if (!ok) st = set_error(VDVC_ERR_CUDA, "fft_rigid_shift: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  if (ok) {
     // C-order index of pix[x,y,z] -> (x,y,z); wrap to (-n/2, n/2]; d = -peak
     long long c = host.cidx;
     const int pz = (int)(c % sz);
@@ -237,16 +336,9 @@ int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz, const voi
       d_out3[a] = -(double)q;
     }
   }
-cleanup:
-  if (have_pf) cufftDestroy(pf);
-  if (have_pi) cufftDestroy(pi);
-  if (fr) cudaFreeAsync(fr, s);
-  if (gr) cudaFreeAsync(gr, s);
-  if (Fc) cudaFreeAsync(Fc, s);
-  if (Gc) cudaFreeAsync(Gc, s);
-  if (partial) cudaFreeAsync(partial, s);
-  if (result) cudaFreeAsync(result, s);
-  if (ticket) cudaFreeAsync(ticket, s);
+  // the stream has finished with the plan and its buffers (synchronised
+  // above); after a failure they are dropped rather than reused
+  fft_release(P, ok);
   return st;
 }
 

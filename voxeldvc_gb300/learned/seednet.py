@@ -148,14 +148,25 @@ class SeedNet:
     _GRAD = (("dp", 1, 16), ("dd2", 1, 32), ("dcat2", 1, 128), ("dd3", 2, 64), ("dcat3", 2, 256),
              ("de4b", 3, 128), ("de4a", 3, 128), ("de3a", 2, 128), ("de2a", 1, 64), ("de1", 0, 32))
 
-    def buffers(self, G, train=True):
+    def buffers(self, G, train=True, slot=0):
         """Activation (and, with train, gradient) buffers for input grid G
-        (cached)."""
+        (cached).  Inference passes that run concurrently (the mirrored
+        passes of predict_nodes) use separate slots."""
         G = tuple(int(v) for v in G)
+        if slot:
+            key = (G, False, slot)
+            if key not in self._bufs:
+                self._bufs[key] = self._alloc(G, False)
+            return self._bufs[key]
         if (G, True) in self._bufs:
             return self._bufs[(G, True)]
         if not train and (G, False) in self._bufs:
             return self._bufs[(G, False)]
+        b = self._alloc(G, train)
+        self._bufs[(G, bool(train))] = b
+        return b
+
+    def _alloc(self, G, train):
         torch = D.torch()
         lv = grids(G)
         bf = lambda level, c: torch.zeros(_npos(lv[level]) * c, dtype=torch.bfloat16, device=D.device())
@@ -170,7 +181,6 @@ class SeedNet:
             ws = max(_lib.lib().vdvc_cnn_wgrad_workspace_bytes(l["cout"], l["cin"]) for l in LAYERS)
         b["ws"] = torch.empty(max(ws, 1 << 16), dtype=torch.uint8, device=D.device())
         b["loss"] = torch.zeros(1, dtype=torch.float64, device=D.device())
-        self._bufs[(G, bool(train))] = b
         return b
 
     # ---- forward / backward --------------------------------------------------------
@@ -186,10 +196,10 @@ class SeedNet:
         _lib.check(_lib.lib().vdvc_cnn_upsample2(src.data_ptr(), scs, scoff, *m, dst.data_ptr(), dcs, dcoff, *n, nch,
                                                  D.stream()), "upsample2")
 
-    def forward(self, G, train=True):
+    def forward(self, G, train=True, slot=0):
         """Run the network on buffers(G)['x']; returns the FP32 output
         (npos(G1) x 8, channels [0,3) used)."""
-        b = self.buffers(G, train)
+        b = self.buffers(G, train, slot)
         g0, g1, g2, g3 = b["lv"]
         self._conv("e1", b["x"], 2, 0, b["e1"], 32, 0, fwd_geom(g0, g0, 1))
         self._conv("e2a", b["e1"], 32, 0, b["e2a"], 64, 0, fwd_geom(g1, g0, 2))
@@ -295,27 +305,65 @@ class SeedNet:
 
     # ---- inputs ------------------------------------------------------------------
 
-    def set_input(self, f_vox, g_vox, shape, train=True):
-        """Pool f and g (FP32 vox-layout CUDA tensors of `shape` voxels) into
-        the input buffer; returns the input grid."""
+    def set_input(self, f_vox, g_vox, shape, train=True, flip=0, slot=0, mean_std=None):
+        """Pool f and g (FP32 vox-layout CUDA tensors of `shape` voxels),
+        mirrored along the axes of `flip` (bit 0 x, 1 y, 2 z), into the input
+        buffer; returns the input grid."""
         G = input_grid(shape)
-        b = self.buffers(G, train)
-        ms = np.array([*_mean_std(f_vox), *_mean_std(g_vox)], np.float64)
-        _lib.check(_lib.lib().vdvc_cnn_pool_input(f_vox.data_ptr(), g_vox.data_ptr(), *shape,
-                                                  ms.ctypes.data_as(_lib.pd), b["x"].data_ptr(), D.stream()),
-                   "cnn_pool_input")
+        b = self.buffers(G, train, slot)
+        ms = mean_std if mean_std is not None else np.array([*_mean_std(f_vox), *_mean_std(g_vox)], np.float64)
+        _lib.check(_lib.lib().vdvc_cnn_pool_input_mirrored(f_vox.data_ptr(), g_vox.data_ptr(), *shape,
+                                                           ms.ctypes.data_as(_lib.pd), int(flip), b["x"].data_ptr(),
+                                                           D.stream()), "cnn_pool_input")
         return G
 
-    def predict_nodes(self, f_vox, g_vox, shape, h, Nx, Ny, Nz):
+    # mirror sets of the test-time average: the pair itself, then mirrored
+    # along x, y and both (the network is not equivariant to mirroring, so
+    # the passes' errors are partly independent)
+    MIRRORS = {1: (0,), 2: (0, 1), 4: (0, 1, 2, 3)}
+
+    def mirrors_for(self, shape, h, Nx, Ny, Nz, passes):
+        """The mirror masks usable for this volume and mesh (a mirrored
+        axis needs the pooled and output grids and the mesh to be symmetric
+        under the mirror)."""
+        ok = [(s - 1) % OUT_STRIDE == 0 and N * h == s - 1 for s, N in zip(shape, (Nx, Ny, Nz))]
+        return tuple(m for m in self.MIRRORS[passes] if all(ok[k] or not (m >> k) & 1 for k in range(3)))
+
+    def predict_nodes(self, f_vox, g_vox, shape, h, Nx, Ny, Nz, passes=1):
         """Seed U (float64 CUDA tensor, 3 (Nx+1)(Ny+1)(Nz+1)) for a mesh of
-        edge h over a volume of `shape` voxels."""
-        G = self.set_input(f_vox, g_vox, shape, train=False)
-        pred = self.forward(G, train=False)
-        n = self.buffers(G, train=False)["lv"][1]
+        edge h over a volume of `shape` voxels.  passes > 1: the mean of the
+        predictions for the pair and its mirror images (1, 2 or 4 passes;
+        the mirrored passes run on side streams, concurrently with the
+        first)."""
+        torch = D.torch()
+        mirrors = self.mirrors_for(shape, h, Nx, Ny, Nz, passes)
+        ms = np.array([*_mean_std(f_vox), *_mean_std(g_vox)], np.float64)
         U = D.empty(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), np.float64)
-        _lib.check(_lib.lib().vdvc_cnn_seed_nodes(pred.data_ptr(), 8, *n, h, Nx, Ny, Nz, U.data_ptr(), D.stream()),
-                   "cnn_seed_nodes")
+        main = torch.cuda.current_stream()
+        ready = torch.cuda.Event()
+        ready.record(main)
+        preds = []
+        for k, flip in enumerate(mirrors):
+            st = main if k == 0 else self._side_stream(k)
+            with torch.cuda.stream(st):
+                st.wait_event(ready)
+                G = self.set_input(f_vox, g_vox, shape, train=False, flip=flip, slot=k, mean_std=ms)
+                preds.append((self.forward(G, train=False, slot=k), flip, st))
+        n = self.buffers(input_grid(shape), train=False)["lv"][1]
+        w = 1.0 / len(mirrors)
+        for k, (pred, flip, st) in enumerate(preds):
+            if st is not main:
+                main.wait_stream(st)
+            _lib.check(_lib.lib().vdvc_cnn_seed_nodes_acc(pred.data_ptr(), 8, *n, h, Nx, Ny, Nz, int(flip), w,
+                                                          int(k > 0), U.data_ptr(), D.stream()), "cnn_seed_nodes")
         return U
+
+    def _side_stream(self, k):
+        streams = self.__dict__.setdefault("_streams", {})
+        key = (D.torch().cuda.current_device(), k)
+        if key not in streams:
+            streams[key] = D.torch().cuda.Stream()
+        return streams[key]
 
 
 def _to_bf16_bits(a):
