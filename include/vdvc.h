@@ -396,6 +396,11 @@ int vdvc_gt_node_oob_fraction(const uint8_t* in_bounds, int nx, int ny,
 int vdvc_dot(const void* a, const void* b, int dtype, long long n,
              double* out_host, void* ws, size_t ws_bytes,
              vdvc_stream_t stream);
+/* The same into device memory (*out_dev, one double), without a
+   synchronisation: several sums can be read back at once. */
+int vdvc_dot_device(const void* a, const void* b, int dtype, long long n,
+                    double* out_dev, void* ws, size_t ws_bytes,
+                    vdvc_stream_t stream);
 
 /* Rigid voxel shift d (host, 3 doubles, pix axis order x,y,z) with
    g(x) ~= f(x - d) by phase correlation of the common corner crop
@@ -548,6 +553,12 @@ int vdvc_gn_pcg(vdvc_gn_solver* solver, int max_iter, double tol, int* iters,
    out8 = {|dU|^2, |U|^2, count, sum, sum^2 of res over the live mask,
            active voxels, b-mask weight, status}. */
 int vdvc_gn_update(vdvc_gn_solver* solver, double* out8, vdvc_stream_t stream);
+/* One whole GN iteration -- sample, rhs, pcg, update -- with a single
+   synchronisation of the stream.  out12: the 8 values of vdvc_gn_update,
+   PCG iterations, PCG relative residual, PCG status, solver status; the
+   return value is that of vdvc_gn_update (e.g. VDVC_ERR_ZERO_DIVISION). */
+int vdvc_gn_iterate(vdvc_gn_solver* solver, int freeze_now, int max_iter,
+                    double tol, double* out12, vdvc_stream_t stream);
 /* Copy a solver buffer to dst (float64 when dst_f64, else float32; masks
    as uint8). */
 int vdvc_gn_read(vdvc_gn_solver* solver, int which, void* dst, int dst_f64,

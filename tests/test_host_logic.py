@@ -156,3 +156,33 @@ def test_owner_walk_equals_reference_quadrature(h):
     assert np.all(seen == 1)
     assert np.array_equal(mults, visits)
     assert np.allclose(W_own, W_ref, rtol=0, atol=1e-14)
+
+
+def test_laplacian_block_structure_check():
+    """The element-Hessian forms take the vector Laplacian as one 8x8 block
+    per displacement component; anything else keeps the matrix-free pass."""
+    from voxeldvc_gb300.engine import correlate_gpu as CG
+    lap = G.build_K_ref_laplacian()
+    assert CG._lap_blockdiag(lap)
+    K2 = lap.copy()
+    K2[0, 1] = K2[1, 0] = 1e-3
+    assert not CG._lap_blockdiag(K2)
+    assert not CG._lap_blockdiag(G.build_K_ref(0.3))
+
+
+def test_seed_mirror_sets():
+    """Mirrored network passes only along axes where the pooled input, the
+    stride-8 output and the mesh are symmetric under the mirror."""
+    from voxeldvc_gb300.learned.seednet import SeedNet
+
+    class _N:
+        MIRRORS = SeedNet.MIRRORS
+
+    m = SeedNet.mirrors_for
+    assert m(_N(), (513, 513, 513), 8, 64, 64, 64, 2) == (0, 1)
+    assert m(_N(), (513, 513, 513), 8, 64, 64, 64, 4) == (0, 1, 2, 3)
+    assert m(_N(), (513, 513, 513), 8, 64, 64, 64, 1) == (0,)
+    # x not symmetric (mesh short of the volume): only the y mirror is left
+    assert m(_N(), (513, 513, 513), 8, 63, 64, 64, 4) == (0, 2)
+    # an odd edge that the stride-8 grid does not reach
+    assert m(_N(), (515, 513, 513), 2, 257, 256, 256, 2) == (0,)

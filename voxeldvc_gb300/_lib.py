@@ -75,6 +75,7 @@ SIGNATURES = {
     "vdvc_sample_deformed": (ci, [vp, vp, ci, ci, ci, ci, cd, cd, cd, vp, cd, ci, ci, ci, ci, vp, vp, vp]),
     "vdvc_interp_field": (ci, [vp, ci, ci, ci, ci, ci, ci, vp, vp]),
     "vdvc_dot": (ci, [vp, vp, ci, C.c_longlong, pd, vp, cz, vp]),
+    "vdvc_dot_device": (ci, [vp, vp, ci, C.c_longlong, vp, vp, cz, vp]),
     "vdvc_push_field": (ci, [vp, ci, vp, ci, ci, ci, ci, ci, cd, vp, vp]),
     "vdvc_zncc": (ci, [vp, vp, ci, vp, C.c_longlong, pd, vp, cz, vp]),
     "vdvc_cast_round": (ci, [vp, C.c_longlong, ci, vp, vp]),
@@ -104,6 +105,7 @@ SIGNATURES = {
     "vdvc_gn_rhs": (ci, [vp, vp]),
     "vdvc_gn_pcg": (ci, [vp, ci, cd, pi, pd, pi, vp]),
     "vdvc_gn_update": (ci, [vp, pd, vp]),
+    "vdvc_gn_iterate": (ci, [vp, ci, ci, cd, vp, vp]),
     "vdvc_gn_read": (ci, [vp, ci, vp, ci, vp]),
     "vdvc_gn_destroy": (None, [vp]),
     "vdvc_gn_batch_create": (ci, [vp, ci, vp, vp, ci, ci, C.POINTER(vp)]),

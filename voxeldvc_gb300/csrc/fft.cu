@@ -256,11 +256,27 @@ extern "C" {
 
 int vdvc_dot(const void* a, const void* b, int dtype, long long n, double* out_host, void* ws, size_t ws_bytes,
              vdvc_stream_t stream) {
-  VDVC_CHECK_ARG(a && out_host && n >= 1, "bad arguments");
+  VDVC_CHECK_ARG(out_host, "bad arguments");
+  Carve cv(ws, ws_bytes);
+  cv.take<double>(kReduceBlocks);
+  cv.take<unsigned int>(1);
+  double* res = cv.take<double>(1);
+  if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "dot needs %zu bytes", cv.off);
+  int st = vdvc_dot_device(a, b, dtype, n, res, ws, ws_bytes, stream);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  VDVC_CUDA(cudaMemcpyAsync(out_host, res, sizeof(double), cudaMemcpyDeviceToHost, s));
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  return VDVC_OK;
+}
+
+int vdvc_dot_device(const void* a, const void* b, int dtype, long long n, double* out_dev, void* ws, size_t ws_bytes,
+                    vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(a && out_dev && n >= 1, "bad arguments");
   Carve cv(ws, ws_bytes);
   double* partials = cv.take<double>(kReduceBlocks);
   unsigned int* ticket = cv.take<unsigned int>(1);
-  double* res = cv.take<double>(1);
+  double* res = out_dev;
   if (!ws || !cv.fits()) return set_error(VDVC_ERR_WORKSPACE, "dot needs %zu bytes", cv.off);
   cudaStream_t s = (cudaStream_t)stream;
   VDVC_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
@@ -274,8 +290,6 @@ int vdvc_dot(const void* a, const void* b, int dtype, long long n, double* out_h
   else
     return set_error(VDVC_ERR_ARG, "dtype %d", dtype);
   VDVC_LAUNCHED();
-  VDVC_CUDA(cudaMemcpyAsync(out_host, res, sizeof(double), cudaMemcpyDeviceToHost, s));
-  VDVC_CUDA(cudaStreamSynchronize(s));
   return VDVC_OK;
 }
 

@@ -651,8 +651,12 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
   return VDVC_OK;
 }
 
+// PCG from dU = 0 on the stream: the graph (or, in the eager mode, the
+// host-launched iterations) and the copy of the final state into the pinned
+// read-back slot.  *graph_ran: whether the graph ran (its launches are
+// counted once the final iteration count is known).
 template <typename T>
-static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res, int* status, cudaStream_t s) {
+static int pcg_enqueue(GnSolver<T>* S, int max_iter, double tol, cudaStream_t s, bool* graph_ran) {
   // A residual normalisation failure of the rhs pass (the reference raises
   // at engine/correlate_gpu.py:1095) leaves a non-finite b: the PCG stops on
   // it at once and vdvc_gn_update reports the rhs status, so the iteration
@@ -661,11 +665,10 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
   int st = launch_pcg_init<T>(S->b, nullptr, S->Minv, S->m.Ndof, S->r, S->z, S->p, false, S->x, S->pcg, red,
                               max_iter, tol, s);
   if (st) return st;
-  bool ran = false;
-  if (!ran && eager_pcg()) {
+  *graph_ran = false;
+  if (eager_pcg()) {
     // the same iteration kernels launched from the host, so that a profiler
     // sees each launch; the device state is read every 16 iterations
-    ran = true;
     for (int it = 0; it < max_iter; ++it) {
       if ((st = pcg_iteration<T>(S, s))) return st;
       if ((it & 15) == 15 || it == max_iter - 1) {
@@ -674,19 +677,37 @@ static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res
         if (S->h_pcg->done) break;
       }
     }
-  }
-  if (!ran) {
+  } else {
     if (!S->gexec && (st = build_graph<T>(S))) return st;
-    if (max_iter > 0) VDVC_CUDA(cudaGraphLaunch(S->gexec, s));
+    if (max_iter > 0) {
+      VDVC_CUDA(cudaGraphLaunch(S->gexec, s));
+      *graph_ran = true;
+    }
   }
   VDVC_CUDA(cudaMemcpyAsync(S->h_pcg, S->pcg, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
-  VDVC_CUDA(cudaStreamSynchronize(s));
+  return VDVC_OK;
+}
+
+// After the stream has synchronised: the final PCG state, and the graph's
+// launches counted.
+template <typename T>
+static const PcgState& pcg_finish(GnSolver<T>* S, bool graph_ran) {
   const PcgState& fin = S->h_pcg[0];
-  if (max_iter > 0 && !ran) {
+  if (graph_ran) {
     // body executions = ceil(iter / chunk); each runs chunk iterations' kernels + the continue kernel
     const long long bodies = (fin.iter + S->chunk - 1) / S->chunk;
     count_launch(bodies * ((long long)S->chunk * S->kernels_per_iter + 1));
   }
+  return fin;
+}
+
+template <typename T>
+static int pcg(GnSolver<T>* S, int max_iter, double tol, int* iters, double* res, int* status, cudaStream_t s) {
+  bool graph_ran = false;
+  int st = pcg_enqueue<T>(S, max_iter, tol, s, &graph_ran);
+  if (st) return st;
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  const PcgState& fin = pcg_finish<T>(S, graph_ran);
   if (iters) *iters = fin.iter;
   if (res) *res = fin.res;
   if (status) *status = fin.status;
@@ -719,6 +740,44 @@ static int update(GnSolver<T>* S, double* out8, cudaStream_t s) {
     out8[5] = h.gstats[3];
     out8[6] = h.gstats[0];
     out8[7] = (double)h.status;
+  }
+  if (h.status != VDVC_OK) {
+    const int code = h.status;
+    cudaMemsetAsync(&S->sc->status, 0, sizeof(int), s);
+    return set_error(code, code == VDVC_ERR_ZERO_DIVISION ? "float division by zero (std of g over the mask is 0)"
+                                                          : "solver status %d", code);
+  }
+  return VDVC_OK;
+}
+
+// One whole GN iteration with a single host synchronisation: sample, rhs,
+// PCG, update, then every scalar of the iteration at once.  out12: the 8
+// values of update(), PCG iterations, PCG relative residual, PCG status, the
+// solver status.
+template <typename T>
+static int iterate(GnSolver<T>* S, int freeze_now, int max_iter, double tol, double* out12, cudaStream_t s) {
+  int st;
+  if ((st = sample<T>(S, freeze_now, s))) return st;
+  if ((st = rhs<T>(S, s))) return st;
+  bool graph_ran = false;
+  if ((st = pcg_enqueue<T>(S, max_iter, tol, s, &graph_ran))) return st;
+  if ((st = update_enqueue<T>(S, s))) return st;
+  VDVC_CUDA(cudaStreamSynchronize(s));
+  const PcgState& fin = pcg_finish<T>(S, graph_ran);
+  const GnScalars& h = *S->h_sc;
+  if (out12) {
+    out12[0] = h.norms[0];
+    out12[1] = h.norms[1];
+    out12[2] = h.dstats[0];
+    out12[3] = h.dstats[1];
+    out12[4] = h.dstats[2];
+    out12[5] = h.gstats[3];
+    out12[6] = h.gstats[0];
+    out12[7] = (double)h.status;
+    out12[8] = (double)fin.iter;
+    out12[9] = fin.res;
+    out12[10] = (double)fin.status;
+    out12[11] = (double)h.status;
   }
   if (h.status != VDVC_OK) {
     const int code = h.status;
@@ -1046,6 +1105,12 @@ int vdvc_gn_pcg(vdvc_gn_solver* solver, int max_iter, double tol, int* iters, do
 
 int vdvc_gn_update(vdvc_gn_solver* solver, double* out8, vdvc_stream_t stream) {
   VDVC_GN_DISPATCH(update<float>(S, out8, (cudaStream_t)stream), update<double>(S, out8, (cudaStream_t)stream));
+}
+
+int vdvc_gn_iterate(vdvc_gn_solver* solver, int freeze_now, int max_iter, double tol, double* out12,
+                    vdvc_stream_t stream) {
+  VDVC_GN_DISPATCH(iterate<float>(S, freeze_now, max_iter, tol, out12, (cudaStream_t)stream),
+                   iterate<double>(S, freeze_now, max_iter, tol, out12, (cudaStream_t)stream));
 }
 
 int vdvc_gn_read(vdvc_gn_solver* solver, int which, void* dst, int dst_f64, vdvc_stream_t stream) {

@@ -98,8 +98,12 @@ def batch_multiscale_correlate_gpu(f_pix, g_pixs, problems, xp, scales=(2, 1, 0)
             l0_i = None if l0_factor is None else l0_factor * h / s
             ls = CG._setup_level(CG._Level(f_i, fs_i, g_i, gs_i), *mesh, h_i, glt=glt, l0=l0_i,
                                  K_ref_laplacian=K_ref_laplacian, dynamic_mask=dynamic_mask, U0=U0,
-                                 maxiter=maxiter, disp=disp, dtype=dtype)
+                                 maxiter=maxiter, disp=disp, dtype=dtype, defer=True)
             setups.append(ls)
+        # every problem's set-up scalars in one read-back
+        scal = D.torch().stack([ls.dsc for ls in setups]).cpu().numpy()
+        for ls, v in zip(setups, scal):
+            CG._finish_setup(ls, v)
         t_setup = time.perf_counter() - t_setup
         info = _solve_batch(L, setups, specs, dynamic_mask, freeze_mask_after, maxiter, eps, pcg_tol, pcg_max_iter,
                             tune, pcg_chunk, concurrent, disp)

@@ -152,13 +152,23 @@ def erode_mask0_vox(mask0_vox, Nvx, Nvy, Nvz, xp):
     return D.out(out.to(D.torch().bool), xp)
 
 
-def _stats_sums(field, mask, h, Nx, Ny, Nz):
+def _stats_sums(field, mask, h, Nx, Ny, Nz, out=None):
+    """count, s1, s2 of field over mask (multiplicity-weighted, float64):
+    host values, or into the device buffer `out` (3 doubles, no sync)."""
     dt = D.np_dtype_of(field)
-    sums = D.empty(3, np.float64)
+    sums = D.empty(3, np.float64) if out is None else out
     ws = D.scratch.get(1 << 16)
     _lib.check(_lib.lib().vdvc_masked_stats(field.data_ptr(), D.code_of(dt), mask.data_ptr(), h, Nx, Ny, Nz,
                                             sums.data_ptr(), ws.data_ptr(), ws.numel(), D.stream()), "masked_stats")
-    return sums.cpu().numpy()
+    return sums.cpu().numpy() if out is None else None
+
+
+def _dot_into(a, b, out):
+    """float64 sum(a*b) into the device double `out` (no sync)."""
+    dt = D.np_dtype_of(a)
+    ws = D.scratch.get(1 << 16)
+    _lib.check(_lib.lib().vdvc_dot_device(a.data_ptr(), D.ptr(b), D.code_of(dt), a.numel(), out.data_ptr(),
+                                          ws.data_ptr(), ws.numel(), D.stream()), "dot")
 
 
 def _mean_std(c, s1, s2):
@@ -302,6 +312,24 @@ def _plane_wave(Nx, Ny, Nz, h, dtype):
     return V
 
 
+# Device copies of the calibration plane wave, per (device, mesh, h, dtype):
+# built with NumPy on the host exactly as the reference builds it (a few
+# milliseconds for a 65^3-node mesh, at every pyramid level of every solve
+# without the cache).
+_PLANE_WAVES = {}
+_PLANE_WAVES_MAX = 16
+
+
+def _plane_wave_device(Nx, Ny, Nz, h, dtype):
+    key = (D.torch().cuda.current_device(), Nx, Ny, Nz, h, np.dtype(dtype).str)
+    V = _PLANE_WAVES.get(key)
+    if V is None:
+        if len(_PLANE_WAVES) >= _PLANE_WAVES_MAX:
+            _PLANE_WAVES.pop(next(iter(_PLANE_WAVES)))
+        V = _PLANE_WAVES[key] = D.to_device(_plane_wave(Nx, Ny, Nz, h, dtype))
+    return V
+
+
 class _LevelSetup:
     """Everything one GN solver of a level needs: the descriptor, its
     workspaces, the device arrays it points to (kept alive here), U0 and the
@@ -326,7 +354,7 @@ def _lap_blockdiag(K):
 def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
                  c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False, U0=None,
                  maxiter=30, disp=True, dtype=np.float32, pcg_chunk=0, precision='plain', mixed_min_h=6,
-                 hessian='auto'):
+                 hessian='auto', defer=False):
     """Level set-up of correlate_gpu (engine/correlate_gpu.py:905-1053):
     gradient, masks, reference stats, regularizer and lambda calibration,
     U0, and the solver descriptor.  Returns a _LevelSetup (ls.empty is set
@@ -337,7 +365,10 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     (element Hessians formed from the same float32 gradient once per GN
     iteration: the same float32 products summed in another order) or 'auto'
     (element Hessians at h >= ELEMENT_MIN_H, where an element's 162 stored
-    entries weigh less than its voxels' gradient and mask, 13 B x h^3)."""
+    entries weigh less than its voxels' gradient and mask, 13 B x h^3).
+
+    defer: leave the level's scalars on the device; the caller completes
+    the set-up with _finish_setup (the batch reads all problems' at once)."""
     dtype = np.dtype(dtype)
     if precision not in ('plain', 'mixed'):
         raise ValueError("precision must be 'plain' or 'mixed'")
@@ -371,8 +402,11 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
                          f"{(Nvx, Nvy, Nvz)}")
     L = _lib.lib()
     grad, mask0 = _grad_vox(lv.f_vox, lv.fshape, dtype, glt)
-    c0, s10, s20 = _stats_sums(lv.f_vox, mask0, h, Nx, Ny, Nz)
-    mean0, std0 = _mean_std(c0, s10, s20)
+    # the level's scalars are reduced into one device buffer (count, s1, s2
+    # of f over mask0; v.Hv and v.Lv of the calibration) and read back once
+    # (_finish_setup), so that a batch reads every problem's in one go
+    dsc = D.zeros(5, np.float64)
+    _stats_sums(lv.f_vox, mask0, h, Nx, Ny, Nz, out=dsc[0:3])
 
     N_stencil, w_stencil = build_N_stencil(h)
     if reg_type not in ('laplacian', 'equilibrium_gap'):
@@ -383,8 +417,9 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     if reg_type == 'equilibrium_gap':
         interior = D.to_device(build_interior_dof_mask(Nx, Ny, Nz), dtype)
 
-    ll = 0.0
     reg_code = _lib.REG_NONE
+    host_HL = None   # (H0, L0) where they are reduced on the host
+    ll_factor = 0.0
     if l0 is not None:
         if K_ref_laplacian is None:
             raise ValueError("K_ref_laplacian is required when l0 is given")
@@ -399,21 +434,15 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
             dH = K.build_diagonal_H(grad.reshape(-1, 3), mask0, N_stencil, w_stencil, h, Nx, Ny, Nz, Ndof,
                                     D.torch())
             dlap = K.build_diagonal_K_ref(K_ref_laplacian, h, Nx, Ny, Nz, Ndof, D.torch())
-            H0 = _dot(dH)
-            L0 = _dot(diag_eq) + eps_reg * _dot(dlap)
+            host_HL = (_dot(dH), _dot(diag_eq) + eps_reg * _dot(dlap))
         else:
             reg_code = _lib.REG_LAPLACIAN
-            V = D.to_device(_plane_wave(Nx, Ny, Nz, h, dtype))
+            V = _plane_wave_device(Nx, Ny, Nz, h, dtype)
             Hv = K.matvec_H(V, grad.reshape(-1, 3), mask0, N_stencil, w_stencil, h, Nx, Ny, Nz, D.torch())
             Lv = K.matvec_K_ref(V, K_ref_laplacian, h, Nx, Ny, Nz, D.torch())
-            H0 = _dot(V, Hv)
-            L0 = _dot(V, Lv)
-        ll = c_reg * (l0 / T_) ** reg_exponent * H0 / L0
-        if disp:
-            print('Regularization: %s with lambda = %2.3e' % (reg_type, ll))
-    else:
-        if disp:
-            print('Regularization: None')
+            _dot_into(V, Hv, dsc[3:4])
+            _dot_into(V, Lv, dsc[4:5])
+        ll_factor = c_reg * (l0 / T_) ** reg_exponent
 
     out_dt = np.dtype(np.float64) if (l0 is not None or dtype == np.float64) else dtype
     # U0 is read in the solve dtype (correlate_gpu.py:1037), kept as float64
@@ -422,11 +451,15 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     if U64.numel() != Ndof:
         raise ValueError(f"U0 has {U64.numel()} entries, expected {Ndof}")
     ls = _LevelSetup()
-    ls.h, ls.Nvox, ls.Ndof, ls.out_dt, ls.U64, ls.ll = h, Nvox, Ndof, out_dt, U64, ll
-    ls.mean0, ls.std0, ls.precision, ls.dynamic_mask = mean0, std0, precision, bool(dynamic_mask)
+    ls.h, ls.Nvox, ls.Ndof, ls.out_dt, ls.U64 = h, Nvox, Ndof, out_dt, U64
+    ls.precision, ls.dynamic_mask = precision, bool(dynamic_mask)
     ls.hessian = 'element' if (element or precision == 'mixed') else 'matrix_free'
     ls.empty = maxiter < 1
+    ls.dsc, ls.host_HL, ls.ll_factor, ls.reg_type, ls.regularized = dsc, host_HL, ll_factor, reg_type, l0 is not None
+    ls.disp, ls.desc = disp, None
     if ls.empty:
+        if not defer:
+            _finish_setup(ls)
         return ls
 
     Klap = np.ascontiguousarray(K_ref_laplacian if K_ref_laplacian is not None else np.zeros((24, 24)),
@@ -439,7 +472,6 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     desc.gx0, desc.gy0, desc.gz0 = (float(o) for o in g_origin)
     desc.glt = float(glt)
     desc.reg_type = reg_code
-    desc.ll = float(ll)
     desc.eps_reg = float(eps_reg)
     desc.K_lap = Klap.ctypes.data_as(_lib.pd)
     desc.K_el = Kel.ctypes.data_as(_lib.pd)
@@ -451,7 +483,6 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     desc.mask0 = mask0.data_ptr()
     desc.interior = D.ptr(interior)
     desc.diag_eqgap = D.ptr(diag_eq)
-    desc.mean0, desc.std0 = mean0, std0
     desc.stream = D.stream()
     nbytes = L.vdvc_gn_workspace_bytes(desc.dtype, h, Nx, Ny, Nz)
     ws = D.torch().empty(nbytes, dtype=D.torch().uint8, device=D.device())
@@ -464,6 +495,29 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     ls.desc, ls.ws, ls.eh_ws, ls.nbytes = desc, ws, eh_ws, nbytes
     # the descriptor holds raw pointers: keep what they point to alive
     ls.keep = (Klap, Kel, grad, mask0, interior, diag_eq, lv)
+    if not defer:
+        _finish_setup(ls)
+    return ls
+
+
+def _finish_setup(ls, host_scalars=None):
+    """The scalars of a level set-up from its device buffer (read here, or
+    passed in by a caller that read several set-ups' at once): mean0 and
+    std0 of f over mask0, the regularization weight, and the descriptor's
+    copies of them."""
+    v = ls.dsc.cpu().numpy() if host_scalars is None else host_scalars
+    ls.mean0, ls.std0 = _mean_std(v[0], v[1], v[2])
+    ls.ll = 0.0
+    if ls.regularized:
+        H0, L0 = ls.host_HL if ls.host_HL is not None else (float(v[3]), float(v[4]))
+        ls.ll = ls.ll_factor * H0 / L0
+        if ls.disp:
+            print('Regularization: %s with lambda = %2.3e' % (ls.reg_type, ls.ll))
+    elif ls.disp:
+        print('Regularization: None')
+    if ls.desc is not None:
+        ls.desc.ll = float(ls.ll)
+        ls.desc.mean0, ls.desc.std0 = ls.mean0, ls.std0
     return ls
 
 
@@ -508,19 +562,16 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
         if not dynamic_mask:
             _lib.check(L.vdvc_gn_frozen_diag(solver, st), "frozen_diag")
         frozen = False
-        out8 = (C.c_double * 8)()
-        iters, pres, pstat = C.c_int(0), C.c_double(0.0), C.c_int(0)
+        out8 = (C.c_double * 12)()
         for ik in range(maxiter):
             freeze_now = freeze_mask_after is not None and not frozen and ik >= freeze_mask_after
-            _lib.check(L.vdvc_gn_sample(solver, int(freeze_now), st), "sample")
+            # sample -> rhs -> pcg -> update, one host synchronisation
+            _lib.check(L.vdvc_gn_iterate(solver, int(freeze_now), int(pcg_max_iter), float(pcg_tol),
+                                         C.cast(out8, _lib.pd), st), "GN iteration")
             frozen = frozen or freeze_now
-            _lib.check(L.vdvc_gn_rhs(solver, st), "rhs")
-            _lib.check(L.vdvc_gn_pcg(solver, int(pcg_max_iter), float(pcg_tol), C.byref(iters), C.byref(pres),
-                                     C.byref(pstat), st), "pcg")
-            _lib.check(L.vdvc_gn_update(solver, C.cast(out8, _lib.pd), st), "update")
             info["gn_iters"] = ik + 1
-            info["pcg_iters"].append(iters.value)
-            info["pcg_status"].append(pstat.value)
+            info["pcg_iters"].append(int(out8[8]))
+            info["pcg_status"].append(int(out8[10]))
             dd, uu = out8[0], out8[1]
             with np.errstate(divide='ignore', invalid='ignore'):
                 err = float(np.sqrt(np.float64(dd)) / np.sqrt(np.float64(uu)))
