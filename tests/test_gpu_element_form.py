@@ -95,14 +95,14 @@ def test_element_form_small_h_against_oracle(api, h):
 
 
 def test_element_form_level_policy(api):
-    # 'auto' takes element Hessians at h >= 6 of a float32 plain solve only
+    # 'auto' takes element Hessians at h >= 4 of a float32 plain solve only
     CG, G = api
     c = load_golden("solve_multiscale.npz")
     kw = dict(scales=(2, 1, 0), K_ref_laplacian=G.build_K_ref_laplacian(), l0=36.0, maxiter=3, disp=False,
               fft_prealign=False)
     stats = []
     CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, stats=stats, **kw)
-    assert [(s["h"], s["hessian"]) for s in stats] == [(2, "matrix_free"), (4, "matrix_free"), (8, "element")]
+    assert [(s["h"], s["hessian"]) for s in stats] == [(2, "matrix_free"), (4, "element"), (8, "element")]
     stats = []
     CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, stats=stats, dtype=np.float64, **kw)
     assert all(s["hessian"] == "matrix_free" for s in stats)

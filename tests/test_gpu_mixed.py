@@ -184,7 +184,7 @@ def test_mixed_level_policy(solve_api):
     CG.multiscale_correlate_gpu(c["f"], c["g"], 4, 3, 2, 8, xp=np, scales=(2, 1, 0),
                                 K_ref_laplacian=G.build_K_ref_laplacian(), l0=36.0, maxiter=3, disp=False,
                                 fft_prealign=False, precision="mixed", stats=stats)
-    assert [(s["h"], s["precision"]) for s in stats] == [(2, "plain"), (4, "plain"), (8, "mixed")]
+    assert [(s["h"], s["precision"]) for s in stats] == [(2, "plain"), (4, "mixed"), (8, "mixed")]
 
 
 def test_mixed_argument_errors(solve_api):

@@ -334,9 +334,16 @@ __global__ void __launch_bounds__(256) k_elem_rhs(const StripArgs<float> a) {
 // Element edges up to this one take the thread-per-element form.
 constexpr int kElemRhsMaxH = 4;
 
+// Without the diagonal (the element-Hessian forms, whose diagonal comes
+// from the element Hessians) the thread-per-element form also serves h = 8
+// (128 registers; measured on the 513^3 learned + precision solve, 3 GN
+// rhs calls: 25.8 -> 25.3 ms).  With the diagonal its 48 register sums
+// take 216 registers; that form keeps the strip kernel.
+constexpr int kElemRhsMaxHNoDiag = 8;
+
 template <int H, bool DG>
 static int launch_rh(const StripArgs<float>& args, cudaStream_t s) {
-  if constexpr (H <= kElemRhsMaxH) {
+  if constexpr (H <= kElemRhsMaxH || (!DG && H == kElemRhsMaxHNoDiag)) {
     // at most kReduceBlocks blocks: the reduction partials hold that many
     long long nb = (args.m.Ne + 255) / 256;
     if (nb > kReduceBlocks) nb = kReduceBlocks;

@@ -337,9 +337,13 @@ class _LevelSetup:
 
 
 # Element edges the element-Hessian kernels are built for, and the smallest
-# edge at which a float32 plain solve takes them by default.
+# edge at which a float32 plain solve takes them by default: from h = 4 an
+# element's 162 stored floats (648 B) weigh less than its voxels' gradient
+# and mask (13 B x h^3 = 832 B at h = 4), and a PCG applies them ~20 times
+# per formation (513^3 benchmark, h = 4 level: 11.8 -> 8.8 ms); at h = 2 the
+# matrix-free pass reads 104 B per element from L2.
 ELEMENT_H = frozenset((1, 2, 3, 4, 6, 8, 12, 16))
-ELEMENT_MIN_H = 6
+ELEMENT_MIN_H = 4
 
 
 def _lap_blockdiag(K):
@@ -353,7 +357,7 @@ def _lap_blockdiag(K):
 
 def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
                  c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False, U0=None,
-                 maxiter=30, disp=True, dtype=np.float32, pcg_chunk=0, precision='plain', mixed_min_h=6,
+                 maxiter=30, disp=True, dtype=np.float32, pcg_chunk=0, precision='plain', mixed_min_h=4,
                  hessian='auto', defer=False):
     """Level set-up of correlate_gpu (engine/correlate_gpu.py:905-1053):
     gradient, masks, reference stats, regularizer and lambda calibration,
@@ -377,7 +381,7 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
     if hessian not in ('auto', 'matrix_free', 'element'):
         raise ValueError("hessian must be 'auto', 'matrix_free' or 'element'")
     # The element-Hessian forms pay where an element's 162 stored entries
-    # weigh less than its voxels' gradient and mask (13 B x h^3): h >= 6.
+    # weigh less than its voxels' gradient and mask (13 B x h^3): h >= 4.
     # Below that the matrix-free FP32 pass moves less data and is kept.
     if precision == 'mixed' and h < mixed_min_h:
         precision = 'plain'
@@ -539,7 +543,7 @@ def _norm_res(out8, std0):
 def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_laplacian=None, reg_exponent=2,
                  c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False,
                  freeze_mask_after=None, U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
-                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=6,
+                 disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=4,
                  hessian='auto'):
     ls = _setup_level(lv, Nx, Ny, Nz, h, g_origin=g_origin, glt=glt, l0=l0, K_ref_laplacian=K_ref_laplacian,
                       reg_exponent=reg_exponent, c_reg=c_reg, reg_type=reg_type, K_ref_elastic=K_ref_elastic,
