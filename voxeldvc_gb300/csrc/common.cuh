@@ -21,6 +21,17 @@ void count_launch(long long n = 1);
 // VDVC_ERR_CUDA.
 int ensure_dyn_smem(const void* func, int bytes);
 
+// Pools of per-solver CUDA objects (lib.cu): idle non-blocking streams and
+// timing-free events of the current device, pinned host blocks of
+// kPinnedSlot bytes.  Returned streams are synchronised first.
+constexpr size_t kPinnedSlot = 4096;
+int pool_stream(cudaStream_t* out);
+void pool_stream_return(cudaStream_t s);
+int pool_event(cudaEvent_t* out);
+void pool_event_return(cudaEvent_t e);
+int pool_pinned(void** out);
+void pool_pinned_return(void* p);
+
 #define VDVC_CHECK_ARG(cond, ...)                                   \
   do {                                                              \
     if (!(cond)) return ::vdvc::set_error(VDVC_ERR_ARG, __VA_ARGS__); \

@@ -492,17 +492,21 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   S->chunk = d->pcg_chunk > 0 ? d->pcg_chunk : 4;
   cudaStream_t s = (cudaStream_t)d->stream;
   int e = VDVC_OK;
+  static_assert(2 * sizeof(PcgState) + sizeof(GnScalars) <= kPinnedSlot, "pinned read-back slot too small");
   auto fail = [&](int code) {
-    if (S->cap_stream) cudaStreamDestroy(S->cap_stream);
-    if (S->h_pcg) cudaFreeHost(S->h_pcg);
+    pool_stream_return(S->cap_stream);
+    pool_event_return(S->ev[0]);
+    pool_event_return(S->ev[1]);
+    pool_pinned_return(S->h_pcg);
     delete S;
     return code;
   };
-  if (cudaStreamCreateWithFlags(&S->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMallocHost((void**)&S->h_pcg, 2 * sizeof(PcgState) + sizeof(GnScalars)) != cudaSuccess ||
-      cudaEventCreateWithFlags(&S->ev[0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&S->ev[1], cudaEventDisableTiming) != cudaSuccess)
+  void* pin = nullptr;
+  if (pool_stream(&S->cap_stream) || pool_pinned(&pin) || pool_event(&S->ev[0]) || pool_event(&S->ev[1])) {
+    S->h_pcg = (PcgState*)pin;
     return fail(set_error(VDVC_ERR_CUDA, "solver stream/event/pinned setup failed"));
+  }
+  S->h_pcg = (PcgState*)pin;
   S->h_sc = (GnScalars*)(S->h_pcg + 2);
   // device-side constants: the fused K pair, zeroed reduction tickets, scalars
   Kpair<T> kh;
@@ -820,10 +824,10 @@ static void destroy(GnSolver<T>* S) {
   if (!S) return;
   if (S->gexec) cudaGraphExecDestroy(S->gexec);
   if (S->graph) cudaGraphDestroy(S->graph);
-  if (S->cap_stream) cudaStreamDestroy(S->cap_stream);
-  if (S->ev[0]) cudaEventDestroy(S->ev[0]);
-  if (S->ev[1]) cudaEventDestroy(S->ev[1]);
-  if (S->h_pcg) cudaFreeHost(S->h_pcg);
+  pool_stream_return(S->cap_stream);
+  pool_event_return(S->ev[0]);
+  pool_event_return(S->ev[1]);
+  pool_pinned_return(S->h_pcg);
   delete S;
 }
 
@@ -1015,10 +1019,10 @@ static void batch_destroy(GnBatch* B) {
   if (!B) return;
   batch_free_graph(B);
   for (auto* S : B->S) destroy<float>(S);
-  for (auto st : B->streams) cudaStreamDestroy(st);
-  for (auto ev : B->done_ev) cudaEventDestroy(ev);
-  if (B->fork_ev) cudaEventDestroy(B->fork_ev);
-  if (B->cap) cudaStreamDestroy(B->cap);
+  for (auto st : B->streams) pool_stream_return(st);
+  for (auto ev : B->done_ev) pool_event_return(ev);
+  pool_event_return(B->fork_ev);
+  pool_stream_return(B->cap);
   if (B->d_states) cudaFree(B->d_states);
   delete B;
 }
@@ -1147,18 +1151,15 @@ int vdvc_gn_batch_create(const vdvc_gn_desc* descs, int n, void* const* ws, cons
     if (st) return fail(st);
     B->S.push_back((GnSolver<float>*)impl);
   }
-  if (cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&B->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+  if (pool_stream(&B->cap) || pool_event(&B->fork_ev) ||
       cudaMalloc((void**)&B->d_states, n * sizeof(PcgState*)) != cudaSuccess)
     return fail(set_error(VDVC_ERR_CUDA, "batch stream/event/state setup failed"));
   for (int i = 0; i < n; ++i) {
-    cudaStream_t st;
-    cudaEvent_t ev;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
-      return fail(set_error(VDVC_ERR_CUDA, "batch stream setup failed"));
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    if (pool_stream(&st)) return fail(set_error(VDVC_ERR_CUDA, "batch stream setup failed"));
     B->streams.push_back(st);
-    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
-      return fail(set_error(VDVC_ERR_CUDA, "batch event setup failed"));
+    if (pool_event(&ev)) return fail(set_error(VDVC_ERR_CUDA, "batch event setup failed"));
     B->done_ev.push_back(ev);
   }
   vdvc_gn_batch* h = new (std::nothrow) vdvc_gn_batch();

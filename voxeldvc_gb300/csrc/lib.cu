@@ -7,6 +7,7 @@
 #include <map>
 #include <mutex>
 #include <utility>
+#include <vector>
 
 #include "common.cuh"
 
@@ -24,6 +25,90 @@ int set_error(int status, const char* fmt, ...) {
 }
 
 void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Pools of the per-solver CUDA objects.  Creating a stream, two events and
+// a pinned read-back block for every solver of every pyramid level costs
+// more than the coarse levels' solves of small problems; returned objects
+// are idle (their owner synchronised) and are handed out again.
+static std::mutex g_pool_mu;
+static std::map<int, std::vector<cudaStream_t>> g_streams;  // device -> idle non-blocking streams
+static std::map<int, std::vector<cudaEvent_t>> g_events;    // device -> idle timing-free events
+static std::vector<void*> g_pinned;                          // idle kPinnedSlot-byte pinned blocks
+
+int pool_stream(cudaStream_t* out) {
+  int dev = 0;
+  VDVC_CUDA(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto& v = g_streams[dev];
+    if (!v.empty()) {
+      *out = v.back();
+      v.pop_back();
+      return VDVC_OK;
+    }
+  }
+  VDVC_CUDA(cudaStreamCreateWithFlags(out, cudaStreamNonBlocking));
+  return VDVC_OK;
+}
+
+void pool_stream_return(cudaStream_t s) {
+  if (!s) return;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaGetLastError();
+    cudaStreamDestroy(s);
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  g_streams[dev].push_back(s);
+}
+
+int pool_event(cudaEvent_t* out) {
+  int dev = 0;
+  VDVC_CUDA(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto& v = g_events[dev];
+    if (!v.empty()) {
+      *out = v.back();
+      v.pop_back();
+      return VDVC_OK;
+    }
+  }
+  VDVC_CUDA(cudaEventCreateWithFlags(out, cudaEventDisableTiming));
+  return VDVC_OK;
+}
+
+void pool_event_return(cudaEvent_t e) {
+  if (!e) return;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    cudaEventDestroy(e);
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  g_events[dev].push_back(e);
+}
+
+int pool_pinned(void** out) {
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pinned.empty()) {
+      *out = g_pinned.back();
+      g_pinned.pop_back();
+      return VDVC_OK;
+    }
+  }
+  VDVC_CUDA(cudaMallocHost(out, kPinnedSlot));
+  return VDVC_OK;
+}
+
+void pool_pinned_return(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  g_pinned.push_back(p);
+}
 
 int ensure_dyn_smem(const void* func, int bytes) {
   static std::mutex mu;
