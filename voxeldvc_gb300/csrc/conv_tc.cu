@@ -275,6 +275,9 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvTcArgs A) {
   const bool fail = __syncthreads_or(!ok) || *s_fail;
   if (!fail) {
     const long long pr = (long long)blockIdx.x * kM + warp * 32 + lane;
+    // BF16 output in 16-byte pieces where a 16-channel group is whole and
+    // aligned (channel stride and offset multiples of 8: every layer here)
+    const bool vec_out = !A.out_f32 && (A.ocs % 8) == 0 && (A.ocoff % 8) == 0 && ((uintptr_t)A.out & 15) == 0;
     for (int c0 = 0; c0 < NT; c0 += 16) {
       float v[16];
       tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
@@ -295,6 +298,28 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvTcArgs A) {
 #pragma unroll
         for (int c = 0; c < 16; ++c)
           if (c0 + c < A.n_out) op[c] = v[c];
+      } else if (vec_out && c0 + 16 <= A.n_out) {
+        uint4* op = (uint4*)((bf16*)A.out + o);
+        uint32_t w[8];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          if (A.accumulate) {
+            const uint4 old = op[q];
+            const uint32_t ow[4] = {old.x, old.y, old.z, old.w};
+#pragma unroll
+            for (int c = 0; c < 8; c += 2) {
+              v[8 * q + c] += __uint_as_float(ow[c / 2] << 16);
+              v[8 * q + c + 1] += __uint_as_float(ow[c / 2] & 0xFFFF0000u);
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 16; c += 2) {
+          const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[c], v[c + 1]);
+          w[c / 2] = *reinterpret_cast<const uint32_t*>(&b2);
+        }
+        op[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        op[1] = make_uint4(w[4], w[5], w[6], w[7]);
       } else {
         bf16* op = (bf16*)A.out + o;
 #pragma unroll
