@@ -311,7 +311,7 @@ class SeedNet:
         buffer; returns the input grid."""
         G = input_grid(shape)
         b = self.buffers(G, train, slot)
-        ms = mean_std if mean_std is not None else np.array([*_mean_std(f_vox), *_mean_std(g_vox)], np.float64)
+        ms = mean_std if mean_std is not None else np.array(_mean_std_many(f_vox, g_vox), np.float64)
         _lib.check(_lib.lib().vdvc_cnn_pool_input_mirrored(f_vox.data_ptr(), g_vox.data_ptr(), *shape,
                                                            ms.ctypes.data_as(_lib.pd), int(flip), b["x"].data_ptr(),
                                                            D.stream()), "cnn_pool_input")
@@ -337,7 +337,7 @@ class SeedNet:
         first)."""
         torch = D.torch()
         mirrors = self.mirrors_for(shape, h, Nx, Ny, Nz, passes)
-        ms = np.array([*_mean_std(f_vox), *_mean_std(g_vox)], np.float64)
+        ms = np.array(_mean_std_many(f_vox, g_vox), np.float64)
         U = D.empty(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), np.float64)
         main = torch.cuda.current_stream()
         ready = torch.cuda.Event()
@@ -380,14 +380,26 @@ def _from_bf16_bits(b):
 def _mean_std(x):
     """(mean, population std) of a float32 CUDA tensor, float64 sums on the
     device (vdvc_dot)."""
+    return tuple(_mean_std_many(x))
+
+
+def _mean_std_many(*xs):
+    """[mean, std, mean, std, ...] of float32 CUDA tensors: the float64
+    sums of every tensor reduced into one device buffer, read back once."""
     L = _lib.lib()
     ws = D.scratch.get(1 << 16)
-    s = C.c_double(0.0)
-    ss = C.c_double(0.0)
-    n = x.numel()
-    _lib.check(L.vdvc_dot(x.data_ptr(), None, _lib.F32, n, C.byref(s), ws.data_ptr(), ws.numel(), D.stream()), "dot")
-    _lib.check(L.vdvc_dot(x.data_ptr(), x.data_ptr(), _lib.F32, n, C.byref(ss), ws.data_ptr(), ws.numel(),
-                          D.stream()), "dot")
-    mean = s.value / n
-    var = max(ss.value / n - mean * mean, 0.0)
-    return mean, float(np.sqrt(var)) if var > 0 else 1.0
+    sums = D.zeros(2 * len(xs), np.float64)
+    for k, x in enumerate(xs):
+        n = x.numel()
+        _lib.check(L.vdvc_dot_device(x.data_ptr(), None, _lib.F32, n, sums[2 * k:2 * k + 1].data_ptr(),
+                                     ws.data_ptr(), ws.numel(), D.stream()), "dot")
+        _lib.check(L.vdvc_dot_device(x.data_ptr(), x.data_ptr(), _lib.F32, n, sums[2 * k + 1:2 * k + 2].data_ptr(),
+                                     ws.data_ptr(), ws.numel(), D.stream()), "dot")
+    h = sums.cpu().numpy()
+    out = []
+    for k, x in enumerate(xs):
+        n = x.numel()
+        mean = h[2 * k] / n
+        var = max(h[2 * k + 1] / n - mean * mean, 0.0)
+        out += [float(mean), float(np.sqrt(var)) if var > 0 else 1.0]
+    return out
