@@ -71,6 +71,17 @@ struct Mesh {
 
 int make_mesh(int h, int Nx, int Ny, int Nz, Mesh* m);
 
+// Element (i, j, k) of element index e (x fastest) in 32-bit arithmetic:
+// make_mesh keeps 3 Nnodes (> Ne) within int32, and a 64-bit division costs
+// tens of instructions per thread.
+__device__ __forceinline__ void elem_ijk(const Mesh& m, long long e, int& i, int& j, int& k) {
+  const unsigned int eu = (unsigned int)e, nx = (unsigned int)m.Nx, ny = (unsigned int)m.Ny;
+  const unsigned int r = eu / nx;
+  i = (int)(eu - r * nx);
+  j = (int)(r % ny);
+  k = (int)(r / ny);
+}
+
 // Local corner a (0..7) of a Hex8 element -> offsets, in the reference's
 // order (000,100,110,010,001,101,111,011) (engine/geometry_dvc.py:14-17).
 __host__ __device__ inline int corner_dx(int a) { return ((a + 1) >> 1) & 1; }

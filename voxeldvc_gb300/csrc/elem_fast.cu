@@ -25,9 +25,8 @@ template <int H, bool PCG>
 __device__ __forceinline__ void elem_hv_body(const StripArgs<float>& a, const Kpair<float>* __restrict__ kp,
                                              long long e, float beta) {
   const Mesh& m = a.m;
-  const int i = (int)(e % m.Nx);
-  const long long rr = e / m.Nx;
-  const int j = (int)(rr % m.Ny), k = (int)(rr / m.Ny);
+  int i, j, k;
+  elem_ijk(m, e, i, j, k);
 
   // nodal values u[dz][dy][dx][c] (PCG: p_new = z + beta p_old)
   float u[2][2][2][3];

@@ -224,10 +224,7 @@ __global__ void __launch_bounds__(kTile) k_eh_matvec_tma(const EhMatvecArgs a) {
   if constexpr (PCG) beta = (float)a.st->beta;
   int ei = 0, ej = 0, ek = 0;
   if (active) {
-    ei = (int)(e % m.Nx);
-    const long long rr = e / m.Nx;
-    ej = (int)(rr % m.Ny);
-    ek = (int)(rr / m.Ny);
+    elem_ijk(m, e, ei, ej, ek);
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
       const long long node = (long long)(ei + corner_dx(b)) + (long long)(ej + corner_dy(b)) * m.Nnx +

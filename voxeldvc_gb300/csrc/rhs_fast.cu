@@ -235,9 +235,8 @@ __global__ void __launch_bounds__(256) k_elem_rhs(const StripArgs<float> a) {
   double dsum[3] = {0.0, 0.0, 0.0};
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m.Ne;
        e += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(e % m.Nx);
-    const long long rr = e / m.Nx;
-    const int j = (int)(rr % m.Ny), k = (int)(rr / m.Ny);
+    int i, j, k;
+    elem_ijk(m, e, i, j, k);
     float o[2][2][2][3], od[2][2][2][3];
 #pragma unroll
     for (int q = 0; q < 24; ++q) {

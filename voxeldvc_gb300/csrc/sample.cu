@@ -237,9 +237,8 @@ __global__ void __launch_bounds__(256) k_elem_sample(const SampleArgs<float> a) 
   const float gxmax = (float)(a.gnx - 1), gymax = (float)(a.gny - 1), gzmax = (float)(a.gnz - 1);
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m.Ne;
        e += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(e % m.Nx);
-    const long long rr = e / m.Nx;
-    const int j = (int)(rr % m.Ny), k = (int)(rr / m.Ny);
+    int i, j, k;
+    elem_ijk(m, e, i, j, k);
     float uc[2][2][2][3];  // [dx][dy][dz][c]
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)

@@ -276,9 +276,10 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
 // n of ev[(3a+c)*Ne + e], a = n's corner in e.  Fixed summation order.
 template <typename T>
 __device__ __forceinline__ void gather_node(const Mesh& m, const T* __restrict__ ev, long long n, T out[3]) {
-  const int ni = (int)(n % m.Nnx);
-  const long long rr = n / m.Nnx;
-  const int nj = (int)(rr % m.Nny), nk = (int)(rr / m.Nny);
+  // 32-bit node coordinates (the launcher rejects 2^32 nodes or more): a
+  // 64-bit division costs tens of instructions per node
+  const unsigned int nu = (unsigned int)n, nnx = (unsigned int)m.Nnx, rr = nu / nnx;
+  const int ni = (int)(nu - rr * nnx), nj = (int)(rr % (unsigned int)m.Nny), nk = (int)(rr / (unsigned int)m.Nny);
   out[0] = out[1] = out[2] = T(0);
 #pragma unroll
   for (int a = 0; a < 8; ++a) {
@@ -352,6 +353,7 @@ long long strip_grid_blocks(const Mesh& m) {
 
 template <typename T>
 int launch_gather(const Mesh& m, const T* ev, T* out, cudaStream_t s) {
+  if (m.Nnodes >= (1ll << 32)) return set_error(VDVC_ERR_UNSUPPORTED, "2^32 nodes or more");
   long long b = (m.Nnodes + 255) / 256;
   if (b > 152 * 32) b = 152 * 32;
   k_gather<T><<<(int)b, 256, 0, s>>>(m, ev, out);
