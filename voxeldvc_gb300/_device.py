@@ -116,18 +116,19 @@ def zeros(n, dtype):
 
 
 class _Scratch:
-    """Grow-only scratch buffer per device, used by one stream at a time."""
+    """Grow-only scratch buffer per (device, stream): work on two streams
+    at once (the batch's set-up on a side stream) never shares one."""
 
     def __init__(self):
         self.bufs = {}
 
     def get(self, nbytes: int):
         T = torch()
-        dev = T.cuda.current_device()
-        b = self.bufs.get(dev)
+        key = (T.cuda.current_device(), T.cuda.current_stream().cuda_stream)
+        b = self.bufs.get(key)
         if b is None or b.numel() < nbytes:
             b = T.empty(max(int(nbytes), 1 << 20), dtype=T.uint8, device=device())
-            self.bufs[dev] = b
+            self.bufs[key] = b
         return b
 
 

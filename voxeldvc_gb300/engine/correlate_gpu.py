@@ -14,6 +14,7 @@ reference's pix[x,y,z] C-order layout.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 import time
 
 import numpy as np
@@ -318,15 +319,17 @@ def _plane_wave(Nx, Ny, Nz, h, dtype):
 # without the cache).
 _PLANE_WAVES = {}
 _PLANE_WAVES_MAX = 16
+_PLANE_WAVES_LOCK = threading.Lock()  # level set-ups may run on two host threads (engine/batch.py)
 
 
 def _plane_wave_device(Nx, Ny, Nz, h, dtype):
     key = (D.torch().cuda.current_device(), Nx, Ny, Nz, h, np.dtype(dtype).str)
-    V = _PLANE_WAVES.get(key)
-    if V is None:
-        if len(_PLANE_WAVES) >= _PLANE_WAVES_MAX:
-            _PLANE_WAVES.pop(next(iter(_PLANE_WAVES)))
-        V = _PLANE_WAVES[key] = D.to_device(_plane_wave(Nx, Ny, Nz, h, dtype))
+    with _PLANE_WAVES_LOCK:
+        V = _PLANE_WAVES.get(key)
+        if V is None:
+            if len(_PLANE_WAVES) >= _PLANE_WAVES_MAX:
+                _PLANE_WAVES.pop(next(iter(_PLANE_WAVES)))
+            V = _PLANE_WAVES[key] = D.to_device(_plane_wave(Nx, Ny, Nz, h, dtype))
     return V
 
 
