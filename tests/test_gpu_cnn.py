@@ -121,6 +121,53 @@ def test_conv_forward_input_grad_wgrad(env, cin, n_out, stride, src):
         assert rel(dw.cpu().numpy().reshape(ref_dw.shape), 2 * ref_dw) < 1e-5
 
 
+@pytest.mark.parametrize("cin,n_out,stride,scs,scoff", [(64, 64, 1, 128, 64), (32, 64, 2, 96, 32),
+                                                        (256, 64, 1, 256, 0), (128, 128, 2, 256, 128)])
+def test_conv_channel_slices_and_accumulate(env, cin, n_out, stride, scs, scoff):
+    """A channel slice of a wider source (the decoder's concatenated
+    buffers) into a channel slice of a wider output, written and then added
+    on top (accumulate); grids that are not multiples of the 8 x 4 x 4
+    output bricks."""
+    torch, L, S = env
+    lib = L.lib()
+    rng = np.random.default_rng(cin + scs + stride)
+    src = (11, 6, 9)
+    sx, sy, sz = src
+    out = tuple((s - 1) // stride + 1 for s in src)
+    xw = O.bf16_round(rng.standard_normal((sz, sy, sx, scs)))
+    x = xw[..., scoff:scoff + cin]
+    W = rng.standard_normal((n_out, 27, cin)) * 0.1
+    Wr = O.bf16_round(W)
+    bvec = rng.standard_normal(n_out).astype(np.float32)
+    ref = O.conv(x, Wr, bvec.astype(np.float64), stride, relu=True)
+    npad8, npad16 = (n_out + 7) // 8 * 8, (n_out + 15) // 16 * 16
+    wf = torch.zeros(npad8 * 27 * cin, dtype=torch.bfloat16, device="cuda")
+    wb = torch.zeros((cin + 7) // 8 * 8 * 27 * npad16, dtype=torch.bfloat16, device="cuda")
+    wt = torch.from_numpy(W.astype(np.float32).reshape(-1)).cuda()
+    L.check(lib.vdvc_cnn_pack_weights(wt.data_ptr(), n_out, cin, wf.data_ptr(), wb.data_ptr(), stream(torch)))
+    ocs, ocoff = n_out + 16, 8
+    npos = out[0] * out[1] * out[2]
+    base = O.bf16_round(rng.standard_normal((npos, ocs)))
+    y = bf(torch, base)
+    g = S.fwd_geom(out, src, stride)
+    xd, bd = bf(torch, xw), torch.from_numpy(bvec).cuda()  # held: the launches are asynchronous
+    L.check(lib.vdvc_cnn_conv(xd.data_ptr(), scs, scoff, cin, wf.data_ptr(), bd.data_ptr(), n_out, 1, y.data_ptr(), 0,
+                              ocs, ocoff, 0, C.byref(g), stream(torch)))
+    yh = host(y).reshape(npos, ocs)
+    r2 = ref.reshape(npos, n_out)
+    tol = 8e-3 * np.abs(r2).max()
+    assert np.allclose(yh[:, ocoff:ocoff + n_out], r2, rtol=8e-3, atol=tol)
+    # channels outside the slice untouched
+    assert np.array_equal(yh[:, :ocoff], base[:, :ocoff])
+    assert np.array_equal(yh[:, ocoff + n_out:], base[:, ocoff + n_out:])
+    L.check(lib.vdvc_cnn_conv(xd.data_ptr(), scs, scoff, cin, wf.data_ptr(), bd.data_ptr(), n_out, 1, y.data_ptr(), 0,
+                              ocs, ocoff, 1, C.byref(g), stream(torch)))
+    yh2 = host(y).reshape(npos, ocs)
+    assert np.allclose(yh2[:, ocoff:ocoff + n_out], 2 * r2, rtol=1.6e-2, atol=2 * tol)
+    assert np.array_equal(yh2[:, :ocoff], base[:, :ocoff])
+    L.check(lib.vdvc_cnn_status(stream(torch)))
+
+
 @pytest.mark.parametrize("m,n", [((3, 4, 5), (5, 7, 9)), ((3, 3, 3), (6, 6, 6))])
 def test_upsample(env, m, n):
     torch, L, S = env

@@ -34,6 +34,9 @@ typedef __nv_bfloat16 bf16;
 int launch_conv_tc(const void* src, int scs, int scoff, int cin, const void* w, int wrows, const float* bias,
                    int n_out, int relu, void* out, int out_f32, int ocs, int ocoff, int accumulate,
                    const vdvc_conv_geom* geom, int* err, cudaStream_t s);
+int launch_conv_tma(const void* src, int scs, int scoff, int cin, const void* w, int wrows, const float* bias,
+                    int n_out, int relu, void* out, int out_f32, int ocs, int ocoff, int accumulate,
+                    const vdvc_conv_geom* geom, int* err, cudaStream_t s);
 
 struct Geo {
   int nx, ny, nz, sx, sy, sz, a, b, c, d;
@@ -601,6 +604,9 @@ int vdvc_cnn_conv(const void* src, int src_cstride, int src_coff, int cin, const
     int* err = nullptr;
     int st = conv_error_flag(&err);
     if (st) return st;
+    st = launch_conv_tma(src, src_cstride, src_coff, cin, w, (n_out + 7) / 8 * 8, bias, n_out, relu, out, out_f32,
+                         out_cstride, out_coff, accumulate, geom, err, s);
+    if (st != VDVC_ERR_UNSUPPORTED) return st;
     st = launch_conv_tc(src, src_cstride, src_coff, cin, w, (n_out + 7) / 8 * 8, bias, n_out, relu, out, out_f32,
                         out_cstride, out_coff, accumulate, geom, err, s);
     if (st != VDVC_ERR_UNSUPPORTED) return st;

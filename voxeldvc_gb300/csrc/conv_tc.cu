@@ -1,31 +1,47 @@
-// 3x3x3 gather convolution (include/vdvc_cnn.h) on the 5th-generation tensor
-// cores: tcgen05.mma kind::f16 (BF16 x BF16 -> FP32 in TMEM).
+// 3x3x3 gather convolutions (include/vdvc_cnn.h) on the 5th-generation
+// tensor cores: tcgen05.mma kind::f16 (BF16 x BF16 -> FP32 in TMEM).
 //
 // GEMM view: D[p][n] = sum_K A[p][K] B[n][K], with p the output positions
 // (M = 128 per CTA), n the output channels (N = n_out rounded up to 16) and
 // K = (tap t, input channel c) in the order t * cin + c -- the order of the
 // packed forward weights [n_pad][27][cin] and of the input-gradient weights
-// [cin_pad][27][n_pad16], so both read unchanged.  One K-block is 64 K
-// values = eight 16-byte chunks of 8 channels; a chunk of row p is 16
-// contiguous bytes of the channels-last source at position q(p, t) (zero
-// when q falls outside the source), copied by cp.async straight into the
-// no-swizzle K-major canonical layout (8-row x 16-byte core matrices).
-// B rows past the packed rows and K past 27 * cin are zero-filled the same
-// way (src-size 0), so no extra padding is needed in global memory.
+// [cin_pad][27][n_pad16], so both read unchanged.
 //
-// Pipeline (128 threads, one output tile per CTA): kStages shared-memory
-// stages of (A, B); every thread copies its own A row's eight chunks and a
-// share of B for a stage, the CTA syncs, one thread issues the four K = 16
-// MMAs and commits them to the stage's mbarrier, and a stage is refilled
-// only after that mbarrier says its MMAs are done.  The epilogue reads the
-// accumulator from TMEM (each warp its 32 lanes = 32 positions), adds the
-// bias, applies ReLU and stores BF16 (optionally added to the output) or
-// FP32.  Every mbarrier wait is bounded: on a timeout the CTA sets *err,
-// skips its stores, waits (bounded) for its MMAs, frees its TMEM and
-// returns; the host reports VDVC_ERR_TIMEOUT.
+// Two kernels share the epilogue (TMEM -> registers, bias, ReLU, BF16 or
+// FP32 stores, each warp its 32 lanes = 32 positions):
+//
+// k_conv_tma -- geometries with a unit source step (d = 1: every forward
+// convolution, stride 1 or 2, and the input gradient of a stride-1 one).
+// The CTA's 128 positions are an 8 x 4 x 4 brick of the output grid, so for
+// tap t and a block of CB input channels the A operand is one box of a 4-D
+// tensor map over the channels-last source (channel, x, y, z): the box starts
+// at q = a * brick origin + b + c * t per axis, walks the source with element
+// step a (the convolution stride), and TMA fills positions outside the
+// source with zeros -- the padding.  B is a box of the packed weights.  Both
+// land in the 128-byte (CB = 64) or 64-byte (CB = 32) swizzled K-major
+// layout the MMA descriptors name.  One thread issues the copies, another
+// the MMAs; full/empty mbarriers per stage, no CTA-wide barrier in the main
+// loop.
+//
+// k_conv_tc -- the other geometries (input gradients of stride-2 layers,
+// d = 2) and channel counts that are multiples of 8 but not of 32.  A K-block
+// is 64 K values = eight 16-byte chunks of 8 channels; a chunk of row p is
+// 16 contiguous bytes of the source at position q(p, t) (zero when q falls
+// outside), copied by cp.async into the no-swizzle K-major layout (8-row x
+// 16-byte core matrices); B rows past the packed rows and K past 27 * cin
+// are zero-filled the same way (src-size 0).  kStages stages; every thread
+// copies its own A row and a share of B, the CTA syncs, one thread issues
+// the MMAs and commits them to the stage's mbarrier.
+//
+// Every mbarrier wait is bounded: on a timeout the CTA sets *err, skips its
+// stores, waits (bounded) for its copies and MMAs in flight, frees its TMEM
+// and returns; the host reports VDVC_ERR_TIMEOUT.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "ops.cuh"
 #include "tma.cuh"
@@ -125,15 +141,82 @@ __device__ __forceinline__ uint32_t chunk_off(int row, int ch, int rows) {
   return (uint32_t)(((ch * (rows >> 3) + (row >> 3)) << 7) + ((row & 7) << 4));
 }
 
+// epilogue parameters (both kernels)
+struct Epi {
+  const float* bias;
+  int n_out, NT;  // NT: n_out rounded up to 16
+  int relu, out_f32, ocs, ocoff, accumulate;
+  void* out;
+};
+
+// Reads this warp's 32 accumulator rows (lane = row) and stores row `pr`
+// (when `valid`): bias, ReLU, then BF16 (optionally added to the output) or
+// FP32.  Every lane of the warp calls it (tcgen05.ld is warp-collective).
+__device__ __forceinline__ void store_rows(uint32_t tmem, int warp, bool valid, long long pr, const Epi& E) {
+  // BF16 output in 16-byte pieces where a 16-channel group is whole and
+  // aligned (channel stride and offset multiples of 8: every layer here)
+  const bool vec_out = !E.out_f32 && (E.ocs % 8) == 0 && (E.ocoff % 8) == 0 && ((uintptr_t)E.out & 15) == 0;
+  for (int c0 = 0; c0 < E.NT; c0 += 16) {
+    float v[16];
+    tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+    if (!valid) continue;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const int n = c0 + c;
+      float x = v[c];
+      if (E.bias && n < E.n_out) x += E.bias[n];
+      if (E.relu) x = fmaxf(x, 0.f);
+      v[c] = x;
+    }
+    const long long o = pr * E.ocs + E.ocoff + c0;
+    // fixed trip counts with a predicate: a data-dependent bound would
+    // index v[] at run time and move it to local memory
+    if (E.out_f32) {
+      float* op = (float*)E.out + o;
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (c0 + c < E.n_out) op[c] = v[c];
+    } else if (vec_out && c0 + 16 <= E.n_out) {
+      uint4* op = (uint4*)((bf16*)E.out + o);
+      uint32_t w[8];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        if (E.accumulate) {
+          const uint4 old = op[q];
+          const uint32_t ow[4] = {old.x, old.y, old.z, old.w};
+#pragma unroll
+          for (int c = 0; c < 8; c += 2) {
+            v[8 * q + c] += __uint_as_float(ow[c / 2] << 16);
+            v[8 * q + c + 1] += __uint_as_float(ow[c / 2] & 0xFFFF0000u);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 16; c += 2) {
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[c], v[c + 1]);
+        w[c / 2] = *reinterpret_cast<const uint32_t*>(&b2);
+      }
+      op[0] = make_uint4(w[0], w[1], w[2], w[3]);
+      op[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    } else {
+      bf16* op = (bf16*)E.out + o;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        if (c0 + c >= E.n_out) continue;
+        float x = v[c];
+        if (E.accumulate) x += __bfloat162float(op[c]);
+        op[c] = __float2bfloat16_rn(x);
+      }
+    }
+  }
+}
+
 struct ConvTcArgs {
   const bf16* src;
   int scs, scoff, cin;
-  const bf16* w;     // [wrows][27 * cin]
-  int wrows;         // packed weight rows (>= n_out)
-  const float* bias;
-  int n_out, NT;     // NT: n_out rounded up to 16
-  int relu, out_f32, ocs, ocoff, accumulate;
-  void* out;
+  const bf16* w;  // [wrows][27 * cin]
+  int wrows;      // packed weight rows (>= n_out)
+  Epi e;
   TcGeo g;
   int* err;
 };
@@ -141,7 +224,7 @@ struct ConvTcArgs {
 __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvTcArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int NT = A.NT;
+  const int NT = A.e.NT;
   const uint32_t bstage = (uint32_t)NT * 128;
   unsigned char* sA = smem;
   unsigned char* sB = smem + kStages * kAStage;
@@ -275,64 +358,186 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvTcArgs A) {
   const bool fail = __syncthreads_or(!ok) || *s_fail;
   if (!fail) {
     const long long pr = (long long)blockIdx.x * kM + warp * 32 + lane;
-    // BF16 output in 16-byte pieces where a 16-channel group is whole and
-    // aligned (channel stride and offset multiples of 8: every layer here)
-    const bool vec_out = !A.out_f32 && (A.ocs % 8) == 0 && (A.ocoff % 8) == 0 && ((uintptr_t)A.out & 15) == 0;
-    for (int c0 = 0; c0 < NT; c0 += 16) {
-      float v[16];
-      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (pr >= npos) continue;
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const int n = c0 + c;
-        float x = v[c];
-        if (A.bias && n < A.n_out) x += A.bias[n];
-        if (A.relu) x = fmaxf(x, 0.f);
-        v[c] = x;
-      }
-      const long long o = pr * A.ocs + A.ocoff + c0;
-      // fixed trip counts with a predicate: a data-dependent bound would
-      // index v[] at run time and move it to local memory
-      if (A.out_f32) {
-        float* op = (float*)A.out + o;
-#pragma unroll
-        for (int c = 0; c < 16; ++c)
-          if (c0 + c < A.n_out) op[c] = v[c];
-      } else if (vec_out && c0 + 16 <= A.n_out) {
-        uint4* op = (uint4*)((bf16*)A.out + o);
-        uint32_t w[8];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          if (A.accumulate) {
-            const uint4 old = op[q];
-            const uint32_t ow[4] = {old.x, old.y, old.z, old.w};
-#pragma unroll
-            for (int c = 0; c < 8; c += 2) {
-              v[8 * q + c] += __uint_as_float(ow[c / 2] << 16);
-              v[8 * q + c + 1] += __uint_as_float(ow[c / 2] & 0xFFFF0000u);
-            }
-          }
-        }
-#pragma unroll
-        for (int c = 0; c < 16; c += 2) {
-          const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[c], v[c + 1]);
-          w[c / 2] = *reinterpret_cast<const uint32_t*>(&b2);
-        }
-        op[0] = make_uint4(w[0], w[1], w[2], w[3]);
-        op[1] = make_uint4(w[4], w[5], w[6], w[7]);
-      } else {
-        bf16* op = (bf16*)A.out + o;
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          if (c0 + c >= A.n_out) continue;
-          float x = v[c];
-          if (A.accumulate) x += __bfloat162float(op[c]);
-          op[c] = __float2bfloat16_rn(x);
-        }
-      }
-    }
+    store_rows(tmem, warp, pr < npos, pr, A.e);
   } else if (tid == 0) {
     atomicExch(A.err, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tc_dealloc(tmem, ncols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_conv_tma
+
+constexpr int kBX = 8, kBY = 4, kBZ = 4;  // output brick = the 128 GEMM rows
+static_assert(kBX * kBY * kBZ == kM, "a brick is one M tile");
+constexpr int kTmaMaxStages = 8;
+constexpr uint32_t kTmaStageBudget = 96 * 1024;  // stages of two CTAs fit one SM
+
+struct ConvTmaArgs {
+  int nx, ny, nz;  // output grid
+  int nbx, nby;    // bricks along x and y
+  int a, b, c;     // source coordinate a * p + b + c * tap, per axis
+  int cin, scoff;  // input channels, their offset in the source's channel stride
+  int ncb, nkb;    // channel blocks per tap, K-blocks (27 * ncb)
+  int stages;
+  Epi e;
+  int* err;
+};
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+
+// K-major descriptor of rows of CB * 2 bytes in the swizzled layout TMA
+// writes (8-row atoms: 1024 B for the 128-byte swizzle, 512 B for 64-byte);
+// the leading-byte offset is unused for swizzled K-major operands.
+template <int CB>
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr) {
+  constexpr uint32_t sbo = 8u * CB * 2u;
+  constexpr uint64_t layout = CB == 64 ? 2 : 4;  // SWIZZLE_128B : SWIZZLE_64B
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= layout << 61;
+  return d;
+}
+
+// Bounded wait (at most 2^22 polls).  Every 256 polls it also gives up once
+// the CTA's other role thread has aborted (`abort`, when given) or -- after
+// `patience` polls -- once any CTA of the launch has reported a failure in
+// *gerr, so that one stuck CTA does not make every other one sit out its
+// own full limit.
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort, volatile int* gerr,
+                                              long long patience) {
+  for (long long i = 0; i < (1LL << 22); ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255) == 255 && ((abort && *abort) || (i >= patience && *gerr))) return false;
+  }
+  return false;
+}
+
+template <int CB>
+__global__ void __launch_bounds__(kThreads) k_conv_tma(const __grid_constant__ CUtensorMap tmA,
+                                                       const __grid_constant__ CUtensorMap tmB, const ConvTmaArgs P) {
+  extern __shared__ unsigned char smem_raw[];
+  // the swizzle atoms need 1024-byte aligned stages
+  const uint32_t raw = smem_addr(smem_raw);
+  unsigned char* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int S = P.stages, NT = P.e.NT;
+  volatile int* gerr = P.err;
+  constexpr uint32_t aBytes = (uint32_t)kM * CB * 2;
+  const uint32_t stageBytes = aBytes + (uint32_t)NT * CB * 2;
+  uint64_t* full = (uint64_t*)(smem + S * stageBytes);
+  uint64_t* empty = full + S;
+  uint64_t* done = empty + S;
+  uint32_t* s_tmem = (uint32_t*)(done + 1);
+  volatile int* s_abort = (volatile int*)(s_tmem + 1);
+  int* s_cnt = (int*)(s_tmem + 2);  // [0] K-blocks whose copies were issued, [1] consumed by MMAs
+
+  uint32_t ncols = 32;
+  while ((int)ncols < NT) ncols <<= 1;
+  if (warp == 0) {
+    tc_alloc(s_tmem, ncols);
+    tc_relinquish();
+  }
+  if (tid == 32) {
+    for (int st = 0; st < S; ++st) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], 1);
+    }
+    mbar_init(done, 1);
+    *s_abort = 0;
+    s_cnt[0] = s_cnt[1] = 0;
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *s_tmem;
+
+  const int bid = blockIdx.x;
+  const int x0 = (bid % P.nbx) * kBX, y0 = ((bid / P.nbx) % P.nby) * kBY, z0 = (bid / (P.nbx * P.nby)) * kBZ;
+
+  if (tid == 0) {
+    // producer: the A box and the B box of each K-block into its stage
+    int kb = 0;
+    for (; kb < P.nkb; ++kb) {
+      const int st = kb % S;
+      if (kb >= S && !wait_or_abort(&empty[st], (uint32_t)((kb / S - 1) & 1), s_abort, gerr, 0)) {
+        *s_abort = 1;
+        atomicExch(P.err, 1);
+        break;
+      }
+      const int t = kb / P.ncb, cb = kb - t * P.ncb;
+      const int tx = t % 3, ty = (t / 3) % 3, tz = t / 9;
+      const uint32_t sa = smem_addr(smem + st * stageBytes), fb = smem_addr(&full[st]);
+      mbar_arrive_expect_tx(&full[st], stageBytes);
+      tma_load_4d(sa, &tmA, P.scoff + cb * CB, P.a * x0 + P.b + P.c * tx, P.a * y0 + P.b + P.c * ty,
+                  P.a * z0 + P.b + P.c * tz, fb);
+      tma_load_2d(sa + aBytes, &tmB, t * P.cin + cb * CB, 0, fb);
+    }
+    s_cnt[0] = kb;
+  } else if (tid == 32) {
+    // MMA issuer: CB / 16 MMAs of K = 16 per K-block, the stage released by
+    // the commit once they have read it
+    const uint32_t idesc = idesc_bf16(kM, NT);
+    int kb = 0;
+    for (; kb < P.nkb; ++kb) {
+      const int st = kb % S;
+      if (!wait_or_abort(&full[st], (uint32_t)((kb / S) & 1), s_abort, gerr, 0)) {
+        *s_abort = 1;
+        atomicExch(P.err, 1);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t sa = smem_addr(smem + st * stageBytes);
+#pragma unroll
+      for (int kk = 0; kk < CB / 16; ++kk)
+        tc_mma(tmem, sw_desc<CB>(sa + kk * 32), sw_desc<CB>(sa + aBytes + kk * 32), idesc,
+               (kb > 0 || kk > 0) ? 1u : 0u);
+      tc_commit(&empty[st]);
+    }
+    s_cnt[1] = kb;
+    tc_commit(done);  // tracks every MMA issued before it
+  }
+  __syncwarp();
+  // the MMAs issued so far always complete: no early exit on *gerr
+  bool ok = wait_or_abort(done, 0, nullptr, gerr, 1LL << 22);
+  tc_fence_after();
+  __syncthreads();
+  // after an abort: copies issued but never consumed must land before exit
+  // (a copy lands within microseconds; past 2^14 polls with a failure
+  // reported it is taken as stuck)
+  if (tid == 0)
+    for (int kb = s_cnt[1]; kb < s_cnt[0]; ++kb)
+      if (!wait_or_abort(&full[kb % S], (uint32_t)((kb / S) & 1), nullptr, gerr, 1LL << 14)) ok = false;
+  const bool fail = __syncthreads_or(!ok || *s_abort != 0 || s_cnt[1] < P.nkb);
+  if (!fail) {
+    const int r = warp * 32 + lane;
+    const int x = x0 + r % kBX, y = y0 + (r / kBX) % kBY, z = z0 + r / (kBX * kBY);
+    store_rows(tmem, warp, x < P.nx && y < P.ny && z < P.nz, ((long long)z * P.ny + y) * P.nx + x, P.e);
+  } else if (tid == 0) {
+    atomicExch(P.err, 1);
   }
   tc_fence_before();
   __syncthreads();
@@ -347,6 +552,97 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvTcArgs A) {
 size_t conv_tc_smem_bytes(int n_out) {
   const int NT = (n_out + 15) / 16 * 16;
   return (size_t)kStages * (kAStage + (size_t)NT * 128) + kStages * 8 + 32;
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+template <int CB>
+int launch_tma_cb(const CUtensorMap& ta, const CUtensorMap& tb, const ConvTmaArgs& a, unsigned nb, size_t smem,
+                  cudaStream_t s) {
+  if (int st = ensure_dyn_smem((const void*)k_conv_tma<CB>, (int)smem)) return st;
+  k_conv_tma<CB><<<nb, kThreads, smem, s>>>(ta, tb, a);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+}  // namespace
+
+// The TMA form: unit source step (d = 1), |c| = 1, 1 <= a <= 4, cin a
+// multiple of 32 with a 16-byte aligned channel range.  VDVC_ERR_UNSUPPORTED
+// (error text untouched) otherwise, and the caller takes k_conv_tc.
+int launch_conv_tma(const void* src, int scs, int scoff, int cin, const void* w, int wrows, const float* bias,
+                    int n_out, int relu, void* out, int out_f32, int ocs, int ocoff, int accumulate,
+                    const vdvc_conv_geom* g, int* err, cudaStream_t s) {
+  if (g->d != 1 || (g->c != 1 && g->c != -1) || g->a < 1 || g->a > 4) return VDVC_ERR_UNSUPPORTED;
+  if (cin < 32 || cin % 32 || scs % 8 || scoff % 8 || n_out > 256 || wrows < n_out) return VDVC_ERR_UNSUPPORTED;
+  if (((uintptr_t)src | (uintptr_t)w) & 15) return VDVC_ERR_UNSUPPORTED;
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode) return VDVC_ERR_UNSUPPORTED;
+  const int CB = cin % 64 == 0 ? 64 : 32;
+  const int NT = (n_out + 15) / 16 * 16;
+  const CUtensorMapSwizzle sw = CB == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+  const cuuint32_t A = (cuuint32_t)g->a;
+  alignas(64) CUtensorMap ta, tb;
+  {
+    const cuuint64_t dim[4] = {(cuuint64_t)scs, (cuuint64_t)g->sx, (cuuint64_t)g->sy, (cuuint64_t)g->sz};
+    const cuuint64_t stride[3] = {(cuuint64_t)scs * 2, (cuuint64_t)scs * 2 * g->sx,
+                                  (cuuint64_t)scs * 2 * g->sx * g->sy};
+    const cuuint32_t box[4] = {(cuuint32_t)CB, kBX * A, kBY * A, kBZ * A};
+    const cuuint32_t step[4] = {1, A, A, A};
+    if (encode(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(src), dim, stride, box, step,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return set_error(VDVC_ERR_CUDA, "cuTensorMapEncodeTiled (convolution source) failed");
+  }
+  {
+    const cuuint64_t dim[2] = {(cuuint64_t)27 * cin, (cuuint64_t)wrows};
+    const cuuint64_t stride[1] = {(cuuint64_t)27 * cin * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)CB, (cuuint32_t)NT};
+    const cuuint32_t step[2] = {1, 1};
+    if (encode(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(w), dim, stride, box, step,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return set_error(VDVC_ERR_CUDA, "cuTensorMapEncodeTiled (convolution weights) failed");
+  }
+  ConvTmaArgs a{};
+  a.nx = g->nx;
+  a.ny = g->ny;
+  a.nz = g->nz;
+  a.nbx = (g->nx + kBX - 1) / kBX;
+  a.nby = (g->ny + kBY - 1) / kBY;
+  const long long nbz = (g->nz + kBZ - 1) / kBZ;
+  a.a = g->a;
+  a.b = g->b;
+  a.c = g->c;
+  a.cin = cin;
+  a.scoff = scoff;
+  a.ncb = cin / CB;
+  a.nkb = 27 * a.ncb;
+  const uint32_t stage = (uint32_t)(kM + NT) * CB * 2;
+  a.stages = (int)(kTmaStageBudget / stage);
+  if (a.stages > kTmaMaxStages) a.stages = kTmaMaxStages;
+  if (a.stages < 2) return VDVC_ERR_UNSUPPORTED;
+  a.e = Epi{bias, n_out, NT, relu, out_f32, ocs, ocoff, accumulate, out};
+  a.err = err;
+  const long long nb = (long long)a.nbx * a.nby * nbz;
+  if (nb >= 0x7fffffffLL) return set_error(VDVC_ERR_ARG, "grid too large");
+  // stages + 1 KB of alignment slack + barriers and flags
+  const size_t smem = (size_t)a.stages * stage + 1024 + (2 * a.stages + 1) * 8 + 16;
+  return CB == 64 ? launch_tma_cb<64>(ta, tb, a, (unsigned)nb, smem, s)
+                  : launch_tma_cb<32>(ta, tb, a, (unsigned)nb, smem, s);
 }
 
 // VDVC_ERR_UNSUPPORTED (error text untouched) when the layer does not fit
@@ -364,15 +660,7 @@ int launch_conv_tc(const void* src, int scs, int scoff, int cin, const void* w, 
   a.cin = cin;
   a.w = (const bf16*)w;
   a.wrows = wrows;
-  a.bias = bias;
-  a.n_out = n_out;
-  a.NT = (n_out + 15) / 16 * 16;
-  a.relu = relu;
-  a.out_f32 = out_f32;
-  a.ocs = ocs;
-  a.ocoff = ocoff;
-  a.accumulate = accumulate;
-  a.out = out;
+  a.e = Epi{bias, n_out, (n_out + 15) / 16 * 16, relu, out_f32, ocs, ocoff, accumulate, out};
   a.g = TcGeo{geom->nx, geom->ny, geom->nz, geom->sx, geom->sy, geom->sz, geom->a, geom->b, geom->c, geom->d};
   a.err = err;
   const long long npos = (long long)geom->nx * geom->ny * geom->nz;
