@@ -111,6 +111,27 @@ int vdvc_cnn_pool_input_mirrored(const float* f_vox, const float* g_vox,
                                  int nx, int ny, int nz,
                                  const double* mean_std, int flip, void* out,
                                  vdvc_stream_t stream);
+/* Device-side statistics of the network input: sums[0..3] (device
+   doubles) = {sum f, sum f^2, sum g, sum g^2} over the n voxels, one read of
+   each image.  ws: >= 4 * 1024 * 8 + 64 bytes of device workspace. */
+int vdvc_cnn_input_moments(const float* f_vox, const float* g_vox, long long n,
+                           double* sums, void* ws, size_t ws_bytes,
+                           vdvc_stream_t stream);
+/* vdvc_cnn_pool_input_mirrored with the standardising mean and std taken
+   on the device from vdvc_cnn_input_moments' sums over the nx*ny*nz
+   voxels (mean = s / n, std = sqrt(s2 / n - mean^2), 1 where that is not
+   positive): no host read-back between the statistics and the pooling. */
+int vdvc_cnn_pool_input_dev(const float* f_vox, const float* g_vox, int nx,
+                            int ny, int nz, const double* sums, int flip,
+                            void* out, vdvc_stream_t stream);
+/* out = the pooled input x (gx*gy*gz positions of 2 BF16 channels)
+   mirrored along the axes of flip.  When (n - 1) % 4 == 0 along each
+   mirrored axis (n the voxel count) the pooling grid is symmetric under the
+   mirror, and this equals pooling the mirrored pair up to the FP32
+   summation order of a window (an element may round to the neighbouring
+   BF16 value) -- at a read of the pooled grid instead of the images. */
+int vdvc_cnn_mirror_input(const void* x, int gx, int gy, int gz, int flip,
+                          void* out, vdvc_stream_t stream);
 
 /* Mean squared error of pred (FP32, channels [0,3) of stride pred_cstride)
    against target (FP32 [npos][3]); *loss (device double) = mean; dpred

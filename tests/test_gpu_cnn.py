@@ -253,6 +253,61 @@ def test_pool_input_mse_adam_seed(env):
     assert np.allclose(U.cpu().numpy(), ref, atol=1e-5)
 
 
+def test_input_moments_device_pool_and_mirror(env):
+    """The one-pass image moments against float64 sums; pooling with the
+    statistics taken on the device equals pooling with the same statistics
+    computed on the host (bit for bit); mirroring the pooled grid equals
+    pooling the mirrored pair where the pooling grid is symmetric (up to the
+    FP32 summation order of a window)."""
+    torch, L, S = env
+    lib = L.lib()
+    rng = np.random.default_rng(9)
+    nx, ny, nz = 21, 13, 9  # (n - 1) % 4 == 0 along every axis
+    f = (rng.random((nz, ny, nx)) * 3 + 1).astype(np.float32)
+    g = (rng.random((nz, ny, nx)) * 2 - 0.5).astype(np.float32)
+    fd, gd = torch.from_numpy(f.reshape(-1)).cuda(), torch.from_numpy(g.reshape(-1)).cuda()
+    n = f.size
+    sums = torch.zeros(4, dtype=torch.float64, device="cuda")
+    ws = torch.empty(1 << 16, dtype=torch.uint8, device="cuda")
+    L.check(lib.vdvc_cnn_input_moments(fd.data_ptr(), gd.data_ptr(), n, sums.data_ptr(), ws.data_ptr(), ws.numel(),
+                                       stream(torch)))
+    hs = sums.cpu().numpy()
+    f64, g64 = f.astype(np.float64), g.astype(np.float64)
+    ref = np.array([f64.sum(), (f64 * f64).sum(), g64.sum(), (g64 * g64).sum()])
+    assert np.allclose(hs, ref, rtol=1e-6)
+    # an unaligned tail (no float4 path) gives the same sums
+    L.check(lib.vdvc_cnn_input_moments(fd[1:].data_ptr(), gd[1:].data_ptr(), n - 1, sums.data_ptr(), ws.data_ptr(),
+                                       ws.numel(), stream(torch)))
+    ref1 = np.array([f64.reshape(-1)[1:].sum(), (f64.reshape(-1)[1:] ** 2).sum(), g64.reshape(-1)[1:].sum(),
+                     (g64.reshape(-1)[1:] ** 2).sum()])
+    assert np.allclose(sums.cpu().numpy(), ref1, rtol=1e-6)
+    mf, mg = hs[0] / n, hs[2] / n
+    ms = np.array([mf, np.sqrt(hs[1] / n - mf * mf), mg, np.sqrt(hs[3] / n - mg * mg)])
+    sums.copy_(torch.from_numpy(hs))
+    gx, gy, gz = (nx - 1) // 4 + 1, (ny - 1) // 4 + 1, (nz - 1) // 4 + 1
+    x0 = torch.zeros(gx * gy * gz * 2, dtype=torch.bfloat16, device="cuda")
+    for flip in range(8):
+        a = torch.zeros_like(x0)
+        b = torch.zeros_like(x0)
+        L.check(lib.vdvc_cnn_pool_input_dev(fd.data_ptr(), gd.data_ptr(), nx, ny, nz, sums.data_ptr(), flip,
+                                            a.data_ptr(), stream(torch)))
+        L.check(lib.vdvc_cnn_pool_input_mirrored(fd.data_ptr(), gd.data_ptr(), nx, ny, nz, ms.ctypes.data_as(L.pd),
+                                                 flip, b.data_ptr(), stream(torch)))
+        assert torch.equal(a, b), flip
+        if flip == 0:
+            x0.copy_(a)
+        else:
+            m = torch.zeros_like(x0)
+            L.check(lib.vdvc_cnn_mirror_input(x0.data_ptr(), gx, gy, gz, flip, m.data_ptr(), stream(torch)))
+            # the same windows summed in the mirrored FP32 order: an element
+            # may round to the neighbouring BF16 value
+            mf32, bf32 = m.float(), b.float()
+            assert torch.allclose(mf32, bf32, rtol=2.0 ** -7, atol=1e-30), flip
+            assert (mf32 != bf32).float().mean().item() < 0.01, flip
+    with pytest.raises(Exception):
+        L.check(lib.vdvc_cnn_mirror_input(x0.data_ptr(), gx, gy, gz, 1, x0.data_ptr(), stream(torch)))
+
+
 def test_mirrored_pool_and_seed(env):
     """The mirrored input pooling equals the pooling of the mirrored images,
     and a mirrored pass's output accumulated into the seed equals the

@@ -137,6 +137,9 @@ SIGNATURES = {
     "vdvc_cnn_upsample2_bwd": (ci, [vp, ci, ci, ci, ci, ci, vp, ci, ci, ci, ci, ci, ci, vp]),
     "vdvc_cnn_pool_input": (ci, [vp, vp, ci, ci, ci, pd, vp, vp]),
     "vdvc_cnn_pool_input_mirrored": (ci, [vp, vp, ci, ci, ci, pd, ci, vp, vp]),
+    "vdvc_cnn_input_moments": (ci, [vp, vp, C.c_longlong, vp, vp, cz, vp]),
+    "vdvc_cnn_pool_input_dev": (ci, [vp, vp, ci, ci, ci, vp, ci, vp, vp]),
+    "vdvc_cnn_mirror_input": (ci, [vp, ci, ci, ci, ci, vp, vp]),
     "vdvc_cnn_mse": (ci, [vp, ci, vp, C.c_longlong, vp, vp, ci, cd, vp, cz, vp]),
     "vdvc_cnn_adam": (ci, [vp, vp, vp, vp, C.c_longlong, cd, cd, cd, cd, ci, vp]),
     "vdvc_cnn_pack_weights": (ci, [vp, ci, ci, vp, vp, vp]),

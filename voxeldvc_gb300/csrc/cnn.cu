@@ -396,11 +396,28 @@ __global__ void k_upsample2_bwd(const bf16* __restrict__ df, int fcs, int fcoff,
   }
 }
 
+// Mean and 1/std of an image from its sums (s, s2) over n voxels, as the
+// host computes them: mean = s / n, var = s2 / n - mean^2, std = sqrt(var)
+// (1 where var <= 0).
+__device__ __forceinline__ void standardise_from_sums(double s, double s2, double n, float& mean, float& inv_std) {
+  const double m = s / n;
+  const double var = __dsub_rn(s2 / n, __dmul_rn(m, m));  // no FMA contraction: the host's rounding
+  mean = (float)m;
+  inv_std = (float)(1.0 / (var > 0.0 ? sqrt(var) : 1.0));
+}
+
 // flip (bit 0 x, 1 y, 2 z): pool the image mirrored along those axes.
+// sums (device {sum f, sum f^2, sum g, sum g^2}, or null): the standardising
+// statistics are computed from them instead of taken from mf..isg.
 __global__ void k_pool_input(const float* __restrict__ f, const float* __restrict__ gimg, int nx, int ny, int nz,
                              int gx, int gy, int gz, float mf, float isf, float mg, float isg, int flip,
-                             bf16* __restrict__ out) {
+                             const double* __restrict__ sums, bf16* __restrict__ out) {
   const long long n = (long long)gx * gy * gz;
+  if (sums) {
+    const double nv = (double)nx * ny * nz;
+    standardise_from_sums(sums[0], sums[1], nv, mf, isf);
+    standardise_from_sums(sums[2], sums[3], nv, mg, isg);
+  }
   const float tw[5] = {1.f, 2.f, 2.f, 2.f, 1.f};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(i % gx);
@@ -429,6 +446,53 @@ __global__ void k_pool_input(const float* __restrict__ f, const float* __restric
     }
     out[2 * i] = __float2bfloat16_rn((sf / sw - mf) * isf);
     out[2 * i + 1] = __float2bfloat16_rn((sg / sw - mg) * isg);
+  }
+}
+
+// Sums of f, f^2, g and g^2 in one read of each image: float4 loads, the
+// four elements' sums in FP32, one FP64 add per quantity and float4 (FP64
+// per element would run on GB300's narrow FP64 pipe).
+__global__ void __launch_bounds__(256) k_moments2(const float* __restrict__ f, const float* __restrict__ g, long long n,
+                                                  bool vec4, GridReduce red, double* __restrict__ out) {
+  __shared__ double s_red[8];
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i0 = 0;
+  if (vec4) {
+    const long long n4 = n >> 2;
+    for (long long q = gtid; q < n4; q += stride) {
+      const float4 x = __ldg((const float4*)f + q), y = __ldg((const float4*)g + q);
+      a0 += (double)((x.x + x.y) + (x.z + x.w));
+      a1 += (double)(x.x * x.x + x.y * x.y + x.z * x.z + x.w * x.w);
+      a2 += (double)((y.x + y.y) + (y.z + y.w));
+      a3 += (double)(y.x * y.x + y.y * y.y + y.z * y.z + y.w * y.w);
+    }
+    i0 = n4 << 2;
+  }
+  for (long long i = i0 + gtid; i < n; i += stride) {
+    const double x = (double)f[i], y = (double)g[i];
+    a0 += x;
+    a1 += x * x;
+    a2 += y;
+    a3 += y * y;
+  }
+  double mine[4] = {block_sum(a0, s_red), block_sum(a1, s_red), block_sum(a2, s_red), block_sum(a3, s_red)}, o[4];
+  if (grid_reduce_sum<4>(red, mine, o, s_red) && threadIdx.x == 0)
+    for (int k = 0; k < 4; ++k) out[k] = o[k];
+}
+
+// out = x mirrored along the axes of flip; one position = two BF16
+// channels = one 32-bit word.
+__global__ void k_mirror_input(const uint32_t* __restrict__ x, int gx, int gy, int gz, int flip,
+                               uint32_t* __restrict__ out) {
+  const long long n = (long long)gx * gy * gz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int px = (int)(i % gx);
+    const long long rr = i / gx;
+    const int py = (int)(rr % gy), pz = (int)(rr / gy);
+    const int sx = (flip & 1) ? gx - 1 - px : px, sy = (flip & 2) ? gy - 1 - py : py, sz = (flip & 4) ? gz - 1 - pz : pz;
+    out[i] = x[((long long)sz * gy + sy) * gx + sx];
   }
 }
 
@@ -760,7 +824,45 @@ int vdvc_cnn_pool_input_mirrored(const float* f_vox, const float* g_vox, int nx,
   const long long n = (long long)gx * gy * gz;
   k_pool_input<<<eblocks(n), 256, 0, (cudaStream_t)stream>>>(f_vox, g_vox, nx, ny, nz, gx, gy, gz, (float)mean_std[0],
                                                              (float)(1.0 / mean_std[1]), (float)mean_std[2],
-                                                             (float)(1.0 / mean_std[3]), flip, (bf16*)out);
+                                                             (float)(1.0 / mean_std[3]), flip, nullptr, (bf16*)out);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_cnn_input_moments(const float* f_vox, const float* g_vox, long long n, double* sums, void* ws,
+                           size_t ws_bytes, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(f_vox && g_vox && sums && n >= 1, "bad arguments");
+  Carve cv(ws, ws_bytes);
+  GridReduce red;
+  red.partials = cv.take<double>(4 * kReduceBlocks);
+  red.ticket = cv.take<unsigned int>(1);
+  VDVC_CHECK_ARG(ws && cv.fits(), "input moments need %zu bytes of workspace", cv.off);
+  cudaStream_t s = (cudaStream_t)stream;
+  VDVC_CUDA(cudaMemsetAsync(red.ticket, 0, sizeof(unsigned int), s));
+  const bool vec4 = (((uintptr_t)f_vox | (uintptr_t)g_vox) & 15u) == 0;
+  k_moments2<<<grid_blocks(vec4 ? (n + 3) / 4 : n, 256, kReduceBlocks), 256, 0, s>>>(f_vox, g_vox, n, vec4, red, sums);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_cnn_pool_input_dev(const float* f_vox, const float* g_vox, int nx, int ny, int nz, const double* sums,
+                            int flip, void* out, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(f_vox && g_vox && out && sums && nx >= 1 && ny >= 1 && nz >= 1, "bad arguments");
+  VDVC_CHECK_ARG(flip >= 0 && flip <= 7, "flip is a bit mask of the axes x (1), y (2), z (4)");
+  const int gx = (nx - 1) / 4 + 1, gy = (ny - 1) / 4 + 1, gz = (nz - 1) / 4 + 1;
+  const long long n = (long long)gx * gy * gz;
+  k_pool_input<<<eblocks(n), 256, 0, (cudaStream_t)stream>>>(f_vox, g_vox, nx, ny, nz, gx, gy, gz, 0.f, 1.f, 0.f, 1.f,
+                                                             flip, sums, (bf16*)out);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_cnn_mirror_input(const void* x, int gx, int gy, int gz, int flip, void* out, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(x && out && x != out && gx >= 1 && gy >= 1 && gz >= 1, "bad arguments");
+  VDVC_CHECK_ARG(flip >= 0 && flip <= 7, "flip is a bit mask of the axes x (1), y (2), z (4)");
+  VDVC_CHECK_ARG(al4(x) && al4(out), "x and out must be 4-byte aligned");
+  const long long n = (long long)gx * gy * gz;
+  k_mirror_input<<<eblocks(n), 256, 0, (cudaStream_t)stream>>>((const uint32_t*)x, gx, gy, gz, flip, (uint32_t*)out);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }

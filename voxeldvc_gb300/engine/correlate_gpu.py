@@ -547,11 +547,23 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
                  c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False,
                  freeze_mask_after=None, U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
                  disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=4,
-                 hessian='auto'):
+                 hessian='auto', U0_async=None):
+    """One pyramid level: set-up, GN iterations, read-back.  U0_async:
+    (U0 float64 CUDA tensor, CUDA event or None) produced on another stream
+    -- the set-up is enqueued first and only the iterations wait for it."""
+    if U0_async is not None and U0 is not None:
+        raise ValueError("give U0 or U0_async, not both")
     ls = _setup_level(lv, Nx, Ny, Nz, h, g_origin=g_origin, glt=glt, l0=l0, K_ref_laplacian=K_ref_laplacian,
                       reg_exponent=reg_exponent, c_reg=c_reg, reg_type=reg_type, K_ref_elastic=K_ref_elastic,
                       eps_reg=eps_reg, dynamic_mask=dynamic_mask, U0=U0, maxiter=maxiter, disp=disp, dtype=dtype,
                       pcg_chunk=pcg_chunk, precision=precision, mixed_min_h=mixed_min_h, hessian=hessian)
+    if U0_async is not None:
+        U0d, ready = U0_async
+        if ready is not None:
+            D.torch().cuda.current_stream().wait_event(ready)
+        if U0d.numel() != ls.Ndof:
+            raise ValueError(f"U0 has {U0d.numel()} entries, expected {ls.Ndof}")
+        ls.U64 = U0d.reshape(-1).to(D.torch().float64)
     out_dt, Nvox, Ndof, U64 = ls.out_dt, ls.Nvox, ls.Ndof, ls.U64
     if ls.empty:
         return U64.to(D.torch_dtype(out_dt)), D.zeros(Nvox, out_dt), D.zeros(Ndof, out_dt), {}

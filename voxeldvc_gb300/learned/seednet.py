@@ -305,12 +305,20 @@ class SeedNet:
 
     # ---- inputs ------------------------------------------------------------------
 
-    def set_input(self, f_vox, g_vox, shape, train=True, flip=0, slot=0, mean_std=None):
+    def set_input(self, f_vox, g_vox, shape, train=True, flip=0, slot=0, mean_std=None, sums=None):
         """Pool f and g (FP32 vox-layout CUDA tensors of `shape` voxels),
         mirrored along the axes of `flip` (bit 0 x, 1 y, 2 z), into the input
-        buffer; returns the input grid."""
+        buffer; returns the input grid.  The standardising statistics come
+        from `mean_std` (host [mean_f, std_f, mean_g, std_g]), or from
+        `sums` (device, input_moments) without a host read-back, or are
+        computed here."""
         G = input_grid(shape)
         b = self.buffers(G, train, slot)
+        if sums is not None:
+            _lib.check(_lib.lib().vdvc_cnn_pool_input_dev(f_vox.data_ptr(), g_vox.data_ptr(), *shape,
+                                                          sums.data_ptr(), int(flip), b["x"].data_ptr(), D.stream()),
+                       "cnn_pool_input_dev")
+            return G
         ms = mean_std if mean_std is not None else np.array(_mean_std_many(f_vox, g_vox), np.float64)
         _lib.check(_lib.lib().vdvc_cnn_pool_input_mirrored(f_vox.data_ptr(), g_vox.data_ptr(), *shape,
                                                            ms.ctypes.data_as(_lib.pd), int(flip), b["x"].data_ptr(),
@@ -329,33 +337,62 @@ class SeedNet:
         ok = [(s - 1) % OUT_STRIDE == 0 and N * h == s - 1 for s, N in zip(shape, (Nx, Ny, Nz))]
         return tuple(m for m in self.MIRRORS[passes] if all(ok[k] or not (m >> k) & 1 for k in range(3)))
 
-    def predict_nodes(self, f_vox, g_vox, shape, h, Nx, Ny, Nz, passes=1):
+    def predict_nodes(self, f_vox, g_vox, shape, h, Nx, Ny, Nz, passes=1, wait=True):
         """Seed U (float64 CUDA tensor, 3 (Nx+1)(Ny+1)(Nz+1)) for a mesh of
         edge h over a volume of `shape` voxels.  passes > 1: the mean of the
-        predictions for the pair and its mirror images (1, 2 or 4 passes;
-        the mirrored passes run on side streams, concurrently with the
-        first)."""
+        predictions for the pair and its mirror images (1, 2 or 4 passes).
+
+        Everything runs on side streams, ordered after the work already on
+        the caller's stream: the image moments and the pooled input of the
+        first pass (no host read-back), the mirrored passes' inputs as
+        mirror images of that pooled grid (mirrors_for only admits axes
+        along which the pooling grid is symmetric; the same windows summed
+        in the mirrored FP32 order), the passes concurrently,
+        then the nodal resampling.  wait=True: the caller's stream waits for
+        the seed and U is returned; wait=False: (U, event) is returned and
+        the caller's stream is free for independent work until it waits on
+        the event."""
         torch = D.torch()
+        L = _lib.lib()
         mirrors = self.mirrors_for(shape, h, Nx, Ny, Nz, passes)
-        ms = np.array(_mean_std_many(f_vox, g_vox), np.float64)
-        U = D.empty(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), np.float64)
         main = torch.cuda.current_stream()
+        U = D.empty(3 * (Nx + 1) * (Ny + 1) * (Nz + 1), np.float64)
         ready = torch.cuda.Event()
         ready.record(main)
-        preds = []
-        for k, flip in enumerate(mirrors):
-            st = main if k == 0 else self._side_stream(k)
+        s0 = self._side_stream(0)
+        with torch.cuda.stream(s0):
+            s0.wait_event(ready)
+            sums = D.zeros(4, np.float64)
+            ws = D.scratch.get(1 << 16)
+            _lib.check(L.vdvc_cnn_input_moments(f_vox.data_ptr(), g_vox.data_ptr(), f_vox.numel(), sums.data_ptr(),
+                                                ws.data_ptr(), ws.numel(), D.stream()), "cnn_input_moments")
+            G = self.set_input(f_vox, g_vox, shape, train=False, flip=mirrors[0], slot=0, sums=sums)
+            pooled = torch.cuda.Event()
+            pooled.record(s0)
+            preds = [(self.forward(G, train=False, slot=0), mirrors[0], s0)]
+        x0 = self.buffers(G, False, 0)["x"]
+        for k, flip in enumerate(mirrors[1:], 1):
+            st = self._side_stream(k)
             with torch.cuda.stream(st):
-                st.wait_event(ready)
-                G = self.set_input(f_vox, g_vox, shape, train=False, flip=flip, slot=k, mean_std=ms)
+                st.wait_event(pooled)
+                _lib.check(L.vdvc_cnn_mirror_input(x0.data_ptr(), *G, int(flip ^ mirrors[0]),
+                                                   self.buffers(G, False, k)["x"].data_ptr(), D.stream()),
+                           "cnn_mirror_input")
                 preds.append((self.forward(G, train=False, slot=k), flip, st))
-        n = self.buffers(input_grid(shape), train=False)["lv"][1]
+        n = self.buffers(G, train=False)["lv"][1]
         w = 1.0 / len(mirrors)
-        for k, (pred, flip, st) in enumerate(preds):
-            if st is not main:
-                main.wait_stream(st)
-            _lib.check(_lib.lib().vdvc_cnn_seed_nodes_acc(pred.data_ptr(), 8, *n, h, Nx, Ny, Nz, int(flip), w,
-                                                          int(k > 0), U.data_ptr(), D.stream()), "cnn_seed_nodes")
+        with torch.cuda.stream(s0):
+            for _, _, st in preds[1:]:
+                s0.wait_stream(st)
+            for k, (pred, flip, _) in enumerate(preds):
+                _lib.check(L.vdvc_cnn_seed_nodes_acc(pred.data_ptr(), 8, *n, h, Nx, Ny, Nz, int(flip), w, int(k > 0),
+                                                     U.data_ptr(), D.stream()), "cnn_seed_nodes")
+            done = torch.cuda.Event()
+            done.record(s0)
+        U.record_stream(s0)
+        if not wait:
+            return U, done
+        main.wait_event(done)
         return U
 
     def _side_stream(self, k):

@@ -48,18 +48,25 @@ def learned_seed(f_pix, g_pix, Nx, Ny, Nz, h, g_origin=(0, 0, 0), net=None, seed
     return _seed_vox(f_vox, fs, g_vox, gs, Nx, Ny, Nz, h, g_origin, net, seed_passes)
 
 
-def _seed_vox(f_vox, fs, g_vox, gs, Nx, Ny, Nz, h, g_origin, net, seed_passes=SEED_PASSES):
+def _seed_vox(f_vox, fs, g_vox, gs, Nx, Ny, Nz, h, g_origin, net, seed_passes=SEED_PASSES, wait=True):
+    """The seed (float64 CUDA, Ndof); wait=False: (seed, event or None), the
+    network running on side streams until the caller's stream waits on the
+    event."""
     net = net or default_net()
     if tuple(fs) != tuple(gs):
         raise ValueError("the learned seed needs f and g of one shape")
-    U0 = net.predict_nodes(f_vox, g_vox, fs, h, Nx, Ny, Nz, passes=seed_passes)
+    U0, ready = net.predict_nodes(f_vox, g_vox, fs, h, Nx, Ny, Nz, passes=seed_passes, wait=False)
     if any(o != 0 for o in g_origin):
         # the network sees g in its own array frame: u = u_array + g_origin
-        Uh = U0.cpu().numpy()
-        for c in range(3):
-            Uh[c::3] += float(g_origin[c])
-        U0 = D.to_device(Uh)
-    return U0
+        torch = D.torch()
+        torch.cuda.current_stream().wait_event(ready)
+        ready = None
+        U0.view(-1, 3).add_(torch.tensor([float(o) for o in g_origin], dtype=torch.float64, device=U0.device))
+    if wait:
+        if ready is not None:
+            D.torch().cuda.current_stream().wait_event(ready)
+        return U0
+    return U0, ready
 
 
 def learned_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0), l0=None, net=None,
@@ -77,19 +84,22 @@ def learned_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0), l
     # and (for a float32 solve) the GN level
     f32, fs = CG.pix_to_vox(f_pix, np.float32)
     g32, gs = CG.pix_to_vox(g_pix, np.float32)
+    # the network runs on side streams while this stream sets the level up
+    # (gradient, masks, statistics, regularization weight); the GN
+    # iterations wait for the seed
     try:
-        U0 = _seed_vox(f32, fs, g32, gs, Nx, Ny, Nz, h, g_origin, net, seed_passes)
+        seed = _seed_vox(f32, fs, g32, gs, Nx, Ny, Nz, h, g_origin, net, seed_passes, wait=False)
     except ValueError as e:
-        U0, reason = None, str(e)
+        seed, reason = None, str(e)
     seed_s = time.perf_counter() - t0
-    if U0 is not None:
+    if seed is not None:
         if dtype == np.float32:
             f_vox, g_vox = f32, g32
         else:
             f_vox, fs = CG.pix_to_vox(f_pix, dtype)
             g_vox, gs = CG.pix_to_vox(g_pix, dtype)
         U, res, dU, info = CG._solve_level(CG._Level(f_vox, fs, g_vox, gs), Nx, Ny, Nz, h, g_origin=g_origin, l0=l0,
-                                           U0=U0, stats=levels, **kwargs)
+                                           U0_async=seed, stats=levels, **kwargs)
         rho = info.get("norm_res", float("inf"))
         if np.isfinite(rho) and rho <= fallback_threshold and info.get("converged", False):
             levels.append(dict(seed="learned", norm_res=rho, seed_s=seed_s))
