@@ -460,13 +460,27 @@ __global__ void __launch_bounds__(256) k_moments2(const float* __restrict__ f, c
   const long long stride = (long long)gridDim.x * blockDim.x;
   long long i0 = 0;
   if (vec4) {
+    // four grid strides per trip: eight 16-byte loads in flight per thread
     const long long n4 = n >> 2;
-    for (long long q = gtid; q < n4; q += stride) {
-      const float4 x = __ldg((const float4*)f + q), y = __ldg((const float4*)g + q);
-      a0 += (double)((x.x + x.y) + (x.z + x.w));
-      a1 += (double)(x.x * x.x + x.y * x.y + x.z * x.z + x.w * x.w);
-      a2 += (double)((y.x + y.y) + (y.z + y.w));
-      a3 += (double)(y.x * y.x + y.y * y.y + y.z * y.z + y.w * y.w);
+    for (long long q0 = gtid; q0 < n4; q0 += 4 * stride) {
+      float4 x[4], y[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const long long q = q0 + u * stride;
+        if (q < n4) {
+          x[u] = __ldg((const float4*)f + q);
+          y[u] = __ldg((const float4*)g + q);
+        } else {
+          x[u] = y[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a0 += (double)((x[u].x + x[u].y) + (x[u].z + x[u].w));
+        a1 += (double)(x[u].x * x[u].x + x[u].y * x[u].y + x[u].z * x[u].z + x[u].w * x[u].w);
+        a2 += (double)((y[u].x + y[u].y) + (y[u].z + y[u].w));
+        a3 += (double)(y[u].x * y[u].x + y[u].y * y[u].y + y[u].z * y[u].z + y[u].w * y[u].w);
+      }
     }
     i0 = n4 << 2;
   }

@@ -7,21 +7,34 @@
 namespace vdvc {
 namespace {
 
-// C-order (nx,ny,nz) -> x-fastest, one y plane per blockIdx.z, 32x32
-// (z,x) tiles staged through shared memory so both sides are coalesced.
+// C-order (nx,ny,nz) -> x-fastest: 32x32 (z,x) tiles of kP2vPlanes
+// consecutive y planes per block (blockIdx.z), staged through shared memory
+// so both sides are coalesced; a thread has 4 * kP2vPlanes loads in flight.
+constexpr int kP2vPlanes = 4;
+
 template <typename Tin, typename Tout>
 __global__ void __launch_bounds__(256) k_pix_to_vox(const Tin* __restrict__ in, Tout* __restrict__ out,
                                                     int nx, int ny, int nz) {
-  __shared__ Tout tile[32][33];
-  const int z0 = blockIdx.x * 32, x0 = blockIdx.y * 32, y = blockIdx.z;
-  for (int r = threadIdx.y; r < 32; r += 8) {
-    const int x = x0 + r, z = z0 + threadIdx.x;
-    if (x < nx && z < nz) tile[r][threadIdx.x] = (Tout)in[((size_t)x * ny + y) * nz + z];
+  __shared__ Tout tile[kP2vPlanes][32][33];
+  const int z0 = blockIdx.x * 32, x0 = blockIdx.y * 32, y0 = blockIdx.z * kP2vPlanes;
+#pragma unroll
+  for (int p = 0; p < kP2vPlanes; ++p) {
+    const int y = y0 + p;
+#pragma unroll
+    for (int r = threadIdx.y; r < 32; r += 8) {
+      const int x = x0 + r, z = z0 + threadIdx.x;
+      if (y < ny && x < nx && z < nz) tile[p][r][threadIdx.x] = (Tout)in[((size_t)x * ny + y) * nz + z];
+    }
   }
   __syncthreads();
-  for (int r = threadIdx.y; r < 32; r += 8) {
-    const int z = z0 + r, x = x0 + threadIdx.x;
-    if (x < nx && z < nz) out[(size_t)x + (size_t)y * nx + (size_t)z * nx * ny] = tile[threadIdx.x][r];
+#pragma unroll
+  for (int p = 0; p < kP2vPlanes; ++p) {
+    const int y = y0 + p;
+#pragma unroll
+    for (int r = threadIdx.y; r < 32; r += 8) {
+      const int z = z0 + r, x = x0 + threadIdx.x;
+      if (y < ny && x < nx && z < nz) out[(size_t)x + (size_t)y * nx + (size_t)z * nx * ny] = tile[p][threadIdx.x][r];
+    }
   }
 }
 
@@ -102,7 +115,7 @@ inline int grid_for(long long n, int threads) {
 
 template <typename Tin, typename Tout>
 int launch_p2v(const void* pix, int nx, int ny, int nz, void* vox, cudaStream_t s) {
-  dim3 grid((nz + 31) / 32, (nx + 31) / 32, ny), block(32, 8);
+  dim3 grid((nz + 31) / 32, (nx + 31) / 32, (ny + kP2vPlanes - 1) / kP2vPlanes), block(32, 8);
   k_pix_to_vox<Tin, Tout><<<grid, block, 0, s>>>((const Tin*)pix, (Tout*)vox, nx, ny, nz);
   VDVC_LAUNCHED();
   return VDVC_OK;

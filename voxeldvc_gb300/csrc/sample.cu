@@ -18,29 +18,55 @@ namespace vdvc {
 
 // Rows (y,z) are distributed over blocks, x over threads, so the y/z
 // multiplicities are uniform per row; per-row float partials are folded into
-// float64 accumulators once per row.
+// float64 accumulators once per row.  A block takes kStatsRows of its rows
+// per trip with every mask byte and value loaded before any is used (the
+// loads of a row would otherwise wait on one another through the mask
+// test); the per-row partials and their fold order are those of one row at
+// a time.
+constexpr int kStatsRows = 4;
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_masked_stats(const T* __restrict__ field, const uint8_t* __restrict__ mask,
                                                       const Mesh m, GridReduce red, double* __restrict__ out3) {
   __shared__ double s_red[8];
   double acc[3] = {0.0, 0.0, 0.0};
   const long long nrows = (long long)m.Nvy * m.Nvz;
-  for (long long row = blockIdx.x; row < nrows; row += gridDim.x) {
-    const int y = (int)(row % m.Nvy), z = (int)(row / m.Nvy);
-    const int myz = axis_multiplicity(y, m.h, m.Ny) * axis_multiplicity(z, m.h, m.Nz);
-    float c = 0.f, s1 = 0.f, s2 = 0.f;
-    const long long base = row * m.Nvx;
-    for (int x = threadIdx.x; x < m.Nvx; x += blockDim.x) {
-      if (!mask[base + x]) continue;
-      const float mult = (float)(myz * axis_multiplicity(x, m.h, m.Nx));
-      const float v = (float)field[base + x];
-      c += mult;
-      s1 += mult * v;
-      s2 += mult * v * v;
+  for (long long row0 = blockIdx.x; row0 < nrows; row0 += (long long)kStatsRows * gridDim.x) {
+    float c[kStatsRows], s1[kStatsRows], s2[kStatsRows];
+    int myz[kStatsRows];
+    long long base[kStatsRows];
+#pragma unroll
+    for (int r = 0; r < kStatsRows; ++r) {
+      const long long row = row0 + (long long)r * gridDim.x;
+      const int y = (int)(row % m.Nvy), z = (int)(row / m.Nvy);
+      myz[r] = row < nrows ? axis_multiplicity(y, m.h, m.Ny) * axis_multiplicity(z, m.h, m.Nz) : 0;
+      base[r] = row < nrows ? row * m.Nvx : 0;
+      c[r] = s1[r] = s2[r] = 0.f;
     }
-    acc[0] += c;
-    acc[1] += s1;
-    acc[2] += s2;
+    for (int x = threadIdx.x; x < m.Nvx; x += blockDim.x) {
+      uint8_t mk[kStatsRows];
+      float v[kStatsRows];
+#pragma unroll
+      for (int r = 0; r < kStatsRows; ++r) {
+        mk[r] = myz[r] ? __ldg(mask + base[r] + x) : (uint8_t)0;
+        v[r] = myz[r] ? (float)__ldg(field + base[r] + x) : 0.f;
+      }
+      const int mx = axis_multiplicity(x, m.h, m.Nx);
+#pragma unroll
+      for (int r = 0; r < kStatsRows; ++r) {
+        if (!mk[r]) continue;
+        const float mult = (float)(myz[r] * mx);
+        c[r] += mult;
+        s1[r] += mult * v[r];
+        s2[r] += mult * v[r] * v[r];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kStatsRows; ++r) {
+      acc[0] += c[r];
+      acc[1] += s1[r];
+      acc[2] += s2[r];
+    }
   }
   double b3[3], o3[3];
   for (int q = 0; q < 3; ++q) b3[q] = block_sum(acc[q], s_red);
