@@ -18,7 +18,8 @@
 // the PCG applies H from T.  Once the b mask is frozen (or with a fixed
 // mask0), H, diag and M^-1 no longer change and are formed only once.
 // VDVC_PREC_ELEMENT forms T from the float32 gradient; VDVC_PREC_MIXED (the
-// precision form) from its BF16 rounding, made once at create.
+// precision form) from its BF16 rounding, made once at create, and keeps T
+// in BF16 (FP32 under the equilibrium-gap regularizer).
 #include <cstdlib>
 #include <new>
 #include <type_traits>
@@ -62,6 +63,7 @@ struct GnSolver {
   // element-Hessian forms
   bool eh;           // the PCG applies H from element Hessians
   bool eh_bf16;      // ... formed from the BF16 gradient (precision form)
+  bool eh_T_bf16;    // ... and stored in BF16 (precision form, no equilibrium-gap term)
   bool eh_fixed;     // T, diag and M^-1 are final (b mask frozen, or mask0)
   float* T_eh;       // [162][Ne] element Hessians
   void* grad_bf16;   // (Nvox,3) BF16 (precision form only)
@@ -343,6 +345,7 @@ static int pcg_iteration(GnSolver<T>* S, cudaStream_t s) {
       EhMatvecArgs ma{};
       ma.m = S->m;
       ma.T = S->T_eh;
+      ma.Tb = S->eh_T_bf16 ? (const void*)S->T_eh : nullptr;  // the precision form keeps BF16 entries
       ma.pitch = eh_pitch(S->m.Ne);
       ma.err = &S->sc->status;  // read with the GN scalars after the iteration
       ma.v = S->z;
@@ -450,6 +453,10 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   carve_solver<T>(m, S, ws, ws_bytes);
   S->eh = d->precision == VDVC_PREC_MIXED || d->precision == VDVC_PREC_ELEMENT;
   S->eh_bf16 = d->precision == VDVC_PREC_MIXED;
+  // The equilibrium-gap system keeps FP32 entries: its PCG runs hundreds of
+  // iterations on a stiff operator and, within a GN iteration cap, ends
+  // where the rounding of H steers the Krylov trajectory.
+  S->eh_T_bf16 = S->eh_bf16 && d->reg_type != VDVC_REG_EQUILIBRIUM_GAP;
   if (d->precision != VDVC_PREC_PLAIN && !S->eh) {
     delete S;
     return set_error(VDVC_ERR_ARG, "precision %d", d->precision);
@@ -555,7 +562,8 @@ static int set_U(GnSolver<T>* S, const double* U0, cudaStream_t s) {
 template <typename T>
 static EhFormArgs eh_form_args(GnSolver<T>* S, const uint8_t* mask) {
   EhFormArgs fa{S->m, S->eh_bf16 ? S->grad_bf16 : S->d.grad, mask, S->T_eh, (float*)S->evD, eh_pitch(S->m.Ne),
-                S->eh_bf16 ? S->gmax : nullptr, &S->sc->status, S->eh_bf16 ? 0 : 1};
+                S->eh_bf16 ? S->gmax : nullptr, &S->sc->status, S->eh_bf16 ? 0 : 1,
+                S->eh_T_bf16 ? (void*)S->T_eh : nullptr};
   return fa;
 }
 

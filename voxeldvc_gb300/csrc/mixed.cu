@@ -2,7 +2,12 @@
 // Gauss-Newton iteration with FP32 accumulation, FP32 element-Hessian
 // matvecs in the PCG.  The gradient is either the float32 gradient itself
 // (VDVC_PREC_ELEMENT: the plain solve's arithmetic in another summation
-// order) or its BF16 rounding (VDVC_PREC_MIXED, the precision form).
+// order) or its BF16 rounding (VDVC_PREC_MIXED, the precision form).  The
+// precision form's GN solver also stores the 162 entries in BF16 (rounded
+// once from their FP32 sums; the matvec accumulates in FP32): half the bytes
+// of the PCG's dominant stream.  The fixed point of the GN iteration is set
+// by the FP32 residual and right-hand side, not by H.  Under the
+// equilibrium-gap regularizer the entries stay FP32 (gn.cu).
 //
 // Element Hessian structure.  With owner-computes quadrature (strip.cuh),
 //   K_e[(a,k),(b,l)] = sum_q w_q m_q N_a(q) N_b(q) g_k(q) g_l(q),
@@ -18,6 +23,8 @@
 // the BF16 gradient itself; from the float32 gradient G is rounded once, as
 // the matrix-free pass rounds its products.
 #include <cuda_bf16.h>
+
+#include <type_traits>
 
 #include "ops.cuh"
 #include "pcg.cuh"
@@ -132,7 +139,11 @@ __global__ void __launch_bounds__(128) k_eh_form(const EhFormArgs a) {
     }
     if (last_strip && e == nel - 1 && sx == 2) s += s_R[nthr * kRP + rest];  // column x = Nx*h: psi = (0,0,1)
     const long long eg = e_base + e;  // tile-major: [tile][162][kEhTile]
-    a.T[((eg / kEhTile) * 162 + o) * kEhTile + (eg % kEhTile)] = s;
+    const long long ti = ((eg / kEhTile) * 162 + o) * kEhTile + (eg % kEhTile);
+    if (a.Tb)
+      ((__nv_bfloat16*)a.Tb)[ti] = __float2bfloat16_rn(s);
+    else
+      a.T[ti] = s;
     // diagonal of K_e: a = (sx/2, sy/2, sz/2) with sx,sy,sz in {0,2}, kl in {00,11,22}
     const int sy = rest / 18, sz = (rest / 6) % 3, kl = rest % 6;
     if ((sx & 1) == 0 && (sy & 1) == 0 && (sz & 1) == 0 && (kl == 0 || kl == 3 || kl == 5)) {
@@ -167,7 +178,7 @@ static int launch_form(const EhFormArgs& args, cudaStream_t s) {
 }
 
 int launch_eh_form(const EhFormArgs& a, cudaStream_t s) {
-  if (!a.grad_f32) {
+  if (!a.grad_f32 && !a.Tb) {
     const int tc = launch_eh_form_tc(a, s);  // tcgen05 formation where it is built (h = 6, 8)
     if (tc != VDVC_ERR_UNSUPPORTED) return tc;
   }
@@ -187,7 +198,8 @@ int launch_eh_form(const EhFormArgs& a, cudaStream_t s) {
 // ---- TMA-staged element-Hessian matvec --------------------------------------
 //
 // T is stored tile-major, [tile][162][kEhTile]: a tile's 162 entry rows of
-// kEhTile elements are one contiguous 41.5 KB span.  A block owns one tile:
+// kEhTile elements are one contiguous 41.5 KB span (20.7 KB for the BF16
+// entries of the precision form, read into FP32 arithmetic).  A block owns one tile:
 // one thread arms an mbarrier and issues a single bulk copy (cp.async.bulk)
 // of the span into shared memory while every thread loads its element's
 // nodal values; after the barrier each thread applies its element Hessian
@@ -197,10 +209,14 @@ int launch_eh_form(const EhFormArgs& a, cudaStream_t s) {
 // block raises *a.err, waits once more (bounded) for its copy and returns.
 constexpr int kTile = kEhTile;
 
-template <bool PCG>
+__device__ __forceinline__ float entry(const float* p) { return *p; }
+__device__ __forceinline__ float entry(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+
+template <bool PCG, typename TT>
 __global__ void __launch_bounds__(kTile) k_eh_matvec_tma(const EhMatvecArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  float* sT = (float*)smem_raw;  // [162][kTile]
+  TT* sT = (TT*)smem_raw;  // [162][kTile]
+  const TT* Tg = std::is_same<TT, float>::value ? (const TT*)a.T : (const TT*)a.Tb;
   __shared__ __align__(8) uint64_t bar;
   if constexpr (PCG) {
     if (a.st->done) return;
@@ -209,12 +225,12 @@ __global__ void __launch_bounds__(kTile) k_eh_matvec_tma(const EhMatvecArgs a) {
   const int t = threadIdx.x;
   const long long e0 = (long long)blockIdx.x * kTile;
   const int n_el = (int)min((long long)kTile, m.Ne - e0);
-  constexpr uint32_t tile_bytes = 162u * kTile * sizeof(float);
+  constexpr uint32_t tile_bytes = 162u * kTile * sizeof(TT);
   if (t == 0) {
     mbar_init(&bar, 1);
     fence_mbar_init();
     mbar_arrive_expect_tx(&bar, tile_bytes);
-    bulk_g2s(sT, a.T + (long long)blockIdx.x * 162 * kTile, tile_bytes, &bar);
+    bulk_g2s(sT, Tg + (long long)blockIdx.x * 162 * kTile, tile_bytes, &bar);
   }
   __syncthreads();
   const long long e = e0 + t;
@@ -255,7 +271,7 @@ __global__ void __launch_bounds__(kTile) k_eh_matvec_tma(const EhMatvecArgs a) {
         const int type = (sx * 3 + sy) * 3 + sz;
         float tv[6];
 #pragma unroll
-        for (int kl = 0; kl < 6; ++kl) tv[kl] = sT[(type * 6 + kl) * kTile + t];
+        for (int kl = 0; kl < 6; ++kl) tv[kl] = entry(sT + (type * 6 + kl) * kTile + t);
 #pragma unroll
         for (int aa = 0; aa < 8; ++aa)
 #pragma unroll
@@ -303,15 +319,20 @@ __global__ void __launch_bounds__(kTile) k_eh_matvec_tma(const EhMatvecArgs a) {
 // Elements rounded up to whole tiles (the T array holds 162 * eh_pitch floats).
 long long eh_pitch(long long Ne) { return (Ne + kTile - 1) / kTile * kTile; }
 
-template <bool PCG>
-int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s) {
-  if (((uintptr_t)a.T & 15u)) return set_error(VDVC_ERR_ARG, "element Hessians misaligned");
-  const size_t smem = (size_t)162 * kTile * sizeof(float);
-  if (int st = ensure_dyn_smem((const void*)k_eh_matvec_tma<PCG>, (int)smem)) return st;
+template <bool PCG, typename TT>
+static int launch_eh_matvec_t(const EhMatvecArgs& a, cudaStream_t s) {
+  const size_t smem = (size_t)162 * kTile * sizeof(TT);
+  if (int st = ensure_dyn_smem((const void*)k_eh_matvec_tma<PCG, TT>, (int)smem)) return st;
   const long long nb = (a.m.Ne + kTile - 1) / kTile;
-  k_eh_matvec_tma<PCG><<<(unsigned)nb, kTile, smem, s>>>(a);
+  k_eh_matvec_tma<PCG, TT><<<(unsigned)nb, kTile, smem, s>>>(a);
   VDVC_LAUNCHED();
   return VDVC_OK;
+}
+
+template <bool PCG>
+int launch_eh_matvec(const EhMatvecArgs& a, cudaStream_t s) {
+  if ((((uintptr_t)a.T | (uintptr_t)a.Tb) & 15u)) return set_error(VDVC_ERR_ARG, "element Hessians misaligned");
+  return a.Tb ? launch_eh_matvec_t<PCG, __nv_bfloat16>(a, s) : launch_eh_matvec_t<PCG, float>(a, s);
 }
 template int launch_eh_matvec<false>(const EhMatvecArgs&, cudaStream_t);
 template int launch_eh_matvec<true>(const EhMatvecArgs&, cudaStream_t);

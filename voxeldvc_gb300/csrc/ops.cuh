@@ -100,11 +100,13 @@ struct EhFormArgs {
   const float* gmax;      // max |g| of the BF16 gradient (device); the tensor-core formation's scale
   int* err;               // set to VDVC_ERR_CUDA if a tensor-core formation wait times out
   int grad_f32;           // 1: grad is the float32 gradient itself (no BF16 rounding)
+  void* Tb;               // when set: the entries are stored here as BF16 (same layout) instead of in T
 };
 
 struct EhMatvecArgs {
   Mesh m;
   const float* T;      // [tiles][162][kEhTile]
+  const void* Tb;      // when set: BF16 entries (same layout) read instead of T
   long long pitch;     // eh_pitch(Ne): elements rounded up to whole tiles
   int* err;            // set to VDVC_ERR_CUDA if a tile's bulk copies time out
   const float* v;      // nodal input (PCG: z)
