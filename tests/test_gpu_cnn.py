@@ -187,6 +187,20 @@ def test_upsample(env, m, n):
     L.check(lib.vdvc_cnn_upsample2_bwd(dfd.data_ptr(), 4, 0, *n, dc.data_ptr(), 4, 0, *m, 4, stream(torch)))
     ref_dc = O.upsample2_adjoint(df, (m[2], m[1], m[0]))
     assert np.allclose(host(dc).reshape(ref_dc.shape), ref_dc, rtol=8e-3, atol=2e-2)
+    # 16 channels at 8-channel-aligned strides and offsets (the 16-byte
+    # form) against the oracle and, bit for bit, against the per-channel
+    # form (an offset of 2 channels keeps that one)
+    c16 = O.bf16_round(rng.standard_normal((m[2], m[1], m[0], 24)))
+    c16d = bf(torch, c16)
+    fa = torch.zeros(n[0] * n[1] * n[2] * 32, dtype=torch.bfloat16, device="cuda")
+    fb = torch.zeros(n[0] * n[1] * n[2] * 32, dtype=torch.bfloat16, device="cuda")
+    L.check(lib.vdvc_cnn_upsample2(c16d.data_ptr(), 24, 8, *m, fa.data_ptr(), 32, 8, *n, 16, stream(torch)))
+    L.check(lib.vdvc_cnn_upsample2(c16d.data_ptr(), 24, 8, *m, fb.data_ptr(), 32, 2, *n, 16, stream(torch)))
+    ref16 = O.upsample2(c16[..., 8:24], (n[2], n[1], n[0]))
+    fa4 = fa.view(n[2], n[1], n[0], 32)
+    assert np.allclose(host(fa4[..., 8:24]), ref16, rtol=8e-3, atol=1e-2)
+    assert torch.equal(fa4[..., 8:24], fb.view(n[2], n[1], n[0], 32)[..., 2:18])
+    assert not torch.any(fa4[..., :8]) and not torch.any(fa4[..., 24:])
 
 
 def test_pool_input_mse_adam_seed(env):

@@ -363,6 +363,57 @@ __device__ __forceinline__ float up_weight(int p, int q, int m) {
   return (lo == q ? wlo : 0.f) + (hi == q ? whi : 0.f);
 }
 
+// The same with one thread per 8-channel group: 16-byte loads of each
+// corner's 8 channels and one 16-byte store, the per-channel arithmetic of
+// k_upsample2 in the same order (bit-identical).  Channel strides, offsets
+// and C multiples of 8, 16-byte aligned tensors.
+__global__ void k_upsample2_v8(const bf16* __restrict__ cz, int ccs, int ccoff, int mx, int my, int mz,
+                               bf16* __restrict__ fz, int fcs, int fcoff, int nx, int ny, int nz, int C) {
+  const int G = C >> 3;
+  const long long n = (long long)nx * ny * nz * G;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int gq = (int)(i % G);
+    const long long p = i / G;
+    const int x = (int)(p % nx);
+    const long long rr = p / nx;
+    const int y = (int)(rr % ny), z = (int)(rr / ny);
+    int xl, xh, yl, yh, zl, zh;
+    float wxl, wxh, wyl, wyh, wzl, wzh;
+    up_taps(x, mx, xl, xh, wxl, wxh);
+    up_taps(y, my, yl, yh, wyl, wyh);
+    up_taps(z, mz, zl, zh, wzl, wzh);
+    const int X[2] = {xl, xh}, Y[2] = {yl, yh}, Z[2] = {zl, zh};
+    const float WX[2] = {wxl, wxh}, WY[2] = {wyl, wyh}, WZ[2] = {wzl, wzh};
+    float v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = 0.f;
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const float wgt = WZ[a] * WY[b] * WX[c];
+          if (wgt == 0.f) continue;
+          const uint4 q = __ldg(
+              (const uint4*)(cz + (((long long)Z[a] * my + Y[b]) * mx + X[c]) * ccs + ccoff + 8 * gq));
+          const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            v[2 * k] += wgt * __uint_as_float(w[k] << 16);
+            v[2 * k + 1] += wgt * __uint_as_float(w[k] & 0xFFFF0000u);
+          }
+        }
+    uint32_t o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+      o[k] = *reinterpret_cast<const uint32_t*>(&b2);
+    }
+    *(uint4*)(fz + p * fcs + fcoff + 8 * gq) = make_uint4(o[0], o[1], o[2], o[3]);
+  }
+}
+
 __global__ void k_upsample2_bwd(const bf16* __restrict__ df, int fcs, int fcoff, int nx, int ny, int nz,
                                 bf16* __restrict__ dc, int ccs, int ccoff, int mx, int my, int mz, int C) {
   const long long n = (long long)mx * my * mz * C;
@@ -423,23 +474,36 @@ __global__ void k_pool_input(const float* __restrict__ f, const float* __restric
     const int x = (int)(i % gx);
     const long long rr = i / gx;
     const int y = (int)(rr % gy), z = (int)(rr / gy);
+    // per axis the 5 taps' (mirrored) source indices and weights; a tap
+    // outside the volume gets weight 0 at a clamped index, so the window is
+    // walked without branches (adding +0 leaves the sums unchanged)
+    int ox[5];
+    long long oy[5], oz[5];
+    float wx[5], wy[5], wz[5];
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+      const int vx = 4 * x + d - 2, vy = 4 * y + d - 2, vz = 4 * z + d - 2;
+      const bool ix = vx >= 0 && vx < nx, iy = vy >= 0 && vy < ny, iz = vz >= 0 && vz < nz;
+      const int cx = ix ? vx : 0, cy = iy ? vy : 0, cz = iz ? vz : 0;
+      ox[d] = (flip & 1) ? nx - 1 - cx : cx;
+      oy[d] = (long long)((flip & 2) ? ny - 1 - cy : cy) * nx;
+      oz[d] = (long long)((flip & 4) ? nz - 1 - cz : cz) * nx * ny;
+      wx[d] = ix ? tw[d] : 0.f;
+      wy[d] = iy ? tw[d] : 0.f;
+      wz[d] = iz ? tw[d] : 0.f;
+    }
     float sf = 0.f, sg = 0.f, sw = 0.f;
-    for (int dz = -2; dz <= 2; ++dz) {
-      const int vz = 4 * z + dz;
-      if (vz < 0 || vz >= nz) continue;
-      for (int dyy = -2; dyy <= 2; ++dyy) {
-        const int vy = 4 * y + dyy;
-        if (vy < 0 || vy >= ny) continue;
-        const float wzy = tw[dz + 2] * tw[dyy + 2];
-        const int sz = (flip & 4) ? nz - 1 - vz : vz, sy = (flip & 2) ? ny - 1 - vy : vy;
-        const long long row = ((long long)sz * ny + sy) * nx;
-        for (int dx = -2; dx <= 2; ++dx) {
-          const int vx = 4 * x + dx;
-          if (vx < 0 || vx >= nx) continue;
-          const int sx = (flip & 1) ? nx - 1 - vx : vx;
-          const float wgt = wzy * tw[dx + 2];
-          sf += wgt * f[row + sx];
-          sg += wgt * gimg[row + sx];
+#pragma unroll
+    for (int dz = 0; dz < 5; ++dz) {
+#pragma unroll
+      for (int dyy = 0; dyy < 5; ++dyy) {
+        const float wzy = wz[dz] * wy[dyy];
+        const long long row = oz[dz] + oy[dyy];
+#pragma unroll
+        for (int dx = 0; dx < 5; ++dx) {
+          const float wgt = wzy * wx[dx];
+          sf += wgt * __ldg(f + row + ox[dx]);
+          sg += wgt * __ldg(gimg + row + ox[dx]);
           sw += wgt;
         }
       }
@@ -804,6 +868,14 @@ int vdvc_cnn_upsample2(const void* coarse, int c_cstride, int ccoff, int mx, int
                  "fine grid must be 2m-1 or 2m per axis");
   VDVC_CHECK_ARG(ccoff >= 0 && ccoff + C <= c_cstride && fcoff >= 0 && fcoff + C <= f_cstride, "channel ranges");
   const long long n = (long long)nx * ny * nz * C;
+  if (C % 8 == 0 && c_cstride % 8 == 0 && ccoff % 8 == 0 && f_cstride % 8 == 0 && fcoff % 8 == 0 &&
+      (((uintptr_t)coarse | (uintptr_t)fine) & 15) == 0) {
+    k_upsample2_v8<<<eblocks(n / 8), 256, 0, (cudaStream_t)stream>>>((const bf16*)coarse, c_cstride, ccoff, mx, my,
+                                                                     mz, (bf16*)fine, f_cstride, fcoff, nx, ny, nz,
+                                                                     C);
+    VDVC_LAUNCHED();
+    return VDVC_OK;
+  }
   k_upsample2<<<eblocks(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)coarse, c_cstride, ccoff, mx, my, mz,
                                                             (bf16*)fine, f_cstride, fcoff, nx, ny, nz, C);
   VDVC_LAUNCHED();
