@@ -465,9 +465,18 @@ __global__ void k_pool_input(const float* __restrict__ f, const float* __restric
                              const double* __restrict__ sums, bf16* __restrict__ out) {
   const long long n = (long long)gx * gy * gz;
   if (sums) {
-    const double nv = (double)nx * ny * nz;
-    standardise_from_sums(sums[0], sums[1], nv, mf, isf);
-    standardise_from_sums(sums[2], sums[3], nv, mg, isg);
+    // once per block (FP64 division and square root on GB300's narrow FP64 pipe)
+    __shared__ float s_std[4];
+    if (threadIdx.x == 0) {
+      const double nv = (double)nx * ny * nz;
+      standardise_from_sums(sums[0], sums[1], nv, s_std[0], s_std[1]);
+      standardise_from_sums(sums[2], sums[3], nv, s_std[2], s_std[3]);
+    }
+    __syncthreads();
+    mf = s_std[0];
+    isf = s_std[1];
+    mg = s_std[2];
+    isg = s_std[3];
   }
   const float tw[5] = {1.f, 2.f, 2.f, 2.f, 1.f};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -513,9 +522,11 @@ __global__ void k_pool_input(const float* __restrict__ f, const float* __restric
   }
 }
 
-// Sums of f, f^2, g and g^2 in one read of each image: float4 loads, the
-// four elements' sums in FP32, one FP64 add per quantity and float4 (FP64
-// per element would run on GB300's narrow FP64 pipe).
+// Sums of f, f^2, g and g^2 in one read of each image: float4 loads, four
+// grid strides per trip, FP32 partials over eight trips (128 elements per
+// image), then one FP64 add per quantity -- GB300's FP64 pipe is narrow: one
+// FP64 add and conversion per float4 made this pass FP64-bound (0.62 ms for
+// 2 x 513^3 voxels), one per trip still 0.35 ms.
 __global__ void __launch_bounds__(256) k_moments2(const float* __restrict__ f, const float* __restrict__ g, long long n,
                                                   bool vec4, GridReduce red, double* __restrict__ out) {
   __shared__ double s_red[8];
@@ -526,6 +537,8 @@ __global__ void __launch_bounds__(256) k_moments2(const float* __restrict__ f, c
   if (vec4) {
     // four grid strides per trip: eight 16-byte loads in flight per thread
     const long long n4 = n >> 2;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int trips = 0;
     for (long long q0 = gtid; q0 < n4; q0 += 4 * stride) {
       float4 x[4], y[4];
 #pragma unroll
@@ -540,12 +553,24 @@ __global__ void __launch_bounds__(256) k_moments2(const float* __restrict__ f, c
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        a0 += (double)((x[u].x + x[u].y) + (x[u].z + x[u].w));
-        a1 += (double)(x[u].x * x[u].x + x[u].y * x[u].y + x[u].z * x[u].z + x[u].w * x[u].w);
-        a2 += (double)((y[u].x + y[u].y) + (y[u].z + y[u].w));
-        a3 += (double)(y[u].x * y[u].x + y[u].y * y[u].y + y[u].z * y[u].z + y[u].w * y[u].w);
+        s0 += (x[u].x + x[u].y) + (x[u].z + x[u].w);
+        s1 += x[u].x * x[u].x + x[u].y * x[u].y + x[u].z * x[u].z + x[u].w * x[u].w;
+        s2 += (y[u].x + y[u].y) + (y[u].z + y[u].w);
+        s3 += y[u].x * y[u].x + y[u].y * y[u].y + y[u].z * y[u].z + y[u].w * y[u].w;
+      }
+      if (++trips == 8) {
+        a0 += (double)s0;
+        a1 += (double)s1;
+        a2 += (double)s2;
+        a3 += (double)s3;
+        s0 = s1 = s2 = s3 = 0.f;
+        trips = 0;
       }
     }
+    a0 += (double)s0;
+    a1 += (double)s1;
+    a2 += (double)s2;
+    a3 += (double)s3;
     i0 = n4 << 2;
   }
   for (long long i = i0 + gtid; i < n; i += stride) {
