@@ -24,6 +24,31 @@ __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
 
+// Residual scalars from the stats of g over the b mask: mean of g, -std0/sd
+// and the reference mean, computed once per block by thread 0 (float64
+// division and square root run on GB300's narrow FP64 pipe) and shared.
+// The whole block must call this.
+__device__ __forceinline__ void residual_scalars(const StripArgs<float>& a, float& gm, float& ratio, float& mean0) {
+  __shared__ float s_sc[3];
+  if (threadIdx.x == 0) {
+    const double c = a.gstats[0];
+    double mean = 0.0, sd = 0.0;
+    if (c >= 1.0) {
+      mean = a.gstats[1] / c;
+      const double var = a.gstats[2] / c - mean * mean;
+      sd = sqrt(var > 0.0 ? var : 0.0);
+    }
+    if (sd == 0.0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) *a.status = VDVC_ERR_ZERO_DIVISION;
+    s_sc[0] = (float)mean;
+    s_sc[1] = (float)(-(a.std0 / sd));
+    s_sc[2] = (float)a.mean0;
+  }
+  __syncthreads();
+  gm = s_sc[0];
+  ratio = s_sc[1];
+  mean0 = s_sc[2];
+}
+
 template <int H, bool DG>
 __global__ void __launch_bounds__(128, 6) k_strip_rhs_fast(const StripArgs<float> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -47,20 +72,7 @@ __global__ void __launch_bounds__(128, 6) k_strip_rhs_fast(const StripArgs<float
 
   // residual scalars from the stats of g over the b mask
   float gm, ratio, mean0;
-  {
-    const double c = a.gstats[0];
-    double mean = 0.0, sd = 0.0;
-    if (c >= 1.0) {
-      mean = a.gstats[1] / c;
-      const double var = a.gstats[2] / c - mean * mean;
-      sd = sqrt(var > 0.0 ? var : 0.0);
-    }
-    if (sd == 0.0 && t == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0)
-      *a.status = VDVC_ERR_ZERO_DIVISION;
-    gm = (float)mean;
-    ratio = (float)(-(a.std0 / sd));
-    mean0 = (float)a.mean0;
-  }
+  residual_scalars(a, gm, ratio, mean0);
   for (int r = 0; r < 25; ++r) {
     s_accA[t * 25 + r] = 0.f;
     if constexpr (DG) s_accD[t * 25 + r] = 0.f;
@@ -68,6 +80,7 @@ __global__ void __launch_bounds__(128, 6) k_strip_rhs_fast(const StripArgs<float
   __syncthreads();
 
   double dsum[3] = {0.0, 0.0, 0.0};
+  float dcol[3] = {0.f, 0.f, 0.f};  // float over the thread's columns (<= 2 x 81 voxels), float64 once
   const long long row_stride = m.Nvx;
   for (int col = 0; col < ncol; ++col) {
     const int qxc = qx + col;
@@ -143,9 +156,9 @@ __global__ void __launch_bounds__(128, 6) k_strip_rhs_fast(const StripArgs<float
           }
         }
       }
-      dsum[0] += (double)ds0;
-      dsum[1] += (double)ds1;
-      dsum[2] += (double)ds2;
+      dcol[0] += ds0;
+      dcol[1] += ds1;
+      dcol[2] += ds2;
       const float gz0 = wz * fz0, gz1 = wz * fz1;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -200,6 +213,7 @@ __global__ void __launch_bounds__(128, 6) k_strip_rhs_fast(const StripArgs<float
     }
   }
 
+  for (int q = 0; q < 3; ++q) dsum[q] += dcol[q];
   double b3[3], out[3];
   for (int q = 0; q < 3; ++q) b3[q] = block_sum(dsum[q], s_red);
   if (grid_reduce_sum<3>(a.red, b3, out, s_red) && t == 0)
@@ -219,19 +233,7 @@ __global__ void __launch_bounds__(256) k_elem_rhs(const StripArgs<float> a) {
   __shared__ double s_red[8];
   const Mesh& m = a.m;
   float gm, ratio, mean0;
-  {
-    const double c = a.gstats[0];
-    double mean = 0.0, sd = 0.0;
-    if (c >= 1.0) {
-      mean = a.gstats[1] / c;
-      const double var = a.gstats[2] / c - mean * mean;
-      sd = sqrt(var > 0.0 ? var : 0.0);
-    }
-    if (sd == 0.0 && threadIdx.x == 0 && blockIdx.x == 0) *a.status = VDVC_ERR_ZERO_DIVISION;
-    gm = (float)mean;
-    ratio = (float)(-(a.std0 / sd));
-    mean0 = (float)a.mean0;
-  }
+  residual_scalars(a, gm, ratio, mean0);
   double dsum[3] = {0.0, 0.0, 0.0};
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m.Ne;
        e += (long long)gridDim.x * blockDim.x) {

@@ -18,11 +18,10 @@ namespace vdvc {
 
 // Rows (y,z) are distributed over blocks, x over threads, so the y/z
 // multiplicities are uniform per row; per-row float partials are folded into
-// float64 accumulators once per row.  A block takes kStatsRows of its rows
-// per trip with every mask byte and value loaded before any is used (the
-// loads of a row would otherwise wait on one another through the mask
-// test); the per-row partials and their fold order are those of one row at
-// a time.
+// float sums of 16 trips and then into float64 accumulators (GB300's FP64
+// pipe is narrow).  A block takes kStatsRows of its rows per trip with every
+// mask byte and value loaded before any is used (the loads of a row would
+// otherwise wait on one another through the mask test).
 constexpr int kStatsRows = 4;
 
 template <typename T>
@@ -30,6 +29,8 @@ __global__ void __launch_bounds__(256) k_masked_stats(const T* __restrict__ fiel
                                                       const Mesh m, GridReduce red, double* __restrict__ out3) {
   __shared__ double s_red[8];
   double acc[3] = {0.0, 0.0, 0.0};
+  float fac[3] = {0.f, 0.f, 0.f};  // float sums of 16 trips per float64 add (narrow FP64 pipe)
+  int trips = 0;
   const long long nrows = (long long)m.Nvy * m.Nvz;
   for (long long row0 = blockIdx.x; row0 < nrows; row0 += (long long)kStatsRows * gridDim.x) {
     float c[kStatsRows], s1[kStatsRows], s2[kStatsRows];
@@ -63,11 +64,19 @@ __global__ void __launch_bounds__(256) k_masked_stats(const T* __restrict__ fiel
     }
 #pragma unroll
     for (int r = 0; r < kStatsRows; ++r) {
-      acc[0] += c[r];
-      acc[1] += s1[r];
-      acc[2] += s2[r];
+      fac[0] += c[r];
+      fac[1] += s1[r];
+      fac[2] += s2[r];
+    }
+    if (++trips == 16) {
+      for (int q = 0; q < 3; ++q) {
+        acc[q] += fac[q];
+        fac[q] = 0.f;
+      }
+      trips = 0;
     }
   }
+  for (int q = 0; q < 3; ++q) acc[q] += fac[q];
   double b3[3], o3[3];
   for (int q = 0; q < 3; ++q) b3[q] = block_sum(acc[q], s_red);
   if (grid_reduce_sum<3>(red, b3, o3, s_red) && threadIdx.x == 0)
@@ -158,7 +167,11 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 6 : 6) : 3) k_s
   }
   __syncthreads();
 
+  // float partials per voxel plane of the column, summed in float over the
+  // thread's columns (at most 2 x 81 voxels) and added to float64 once:
+  // GB300's FP64 pipe is narrow
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  float c4[4] = {0.f, 0.f, 0.f, 0.f};
   const T gxmax = (T)(a.gnx - 1), gymax = (T)(a.gny - 1), gzmax = (T)(a.gnz - 1);
 
   for (int col = 0; col < ncol; ++col) {
@@ -233,14 +246,15 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 6 : 6) : 3) k_s
         }
       }
       if constexpr (STATS) {
-        acc[0] += r0;
-        acc[1] += r1;
-        acc[2] += r2;
-        acc[3] += r3;
+        c4[0] += r0;
+        c4[1] += r1;
+        c4[2] += r2;
+        c4[3] += r3;
       }
     }
   }
   if constexpr (STATS) {
+    for (int q = 0; q < 4; ++q) acc[q] += c4[q];
     double b4[4], o4[4];
     for (int q = 0; q < 4; ++q) b4[q] = block_sum(acc[q], s_red);
     if (grid_reduce_sum<4>(a.red, b4, o4, s_red) && t == 0)
