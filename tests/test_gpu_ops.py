@@ -154,6 +154,12 @@ def test_fft_rigid_shift(api):
     c = load_golden("fft.npz")
     assert np.array_equal(CG.fft_rigid_shift(c["f1"], c["g1"], np), c["d1"])
     assert np.array_equal(CG.fft_rigid_shift(c["f2"], c["g2"], np), c["d2"])
+    # float32 volumes transform in single precision (complex64, as the
+    # reference's fftn does for float32 arrays under CuPy): the same shifts
+    for a, b, d in ((c["f1"], c["g1"], c["d1"]), (c["f2"], c["g2"], c["d2"])):
+        fv, fs = CG.pix_to_vox(a, np.float32)
+        gv, gs = CG.pix_to_vox(b, np.float32)
+        assert np.array_equal(CG._fft_shift_vox(fv, fs, gv, gs, np.float32), d)
 
 
 def test_pix_to_vox_dtypes(api):

@@ -2,8 +2,13 @@
 // engine/correlate_gpu.py:381-414), plus a float64 dot/sum reduction.
 //
 // The volumes are vox layout (x fastest), i.e. C-order arrays of shape
-// (nz, ny, nx); the transforms are cuFFT D2Z/Z2D of that shape (library
+// (nz, ny, nx); the transforms are cuFFT transforms of that shape (library
 // calls), the cross-power normalisation and the arg-max are kernels here.
+// Precision follows the volumes' dtype, as the reference's fftn does (its
+// float64 cast is commented out, so its CuPy path transforms float32 volumes
+// in complex64): float32 volumes take R2C/C2R, float64 ones D2Z/Z2D -- the
+// single-precision transforms also keep the 129^3 coarse level's FFTs
+// (radix 3 x 43) off GB300's narrow FP64 pipe.
 // numpy's argmax returns the first maximum in C order of pix[x,y,z]
 // (x slowest); the arg-max kernel breaks ties the same way.
 #include <cstdint>
@@ -17,26 +22,29 @@
 
 namespace vdvc {
 
-template <typename T>
-__global__ void k_crop_to_f64(const T* __restrict__ in, int nx, int ny, int sx, int sy, int sz,
-                              double* __restrict__ out) {
+template <typename T, typename U>
+__global__ void k_crop_to(const T* __restrict__ in, int nx, int ny, int sx, int sy, int sz, U* __restrict__ out) {
   const long long n = (long long)sx * sy * sz;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(t % sx);
     const long long r = t / sx;
     const int y = (int)(r % sy), z = (int)(r / sy);
-    out[t] = (double)in[(long long)x + (long long)y * nx + (long long)z * nx * ny];
+    out[t] = (U)in[(long long)x + (long long)y * nx + (long long)z * nx * ny];
   }
 }
 
-// R = F conj(G) / (|F conj(G)| + 1e-12), written over F.
-__global__ void k_cross_power(cufftDoubleComplex* __restrict__ F, const cufftDoubleComplex* __restrict__ G,
-                              long long n) {
+// R = F conj(G) / (|F conj(G)| + 1e-12), written over F, in the transforms'
+// precision.
+__device__ __forceinline__ double cabs_of(double re, double im) { return hypot(re, im); }
+__device__ __forceinline__ float cabs_of(float re, float im) { return hypotf(re, im); }
+
+template <typename C, typename R>
+__global__ void k_cross_power(C* __restrict__ F, const C* __restrict__ G, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const cufftDoubleComplex a = F[i], b = G[i];
-    const double re = a.x * b.x + a.y * b.y;  // a * conj(b)
-    const double im = a.y * b.x - a.x * b.y;
-    const double den = hypot(re, im) + 1e-12;
+    const C a = F[i], b = G[i];
+    const R re = a.x * b.x + a.y * b.y;  // a * conj(b)
+    const R im = a.y * b.x - a.x * b.y;
+    const R den = cabs_of(re, im) + (R)1e-12;
     F[i].x = re / den;
     F[i].y = im / den;
   }
@@ -52,7 +60,8 @@ __device__ __forceinline__ ArgMax better(ArgMax a, ArgMax b) {
   return a;
 }
 
-__global__ void __launch_bounds__(256) k_argmax(const double* __restrict__ r, int sx, int sy, int sz,
+template <typename T>
+__global__ void __launch_bounds__(256) k_argmax(const T* __restrict__ r, int sx, int sy, int sz,
                                                 ArgMax* __restrict__ partial, unsigned int* ticket,
                                                 ArgMax* __restrict__ result) {
   __shared__ ArgMax s[256];
@@ -63,7 +72,7 @@ __global__ void __launch_bounds__(256) k_argmax(const double* __restrict__ r, in
     const int x = (int)(t % sx);
     const long long q = t / sx;
     const int y = (int)(q % sy), z = (int)(q / sy);
-    const ArgMax c{r[t], ((long long)x * sy + y) * sz + z};
+    const ArgMax c{(double)r[t], ((long long)x * sy + y) * sz + z};
     best = better(best, c);
   }
   s[threadIdx.x] = best;
@@ -134,9 +143,10 @@ __global__ void __launch_bounds__(256) k_dot(const T* __restrict__ a, const T* _
 // put back after the call's stream has finished with it.
 struct FftPlan {
   int dev, sx, sy, sz;
+  bool single;  // R2C / C2R on float and cufftComplex buffers (else D2Z / Z2D on double)
   cufftHandle pf, pi;
-  double *fr, *gr;
-  cufftDoubleComplex *Fc, *Gc;
+  void *fr, *gr;  // real volumes
+  void *Fc, *Gc;  // half spectra
   ArgMax *partial, *result;
   unsigned int* ticket;
   size_t bytes;
@@ -167,14 +177,14 @@ static void fft_destroy(FftPlan* P) {
   delete P;
 }
 
-static int fft_acquire(int sx, int sy, int sz, FftPlan** out) {
+static int fft_acquire(int sx, int sy, int sz, bool single, FftPlan** out) {
   int dev = 0;
   VDVC_CUDA(cudaGetDevice(&dev));
   {
     std::lock_guard<std::mutex> lk(g_fft_mu);
     for (size_t i = 0; i < g_fft_cache.size(); ++i) {
       FftPlan* P = g_fft_cache[i];
-      if (P->dev == dev && P->sx == sx && P->sy == sy && P->sz == sz) {
+      if (P->dev == dev && P->sx == sx && P->sy == sy && P->sz == sz && P->single == single) {
         g_fft_cache.erase(g_fft_cache.begin() + i);
         *out = P;
         return VDVC_OK;
@@ -189,11 +199,12 @@ static int fft_acquire(int sx, int sy, int sz, FftPlan** out) {
   P->sx = sx;
   P->sy = sy;
   P->sz = sz;
-  P->bytes = (size_t)(2 * n) * sizeof(double) + (size_t)(2 * nc) * sizeof(cufftDoubleComplex);
-  if (cudaMalloc((void**)&P->fr, n * sizeof(double)) != cudaSuccess ||
-      cudaMalloc((void**)&P->gr, n * sizeof(double)) != cudaSuccess ||
-      cudaMalloc((void**)&P->Fc, nc * sizeof(cufftDoubleComplex)) != cudaSuccess ||
-      cudaMalloc((void**)&P->Gc, nc * sizeof(cufftDoubleComplex)) != cudaSuccess ||
+  P->single = single;
+  const size_t rb = single ? sizeof(float) : sizeof(double);
+  const size_t cb = single ? sizeof(cufftComplex) : sizeof(cufftDoubleComplex);
+  P->bytes = (size_t)(2 * n) * rb + (size_t)(2 * nc) * cb;
+  if (cudaMalloc(&P->fr, n * rb) != cudaSuccess || cudaMalloc(&P->gr, n * rb) != cudaSuccess ||
+      cudaMalloc(&P->Fc, nc * cb) != cudaSuccess || cudaMalloc(&P->Gc, nc * cb) != cudaSuccess ||
       cudaMalloc((void**)&P->partial, kReduceBlocks * sizeof(ArgMax)) != cudaSuccess ||
       cudaMalloc((void**)&P->result, sizeof(ArgMax)) != cudaSuccess ||
       cudaMalloc((void**)&P->ticket, sizeof(unsigned int)) != cudaSuccess) {
@@ -201,12 +212,12 @@ static int fft_acquire(int sx, int sy, int sz, FftPlan** out) {
     fft_destroy(P);
     return set_error(VDVC_ERR_CUDA, "fft_rigid_shift: device allocation failed");
   }
-  if (cufftPlan3d(&P->pf, sz, sy, sx, CUFFT_D2Z) != CUFFT_SUCCESS) {
+  if (cufftPlan3d(&P->pf, sz, sy, sx, single ? CUFFT_R2C : CUFFT_D2Z) != CUFFT_SUCCESS) {
     P->pf = 0;
     fft_destroy(P);
     return set_error(VDVC_ERR_CUFFT, "fft_rigid_shift: plan creation failed");
   }
-  if (cufftPlan3d(&P->pi, sz, sy, sx, CUFFT_Z2D) != CUFFT_SUCCESS) {
+  if (cufftPlan3d(&P->pi, sz, sy, sx, single ? CUFFT_C2R : CUFFT_Z2D) != CUFFT_SUCCESS) {
     P->pi = 0;
     fft_destroy(P);
     return set_error(VDVC_ERR_CUFFT, "fft_rigid_shift: plan creation failed");
@@ -302,35 +313,52 @@ int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz, const voi
   const long long n = (long long)sx * sy * sz;
   const long long nc = (long long)sz * sy * (sx / 2 + 1);
   cudaStream_t s = (cudaStream_t)stream;
+  const bool single = dtype == VDVC_F32;
   FftPlan* P = nullptr;
-  int st = fft_acquire(sx, sy, sz, &P);
+  int st = fft_acquire(sx, sy, sz, single, &P);
   if (st) return st;
   const int nb = grid_blocks(n, 256, kReduceBlocks);
   ArgMax host;
   bool ok = cudaMemsetAsync(P->ticket, 0, sizeof(unsigned int), s) == cudaSuccess;
   if (ok) {
-    if (dtype == VDVC_F32) {
-      k_crop_to_f64<float><<<nb, 256, 0, s>>>((const float*)f_vox, fnx, fny, sx, sy, sz, P->fr);
-      k_crop_to_f64<float><<<nb, 256, 0, s>>>((const float*)g_vox, gnx, gny, sx, sy, sz, P->gr);
+    if (single) {
+      k_crop_to<float, float><<<nb, 256, 0, s>>>((const float*)f_vox, fnx, fny, sx, sy, sz, (float*)P->fr);
+      k_crop_to<float, float><<<nb, 256, 0, s>>>((const float*)g_vox, gnx, gny, sx, sy, sz, (float*)P->gr);
     } else {
-      k_crop_to_f64<double><<<nb, 256, 0, s>>>((const double*)f_vox, fnx, fny, sx, sy, sz, P->fr);
-      k_crop_to_f64<double><<<nb, 256, 0, s>>>((const double*)g_vox, gnx, gny, sx, sy, sz, P->gr);
+      k_crop_to<double, double><<<nb, 256, 0, s>>>((const double*)f_vox, fnx, fny, sx, sy, sz, (double*)P->fr);
+      k_crop_to<double, double><<<nb, 256, 0, s>>>((const double*)g_vox, gnx, gny, sx, sy, sz, (double*)P->gr);
     }
     count_launch(2);
-    ok = cufftSetStream(P->pf, s) == CUFFT_SUCCESS && cufftSetStream(P->pi, s) == CUFFT_SUCCESS &&
-         cufftExecD2Z(P->pf, P->fr, P->Fc) == CUFFT_SUCCESS && cufftExecD2Z(P->pf, P->gr, P->Gc) == CUFFT_SUCCESS;
+    ok = cufftSetStream(P->pf, s) == CUFFT_SUCCESS && cufftSetStream(P->pi, s) == CUFFT_SUCCESS;
+    if (ok && single)
+      ok = cufftExecR2C(P->pf, (cufftReal*)P->fr, (cufftComplex*)P->Fc) == CUFFT_SUCCESS &&
+           cufftExecR2C(P->pf, (cufftReal*)P->gr, (cufftComplex*)P->Gc) == CUFFT_SUCCESS;
+    else if (ok)
+      ok = cufftExecD2Z(P->pf, (cufftDoubleReal*)P->fr, (cufftDoubleComplex*)P->Fc) == CUFFT_SUCCESS &&
+           cufftExecD2Z(P->pf, (cufftDoubleReal*)P->gr, (cufftDoubleComplex*)P->Gc) == CUFFT_SUCCESS;
     if (!ok) st = set_error(VDVC_ERR_CUFFT, "fft_rigid_shift: forward transforms failed");
   } else {
     st = set_error(VDVC_ERR_CUDA, "memset");
   }
   if (ok) {
-    k_cross_power<<<grid_blocks(nc, 256, 152 * 16), 256, 0, s>>>(P->Fc, P->Gc, nc);
-    count_launch();
-    ok = cufftExecZ2D(P->pi, P->Fc, P->fr) == CUFFT_SUCCESS;
+    const int nbc = grid_blocks(nc, 256, 152 * 16);
+    if (single) {
+      k_cross_power<cufftComplex, float><<<nbc, 256, 0, s>>>((cufftComplex*)P->Fc, (const cufftComplex*)P->Gc, nc);
+      count_launch();
+      ok = cufftExecC2R(P->pi, (cufftComplex*)P->Fc, (cufftReal*)P->fr) == CUFFT_SUCCESS;
+    } else {
+      k_cross_power<cufftDoubleComplex, double><<<nbc, 256, 0, s>>>((cufftDoubleComplex*)P->Fc,
+                                                                     (const cufftDoubleComplex*)P->Gc, nc);
+      count_launch();
+      ok = cufftExecZ2D(P->pi, (cufftDoubleComplex*)P->Fc, (cufftDoubleReal*)P->fr) == CUFFT_SUCCESS;
+    }
     if (!ok) st = set_error(VDVC_ERR_CUFFT, "fft_rigid_shift: inverse transform failed");
   }
   if (ok) {
-    k_argmax<<<nb, 256, 0, s>>>(P->fr, sx, sy, sz, P->partial, P->ticket, P->result);
+    if (single)
+      k_argmax<float><<<nb, 256, 0, s>>>((const float*)P->fr, sx, sy, sz, P->partial, P->ticket, P->result);
+    else
+      k_argmax<double><<<nb, 256, 0, s>>>((const double*)P->fr, sx, sy, sz, P->partial, P->ticket, P->result);
     count_launch();
     ok = cudaMemcpyAsync(&host, P->result, sizeof(ArgMax), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
          cudaStreamSynchronize(s) == cudaSuccess;
