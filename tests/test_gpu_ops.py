@@ -97,6 +97,38 @@ def test_voxel_fields(api, case):
     assert np.array_equal(am, gm)
 
 
+@pytest.mark.parametrize("case", OPS_CASES)
+def test_image_grad_stats_fused(api, case):
+    """The level set-up's fused pass: gradient and mask0 bit-identical to
+    vdvc_image_grad, the sums of f over mask0 those of vdvc_masked_stats
+    (float64 sums of float32 partials in another order)."""
+    import torch
+    from voxeldvc_gb300 import _lib
+    K, CG, G = api
+    c = load_golden(f"ops_{case}.npz")
+    Nx, Ny, Nz, h = (int(x) for x in c["dims"])
+    Nvx, Nvy, Nvz = Nx * h + 1, Ny * h + 1, Nz * h + 1
+    f_vox, fs = CG.pix_to_vox(c["f_pix"], np.float32)
+    glt = float(np.quantile(c["f_pix"], 0.2))  # a threshold that leaves mask0 partial
+    grad_ref, m_ref = CG._grad_vox(f_vox, fs, np.float32, glt)
+    ref3 = CG._stats_sums(f_vox, m_ref, h, Nx, Ny, Nz)
+    n = Nvx * Nvy * Nvz
+    grad = torch.empty(3 * n, dtype=torch.float32, device="cuda")
+    m0 = torch.empty(n, dtype=torch.uint8, device="cuda")
+    out3 = torch.zeros(3, dtype=torch.float64, device="cuda")
+    ws = torch.empty(1 << 16, dtype=torch.uint8, device="cuda")
+    L = _lib.lib()
+    s = torch.cuda.current_stream().cuda_stream
+    _lib.check(L.vdvc_image_grad_stats(f_vox.data_ptr(), Nvx, Nvy, Nvz, glt, grad.data_ptr(), m0.data_ptr(), h, Nx,
+                                       Ny, Nz, out3.data_ptr(), ws.data_ptr(), ws.numel(), s))
+    assert torch.equal(grad, grad_ref) and torch.equal(m0, m_ref)
+    assert 0 < m0.sum().item() < n
+    assert np.allclose(out3.cpu().numpy(), ref3, rtol=1e-6)
+    with pytest.raises(Exception):  # an image that is not the mesh's voxel grid
+        _lib.check(L.vdvc_image_grad_stats(f_vox.data_ptr(), Nvx, Nvy, Nvz, glt, grad.data_ptr(), m0.data_ptr(), h,
+                                           Nx + 1, Ny, Nz, out3.data_ptr(), ws.data_ptr(), ws.numel(), s))
+
+
 @pytest.mark.parametrize("case", ["A", "B", "C"])
 def test_generic_pcg(api, case):
     K, CG, G = api

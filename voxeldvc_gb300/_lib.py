@@ -51,6 +51,7 @@ SIGNATURES = {
     "vdvc_pix_to_vox": (ci, [vp, ci, ci, ci, ci, vp, ci, vp]),
     "vdvc_decimate": (ci, [vp, ci, ci, ci, ci, ci, vp, vp]),
     "vdvc_image_grad": (ci, [vp, ci, ci, ci, ci, cd, vp, vp, vp]),
+    "vdvc_image_grad_stats": (ci, [vp, ci, ci, ci, cd, vp, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_erode_mask": (ci, [vp, ci, ci, ci, vp, vp]),
     "vdvc_masked_stats": (ci, [vp, ci, vp, ci, ci, ci, ci, vp, vp, cz, vp]),
     "vdvc_matvec_H": (ci, [vp, vp, vp, ci, ci, ci, ci, ci, vp, vp, cz, vp]),

@@ -1,8 +1,8 @@
 // Image layout and reference-image preparation kernels:
 //   pix -> vox transpose with cast, strided decimation, the xp.gradient
-//   stencil with the mask0 / 6-neighbour erosion fused in, and the erosion
-//   on its own.
-#include "common.cuh"
+//   stencil with the mask0 / 6-neighbour erosion fused in (and, for a GN
+//   level, the reference statistics over mask0), and the erosion on its own.
+#include "ops.cuh"
 
 namespace vdvc {
 namespace {
@@ -91,6 +91,63 @@ __global__ void __launch_bounds__(256) k_image_grad(const T* __restrict__ f, int
     grad[3 * v + 1] = gy;
     grad[3 * v + 2] = gz;
   }
+}
+
+// k_image_grad<float> with mask0 plus the multiplicity-weighted sums of f
+// over mask0 (vdvc_masked_stats' count, sum, sum of squares) in the same
+// read of f: 32-bit voxel indices, float partials folded into float64
+// every 64 voxels of a thread (GB300's FP64 pipe is narrow), one block
+// partial each, grid-reduced.
+__global__ void __launch_bounds__(256) k_image_grad_stats(const float* __restrict__ f, int nx, int ny, int nz,
+                                                          float glt, float* __restrict__ grad,
+                                                          uint8_t* __restrict__ mask0, int h, int Ex, int Ey,
+                                                          int Ez, GridReduce red, double* __restrict__ out3) {
+  __shared__ double s_red[8];
+  const unsigned int unx = (unsigned int)nx, uny = (unsigned int)ny;
+  const unsigned int nxy = unx * uny, n = nxy * (unsigned int)nz;
+  double acc[3] = {0.0, 0.0, 0.0};
+  float fc = 0.f, f1 = 0.f, f2 = 0.f;
+  int cnt = 0;
+  for (unsigned int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const unsigned int r = v / unx;
+    const int x = (int)(v - r * unx), y = (int)(r % uny), z = (int)(r / uny);
+    const unsigned int xm = v - (x > 0), xp = v + (x < nx - 1);
+    const unsigned int ym = v - (y > 0) * unx, yp = v + (y < ny - 1) * unx;
+    const unsigned int zm = v - (z > 0) * nxy, zp = v + (z < nz - 1) * nxy;
+    const float c = f[v];
+    const float fxm = f[xm], fxp = f[xp], fym = f[ym], fyp = f[yp], fzm = f[zm], fzp = f[zp];
+    float gx = gradient_1d(fxm, c, fxp, x, nx);
+    float gy = gradient_1d(fym, c, fyp, y, ny);
+    float gz = gradient_1d(fzm, c, fzp, z, nz);
+    const bool m = c > glt;
+    const bool keep = m && (fxm > glt) && (fxp > glt) && (fym > glt) && (fyp > glt) && (fzm > glt) && (fzp > glt);
+    mask0[v] = m ? 1 : 0;
+    if (!keep) gx = gy = gz = 0.f;
+    grad[3 * (size_t)v + 0] = gx;
+    grad[3 * (size_t)v + 1] = gy;
+    grad[3 * (size_t)v + 2] = gz;
+    if (m) {
+      const float mult =
+          (float)(axis_multiplicity(x, h, Ex) * axis_multiplicity(y, h, Ey) * axis_multiplicity(z, h, Ez));
+      fc += mult;
+      f1 += mult * c;
+      f2 += mult * c * c;
+    }
+    if (++cnt == 64) {
+      acc[0] += fc;
+      acc[1] += f1;
+      acc[2] += f2;
+      fc = f1 = f2 = 0.f;
+      cnt = 0;
+    }
+  }
+  acc[0] += fc;
+  acc[1] += f1;
+  acc[2] += f2;
+  double b3[3], o3[3];
+  for (int q = 0; q < 3; ++q) b3[q] = block_sum(acc[q], s_red);
+  if (grid_reduce_sum<3>(red, b3, o3, s_red) && threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q) out3[q] = o3[q];
 }
 
 __global__ void k_erode(const uint8_t* __restrict__ m, int nx, int ny, int nz, uint8_t* __restrict__ out) {
@@ -189,6 +246,29 @@ int vdvc_image_grad(const void* f_vox, int dtype, int Nvx, int Nvy, int Nvz, dou
                                                     mask0, mask0 != nullptr);
   else
     return set_error(VDVC_ERR_ARG, "dtype %d must be VDVC_F32 or VDVC_F64", dtype);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+int vdvc_image_grad_stats(const float* f_vox, int Nvx, int Nvy, int Nvz, double glt, float* grad, uint8_t* mask0,
+                          int h, int Nx, int Ny, int Nz, double* out3, void* ws, size_t ws_bytes,
+                          vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(f_vox && grad && mask0 && out3, "null pointer");
+  VDVC_CHECK_ARG(Nvx >= 2 && Nvy >= 2 && Nvz >= 2, "gradient needs >= 2 voxels per axis");
+  Mesh m;
+  if (int st = make_mesh(h, Nx, Ny, Nz, &m)) return st;
+  VDVC_CHECK_ARG(m.Nvx == Nvx && m.Nvy == Nvy && m.Nvz == Nvz, "image (%d,%d,%d) is not the mesh's voxel grid",
+                 Nvx, Nvy, Nvz);
+  Carve cv(ws, ws_bytes);
+  GridReduce red;
+  red.partials = cv.take<double>(3 * kReduceBlocks);
+  red.ticket = cv.take<unsigned int>(1);
+  VDVC_CHECK_ARG(ws && cv.fits(), "image_grad_stats needs %zu bytes of workspace", cv.off);
+  cudaStream_t s = (cudaStream_t)stream;
+  VDVC_CUDA(cudaMemsetAsync(red.ticket, 0, sizeof(unsigned int), s));
+  const long long n = (long long)Nvx * Nvy * Nvz;
+  k_image_grad_stats<<<grid_blocks(n, 256, kReduceBlocks), 256, 0, s>>>(f_vox, Nvx, Nvy, Nvz, (float)glt, grad,
+                                                                       mask0, h, Nx, Ny, Nz, red, out3);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }

@@ -408,12 +408,21 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
         raise ValueError(f"f_pix has shape {tuple(lv.fshape)}, expected (Nx*h+1, Ny*h+1, Nz*h+1) = "
                          f"{(Nvx, Nvy, Nvz)}")
     L = _lib.lib()
-    grad, mask0 = _grad_vox(lv.f_vox, lv.fshape, dtype, glt)
     # the level's scalars are reduced into one device buffer (count, s1, s2
     # of f over mask0; v.Hv and v.Lv of the calibration) and read back once
     # (_finish_setup), so that a batch reads every problem's in one go
     dsc = D.zeros(5, np.float64)
-    _stats_sums(lv.f_vox, mask0, h, Nx, Ny, Nz, out=dsc[0:3])
+    if dtype == np.float32:
+        # gradient, mask0 and the statistics of f over mask0 in one read of f
+        grad = D.empty(3 * Nvox, dtype)
+        mask0 = D.empty(Nvox, np.uint8)
+        ws_ = D.scratch.get(1 << 16)
+        _lib.check(L.vdvc_image_grad_stats(lv.f_vox.data_ptr(), Nvx, Nvy, Nvz, float(glt), grad.data_ptr(),
+                                           mask0.data_ptr(), h, Nx, Ny, Nz, dsc.data_ptr(), ws_.data_ptr(),
+                                           ws_.numel(), D.stream()), "image_grad_stats")
+    else:
+        grad, mask0 = _grad_vox(lv.f_vox, lv.fshape, dtype, glt)
+        _stats_sums(lv.f_vox, mask0, h, Nx, Ny, Nz, out=dsc[0:3])
 
     N_stencil, w_stencil = build_N_stencil(h)
     if reg_type not in ('laplacian', 'equilibrium_gap'):
