@@ -96,6 +96,16 @@ size_t vdvc_workspace_bytes(int dtype, int h, int Nx, int Ny, int Nz);
    (engine/correlate_gpu.py:59-60, :938-939). */
 int vdvc_pix_to_vox(const void* pix, int pix_dtype, int nx, int ny, int nz,
                     void* vox, int dtype, vdvc_stream_t stream);
+/* The same on every step-th voxel per axis: vox = the vox layout of
+   pix[::step, ::step, ::step] (ceil(n / step) per axis), reading only those
+   voxels: a pyramid level straight from the source image, as the reference
+   takes it (xp.asarray(f_pix)[::s, ::s, ::s], engine/correlate_gpu.py:
+   1257-1258).  max_blocks > 0 bounds the grid (blocks then walk the tiles):
+   a copy from host memory run in the background of other kernels keeps its
+   blocks, which mostly wait on the host link, off most of the SMs. */
+int vdvc_pix_to_vox_strided(const void* pix, int pix_dtype, int nx, int ny,
+                            int nz, int step, int max_blocks, void* vox,
+                            int dtype, vdvc_stream_t stream);
 
 /* Strided decimation in vox layout: out = in[::s, ::s, ::s]
    (engine/correlate_gpu.py:1257-1258).  out has ceil(n/s) per axis. */

@@ -119,6 +119,52 @@ def test_host_array_layout(api, cuda, dtype):
     assert np.array_equal(v_host.cpu().numpy(), a.transpose(2, 1, 0).reshape(-1).astype(np.float32))
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.uint16])
+def test_strided_layout(api, cuda, dtype):
+    """vdvc_pix_to_vox_strided = pix_to_vox then the strided decimation, bit
+    for bit, from host memory (where the device reads it in place) and from
+    device tensors, for steps 1-4 and extents that are not multiples of the
+    step."""
+    torch = cuda
+    CG, G = api
+    from voxeldvc_gb300 import _lib, _device as D
+    rng = np.random.default_rng(8)
+    a = (rng.random((97, 83, 71)) * 200).astype(dtype)
+    full, fs = CG.pix_to_vox(a, np.float32)
+    t = torch.from_numpy(a.astype(np.float64)).cuda()
+    for s in (1, 2, 3, 4):
+        ref, o = CG._decimate(full, fs, s, np.float32)
+        if CG._host_readable(a):
+            got, og = CG._pix_to_vox_strided_host(a, s, np.float32)
+            torch.cuda.synchronize()
+            assert og == o and torch.equal(got, ref)
+        out = D.empty(ref.numel(), np.float32)
+        for mb in (0, 7):  # one block per tile, and a bounded grid walking the tiles
+            out.zero_()
+            _lib.check(_lib.lib().vdvc_pix_to_vox_strided(t.data_ptr(), _lib.F64, *a.shape, s, mb, out.data_ptr(),
+                                                          _lib.F32, D.stream()))
+            assert torch.equal(out, ref), (s, mb)
+
+
+def test_multiscale_host_arrays_overlap(api, cuda):
+    """A multiscale solve from host arrays (coarsest level read in place at
+    its step, the full-resolution layout on a side stream under it) equals
+    the same solve from device tensors bit for bit."""
+    torch = cuda
+    CG, G = api
+    from voxeldvc_gb300 import synth
+    f = synth.texture((129, 129, 129), 200, seed=3, cyl_seed=4)
+    fh = f.view(129, 129, 129).permute(2, 1, 0).contiguous().cpu().numpy()
+    g = np.roll(fh, (2, -1, 1), axis=(0, 1, 2)).copy()
+    kw = dict(scales=(2, 1, 0), K_ref_laplacian=G.build_K_ref_laplacian(), l0=4.5 * 8, maxiter=4, disp=False,
+              fft_prealign=True, dynamic_mask=True, freeze_mask_after=2)
+    assert CG._host_readable(fh) or not CG._host_direct()
+    Uh, rh, dh = CG.multiscale_correlate_gpu(fh, g, 16, 16, 16, 8, xp=np, **kw)
+    Ud, rd, dd = CG.multiscale_correlate_gpu(torch.from_numpy(fh).cuda(), torch.from_numpy(g).cuda(), 16, 16, 16, 8,
+                                             xp=np, **kw)
+    assert np.array_equal(Uh, Ud) and np.array_equal(rh, rd) and np.array_equal(dh, dd)
+
+
 def test_error_paths(api):
     CG, G = api
     c = load_golden("solve_sinusoid.npz")

@@ -172,6 +172,22 @@ class _HostPool:
 host_pool = _HostPool()
 
 
+def host_result(n, dtype):
+    """A pinned host buffer (pool entry) of n elements that a kernel may
+    write directly (pinned memory is mapped into the device's address
+    space), or None when the pool has none free; hand it out with
+    claim_host_result once the writing stream has finished."""
+    if n * np.dtype(dtype).itemsize < _HostPool.MIN_BYTES:
+        return None
+    return host_pool.take((n,), torch_dtype(dtype))
+
+
+def claim_host_result(ent):
+    a = ent[0].numpy()
+    ent[1] = weakref.ref(a)
+    return a
+
+
 def out(t, xp):
     if wants_host(xp):
         t = t.detach()

@@ -49,6 +49,7 @@ SIGNATURES = {
     "vdvc_launch_count": (C.c_longlong, []),
     "vdvc_workspace_bytes": (cz, [ci, ci, ci, ci, ci]),
     "vdvc_pix_to_vox": (ci, [vp, ci, ci, ci, ci, vp, ci, vp]),
+    "vdvc_pix_to_vox_strided": (ci, [vp, ci, ci, ci, ci, ci, ci, vp, ci, vp]),
     "vdvc_decimate": (ci, [vp, ci, ci, ci, ci, ci, vp, vp]),
     "vdvc_image_grad": (ci, [vp, ci, ci, ci, ci, cd, vp, vp, vp]),
     "vdvc_image_grad_stats": (ci, [vp, ci, ci, ci, cd, vp, vp, ci, ci, ci, ci, vp, vp, cz, vp]),

@@ -806,7 +806,8 @@ static int read(GnSolver<T>* S, int which, void* dst, int dst_f64, cudaStream_t 
   switch (which) {
     case VDVC_GN_U:
       if (dst_f64) {
-        VDVC_CUDA(cudaMemcpyAsync(dst, S->U64, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        // dst may be device or (pinned, mapped) host memory
+        VDVC_CUDA(cudaMemcpyAsync(dst, S->U64, nd * sizeof(double), cudaMemcpyDefault, s));
       } else {
         k_copy_out<double><<<nblk(nd), 256, 0, s>>>(S->U64, nd, dst, 0);
         VDVC_LAUNCHED();
@@ -821,7 +822,7 @@ static int read(GnSolver<T>* S, int which, void* dst, int dst_f64, cudaStream_t 
       VDVC_LAUNCHED();
       return VDVC_OK;
     case VDVC_GN_LIVE_MASK:
-      VDVC_CUDA(cudaMemcpyAsync(dst, S->live, nv, cudaMemcpyDeviceToDevice, s));
+      VDVC_CUDA(cudaMemcpyAsync(dst, S->live, nv, cudaMemcpyDefault, s));
       return VDVC_OK;
   }
   return set_error(VDVC_ERR_ARG, "unknown buffer %d", which);

@@ -10,30 +10,44 @@ namespace {
 // C-order (nx,ny,nz) -> x-fastest: 32x32 (z,x) tiles of kP2vPlanes
 // consecutive y planes per block (blockIdx.z), staged through shared memory
 // so both sides are coalesced; a thread has 4 * kP2vPlanes loads in flight.
+// With a step s > 1 the output is the every-s-th-voxel grid
+// (nx, ny, nz here being its extents): the transpose of the strided
+// decimation, reading only those voxels (a warp's 32 z-values span 32 s
+// consecutive source elements).
 constexpr int kP2vPlanes = 4;
 
+// Tiles are numbered z-tile fastest; a block walks tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... (one tile per block, or a bounded grid for a
+// transpose that runs in the background of other work).
 template <typename Tin, typename Tout>
 __global__ void __launch_bounds__(256) k_pix_to_vox(const Tin* __restrict__ in, Tout* __restrict__ out,
-                                                    int nx, int ny, int nz) {
+                                                    int nx, int ny, int nz, int s, int sny, int snz) {
   __shared__ Tout tile[kP2vPlanes][32][33];
-  const int z0 = blockIdx.x * 32, x0 = blockIdx.y * 32, y0 = blockIdx.z * kP2vPlanes;
+  const long long nzt = (nz + 31) / 32, nxt = (nx + 31) / 32, nyt = (ny + kP2vPlanes - 1) / kP2vPlanes;
+  for (long long tl = blockIdx.x; tl < nzt * nxt * nyt; tl += gridDim.x) {
+    const int z0 = (int)(tl % nzt) * 32, x0 = (int)((tl / nzt) % nxt) * 32;
+    const int y0 = (int)(tl / (nzt * nxt)) * kP2vPlanes;
+    __syncthreads();  // the previous tile's reads of `tile` are done
 #pragma unroll
-  for (int p = 0; p < kP2vPlanes; ++p) {
-    const int y = y0 + p;
+    for (int p = 0; p < kP2vPlanes; ++p) {
+      const int y = y0 + p;
 #pragma unroll
-    for (int r = threadIdx.y; r < 32; r += 8) {
-      const int x = x0 + r, z = z0 + threadIdx.x;
-      if (y < ny && x < nx && z < nz) tile[p][r][threadIdx.x] = (Tout)in[((size_t)x * ny + y) * nz + z];
+      for (int r = threadIdx.y; r < 32; r += 8) {
+        const int x = x0 + r, z = z0 + threadIdx.x;
+        if (y < ny && x < nx && z < nz)
+          tile[p][r][threadIdx.x] = (Tout)in[((size_t)x * s * sny + (size_t)y * s) * snz + (size_t)z * s];
+      }
     }
-  }
-  __syncthreads();
+    __syncthreads();
 #pragma unroll
-  for (int p = 0; p < kP2vPlanes; ++p) {
-    const int y = y0 + p;
+    for (int p = 0; p < kP2vPlanes; ++p) {
+      const int y = y0 + p;
 #pragma unroll
-    for (int r = threadIdx.y; r < 32; r += 8) {
-      const int z = z0 + r, x = x0 + threadIdx.x;
-      if (y < ny && x < nx && z < nz) out[(size_t)x + (size_t)y * nx + (size_t)z * nx * ny] = tile[p][threadIdx.x][r];
+      for (int r = threadIdx.y; r < 32; r += 8) {
+        const int z = z0 + r, x = x0 + threadIdx.x;
+        if (y < ny && x < nx && z < nz)
+          out[(size_t)x + (size_t)y * nx + (size_t)z * nx * ny] = tile[p][threadIdx.x][r];
+      }
     }
   }
 }
@@ -170,23 +184,30 @@ inline int grid_for(long long n, int threads) {
   return (int)b;
 }
 
+// (nx, ny, nz): the source; the output grid is ceil(n / step) per axis;
+// max_blocks > 0 bounds the grid (the blocks then walk the tiles)
 template <typename Tin, typename Tout>
-int launch_p2v(const void* pix, int nx, int ny, int nz, void* vox, cudaStream_t s) {
-  dim3 grid((nz + 31) / 32, (nx + 31) / 32, (ny + kP2vPlanes - 1) / kP2vPlanes), block(32, 8);
-  k_pix_to_vox<Tin, Tout><<<grid, block, 0, s>>>((const Tin*)pix, (Tout*)vox, nx, ny, nz);
+int launch_p2v(const void* pix, int nx, int ny, int nz, int step, long long max_blocks, void* vox, cudaStream_t s) {
+  const int ox = (nx + step - 1) / step, oy = (ny + step - 1) / step, oz = (nz + step - 1) / step;
+  long long tiles = (long long)((oz + 31) / 32) * ((ox + 31) / 32) * ((oy + kP2vPlanes - 1) / kP2vPlanes);
+  if (max_blocks > 0 && tiles > max_blocks) tiles = max_blocks;
+  if (tiles >= 0x7fffffffLL) return set_error(VDVC_ERR_ARG, "image too large");
+  k_pix_to_vox<Tin, Tout><<<(unsigned)tiles, dim3(32, 8), 0, s>>>((const Tin*)pix, (Tout*)vox, ox, oy, oz, step, ny,
+                                                                  nz);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
 
 template <typename Tout>
-int p2v_dispatch(const void* pix, int pix_dtype, int nx, int ny, int nz, void* vox, cudaStream_t s) {
+int p2v_dispatch(const void* pix, int pix_dtype, int nx, int ny, int nz, int step, long long mb, void* vox,
+                 cudaStream_t s) {
   switch (pix_dtype) {
-    case VDVC_F32: return launch_p2v<float, Tout>(pix, nx, ny, nz, vox, s);
-    case VDVC_F64: return launch_p2v<double, Tout>(pix, nx, ny, nz, vox, s);
-    case VDVC_U8: return launch_p2v<uint8_t, Tout>(pix, nx, ny, nz, vox, s);
-    case VDVC_U16: return launch_p2v<uint16_t, Tout>(pix, nx, ny, nz, vox, s);
-    case VDVC_I16: return launch_p2v<int16_t, Tout>(pix, nx, ny, nz, vox, s);
-    case VDVC_I32: return launch_p2v<int32_t, Tout>(pix, nx, ny, nz, vox, s);
+    case VDVC_F32: return launch_p2v<float, Tout>(pix, nx, ny, nz, step, mb, vox, s);
+    case VDVC_F64: return launch_p2v<double, Tout>(pix, nx, ny, nz, step, mb, vox, s);
+    case VDVC_U8: return launch_p2v<uint8_t, Tout>(pix, nx, ny, nz, step, mb, vox, s);
+    case VDVC_U16: return launch_p2v<uint16_t, Tout>(pix, nx, ny, nz, step, mb, vox, s);
+    case VDVC_I16: return launch_p2v<int16_t, Tout>(pix, nx, ny, nz, step, mb, vox, s);
+    case VDVC_I32: return launch_p2v<int32_t, Tout>(pix, nx, ny, nz, step, mb, vox, s);
   }
   return set_error(VDVC_ERR_ARG, "pix_dtype %d not supported", pix_dtype);
 }
@@ -203,8 +224,20 @@ int vdvc_pix_to_vox(const void* pix, int pix_dtype, int nx, int ny, int nz, void
   VDVC_CHECK_ARG(pix && vox, "null pointer");
   VDVC_CHECK_ARG(nx >= 1 && ny >= 1 && nz >= 1 && ny <= 65535, "bad image shape (%d,%d,%d)", nx, ny, nz);
   cudaStream_t s = (cudaStream_t)stream;
-  if (dtype == VDVC_F32) return p2v_dispatch<float>(pix, pix_dtype, nx, ny, nz, vox, s);
-  if (dtype == VDVC_F64) return p2v_dispatch<double>(pix, pix_dtype, nx, ny, nz, vox, s);
+  if (dtype == VDVC_F32) return p2v_dispatch<float>(pix, pix_dtype, nx, ny, nz, 1, 0, vox, s);
+  if (dtype == VDVC_F64) return p2v_dispatch<double>(pix, pix_dtype, nx, ny, nz, 1, 0, vox, s);
+  return set_error(VDVC_ERR_ARG, "dtype %d must be VDVC_F32 or VDVC_F64", dtype);
+}
+
+int vdvc_pix_to_vox_strided(const void* pix, int pix_dtype, int nx, int ny, int nz, int step, int max_blocks,
+                            void* vox, int dtype, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(pix && vox, "null pointer");
+  VDVC_CHECK_ARG(step >= 1 && step <= 64, "step %d must be in [1, 64]", step);
+  VDVC_CHECK_ARG(max_blocks >= 0, "max_blocks must be >= 0");
+  VDVC_CHECK_ARG(nx >= 1 && ny >= 1 && nz >= 1, "bad image shape (%d,%d,%d)", nx, ny, nz);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == VDVC_F32) return p2v_dispatch<float>(pix, pix_dtype, nx, ny, nz, step, max_blocks, vox, s);
+  if (dtype == VDVC_F64) return p2v_dispatch<double>(pix, pix_dtype, nx, ny, nz, step, max_blocks, vox, s);
   return set_error(VDVC_ERR_ARG, "dtype %d must be VDVC_F32 or VDVC_F64", dtype);
 }
 

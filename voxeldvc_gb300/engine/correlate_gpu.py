@@ -72,17 +72,15 @@ def pix_to_vox(pix, dtype=np.float32):
     Returns (tensor (Nvox,), shape).  A large host array is read in place by
     the transpose kernel where the device reads pageable host memory
     (vdvc_device_reads_pageable), else staged through a device copy."""
-    if not D.is_tensor(pix):
+    if _host_readable(pix):
         a = np.asarray(pix)
-        if (a.ndim == 3 and a.nbytes >= _DIRECT_MIN_BYTES and a.flags.c_contiguous and
-                a.dtype in (np.float32, np.float64, np.uint8, np.uint16, np.int16, np.int32) and _host_direct()):
-            nx, ny, nz = a.shape
-            out = D.empty(nx * ny * nz, dtype)
-            _lib.check(_lib.lib().vdvc_pix_to_vox(a.ctypes.data, D.code_of(a.dtype), nx, ny, nz, out.data_ptr(),
-                                                  D.code_of(dtype), D.stream()), "pix_to_vox")
-            # the kernel reads `a`: finish before the caller may free or change it
-            D.torch().cuda.current_stream().synchronize()
-            return out, (nx, ny, nz)
+        nx, ny, nz = a.shape
+        out = D.empty(nx * ny * nz, dtype)
+        _lib.check(_lib.lib().vdvc_pix_to_vox(a.ctypes.data, D.code_of(a.dtype), nx, ny, nz, out.data_ptr(),
+                                              D.code_of(dtype), D.stream()), "pix_to_vox")
+        # the kernel reads `a`: finish before the caller may free or change it
+        D.torch().cuda.current_stream().synchronize()
+        return out, (nx, ny, nz)
     t, code, shape = _pix_code_and_tensor(pix)
     if len(shape) != 3:
         raise ValueError(f"expected a 3-D volume, got shape {shape}")
@@ -91,6 +89,38 @@ def pix_to_vox(pix, dtype=np.float32):
     _lib.check(_lib.lib().vdvc_pix_to_vox(t.data_ptr(), code, nx, ny, nz, out.data_ptr(), D.code_of(dtype),
                                           D.stream()), "pix_to_vox")
     return out, (nx, ny, nz)
+
+
+def _host_readable(pix):
+    """pix is a host array that the layout kernel may read in place."""
+    if D.is_tensor(pix):
+        return False
+    a = np.asarray(pix)
+    return (a.ndim == 3 and a.nbytes >= _DIRECT_MIN_BYTES and a.flags.c_contiguous and
+            a.dtype in (np.float32, np.float64, np.uint8, np.uint16, np.int16, np.int32) and _host_direct())
+
+
+def _pix_to_vox_strided_host(a, s, dtype):
+    """Vox layout of a[::s, ::s, ::s] read in place from the host array `a`
+    (the caller keeps `a` alive until the current stream has finished)."""
+    nx, ny, nz = a.shape
+    o = ((nx + s - 1) // s, (ny + s - 1) // s, (nz + s - 1) // s)
+    out = D.empty(o[0] * o[1] * o[2], dtype)
+    _lib.check(_lib.lib().vdvc_pix_to_vox_strided(a.ctypes.data, D.code_of(a.dtype), nx, ny, nz, s, 0,
+                                                  out.data_ptr(), D.code_of(dtype), D.stream()), "pix_to_vox_strided")
+    return out, o
+
+
+_LAYOUT_STREAMS = {}
+_BACKGROUND_LAYOUT_BLOCKS = 2 * 152  # two 256-thread blocks per SM of a GB300
+
+
+def _layout_stream():
+    torch = D.torch()
+    key = torch.cuda.current_device()
+    if key not in _LAYOUT_STREAMS:
+        _LAYOUT_STREAMS[key] = torch.cuda.Stream()
+    return _LAYOUT_STREAMS[key]
 
 
 def _vox_to_pix_host(vox, shape):
@@ -556,10 +586,12 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
                  c_reg=1.0, reg_type='laplacian', K_ref_elastic=None, eps_reg=1e-3, dynamic_mask=False,
                  freeze_mask_after=None, U0=None, maxiter=30, eps=1e-3, pcg_tol=1e-6, pcg_max_iter=2000,
                  disp=True, dtype=np.float32, pcg_chunk=0, stats=None, precision='plain', mixed_min_h=4,
-                 hessian='auto', U0_async=None):
+                 hessian='auto', U0_async=None, res_dst=None):
     """One pyramid level: set-up, GN iterations, read-back.  U0_async:
     (U0 float64 CUDA tensor, CUDA event or None) produced on another stream
-    -- the set-up is enqueued first and only the iterations wait for it."""
+    -- the set-up is enqueued first and only the iterations wait for it.
+    res_dst: a pinned host tensor of the residual's size and output dtype
+    that the read-back writes directly (returned as res)."""
     if U0_async is not None and U0 is not None:
         raise ValueError("give U0 or U0_async, not both")
     ls = _setup_level(lv, Nx, Ny, Nz, h, g_origin=g_origin, glt=glt, l0=l0, K_ref_laplacian=K_ref_laplacian,
@@ -611,7 +643,7 @@ def _solve_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
         info["converged"] = bool(err < eps)
         info["norm_res"] = _norm_res(out8, ls.std0)
         Uo = D.empty(Ndof, out_dt)
-        res = D.empty(Nvox, out_dt)
+        res = res_dst if res_dst is not None else D.empty(Nvox, out_dt)
         dU = D.empty(Ndof, out_dt)
         f64 = int(out_dt == np.float64)
         _lib.check(L.vdvc_gn_read(solver, _lib.GN_U, Uo.data_ptr(), f64, st), "read")
@@ -709,18 +741,61 @@ def multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, scales=(2, 1, 0),
                   % (rx, ry, rz, sx, sy, sz, t_aff[0], t_aff[1], t_aff[2],
                      aff_info['cost_translation_only'], aff_info['cost_final']))
 
-    # full-resolution images on the device once, vox layout, solve dtype
-    f_full, fs = pix_to_vox(f_pix, dtype)
-    g_full, gs = pix_to_vox(g_pix, dtype)
+    # full-resolution images on the device once, vox layout, solve dtype.
+    # Host images that the device reads in place: the coarsest level reads
+    # its every-s-th voxels straight from them, and the full-resolution
+    # layout runs on a side stream under that level's iterations; the finer
+    # levels wait for it.
+    coarse = {}
+    full_ready = None
+    if scales[0] > 0 and _host_readable(f_pix) and _host_readable(g_pix):
+        torch = D.torch()
+        fa, ga = np.asarray(f_pix), np.asarray(g_pix)
+        s0 = 2 ** scales[0]
+        coarse[s0] = (_pix_to_vox_strided_host(fa, s0, dtype), _pix_to_vox_strided_host(ga, s0, dtype))
+        fs, gs = tuple(fa.shape), tuple(ga.shape)
+        f_full = D.empty(fa.size, dtype)  # allocated on this stream: the side stream only writes them
+        g_full = D.empty(ga.size, dtype)
+        main, side = torch.cuda.current_stream(), _layout_stream()
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            # a bounded grid: its blocks mostly wait on the host link and
+            # would otherwise hold every SM against the level's kernels
+            for a, out in ((fa, f_full), (ga, g_full)):
+                _lib.check(_lib.lib().vdvc_pix_to_vox_strided(a.ctypes.data, D.code_of(a.dtype), *a.shape, 1,
+                                                              _BACKGROUND_LAYOUT_BLOCKS, out.data_ptr(),
+                                                              D.code_of(dtype), D.stream()), "pix_to_vox")
+            full_ready = torch.cuda.Event()
+            full_ready.record(side)
+    else:
+        f_full, fs = pix_to_vox(f_pix, dtype)
+        g_full, gs = pix_to_vox(g_pix, dtype)
 
+    try:
+        return _pyramid(f_full, fs, g_full, gs, coarse, full_ready, scales, Nx, Ny, Nz, h, dtype, g_origin, l0, A_aff,
+                        t_aff, c_aff, fft_prealign, disp, xp, kwargs)
+    finally:
+        if full_ready is not None:
+            # both streams have finished reading the caller's arrays
+            full_ready.synchronize()
+            D.torch().cuda.current_stream().synchronize()
+
+
+def _pyramid(f_full, fs, g_full, gs, coarse, full_ready, scales, Nx, Ny, Nz, h, dtype, g_origin, l0, A_aff, t_aff,
+             c_aff, fft_prealign, disp, xp, kwargs):
     U = None
     prev_s = None
     res = dU = None
     for iscale in scales:
         s = 2 ** iscale
         h_i = h // s
-        f_i, fs_i = _decimate(f_full, fs, s, dtype)
-        g_i, gs_i = _decimate(g_full, gs, s, dtype)
+        if s in coarse:
+            (f_i, fs_i), (g_i, gs_i) = coarse.pop(s)
+        else:
+            if full_ready is not None:
+                D.torch().cuda.current_stream().wait_event(full_ready)
+            f_i, fs_i = _decimate(f_full, fs, s, dtype)
+            g_i, gs_i = _decimate(g_full, gs, s, dtype)
         g_origin_i = tuple(o // s for o in g_origin)
         l0_i = None if l0 is None else l0 / s
 
@@ -743,10 +818,20 @@ def multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, scales=(2, 1, 0),
         if disp:
             print("=== MULTISCALE: scale 2^%d (image decimated by %d, h_i=%d/%d=%d) ==="
                   % (iscale, s, h, s, h_i))
+        # host results: the finest level's residual field (the one large
+        # output) is converted straight into pinned host memory by the
+        # read-back kernel instead of a device copy and a transfer; its
+        # dtype follows the level set-up's rule (float64 when regularized
+        # or in a float64 solve)
+        res_ent = None
+        if iscale == scales[-1] and D.wants_host(xp) and kwargs.get('maxiter', 30) >= 1:
+            res_dt = np.dtype(np.float64) if (l0 is not None or dtype == np.float64) else dtype
+            res_ent = D.host_result(fs_i[0] * fs_i[1] * fs_i[2], res_dt)
         U, res, dU, _ = _solve_level(_Level(f_i, fs_i, g_i, gs_i), Nx, Ny, Nz, h_i, g_origin=g_origin_i, l0=l0_i,
-                                     U0=U, **kwargs)
+                                     U0=U, res_dst=None if res_ent is None else res_ent[0], **kwargs)
         prev_s = s
-    return D.out(U, xp), D.out(res, xp), D.out(dU, xp)
+    res_out = D.claim_host_result(res_ent) if res_ent is not None else D.out(res, xp)
+    return D.out(U, xp), res_out, D.out(dU, xp)
 
 
 # ---------------------------------------------------------------------------

@@ -98,12 +98,20 @@ def learned_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, g_origin=(0, 0, 0), l
         else:
             f_vox, fs = CG.pix_to_vox(f_pix, dtype)
             g_vox, gs = CG.pix_to_vox(g_pix, dtype)
+        # host results: the residual field is written straight into pinned
+        # host memory by the read-back (float64 when regularized or float64)
+        res_ent = None
+        if D.wants_host(xp) and kwargs.get("maxiter", 30) >= 1:
+            res_dt = np.dtype(np.float64) if (l0 is not None or dtype == np.float64) else dtype
+            res_ent = D.host_result(fs[0] * fs[1] * fs[2], res_dt)
         U, res, dU, info = CG._solve_level(CG._Level(f_vox, fs, g_vox, gs), Nx, Ny, Nz, h, g_origin=g_origin, l0=l0,
-                                           U0_async=seed, stats=levels, **kwargs)
+                                           U0_async=seed, stats=levels,
+                                           res_dst=None if res_ent is None else res_ent[0], **kwargs)
         rho = info.get("norm_res", float("inf"))
         if np.isfinite(rho) and rho <= fallback_threshold and info.get("converged", False):
             levels.append(dict(seed="learned", norm_res=rho, seed_s=seed_s))
-            return D.out(U, xp), D.out(res, xp), D.out(dU, xp)
+            res_out = D.claim_host_result(res_ent) if res_ent is not None else D.out(res, xp)
+            return D.out(U, xp), res_out, D.out(dU, xp)
         reason = f"normalised residual {rho:.4f}" if rho > fallback_threshold or not np.isfinite(rho) \
             else "GN tolerance not met"
     U, res, dU = CG.multiscale_correlate_gpu(f_pix, g_pix, Nx, Ny, Nz, h, xp, scales=scales, g_origin=g_origin,
