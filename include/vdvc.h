@@ -126,7 +126,7 @@ int vdvc_image_grad(const void* f_vox, int dtype, int Nvx, int Nvy, int Nvz,
    sums of vdvc_masked_stats over mask0 for the mesh (h, Nx, Ny, Nz) whose
    voxel grid f is: out3 (device) = count, sum f, sum f^2 -- the level
    set-up's reference statistics (engine/correlate_gpu.py:951-962).
-   ws: >= 3 * 1024 * 8 + 512 bytes. */
+   ws: >= 3 * 8192 * 8 + 512 bytes. */
 int vdvc_image_grad_stats(const float* f_vox, int Nvx, int Nvy, int Nvz,
                           double glt, float* grad, uint8_t* mask0, int h,
                           int Nx, int Ny, int Nz, double* out3, void* ws,

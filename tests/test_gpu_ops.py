@@ -116,7 +116,7 @@ def test_image_grad_stats_fused(api, case):
     grad = torch.empty(3 * n, dtype=torch.float32, device="cuda")
     m0 = torch.empty(n, dtype=torch.uint8, device="cuda")
     out3 = torch.zeros(3, dtype=torch.float64, device="cuda")
-    ws = torch.empty(1 << 16, dtype=torch.uint8, device="cuda")
+    ws = torch.empty(1 << 18, dtype=torch.uint8, device="cuda")
     L = _lib.lib()
     s = torch.cuda.current_stream().cuda_stream
     _lib.check(L.vdvc_image_grad_stats(f_vox.data_ptr(), Nvx, Nvy, Nvz, glt, grad.data_ptr(), m0.data_ptr(), h, Nx,

@@ -107,6 +107,11 @@ __global__ void __launch_bounds__(256) k_image_grad(const T* __restrict__ f, int
   }
 }
 
+// Blocks of the fused pass: enough 256-thread blocks for ~7 voxel loads in
+// flight per thread to cover HBM latency (1024 left it latency-bound), one
+// float64 partial triple each.
+constexpr int kImageGradStatsBlocks = 8192;
+
 // k_image_grad<float> with mask0 plus the multiplicity-weighted sums of f
 // over mask0 (vdvc_masked_stats' count, sum, sum of squares) in the same
 // read of f: 32-bit voxel indices, float partials folded into float64
@@ -294,14 +299,14 @@ int vdvc_image_grad_stats(const float* f_vox, int Nvx, int Nvy, int Nvz, double 
                  Nvx, Nvy, Nvz);
   Carve cv(ws, ws_bytes);
   GridReduce red;
-  red.partials = cv.take<double>(3 * kReduceBlocks);
+  red.partials = cv.take<double>(3 * kImageGradStatsBlocks);
   red.ticket = cv.take<unsigned int>(1);
   VDVC_CHECK_ARG(ws && cv.fits(), "image_grad_stats needs %zu bytes of workspace", cv.off);
   cudaStream_t s = (cudaStream_t)stream;
   VDVC_CUDA(cudaMemsetAsync(red.ticket, 0, sizeof(unsigned int), s));
   const long long n = (long long)Nvx * Nvy * Nvz;
-  k_image_grad_stats<<<grid_blocks(n, 256, kReduceBlocks), 256, 0, s>>>(f_vox, Nvx, Nvy, Nvz, (float)glt, grad,
-                                                                       mask0, h, Nx, Ny, Nz, red, out3);
+  k_image_grad_stats<<<grid_blocks(n, 256, kImageGradStatsBlocks), 256, 0, s>>>(f_vox, Nvx, Nvy, Nvz, (float)glt,
+                                                                               grad, mask0, h, Nx, Ny, Nz, red, out3);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }

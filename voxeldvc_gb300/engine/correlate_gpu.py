@@ -446,7 +446,7 @@ def _setup_level(lv, Nx, Ny, Nz, h, g_origin=(0, 0, 0), glt=0.0, l0=None, K_ref_
         # gradient, mask0 and the statistics of f over mask0 in one read of f
         grad = D.empty(3 * Nvox, dtype)
         mask0 = D.empty(Nvox, np.uint8)
-        ws_ = D.scratch.get(1 << 16)
+        ws_ = D.scratch.get(1 << 18)
         _lib.check(L.vdvc_image_grad_stats(lv.f_vox.data_ptr(), Nvx, Nvy, Nvz, float(glt), grad.data_ptr(),
                                            mask0.data_ptr(), h, Nx, Ny, Nz, dsc.data_ptr(), ws_.data_ptr(),
                                            ws_.numel(), D.stream()), "image_grad_stats")
