@@ -7,11 +7,12 @@
 // packed forward weights [n_pad][27][cin] and of the input-gradient weights
 // [cin_pad][27][n_pad16], so both read unchanged.
 //
-// Two kernels share the epilogue (TMEM -> registers, bias, ReLU, BF16 or
+// The kernels share the epilogue (TMEM -> registers, bias, ReLU, BF16 or
 // FP32 stores, each warp its 32 lanes = 32 positions):
 //
-// k_conv_tma -- geometries with a unit source step (d = 1: every forward
-// convolution, stride 1 or 2, and the input gradient of a stride-1 one).
+// k_conv_tma, k_conv_tma_p -- geometries with a unit source step (d = 1:
+// every forward convolution, stride 1 or 2, and the input gradient of a
+// stride-1 one).
 // The CTA's 128 positions are an 8 x 4 x 4 brick of the output grid, so for
 // tap t and a block of CB input channels the A operand is one box of a 4-D
 // tensor map over the channels-last source (channel, x, y, z): the box starts
@@ -21,7 +22,9 @@
 // land in the 128-byte (CB = 64) or 64-byte (CB = 32) swizzled K-major
 // layout the MMA descriptors name.  One thread issues the copies, another
 // the MMAs; full/empty mbarriers per stage, no CTA-wide barrier in the main
-// loop.
+// loop.  k_conv_tma_p is the persistent form (two CTAs per SM walking the
+// bricks, two TMEM accumulators so that a brick's epilogue runs under the
+// next brick's main loop), used for N >= 32.
 //
 // k_conv_tc -- the other geometries (input gradients of stride-2 layers,
 // d = 2) and channel counts that are multiples of 8 but not of 32.  A K-block
@@ -547,6 +550,164 @@ __global__ void __launch_bounds__(kThreads) k_conv_tma(const __grid_constant__ C
   }
 }
 
+// ---------------------------------------------------------------------------
+// k_conv_tma_p: the same convolution as a persistent kernel, two CTAs per SM
+// each walking bricks blockIdx.x, blockIdx.x + gridDim.x, ...  Warp 0's lane 0
+// issues the copies of every K-block of every brick through a ring of S
+// stages (it never waits for a brick to finish), warp 1's lane 0 issues the
+// MMAs into one of two TMEM accumulators (alternating per brick), and warps
+// 2-5 (one per TMEM lane quarter) read a finished accumulator, store it and
+// hand it back -- a brick's epilogue runs under the next brick's main loop.
+// Barriers: full/empty per stage, accumulator full (MMA commit) / empty (one
+// arrival per epilogue warp) per accumulator.  Every wait is bounded and
+// gives up once the CTA or the launch has reported a failure; copies and
+// MMAs in flight are drained (bounded) before the TMEM is freed.
+
+constexpr int kPThreads = 192;
+constexpr uint32_t kPStageBudget = 96 * 1024;
+constexpr int kPMaxStages = 12;
+
+template <int CB>
+__global__ void __launch_bounds__(kPThreads, 2) k_conv_tma_p(const __grid_constant__ CUtensorMap tmA,
+                                                             const __grid_constant__ CUtensorMap tmB,
+                                                             const ConvTmaArgs P, int ntiles) {
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = smem_addr(smem_raw);
+  unsigned char* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int S = P.stages, NT = P.e.NT;
+  volatile int* gerr = P.err;
+  constexpr uint32_t aBytes = (uint32_t)kM * CB * 2;
+  const uint32_t stageBytes = aBytes + (uint32_t)NT * CB * 2;
+  uint64_t* full = (uint64_t*)(smem + S * stageBytes);
+  uint64_t* empty = full + S;
+  uint64_t* accf = empty + S;  // [2]
+  uint64_t* acce = accf + 2;   // [2]
+  uint64_t* done = acce + 2;
+  uint32_t* s_tmem = (uint32_t*)(done + 1);
+  volatile int* s_abort = (volatile int*)(s_tmem + 1);
+  int* s_cnt = (int*)(s_tmem + 2);  // [0] K-blocks whose copies were issued, [1] consumed by MMAs
+
+  uint32_t ncols = 32;
+  while ((int)ncols < 2 * NT) ncols <<= 1;
+  if (warp == 0) {
+    tc_alloc(s_tmem, ncols);
+    tc_relinquish();
+  }
+  if (tid == 32) {
+    for (int st = 0; st < S; ++st) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], 1);
+    }
+    for (int q = 0; q < 2; ++q) {
+      mbar_init(&accf[q], 1);
+      mbar_init(&acce[q], 4);
+    }
+    mbar_init(done, 1);
+    *s_abort = 0;
+    s_cnt[0] = s_cnt[1] = 0;
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *s_tmem;
+  const int nkb = P.nkb;
+
+  if (tid == 0) {
+    // producer
+    int g = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      const int x0 = (tile % P.nbx) * kBX, y0 = ((tile / P.nbx) % P.nby) * kBY, z0 = (tile / (P.nbx * P.nby)) * kBZ;
+      for (int kb = 0; kb < nkb; ++kb, ++g) {
+        const int st = g % S;
+        if (g >= S && !wait_or_abort(&empty[st], (uint32_t)((g / S - 1) & 1), s_abort, gerr, 0)) {
+          *s_abort = 1;
+          atomicExch(P.err, 1);
+          ok = false;
+          break;
+        }
+        const int t = kb / P.ncb, cb = kb - t * P.ncb;
+        const int tx = t % 3, ty = (t / 3) % 3, tz = t / 9;
+        const uint32_t sa = smem_addr(smem + st * stageBytes), fb = smem_addr(&full[st]);
+        mbar_arrive_expect_tx(&full[st], stageBytes);
+        tma_load_4d(sa, &tmA, P.scoff + cb * CB, P.a * x0 + P.b + P.c * tx, P.a * y0 + P.b + P.c * ty,
+                    P.a * z0 + P.b + P.c * tz, fb);
+        tma_load_2d(sa + aBytes, &tmB, t * P.cin + cb * CB, 0, fb);
+      }
+    }
+    s_cnt[0] = g;
+  } else if (tid == 32) {
+    // MMA issuer
+    const uint32_t idesc = idesc_bf16(kM, NT);
+    int g = 0, it = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++it) {
+      const int acc = it & 1;
+      if (it >= 2 && !wait_or_abort(&acce[acc], (uint32_t)((it / 2 - 1) & 1), s_abort, gerr, 0)) {
+        *s_abort = 1;
+        atomicExch(P.err, 1);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + (uint32_t)(acc * NT);
+      for (int kb = 0; kb < nkb; ++kb, ++g) {
+        const int st = g % S;
+        if (!wait_or_abort(&full[st], (uint32_t)((g / S) & 1), s_abort, gerr, 0)) {
+          *s_abort = 1;
+          atomicExch(P.err, 1);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t sa = smem_addr(smem + st * stageBytes);
+#pragma unroll
+        for (int kk = 0; kk < CB / 16; ++kk)
+          tc_mma(d, sw_desc<CB>(sa + kk * 32), sw_desc<CB>(sa + aBytes + kk * 32), idesc,
+                 (kb > 0 || kk > 0) ? 1u : 0u);
+        tc_commit(&empty[st]);
+      }
+      if (ok) tc_commit(&accf[acc]);
+    }
+    s_cnt[1] = g;
+    tc_commit(done);  // tracks every MMA issued before it
+  } else if (warp >= 2) {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31
+    const int q = warp & 3;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      const int acc = it & 1;
+      if (!wait_or_abort(&accf[acc], (uint32_t)((it / 2) & 1), s_abort, gerr, 0)) break;
+      tc_fence_after();
+      const int x0 = (tile % P.nbx) * kBX, y0 = ((tile / P.nbx) % P.nby) * kBY, z0 = (tile / (P.nbx * P.nby)) * kBZ;
+      const int r = q * 32 + lane;
+      const int x = x0 + r % kBX, y = y0 + (r / kBX) % kBY, z = z0 + r / (kBX * kBY);
+      store_rows(tmem + (uint32_t)(acc * NT), q, x < P.nx && y < P.ny && z < P.nz,
+                 ((long long)z * P.ny + y) * P.nx + x, P.e);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[acc]);
+    }
+  }
+  __syncwarp();
+  // MMAs issued so far always complete: no early exit on *gerr
+  bool ok = wait_or_abort(done, 0, nullptr, gerr, 1LL << 22);
+  tc_fence_after();
+  __syncthreads();
+  if (tid == 0)
+    for (int g = s_cnt[1]; g < s_cnt[0]; ++g)
+      if (!wait_or_abort(&full[g % S], (uint32_t)((g / S) & 1), nullptr, gerr, 1LL << 14)) ok = false;
+  const bool fail = __syncthreads_or(!ok || *s_abort != 0);
+  if (fail && tid == 0) atomicExch(P.err, 1);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tc_dealloc(tmem, ncols);
+  }
+}
+
 }  // namespace
 
 size_t conv_tc_smem_bytes(int n_out) {
@@ -574,6 +735,23 @@ int launch_tma_cb(const CUtensorMap& ta, const CUtensorMap& tb, const ConvTmaArg
                   cudaStream_t s) {
   if (int st = ensure_dyn_smem((const void*)k_conv_tma<CB>, (int)smem)) return st;
   k_conv_tma<CB><<<nb, kThreads, smem, s>>>(ta, tb, a);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
+}
+
+template <int CB>
+int launch_tma_p(const CUtensorMap& ta, const CUtensorMap& tb, ConvTmaArgs a, long long ntiles, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  VDVC_CUDA(cudaGetDevice(&dev));
+  VDVC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t stage = (uint32_t)(kM + a.e.NT) * CB * 2;
+  a.stages = (int)(kPStageBudget / stage);
+  if (a.stages > kPMaxStages) a.stages = kPMaxStages;
+  if (a.stages < 2) return VDVC_ERR_UNSUPPORTED;
+  const size_t smem = (size_t)a.stages * stage + 1024 + (2 * a.stages + 5) * 8 + 16;
+  if (int st = ensure_dyn_smem((const void*)k_conv_tma_p<CB>, (int)smem)) return st;
+  const long long nb = ntiles < 2LL * sms ? ntiles : 2LL * sms;
+  k_conv_tma_p<CB><<<(unsigned)nb, kPThreads, smem, s>>>(ta, tb, a, (int)ntiles);
   VDVC_LAUNCHED();
   return VDVC_OK;
 }
@@ -641,6 +819,11 @@ int launch_conv_tma(const void* src, int scs, int scoff, int cin, const void* w,
   if (nb >= 0x7fffffffLL) return set_error(VDVC_ERR_ARG, "grid too large");
   // stages + 1 KB of alignment slack + barriers and flags
   const size_t smem = (size_t)a.stages * stage + 1024 + (2 * a.stages + 1) * 8 + 16;
+  // the persistent form where a brick's stages are large (N >= 32: at most
+  // two one-brick CTAs would fit an SM anyway); with N = 16 the one-brick
+  // form keeps three CTAs per SM and is faster (513^3 output layer 78 vs
+  // 108 us; e2b 140 vs 113 us the other way round)
+  if (NT >= 32) return CB == 64 ? launch_tma_p<64>(ta, tb, a, nb, s) : launch_tma_p<32>(ta, tb, a, nb, s);
   return CB == 64 ? launch_tma_cb<64>(ta, tb, a, (unsigned)nb, smem, s)
                   : launch_tma_cb<32>(ta, tb, a, (unsigned)nb, smem, s);
 }
