@@ -43,7 +43,10 @@ typedef struct vdvc_conv_geom {
    channel stride and offset multiples of 8, src and w 16-byte aligned;
    n_out <= 256), else mma.sync m16n8k16 (n_out <= 80).
    cin: a multiple of 16, or 2 (then w is [n_pad][64] with k = 2t + ci and
-   zero rows k >= 54, mma.sync).  Otherwise w is BF16 [n_pad][27][cin].
+   zero rows k >= 54; a forward stride-1 layer with n_out <= 64 on a
+   contiguous 2-channel source runs on tcgen05 with its A tile built in
+   shared memory from the brick's source halo, other 2-channel layers on
+   mma.sync).  Otherwise w is BF16 [n_pad][27][cin].
    n_pad = n_out rounded up to 8; rows n >= n_out must be zero.
    bias: FP32 (n_out) or NULL.  relu: apply max(0, .).
    out_f32: store FP32 instead of BF16.  accumulate (BF16 output only):

@@ -1,7 +1,8 @@
 // Kernels of the learned initial guess (include/vdvc_cnn.h): BF16 3x3x3
-// convolutions as implicit GEMMs on the tensor cores (mma.sync m16n8k16,
-// FP32 accumulation), their weight gradients, and the small elementwise
-// pieces of training and inference.
+// convolutions as implicit GEMMs on the tensor cores -- the tcgen05 forms
+// live in conv_tc.cu; here the mma.sync m16n8k16 form (FP32 accumulation)
+// for the layers those do not take -- their weight gradients, and the small
+// elementwise pieces of training and inference.
 //
 // Convolution = gather GEMM.  Output positions are the GEMM rows (M), output
 // channels the columns (N), and (tap, input channel) the reduction (K).  A
@@ -37,6 +38,9 @@ int launch_conv_tc(const void* src, int scs, int scoff, int cin, const void* w, 
 int launch_conv_tma(const void* src, int scs, int scoff, int cin, const void* w, int wrows, const float* bias,
                     int n_out, int relu, void* out, int out_f32, int ocs, int ocoff, int accumulate,
                     const vdvc_conv_geom* geom, int* err, cudaStream_t s);
+int launch_conv_first(const void* src, int scs, int scoff, const void* w, int wrows, const float* bias, int n_out,
+                      int relu, void* out, int out_f32, int ocs, int ocoff, int accumulate, const vdvc_conv_geom* g,
+                      int* err, cudaStream_t s);
 
 struct Geo {
   int nx, ny, nz, sx, sy, sz, a, b, c, d;
@@ -766,8 +770,15 @@ int vdvc_cnn_conv(const void* src, int src_cstride, int src_coff, int cin, const
   VDVC_CHECK_ARG(al4(src) && al4(w), "src and w must be 4-byte aligned");
   VDVC_CHECK_ARG(!(accumulate && out_f32), "accumulate needs a BF16 output");
   cudaStream_t s = (cudaStream_t)stream;
-  // the tensor-core form wherever the channel chunks are 16-byte aligned
-  if (cin != 2) {
+  // the tensor-core forms wherever the channel chunks are 16-byte aligned
+  if (cin == 2) {
+    int* err = nullptr;
+    int st = conv_error_flag(&err);
+    if (st) return st;
+    st = launch_conv_first(src, src_cstride, src_coff, w, (n_out + 7) / 8 * 8, bias, n_out, relu, out, out_f32,
+                           out_cstride, out_coff, accumulate, geom, err, s);
+    if (st != VDVC_ERR_UNSUPPORTED) return st;
+  } else {
     int* err = nullptr;
     int st = conv_error_flag(&err);
     if (st) return st;

@@ -26,6 +26,9 @@
 // bricks, two TMEM accumulators so that a brick's epilogue runs under the
 // next brick's main loop), used for N >= 32.
 //
+// k_conv_first -- the 2-channel first layer (K = 54), its A tile built in
+// shared memory from the brick's source halo (below).
+//
 // k_conv_tc -- the other geometries (input gradients of stride-2 layers,
 // d = 2) and channel counts that are multiples of 8 but not of 32.  A K-block
 // is 64 K values = eight 16-byte chunks of 8 channels; a chunk of row p is
@@ -708,6 +711,118 @@ __global__ void __launch_bounds__(kPThreads, 2) k_conv_tma_p(const __grid_consta
   }
 }
 
+// ---------------------------------------------------------------------------
+// k_conv_first: the 2-channel first layer (stride 1, K = 27 taps x 2
+// channels = 54, padded to 64) on the tensor cores.  Per CTA one 8 x 4 x 4
+// brick: the brick's 10 x 6 x 6 source halo (2 BF16 channels = one 32-bit
+// word per position, zero outside the volume: the padding) is loaded once
+// into shared memory, the 128 x 64 A tile is built from it there (row =
+// position, K = 2 t + c as the packed first-layer weights [n_pad8][64]
+// order it; one 16-byte chunk = 4 taps), B (<= 64 x 64) is staged from the
+// packed weights, and one thread issues the four K = 16 MMAs into TMEM.
+// No per-row or per-tap copies: the layer's whole input footprint is read
+// about once per brick instead of 27 times.
+
+constexpr int kHX = kBX + 2, kHY = kBY + 2, kHZ = kBZ + 2;  // halo of a brick
+constexpr int kHalo = kHX * kHY * kHZ;                      // 360 positions
+
+struct ConvFirstArgs {
+  const uint32_t* src;  // 2 BF16 channels per position (channel stride 2)
+  const bf16* w;        // [wrows][64]
+  int wrows;
+  int nx, ny, nz, nbx, nby;
+  Epi e;
+  int* err;
+};
+
+__global__ void __launch_bounds__(kThreads) k_conv_first(const ConvFirstArgs P) {
+  __shared__ __align__(128) unsigned char sA[kM * 64 * 2];  // 16 KB, no-swizzle K-major
+  __shared__ __align__(128) unsigned char sB[64 * 64 * 2];  // up to 64 rows
+  __shared__ uint32_t sH[kHalo];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int NT = P.e.NT;
+  uint32_t ncols = 32;
+  while ((int)ncols < NT) ncols <<= 1;
+  if (warp == 0) {
+    tc_alloc(&s_tmem, ncols);
+    tc_relinquish();
+  }
+  if (tid == 32) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  const int bid = blockIdx.x;
+  const int x0 = (bid % P.nbx) * kBX, y0 = ((bid / P.nbx) % P.nby) * kBY, z0 = (bid / (P.nbx * P.nby)) * kBZ;
+  // halo: positions (x0 - 1 .. x0 + 8, y0 - 1 .. y0 + 4, z0 - 1 .. z0 + 4)
+  for (int i = tid; i < kHalo; i += kThreads) {
+    const int hx = i % kHX, hy = (i / kHX) % kHY, hz = i / (kHX * kHY);
+    const int x = x0 - 1 + hx, y = y0 - 1 + hy, z = z0 - 1 + hz;
+    uint32_t v = 0u;
+    if (x >= 0 && y >= 0 && z >= 0 && x < P.nx && y < P.ny && z < P.nz)
+      v = __ldg(P.src + ((size_t)z * P.ny + y) * P.nx + x);
+    sH[i] = v;
+  }
+  // B: NT rows of 8 chunks (zero past the packed rows)
+  for (int q = tid; q < NT * 8; q += kThreads) {
+    const int n = q >> 3, c = q & 7;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (n < P.wrows) v = __ldg((const uint4*)(P.w + (size_t)n * 64) + c);
+    *(uint4*)(sB + c * (NT * 16) + (n >> 3) * 128 + (n & 7) * 16) = v;
+  }
+  __syncthreads();
+  // A: row r = this thread's position in the brick; chunk c = taps 4c .. 4c+3
+  {
+    const int r = tid;
+    const int rx = r % kBX, ry = (r / kBX) % kBY, rz = r / (kBX * kBY);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      uint32_t wv[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int t = 4 * c + j;
+        wv[j] = 0u;
+        if (t < 27) {
+          const int dx = t % 3, dy = (t / 3) % 3, dz = t / 9;
+          wv[j] = sH[(rx + dx) + kHX * ((ry + dy) + kHY * (rz + dz))];
+        }
+      }
+      *(uint4*)(sA + c * 2048 + (r >> 3) * 128 + (r & 7) * 16) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+    }
+  }
+  fence_proxy_async_smem();  // the tiles' generic stores before the tensor core reads them
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  if (tid == 0) {
+    const uint32_t a0 = smem_addr(sA), b0 = smem_addr(sB), bL = (uint32_t)NT * 16;
+    const uint32_t idesc = idesc_bf16(kM, NT);
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk)
+      tc_mma(tmem, smem_desc(a0 + kk * 2 * 2048, 2048, 128), smem_desc(b0 + kk * 2 * bL, bL, 128), idesc,
+             kk > 0 ? 1u : 0u);
+    tc_commit(&bar);
+  }
+  __syncwarp();
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  tc_fence_after();
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) atomicExch(P.err, 1);
+  } else {
+    const int r = warp * 32 + lane;
+    const int x = x0 + r % kBX, y = y0 + (r / kBX) % kBY, z = z0 + r / (kBX * kBY);
+    store_rows(tmem, warp, x < P.nx && y < P.ny && z < P.nz, ((long long)z * P.ny + y) * P.nx + x, P.e);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tc_dealloc(tmem, ncols);
+  }
+}
+
 }  // namespace
 
 size_t conv_tc_smem_bytes(int n_out) {
@@ -826,6 +941,34 @@ int launch_conv_tma(const void* src, int scs, int scoff, int cin, const void* w,
   if (NT >= 32) return CB == 64 ? launch_tma_p<64>(ta, tb, a, nb, s) : launch_tma_p<32>(ta, tb, a, nb, s);
   return CB == 64 ? launch_tma_cb<64>(ta, tb, a, (unsigned)nb, smem, s)
                   : launch_tma_cb<32>(ta, tb, a, (unsigned)nb, smem, s);
+}
+
+// The first-layer form: cin = 2 (packed [wrows][64] weights), forward
+// stride 1 (a = 1, b = -1, c = 1, d = 1, source grid = output grid),
+// n_out <= 64, a contiguous 2-channel source, 4-byte aligned.
+// VDVC_ERR_UNSUPPORTED otherwise (the caller keeps the mma.sync kernel).
+int launch_conv_first(const void* src, int scs, int scoff, const void* w, int wrows, const float* bias, int n_out,
+                      int relu, void* out, int out_f32, int ocs, int ocoff, int accumulate, const vdvc_conv_geom* g,
+                      int* err, cudaStream_t s) {
+  if (g->a != 1 || g->b != -1 || g->c != 1 || g->d != 1 || g->sx != g->nx || g->sy != g->ny || g->sz != g->nz)
+    return VDVC_ERR_UNSUPPORTED;
+  if (scs != 2 || scoff != 0 || n_out > 64 || (((uintptr_t)src | (uintptr_t)w) & 15)) return VDVC_ERR_UNSUPPORTED;
+  ConvFirstArgs a{};
+  a.src = (const uint32_t*)src;
+  a.w = (const bf16*)w;
+  a.wrows = wrows;
+  a.nx = g->nx;
+  a.ny = g->ny;
+  a.nz = g->nz;
+  a.nbx = (g->nx + kBX - 1) / kBX;
+  a.nby = (g->ny + kBY - 1) / kBY;
+  a.e = Epi{bias, n_out, (n_out + 15) / 16 * 16, relu, out_f32, ocs, ocoff, accumulate, out};
+  a.err = err;
+  const long long nb = (long long)a.nbx * a.nby * ((g->nz + kBZ - 1) / kBZ);
+  if (nb >= 0x7fffffffLL) return set_error(VDVC_ERR_ARG, "grid too large");
+  k_conv_first<<<(unsigned)nb, kThreads, 0, s>>>(a);
+  VDVC_LAUNCHED();
+  return VDVC_OK;
 }
 
 // VDVC_ERR_UNSUPPORTED (error text untouched) when the layer does not fit
