@@ -121,6 +121,36 @@ def test_conv_forward_input_grad_wgrad(env, cin, n_out, stride, src):
         assert rel(dw.cpu().numpy().reshape(ref_dw.shape), 2 * ref_dw) < 1e-5
 
 
+@pytest.mark.parametrize("cin,n_out,stride,src", [(64, 64, 1, (33, 33, 65)), (32, 32, 2, (65, 65, 129)),
+                                                  (128, 128, 1, (33, 17, 49))])
+def test_conv_persistent_many_bricks(env, cin, n_out, stride, src):
+    """More output bricks than resident CTAs (2 per SM): every CTA of the
+    persistent form walks several bricks through its stage ring, the two
+    TMEM accumulators alternating -- against the oracle."""
+    torch, L, S = env
+    lib = L.lib()
+    rng = np.random.default_rng(cin + n_out + stride)
+    sx, sy, sz = src
+    out = tuple((s - 1) // stride + 1 for s in src)
+    nbricks = -(-out[0] // 8) * -(-out[1] // 4) * -(-out[2] // 4)
+    assert nbricks > 2 * torch.cuda.get_device_properties(0).multi_processor_count
+    x = O.bf16_round(rng.standard_normal((sz, sy, sx, cin)))
+    W = rng.standard_normal((n_out, 27, cin)) * 0.1
+    bvec = rng.standard_normal(n_out).astype(np.float32)
+    ref = O.conv(x, O.bf16_round(W), bvec.astype(np.float64), stride, relu=True)
+    wf = torch.zeros((n_out + 7) // 8 * 8 * 27 * cin, dtype=torch.bfloat16, device="cuda")
+    wt = torch.from_numpy(W.astype(np.float32).reshape(-1)).cuda()
+    L.check(lib.vdvc_cnn_pack_weights(wt.data_ptr(), n_out, cin, wf.data_ptr(), None, stream(torch)))
+    xd, bd = bf(torch, x), torch.from_numpy(bvec).cuda()
+    y = torch.zeros(out[0] * out[1] * out[2] * n_out, dtype=torch.bfloat16, device="cuda")
+    g = S.fwd_geom(out, src, stride)
+    L.check(lib.vdvc_cnn_conv(xd.data_ptr(), cin, 0, cin, wf.data_ptr(), bd.data_ptr(), n_out, 1, y.data_ptr(), 0,
+                              n_out, 0, 0, C.byref(g), stream(torch)))
+    L.check(lib.vdvc_cnn_status(stream(torch)))
+    yh = host(y).reshape(ref.shape)
+    assert np.allclose(yh, ref, rtol=8e-3, atol=8e-3 * np.abs(ref).max())
+
+
 @pytest.mark.parametrize("cin,n_out,stride,scs,scoff", [(64, 64, 1, 128, 64), (32, 64, 2, 96, 32),
                                                         (256, 64, 1, 256, 0), (128, 128, 2, 256, 128)])
 def test_conv_channel_slices_and_accumulate(env, cin, n_out, stride, scs, scoff):
