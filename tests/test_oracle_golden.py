@@ -1,6 +1,6 @@
 """The CPU oracle against golden vectors produced by the reference's own code
 (tests/golden/make_golden.py).  This pins the oracle before it is used to
-judge the CUDA path."""
+check the CUDA path."""
 import numpy as np
 import pytest
 

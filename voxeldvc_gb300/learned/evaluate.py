@@ -16,7 +16,7 @@ inside the mesh border, with a true deformed position at least one element
 inside the volume: elsewhere the deformed position leaves g or its support
 is truncated), the fallback rate and the solve times.  Where the plain
 pyramid itself lands in a wrong minimum (large rotations), the FP64 solve
-does too, and the learned solve is judged against the true field.
+does too, and the learned solve is measured against the true field.
 
     python -m voxeldvc_gb300.learned.evaluate --pairs 200 --out eval.json
 """
