@@ -429,6 +429,12 @@ int vdvc_dot_device(const void* a, const void* b, int dtype, long long n,
 int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz,
                          const void* g_vox, int gnx, int gny, int gnz,
                          int dtype, double* d_out3, vdvc_stream_t stream);
+/* The same with the shift left on the device (d_dev3: 3 doubles) and no
+   host synchronisation: a seed consumed by device work on the same stream. */
+int vdvc_fft_rigid_shift_device(const void* f_vox, int fnx, int fny, int fnz,
+                                const void* g_vox, int gnx, int gny, int gnz,
+                                int dtype, double* d_dev3,
+                                vdvc_stream_t stream);
 
 /* ---- affine pre-alignment (engine/correlate_gpu.py:417-825) ------------ */
 /* Scratch bytes of the affine entry points below. */

@@ -95,6 +95,7 @@ SIGNATURES = {
     "vdvc_gt_node_oob_fraction": (ci, [vp, ci, ci, ci, ci, ci, ci, ci, C.POINTER(C.c_longlong), vp, vp]),
     "vdvc_unsafe_masks": (ci, [vp, vp, ci, ci, ci, ci, cd, cd, vp, vp, vp, vp, vp, cz, vp]),
     "vdvc_fft_rigid_shift": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, ci, pd, vp]),
+    "vdvc_fft_rigid_shift_device": (ci, [vp, ci, ci, ci, vp, ci, ci, ci, ci, vp, vp]),
     "vdvc_pcg_workspace_bytes": (cz, []),
     "vdvc_pcg_begin": (ci, [vp, vp, vp, ci, C.c_longlong, vp, vp, vp, ci, cd, vp, cz, vp]),
     "vdvc_pcg_step": (ci, [vp, vp, ci, C.c_longlong, vp, vp, vp, vp, vp, cz, pd, pi, vp]),

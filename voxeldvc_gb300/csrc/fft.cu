@@ -149,6 +149,7 @@ struct FftPlan {
   void *Fc, *Gc;  // half spectra
   ArgMax *partial, *result;
   unsigned int* ticket;
+  cudaEvent_t done;  // recorded after a call's last use; the next user's stream waits on it
   size_t bytes;
   unsigned long long stamp;
 };
@@ -164,6 +165,10 @@ static void fft_destroy(FftPlan* P) {
   int cur = 0;
   cudaGetDevice(&cur);
   if (cur != P->dev) cudaSetDevice(P->dev);
+  if (P->done) {
+    cudaEventSynchronize(P->done);  // no call still uses the buffers
+    cudaEventDestroy(P->done);
+  }
   if (P->pf) cufftDestroy(P->pf);
   if (P->pi) cufftDestroy(P->pi);
   cudaFree(P->fr);
@@ -177,7 +182,7 @@ static void fft_destroy(FftPlan* P) {
   delete P;
 }
 
-static int fft_acquire(int sx, int sy, int sz, bool single, FftPlan** out) {
+static int fft_acquire(int sx, int sy, int sz, bool single, cudaStream_t s, FftPlan** out) {
   int dev = 0;
   VDVC_CUDA(cudaGetDevice(&dev));
   {
@@ -187,6 +192,8 @@ static int fft_acquire(int sx, int sy, int sz, bool single, FftPlan** out) {
       if (P->dev == dev && P->sx == sx && P->sy == sy && P->sz == sz && P->single == single) {
         g_fft_cache.erase(g_fft_cache.begin() + i);
         *out = P;
+        // the previous call may still be running on its stream
+        VDVC_CUDA(cudaStreamWaitEvent(s, P->done, 0));
         return VDVC_OK;
       }
     }
@@ -207,7 +214,8 @@ static int fft_acquire(int sx, int sy, int sz, bool single, FftPlan** out) {
       cudaMalloc(&P->Fc, nc * cb) != cudaSuccess || cudaMalloc(&P->Gc, nc * cb) != cudaSuccess ||
       cudaMalloc((void**)&P->partial, kReduceBlocks * sizeof(ArgMax)) != cudaSuccess ||
       cudaMalloc((void**)&P->result, sizeof(ArgMax)) != cudaSuccess ||
-      cudaMalloc((void**)&P->ticket, sizeof(unsigned int)) != cudaSuccess) {
+      cudaMalloc((void**)&P->ticket, sizeof(unsigned int)) != cudaSuccess ||
+      cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     fft_destroy(P);
     return set_error(VDVC_ERR_CUDA, "fft_rigid_shift: device allocation failed");
@@ -226,8 +234,8 @@ static int fft_acquire(int sx, int sy, int sz, bool single, FftPlan** out) {
   return VDVC_OK;
 }
 
-static void fft_release(FftPlan* P, bool reuse) {
-  if (!reuse) {
+static void fft_release(FftPlan* P, bool reuse, cudaStream_t s) {
+  if (!reuse || cudaEventRecord(P->done, s) != cudaSuccess) {
     fft_destroy(P);
     return;
   }
@@ -304,18 +312,35 @@ int vdvc_dot_device(const void* a, const void* b, int dtype, long long n, double
   return VDVC_OK;
 }
 
-int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz, const void* g_vox, int gnx, int gny, int gnz,
-                         int dtype, double* d_out3, vdvc_stream_t stream) {
-  VDVC_CHECK_ARG(f_vox && g_vox && d_out3, "null pointer");
-  VDVC_CHECK_ARG(fnx >= 1 && fny >= 1 && fnz >= 1 && gnx >= 1 && gny >= 1 && gnz >= 1, "bad shapes");
-  VDVC_CHECK_ARG(dtype == VDVC_F32 || dtype == VDVC_F64, "dtype %d", dtype);
+// The shift from the arg-max's C-order index of pix[x,y,z]: (x,y,z)
+// wrapped to (-n/2, n/2] per axis, d = -peak.
+__host__ __device__ inline void shift_from_cidx(long long c, int sx, int sy, int sz, double* d) {
+  const int pz = (int)(c % sz);
+  c /= sz;
+  const int py = (int)(c % sy);
+  const int px = (int)(c / sy);
+  const int p[3] = {px, py, pz}, ns[3] = {sx, sy, sz};
+  for (int a = 0; a < 3; ++a) {
+    int q = p[a];
+    if (q > ns[a] / 2) q -= ns[a];
+    d[a] = -(double)q;
+  }
+}
+
+__global__ void k_shift_out(const ArgMax* __restrict__ r, int sx, int sy, int sz, double* __restrict__ d) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) shift_from_cidx(r->cidx, sx, sy, sz, d);
+}
+
+// Enqueues the phase correlation; the shift goes to d_dev (device, no host
+// synchronisation) or, when d_dev is null, to d_host after a synchronisation.
+static int fft_shift(const void* f_vox, int fnx, int fny, int fnz, const void* g_vox, int gnx, int gny, int gnz,
+                     int dtype, double* d_host, double* d_dev, cudaStream_t s) {
   const int sx = fnx < gnx ? fnx : gnx, sy = fny < gny ? fny : gny, sz = fnz < gnz ? fnz : gnz;
   const long long n = (long long)sx * sy * sz;
   const long long nc = (long long)sz * sy * (sx / 2 + 1);
-  cudaStream_t s = (cudaStream_t)stream;
   const bool single = dtype == VDVC_F32;
   FftPlan* P = nullptr;
-  int st = fft_acquire(sx, sy, sz, single, &P);
+  int st = fft_acquire(sx, sy, sz, single, s, &P);
   if (st) return st;
   const int nb = grid_blocks(n, 256, kReduceBlocks);
   ArgMax host;
@@ -360,28 +385,37 @@ int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz, const voi
     else
       k_argmax<double><<<nb, 256, 0, s>>>((const double*)P->fr, sx, sy, sz, P->partial, P->ticket, P->result);
     count_launch();
-    ok = cudaMemcpyAsync(&host, P->result, sizeof(ArgMax), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
-         cudaStreamSynchronize(s) == cudaSuccess;
+    if (d_dev) {
+      k_shift_out<<<1, 32, 0, s>>>(P->result, sx, sy, sz, d_dev);
+      count_launch();
+      ok = cudaGetLastError() == cudaSuccess;
+    } else {
+      ok = cudaMemcpyAsync(&host, P->result, sizeof(ArgMax), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+           cudaStreamSynchronize(s) == cudaSuccess;
+    }
     if (!ok) st = set_error(VDVC_ERR_CUDA, "fft_rigid_shift: %s", cudaGetErrorString(cudaGetLastError()));
   }
-  if (ok) {
-    // C-order index of pix[x,y,z] -> (x,y,z); wrap to (-n/2, n/2]; d = -peak
-    long long c = host.cidx;
-    const int pz = (int)(c % sz);
-    c /= sz;
-    const int py = (int)(c % sy);
-    const int px = (int)(c / sy);
-    const int p[3] = {px, py, pz}, ns[3] = {sx, sy, sz};
-    for (int a = 0; a < 3; ++a) {
-      int q = p[a];
-      if (q > ns[a] / 2) q -= ns[a];
-      d_out3[a] = -(double)q;
-    }
-  }
-  // the stream has finished with the plan and its buffers (synchronised
-  // above); after a failure they are dropped rather than reused
-  fft_release(P, ok);
+  if (ok && !d_dev) shift_from_cidx(host.cidx, sx, sy, sz, d_host);
+  // the plan goes back with an event after its last use on this stream (the
+  // next user's stream waits on it); after a failure it is dropped
+  fft_release(P, ok, s);
   return st;
+}
+
+int vdvc_fft_rigid_shift(const void* f_vox, int fnx, int fny, int fnz, const void* g_vox, int gnx, int gny, int gnz,
+                         int dtype, double* d_out3, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(f_vox && g_vox && d_out3, "null pointer");
+  VDVC_CHECK_ARG(fnx >= 1 && fny >= 1 && fnz >= 1 && gnx >= 1 && gny >= 1 && gnz >= 1, "bad shapes");
+  VDVC_CHECK_ARG(dtype == VDVC_F32 || dtype == VDVC_F64, "dtype %d", dtype);
+  return fft_shift(f_vox, fnx, fny, fnz, g_vox, gnx, gny, gnz, dtype, d_out3, nullptr, (cudaStream_t)stream);
+}
+
+int vdvc_fft_rigid_shift_device(const void* f_vox, int fnx, int fny, int fnz, const void* g_vox, int gnx, int gny,
+                                int gnz, int dtype, double* d_dev3, vdvc_stream_t stream) {
+  VDVC_CHECK_ARG(f_vox && g_vox && d_dev3, "null pointer");
+  VDVC_CHECK_ARG(fnx >= 1 && fny >= 1 && fnz >= 1 && gnx >= 1 && gny >= 1 && gnz >= 1, "bad shapes");
+  VDVC_CHECK_ARG(dtype == VDVC_F32 || dtype == VDVC_F64, "dtype %d", dtype);
+  return fft_shift(f_vox, fnx, fny, fnz, g_vox, gnx, gny, gnz, dtype, nullptr, d_dev3, (cudaStream_t)stream);
 }
 
 }  // extern "C"

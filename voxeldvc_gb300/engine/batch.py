@@ -96,11 +96,9 @@ def batch_multiscale_correlate_gpu(f_pix, g_pixs, problems, xp, scales=(2, 1, 0)
             h_i = h // s
             U0 = None
             if fft_seed and fft_prealign:
-                d = CG._fft_shift_vox(f_i, fs_i, g_i, gs_i, dtype)
-                nn = (mesh[0] + 1) * (mesh[1] + 1) * (mesh[2] + 1)
-                Uh = np.zeros(3 * nn, dtype=dtype)
-                Uh[0::3], Uh[1::3], Uh[2::3] = d[0], d[1], d[2]
-                U0 = D.to_device(Uh)
+                # the shift stays on the device: no host synchronisation per problem
+                d = CG._fft_shift_device(f_i, fs_i, g_i, gs_i, dtype)
+                U0 = CG._uniform_U0(d, (mesh[0] + 1) * (mesh[1] + 1) * (mesh[2] + 1), dtype)
             l0_i = None if l0_factor is None else l0_factor * h / s
             ls = CG._setup_level(CG._Level(f_i, fs_i, g_i, gs_i), *mesh, h_i, glt=glt, l0=l0_i,
                                  K_ref_laplacian=K_ref_laplacian, dynamic_mask=dynamic_mask, U0=U0,

@@ -312,6 +312,20 @@ def _fft_shift_vox(f_vox, fshape, g_vox, gshape, dt):
     return np.array([d[0], d[1], d[2]], dtype=np.float64)
 
 
+def _fft_shift_device(f_vox, fshape, g_vox, gshape, dt):
+    """The shift as a float64 CUDA tensor of 3, left on the device (no host
+    synchronisation)."""
+    d = D.empty(3, np.float64)
+    _lib.check(_lib.lib().vdvc_fft_rigid_shift_device(f_vox.data_ptr(), *fshape, g_vox.data_ptr(), *gshape,
+                                                      D.code_of(dt), d.data_ptr(), D.stream()), "fft_rigid_shift")
+    return d
+
+
+def _uniform_U0(d, n_nodes, dtype):
+    """Nodal field equal to the shift d (device, 3) at every node, in dtype."""
+    return d.to(D.torch_dtype(dtype)).repeat(n_nodes)
+
+
 def fft_rigid_shift(f_pix, g_pix, xp):
     """Integer voxel shift d with g(x) ~= f(x - d) by phase correlation.
     Reference: engine/correlate_gpu.py:381-414."""
@@ -806,12 +820,10 @@ def _pyramid(f_full, fs, g_full, gs, coarse, full_ready, scales, Nx, Ny, Nz, h, 
         elif A_aff is not None:
             U = D.to_device(_affine_U0(A_aff, t_aff, c_aff, s, h_i, Nx, Ny, Nz).astype(dtype))
         elif fft_prealign:
-            d = _fft_shift_vox(f_i, fs_i, g_i, gs_i, dtype)
-            n_nodes = (Nx + 1) * (Ny + 1) * (Nz + 1)
-            Uh = np.zeros(3 * n_nodes, dtype=dtype)
-            Uh[0::3], Uh[1::3], Uh[2::3] = d[0], d[1], d[2]
-            U = D.to_device(Uh)
+            dd = _fft_shift_device(f_i, fs_i, g_i, gs_i, dtype)
+            U = _uniform_U0(dd, (Nx + 1) * (Ny + 1) * (Nz + 1), dtype)
             if disp:
+                d = dd.cpu().numpy()
                 print("FFT pre-alignment: rigid shift d = (%.1f, %.1f, %.1f) voxels"
                       % (d[0] * s, d[1] * s, d[2] * s))
 
