@@ -227,13 +227,13 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 6 : 6) : 3) k_s
           const T ccz = tmin(tmax(cz, T(0)), gzmax);
           const bool inb = (ccx == cx) & (ccy == cy) & (ccz == cz);
           const T gv = trilinear(a.g, a.gnx, a.gny, a.gnz, ccx, ccy, ccz);
-          const bool m0 = a.mask0 ? (a.mask0[vv] != 0) : true;
+          const bool m0 = a.mask0 ? (__ldg(a.mask0 + vv) != 0) : true;
           const bool mk = inb && m0 && (gv > a.glt);
           a.gvals[vv] = gv;
           a.mask_out[vv] = mk ? 1 : 0;
           if constexpr (STATS) {
             if (a.freeze_out) a.freeze_out[vv] = mk ? 1 : 0;
-            const bool bm = a.bmask_frozen ? (a.bmask_frozen[vv] != 0) : mk;
+            const bool bm = a.bmask_frozen ? (__ldg(a.bmask_frozen + vv) != 0) : mk;
             if (bm) {
               const float mult = (float)(mxz * ((qy == 0 && j > 0) ? 2 : 1));
               const float gf = (float)gv;
@@ -333,12 +333,12 @@ __global__ void __launch_bounds__(256) k_elem_sample(const SampleArgs<float> a) 
           const float ccz = fminf(fmaxf(cz, 0.f), gzmax);
           const bool inb = (ccx == cx) & (ccy == cy) & (ccz == cz);
           const float gv = trilinear(a.g, a.gnx, a.gny, a.gnz, ccx, ccy, ccz);
-          const bool m0 = a.mask0 ? (a.mask0[vv] != 0) : true;
+          const bool m0 = a.mask0 ? (__ldg(a.mask0 + vv) != 0) : true;
           const bool mk = inb && m0 && (gv > a.glt);
           a.gvals[vv] = gv;
           a.mask_out[vv] = mk ? 1 : 0;
           if (a.freeze_out) a.freeze_out[vv] = mk ? 1 : 0;
-          const bool bm = a.bmask_frozen ? (a.bmask_frozen[vv] != 0) : mk;
+          const bool bm = a.bmask_frozen ? (__ldg(a.bmask_frozen + vv) != 0) : mk;
           if (bm) {
             const float mult = (float)(mxz * ((qy == 0 && j > 0) ? 2 : 1));
             r0 += mult;

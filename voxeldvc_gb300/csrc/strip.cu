@@ -146,8 +146,10 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
         const long long vv = vbase + (long long)qy * m.Nvx;
         const int vy = j * h + qy;
         const T wy = (vy == 0 || vy == m.Nvy - 1) ? T(0.5) : T(1);
-        const T g0 = a.grad[3 * vv + 0], g1 = a.grad[3 * vv + 1], g2 = a.grad[3 * vv + 2];
-        const bool mm = a.mask[vv] != 0;
+        // read-only inputs through the non-coherent path: the residual's
+        // store below would otherwise keep them from being hoisted
+        const T g0 = __ldg(a.grad + 3 * vv), g1 = __ldg(a.grad + 3 * vv + 1), g2 = __ldg(a.grad + 3 * vv + 2);
+        const bool mm = __ldg(a.mask + vv) != 0;
         if constexpr (HV) {
           const T uu0 = u0[0] + fy1 * du[0], uu1 = u0[1] + fy1 * du[1], uu2 = u0[2] + fy1 * du[2];
           T d = g0 * uu0 + g1 * uu1 + g2 * uu2;
@@ -159,11 +161,11 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
         if constexpr (BB) {
           T r;
           if constexpr (RS) {
-            const T fc = rn_sub(a.f[vv], mean0);
-            const T rv = rn_add(rn_mul(rn_sub(a.gvals[vv], gm), ratio), fc);
+            const T fc = rn_sub(__ldg(a.f + vv), mean0);
+            const T rv = rn_add(rn_mul(rn_sub(__ldg(a.gvals + vv), gm), ratio), fc);
             r = mm ? rv : T(0);
             a.res_out[vv] = r;
-            if (a.live[vv]) {
+            if (__ldg(a.live + vv)) {
               const int mult = mxz * ((qy == 0 && j > 0) ? 2 : 1);
               const float rf = (float)r, mf = (float)mult;
               ds0 += mf;
@@ -171,7 +173,7 @@ __global__ void __launch_bounds__(128) k_strip(const StripArgs<T> a, const Kpair
               ds2 += mf * rf * rf;
             }
           } else {
-            r = mm ? a.res_in[vv] : T(0);
+            r = mm ? __ldg(a.res_in + vv) : T(0);
           }
           r *= wy;
           const T t0 = r * g0, t1 = r * g1, t2 = r * g2;
