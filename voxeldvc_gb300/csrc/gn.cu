@@ -70,6 +70,8 @@ struct GnSolver {
   float* gmax;       // max |g| of grad_bf16 (the tensor-core formation's scale)
   // PCG graph
   cudaStream_t cap_stream;
+  cudaStream_t side;              // element-Hessian formation beside the residual pass
+  cudaEvent_t ev_fork, ev_join;
   cudaGraph_t graph;
   cudaGraphExec_t gexec;
   int chunk, kernels_per_iter;
@@ -502,14 +504,18 @@ static int create(const vdvc_gn_desc* d, void* ws, size_t ws_bytes, void** out) 
   static_assert(2 * sizeof(PcgState) + sizeof(GnScalars) <= kPinnedSlot, "pinned read-back slot too small");
   auto fail = [&](int code) {
     pool_stream_return(S->cap_stream);
+    pool_stream_return(S->side);
     pool_event_return(S->ev[0]);
     pool_event_return(S->ev[1]);
+    pool_event_return(S->ev_fork);
+    pool_event_return(S->ev_join);
     pool_pinned_return(S->h_pcg);
     delete S;
     return code;
   };
   void* pin = nullptr;
-  if (pool_stream(&S->cap_stream) || pool_pinned(&pin) || pool_event(&S->ev[0]) || pool_event(&S->ev[1])) {
+  if (pool_stream(&S->cap_stream) || pool_pinned(&pin) || pool_event(&S->ev[0]) || pool_event(&S->ev[1]) ||
+      (S->eh && (pool_stream(&S->side) || pool_event(&S->ev_fork) || pool_event(&S->ev_join)))) {
     S->h_pcg = (PcgState*)pin;
     return fail(set_error(VDVC_ERR_CUDA, "solver stream/event/pinned setup failed"));
   }
@@ -642,15 +648,28 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
   // diag H from the strip pass (matrix-free), from the element Hessians, or
   // not at all once it is final
   const bool with_diag = d.dynamic_mask && !S->eh_fixed;
+  const bool form = with_diag && S->eh;
+  if (form) {
+    // The element Hessians (gradient and b mask) and the residual pass
+    // (f, g values, b and live masks) are independent: the formation runs
+    // on the solver's side stream, beside the residual pass, and the
+    // gather below waits for both.
+    VDVC_CUDA(cudaEventRecord(S->ev_fork, s));
+    VDVC_CUDA(cudaStreamWaitEvent(S->side, S->ev_fork, 0));
+    if ((st = launch_eh_form(eh_form_args(S, S->frozen), S->side))) return st;
+    VDVC_CUDA(cudaEventRecord(S->ev_join, S->side));
+  }
   if (with_diag && !S->eh)
     st = launch_strip<T, kModeB | kModeRes | kModeDiag>(a, nullptr, s);
   else
     st = launch_strip<T, kModeB | kModeRes>(a, nullptr, s);
-  if (st) return st;
-  if (with_diag && S->eh) {
-    if ((st = launch_eh_form(eh_form_args(S, S->frozen), s))) return st;
+  if (form) {
+    // joined even when the residual launch failed: nothing is left pending
+    // on the side stream behind the caller's stream
+    VDVC_CUDA(cudaStreamWaitEvent(s, S->ev_join, 0));
     if (S->frozen_set) S->eh_fixed = true;
   }
+  if (st) return st;
   GridReduce red{S->partials, S->ticket};
   k_gn_gather_rhs<T><<<grid_blocks(S->m.Nnodes, 256, (long long)S->n_partials), 256, 0, s>>>(
       S->m, S->evA, S->evD, reg ? S->ru : nullptr, d.ll, d.reg_type != VDVC_REG_NONE ? S->diag_reg_t : nullptr, S->b,
@@ -834,8 +853,11 @@ static void destroy(GnSolver<T>* S) {
   if (S->gexec) cudaGraphExecDestroy(S->gexec);
   if (S->graph) cudaGraphDestroy(S->graph);
   pool_stream_return(S->cap_stream);
+  pool_stream_return(S->side);
   pool_event_return(S->ev[0]);
   pool_event_return(S->ev[1]);
+  pool_event_return(S->ev_fork);
+  pool_event_return(S->ev_join);
   pool_pinned_return(S->h_pcg);
   delete S;
 }
