@@ -53,6 +53,7 @@ struct GnSolver {
   double* diag_reg;  // h diag(K_lap) [+ equilibrium-gap diagonal], float64
   T* diag_reg_t;     // the same in the solve type
   uint8_t *live, *frozen;
+  bool live_is_b;    // the last sampling pass wrote the live mask into the b mask buffer only
   double* partials;
   size_t n_partials;
   unsigned int* ticket;
@@ -610,11 +611,13 @@ static int sample(GnSolver<T>* S, int freeze_now, cudaStream_t s) {
   a.mask0 = d.mask0;
   a.glt = (T)d.glt;
   a.gvals = S->gvals;
-  a.mask_out = S->live;
   // S->frozen is the b mask buffer: it follows the live mask until the freeze
   // iteration (engine/correlate_gpu.py:1079-1081) and is kept after it.
+  // Until then the live mask is written there alone (one byte stream per
+  // voxel, not two), after it into S->live.
+  a.mask_out = S->frozen_set ? S->live : S->frozen;
   a.bmask_frozen = S->frozen_set ? S->frozen : nullptr;
-  a.freeze_out = S->frozen_set ? nullptr : S->frozen;
+  S->live_is_b = !S->frozen_set;
   a.red = GridReduce{S->partials, S->ticket};
   a.stats = S->sc->gstats;
   int st = launch_sample<T, true, false>(a, s);
@@ -635,7 +638,7 @@ static int rhs(GnSolver<T>* S, cudaStream_t s) {
   a.mask = S->frozen;  // b mask
   a.f = (const T*)d.f_vox;
   a.gvals = S->gvals;
-  a.live = S->live;
+  a.live = S->live_is_b ? S->frozen : S->live;
   a.gstats = S->sc->gstats;
   a.mean0 = d.mean0;
   a.std0 = d.std0;
@@ -841,7 +844,7 @@ static int read(GnSolver<T>* S, int which, void* dst, int dst_f64, cudaStream_t 
       VDVC_LAUNCHED();
       return VDVC_OK;
     case VDVC_GN_LIVE_MASK:
-      VDVC_CUDA(cudaMemcpyAsync(dst, S->live, nv, cudaMemcpyDefault, s));
+      VDVC_CUDA(cudaMemcpyAsync(dst, S->live_is_b ? S->frozen : S->live, nv, cudaMemcpyDefault, s));
       return VDVC_OK;
   }
   return set_error(VDVC_ERR_ARG, "unknown buffer %d", which);

@@ -74,7 +74,6 @@ struct SampleArgs {
   uint8_t* mask_out;      // out (Nvox)
   // GN extras (stats != null): stats of g over the b mask and the active count
   const uint8_t* bmask_frozen;  // null: b mask = live mask
-  uint8_t* freeze_out;          // non-null: also write the live mask here (freezing now)
   GridReduce red;
   double* stats;                // out: count, s1, s2 over the b mask, n_active
   // interp mode (uvox != null): write u(x) instead of sampling

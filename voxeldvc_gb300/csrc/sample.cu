@@ -232,7 +232,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (STATS ? 6 : 6) : 3) k_s
           a.gvals[vv] = gv;
           a.mask_out[vv] = mk ? 1 : 0;
           if constexpr (STATS) {
-            if (a.freeze_out) a.freeze_out[vv] = mk ? 1 : 0;
             const bool bm = a.bmask_frozen ? (__ldg(a.bmask_frozen + vv) != 0) : mk;
             if (bm) {
               const float mult = (float)(mxz * ((qy == 0 && j > 0) ? 2 : 1));
@@ -337,7 +336,6 @@ __global__ void __launch_bounds__(256) k_elem_sample(const SampleArgs<float> a) 
           const bool mk = inb && m0 && (gv > a.glt);
           a.gvals[vv] = gv;
           a.mask_out[vv] = mk ? 1 : 0;
-          if (a.freeze_out) a.freeze_out[vv] = mk ? 1 : 0;
           const bool bm = a.bmask_frozen ? (__ldg(a.bmask_frozen + vv) != 0) : mk;
           if (bm) {
             const float mult = (float)(mxz * ((qy == 0 && j > 0) ? 2 : 1));
